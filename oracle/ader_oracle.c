@@ -1,0 +1,1785 @@
+/*
+ * ader_oracle.c -- plain-C restatement of PyPDE's ADER-WENO step.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU library, and the timed
+ * CPU baseline of bench.py.  Nothing of the product may include, link or
+ * call this file.
+ *
+ * Paths cited as file:line are relative to haranjackson/PyPDE.  The port is
+ * pinned against the reference itself by the golden vectors in tests/golden
+ * (made by oracle/ref_driver.cpp from the reference compiled from source).
+ *
+ * Deliberate differences from the reference, all at rounding level or in
+ * behaviour the reference leaves undefined:
+ *  - WENO and DG linear systems use precomputed inverses instead of a
+ *    ColPivHouseholderQR solve per call (weno.cpp:28, dg.cpp:192).
+ *  - max|eig| uses a Hessenberg + Francis double-shift QR for every V, where
+ *    the reference uses Eigen::EigenSolver for V<6 and Spectra Arnoldi with
+ *    ncv=V for V>=6 (eigs/system.cpp:28-43); both return the exact spectrum
+ *    of the same FD Jacobian up to rounding.
+ *  - stiff=True: the reference's Newton-Krylov (scipy/algos, tolerance 6e-6
+ *    absolute) is replaced by the per-cell locally implicit Newton iteration
+ *    of the GPU form (Newton on the source terms, fixed point on the fluxes)
+ *    iterated to ||obj||_inf <= newton_tol.  Both solve obj(q)=0 of
+ *    dg.cpp:128-154; the tolerance-tightened reference build checks it.
+ *  - NaN rows (iterator.cpp:141-145) are written only while in range; the
+ *    reference writes past ret's last row.
+ */
+#define _GNU_SOURCE
+#include "ader_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#define SQRT_EPS 1.4901161193847656e-08 /* sqrt(2^-52) = 2^-26, NumericalDiff.h:9 */
+#define WENO_LAMS 1.0                   /* weno.h:8 */
+#define WENO_LAMC 1e5                   /* weno.h:9 */
+#define WENO_EPS 1e-14                  /* weno.h:10 */
+#define DG_IT 50                        /* dg.h:8 */
+#define DG_TOL 6e-6                     /* dg.h:9 */
+#define NEWTON_MAXIT 200
+
+static int ipow(int b, int e) {
+  int r = 1;
+  while (e-- > 0)
+    r *= b;
+  return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* Power-basis polynomials (scipy/math/polynomials.cpp:6-66)           */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int n;
+  double c[2 * ORA_MAXN + 2];
+} poly_t;
+
+static double poly_eval(const poly_t *p, double x) { /* polynomials.cpp:24-31 */
+  double r = 0;
+  for (int i = 0; i < p->n; i++)
+    r += p->c[i] * pow(x, (double)i);
+  return r;
+}
+static poly_t poly_diff1(const poly_t *p) { /* polynomials.cpp:15-22 */
+  poly_t r;
+  r.n = p->n - 1;
+  for (int i = 0; i < r.n; i++)
+    r.c[i] = p->c[i + 1] * (i + 1);
+  return r;
+}
+static poly_t poly_diff(const poly_t *p, int k) {
+  poly_t r = *p;
+  for (int i = 0; i < k; i++)
+    r = poly_diff1(&r);
+  return r;
+}
+static poly_t poly_int(const poly_t *p) { /* polynomials.cpp:6-13 */
+  poly_t r;
+  r.n = p->n + 1;
+  r.c[0] = 0;
+  for (int i = 1; i < r.n; i++)
+    r.c[i] = p->c[i - 1] / i;
+  return r;
+}
+static poly_t poly_mul(const poly_t *a, const poly_t *b) { /* :33-43 */
+  poly_t r;
+  r.n = a->n + b->n - 1;
+  for (int i = 0; i < r.n; i++)
+    r.c[i] = 0;
+  for (int i = 0; i < a->n; i++)
+    for (int j = 0; j < b->n; j++)
+      r.c[i + j] += a->c[i] * b->c[j];
+  return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* Gauss-Legendre (scipy/math/legendre.cpp:136-197): roots of P_N by   */
+/* Newton from the Chebyshev-like guess, then the reference's one extra */
+/* Newton step, Clenshaw-based weights, symmetrisation, normalisation.  */
+/* ------------------------------------------------------------------ */
+static double legval_cn(double x, const double *c, int nc) { /* legendre.cpp:5-60 */
+  if (nc == 1)
+    return c[0];
+  if (nc == 2)
+    return c[0] + c[1] * x;
+  int nd = nc - 1;
+  double c0 = c[nc - 3] - (c[nc - 1] * (nd - 1)) / nd;
+  double c1 = c[nc - 2] + (c[nc - 1] * x * (2 * nd - 1)) / nd;
+  if (nc == 3)
+    return c0 + c1 * x;
+  nd -= 1;
+  double c00 = c[nc - 4] - (c1 * (nd - 1)) / nd;
+  double c11 = c0 + (c1 * x * (2 * nd - 1)) / nd;
+  for (int i = 5; i < nc + 1; i++) {
+    double tmp = c00;
+    nd -= 1;
+    c00 = c[nc - i] - (c11 * (nd - 1)) / nd;
+    c11 = tmp + (c11 * x * (2 * nd - 1)) / nd;
+  }
+  return c00 + c11 * x;
+}
+static void legder_c(const double *cin, int nc, double *der) { /* :96-134 */
+  double c[ORA_MAXN + 2];
+  int n = nc - 1;
+  memcpy(c, cin, sizeof(double) * nc);
+  for (int j = 0; j < n; j++)
+    der[j] = 0;
+  for (int j = n; j > 2; j--) {
+    der[j - 1] = (2 * j - 1) * c[j];
+    c[j - 2] += c[j];
+  }
+  if (n > 1)
+    der[1] = 3 * c[2];
+  der[0] = c[1];
+}
+static void leggauss(int deg, double *x, double *w) {
+  double c[ORA_MAXN + 2], dc[ORA_MAXN + 2];
+  for (int i = 0; i <= deg; i++)
+    c[i] = 0;
+  c[deg] = 1;
+  legder_c(c, deg + 1, dc);
+  /* roots, ascending */
+  for (int k = 0; k < deg; k++) {
+    double r = -cos(M_PI * (k + 0.75) / (deg + 0.5));
+    for (int it = 0; it < 100; it++) {
+      double dr = legval_cn(r, c, deg + 1) / legval_cn(r, dc, deg);
+      r -= dr;
+      if (fabs(dr) <= 1e-17)
+        break;
+    }
+    x[k] = r;
+  }
+  double df[ORA_MAXN], fm[ORA_MAXN];
+  for (int k = 0; k < deg; k++) { /* one Newton step, legendre.cpp:172-175 */
+    double dy = legval_cn(x[k], c, deg + 1);
+    df[k] = legval_cn(x[k], dc, deg);
+    x[k] -= dy / df[k];
+  }
+  double fmax = 0, dmax = 0;
+  for (int k = 0; k < deg; k++) {
+    fm[k] = legval_cn(x[k], c + 1, deg);
+    if (fabs(fm[k]) > fmax)
+      fmax = fabs(fm[k]);
+    if (fabs(df[k]) > dmax)
+      dmax = fabs(df[k]);
+  }
+  double ws[ORA_MAXN], xs[ORA_MAXN], sum = 0;
+  for (int k = 0; k < deg; k++)
+    ws[k] = 1. / ((fm[k] / fmax) * (df[k] / dmax));
+  for (int k = 0; k < deg; k++) {
+    w[k] = (ws[k] + ws[deg - 1 - k]) / 2;
+    xs[k] = (x[k] - x[deg - 1 - k]) / 2;
+  }
+  for (int k = 0; k < deg; k++) {
+    x[k] = xs[k];
+    sum += w[k];
+  }
+  for (int k = 0; k < deg; k++)
+    w[k] *= 2. / sum;
+}
+
+/* Gauss-Jordan inverse with partial pivoting (n <= ORA_MAXN) */
+static int mat_inverse(const double *a, int n, double *inv) {
+  double m[ORA_MAXN][2 * ORA_MAXN];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      m[i][j] = a[i * n + j];
+      m[i][n + j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int col = 0; col < n; col++) {
+    int piv = col;
+    for (int r = col + 1; r < n; r++)
+      if (fabs(m[r][col]) > fabs(m[piv][col]))
+        piv = r;
+    if (m[piv][col] == 0.0)
+      return -1;
+    if (piv != col)
+      for (int j = 0; j < 2 * n; j++) {
+        double t = m[col][j];
+        m[col][j] = m[piv][j];
+        m[piv][j] = t;
+      }
+    double p = m[col][col];
+    for (int j = 0; j < 2 * n; j++)
+      m[col][j] /= p;
+    for (int r = 0; r < n; r++)
+      if (r != col && m[r][col] != 0.0) {
+        double f = m[r][col];
+        for (int j = 0; j < 2 * n; j++)
+          m[r][j] -= f * m[col][j];
+      }
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      inv[i * n + j] = m[i][n + j];
+  return 0;
+}
+
+void ora_make_tables(int N, ora_tables *T) {
+  memset(T, 0, sizeof(*T));
+  T->N = N;
+  double x[ORA_MAXN], w[ORA_MAXN];
+  leggauss(N, x, w);
+  for (int i = 0; i < N; i++) { /* poly/basis.cpp:7-20 */
+    T->nodes[i] = (x[i] + 1) / 2;
+    T->wghts[i] = w[i] / 2;
+  }
+  poly_t psi[ORA_MAXN]; /* basis.cpp:22-53 */
+  for (int i = 0; i < N; i++) {
+    poly_t p = {1, {1.0}};
+    for (int j = 0; j < N; j++) {
+      if (j == i)
+        continue;
+      poly_t q = {2, {-T->nodes[j], 1.0}};
+      p = poly_mul(&p, &q);
+      double den = T->nodes[i] - T->nodes[j];
+      for (int k = 0; k < p.n; k++)
+        p.c[k] /= den;
+    }
+    psi[i] = p;
+  }
+  for (int j = 0; j < N; j++) { /* basis.cpp:55-66 */
+    T->endvals[j] = poly_eval(&psi[j], 0.);
+    T->endvals[N + j] = poly_eval(&psi[j], 1.);
+  }
+  for (int i = 0; i < N; i++) /* basis.cpp:68-76 */
+    for (int j = 0; j < N; j++) {
+      poly_t dp = poly_diff(&psi[j], 1);
+      T->dervals[i * N + j] = poly_eval(&dp, T->nodes[i]);
+    }
+  /* WENO matrices, weno_matrices.cpp:8-34 */
+  int FN2 = (int)floor((N - 1) / 2.), CN2 = (int)ceil((N - 1) / 2.);
+  double m[4][ORA_MAXN * ORA_MAXN];
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      poly_t P = poly_int(&psi[j]);
+      m[0][i * N + j] = poly_eval(&P, i - N + 2) - poly_eval(&P, i - N + 1);
+      m[1][i * N + j] = poly_eval(&P, i + 1) - poly_eval(&P, i);
+      m[2][i * N + j] = poly_eval(&P, i - CN2 + 1) - poly_eval(&P, i - CN2);
+      m[3][i * N + j] = poly_eval(&P, i - FN2 + 1) - poly_eval(&P, i - FN2);
+    }
+  for (int k = 0; k < 4; k++)
+    mat_inverse(m[k], N, T->weno_inv[k]);
+  for (int i = 0; i < N; i++) /* weno_matrices.cpp:36-51 */
+    for (int j = 0; j < N; j++) {
+      double s = 0;
+      for (int a = 1; a < N; a++) {
+        poly_t di = poly_diff(&psi[i], a), dj = poly_diff(&psi[j], a);
+        poly_t p = poly_mul(&di, &dj);
+        poly_t P = poly_int(&p);
+        s += poly_eval(&P, 1) - poly_eval(&P, 0);
+      }
+      T->sig[i * N + j] = s;
+    }
+  /* DG matrices, dg_matrices.cpp:32-55 and dg.cpp:38-40 */
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      double end = poly_eval(&psi[i], 1) * poly_eval(&psi[j], 1);
+      double der; /* DG_DER(j, i), transposed below */
+      if (i == j) {
+        double e0 = poly_eval(&psi[j], 0), e1 = poly_eval(&psi[j], 1);
+        der = (e1 * e1 - e0 * e0) / 2;
+      } else {
+        poly_t dp = poly_diff(&psi[i], 1);
+        der = T->wghts[j] * poly_eval(&dp, T->nodes[j]);
+      }
+      T->dgmat[i * N + j] = end - der;
+    }
+  mat_inverse(T->dgmat, N, T->dgmat_inv);
+}
+
+/* ------------------------------------------------------------------ */
+/* a1: ghost fill, grid/boundaries.cpp:7-53                            */
+/* ------------------------------------------------------------------ */
+static int renorm_index(int ind, int N, int type, int bound) {
+  int r = ind - N;
+  if (r < 0)
+    return type == 0 ? 0 : bound + r;
+  if (r >= bound)
+    return type == 0 ? bound - 1 : r - bound;
+  return r;
+}
+
+void ora_boundaries(const double *u, const int *nX, int ndim, const int *bt,
+                    int N, int V, double *ub) {
+  int nb[3], inds[3] = {0, 0, 0};
+  long ncell = 1;
+  for (int d = 0; d < ndim; d++) {
+    nb[d] = nX[d] + 2 * N;
+    ncell *= nb[d];
+  }
+  for (long idx = 0; idx < ncell; idx++) {
+    long src = 0;
+    for (int d = 0; d < ndim; d++)
+      src = src * nX[d] + renorm_index(inds[d], N, bt[d], nX[d]);
+    memcpy(ub + idx * V, u + src * V, sizeof(double) * V);
+    for (int d = ndim - 1; d >= 0; d--) { /* indexing.cpp:3-17 */
+      if (++inds[d] < nb[d])
+        break;
+      inds[d] = 0;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* a2: WENO, solvers/weno/weno.cpp:26-121                              */
+/* ------------------------------------------------------------------ */
+static void weno_coeffs(const ora_tables *T, const double *data, long dstride,
+                        int V, double *out /* N x V, row stride V */) {
+  int N = T->N;
+  int FN2 = (N - 1) / 2, CN2 = N / 2;
+  double num[ORA_MAXN * ORA_MAXV], den[ORA_MAXV], c[ORA_MAXN * ORA_MAXV];
+  for (int i = 0; i < N * V; i++)
+    num[i] = 0;
+  for (int v = 0; v < V; v++)
+    den[v] = 0;
+  int starts[4] = {0, N - 1, FN2, CN2};
+  double lams[4] = {WENO_LAMS, WENO_LAMS, WENO_LAMC, WENO_LAMC};
+  int nst = 2;
+  if (N > 2)
+    nst = (N % 2 == 0) ? 4 : 3;
+  for (int k = 0; k < nst; k++) { /* weno.cpp:26-39 */
+    const double *Mi = T->weno_inv[k];
+    for (int i = 0; i < N; i++)
+      for (int v = 0; v < V; v++) {
+        double s = 0;
+        for (int j = 0; j < N; j++)
+          s += Mi[i * N + j] * data[(starts[k] + j) * dstride + v];
+        c[i * V + v] = s;
+      }
+    for (int v = 0; v < V; v++) {
+      double p = 0;
+      for (int j = 0; j < N; j++) {
+        double r = 0;
+        for (int i = 0; i < N; i++)
+          r += c[i * V + v] * T->sig[i * N + j];
+        p += r * c[j * V + v];
+      }
+      p += WENO_EPS;
+      double p2 = p * p, p4 = p2 * p2, p8 = p4 * p4;
+      double o = lams[k] / p8;
+      for (int i = 0; i < N; i++)
+        num[i * V + v] += o * c[i * V + v];
+      den[v] += o;
+    }
+  }
+  for (int i = 0; i < N; i++)
+    for (int v = 0; v < V; v++)
+      out[i * V + v] = num[i * V + v] / den[v];
+}
+
+void ora_weno(const double *ub, const int *nXb, int ndim, int N, int V,
+              double *w) {
+  ora_tables T;
+  ora_make_tables(N, &T);
+  int shape[3];
+  long total = V;
+  for (int d = 0; d < ndim; d++) {
+    shape[d] = nXb[d];
+    total *= nXb[d];
+  }
+  double *rec = malloc(sizeof(double) * total);
+  memcpy(rec, ub, sizeof(double) * total);
+  for (int d = 0; d < ndim; d++) { /* weno.cpp:71-118 */
+    long n1 = 1, n3 = 1;
+    for (int i = 0; i < d; i++)
+      n1 *= shape[i];
+    int n2 = shape[d] - 2 * (N - 1);
+    for (int i = d + 1; i < ndim; i++)
+      n3 *= shape[i];
+    long n4 = ipow(N, d);
+    long outsz = n1 * n2 * n3 * n4 * N * V;
+    double *rec2 = malloc(sizeof(double) * outsz);
+    long stride = n3 * n4 * V;
+    double tmp[ORA_MAXN * ORA_MAXV];
+    for (long i1 = 0; i1 < n1; i1++)
+      for (long i3 = 0; i3 < n3; i3++)
+        for (long i4 = 0; i4 < n4; i4++) {
+          long indu = ((i1 * shape[d] * n3 + i3) * n4 + i4) * V;
+          long indw = ((i1 * n2 * n3 + i3) * n4 + i4) * N * V;
+          for (int i = 0; i < n2; i++) {
+            weno_coeffs(&T, rec + indu + i * stride, stride, V, tmp);
+            memcpy(rec2 + indw + i * N * stride, tmp, sizeof(double) * N * V);
+          }
+        }
+    free(rec);
+    rec = rec2;
+    shape[d] -= 2 * (N - 1);
+  }
+  long outrows = 1;
+  for (int d = 0; d < ndim; d++)
+    outrows *= shape[d];
+  memcpy(w, rec, sizeof(double) * outrows * ipow(N, ndim) * V);
+  free(rec);
+}
+
+/* ------------------------------------------------------------------ */
+/* Node-block helpers, poly/evaluations.cpp:23-70                      */
+/* ------------------------------------------------------------------ */
+/* ret[idx] = (sum_j DERVALS[i_d][j] q[idx with i_d=j]) / dX  over an Nd x V
+ * block (rows strided by rstride doubles) */
+static void derivs(const ora_tables *T, const double *q, long rstride,
+                   double *ret, long ostride, int d, int ndim, int V,
+                   double dXd) {
+  int N = T->N, Nd = ipow(N, ndim);
+  int sd = ipow(N, ndim - d - 1);
+  for (int idx = 0; idx < Nd; idx++) {
+    int id = (idx / sd) % N;
+    int base = idx - id * sd;
+    for (int v = 0; v < V; v++) {
+      double s = 0;
+      for (int j = 0; j < N; j++)
+        s += T->dervals[id * N + j] * q[(base + j * sd) * rstride + v];
+      ret[idx * ostride + v] = s / dXd;
+    }
+  }
+}
+
+/* ret[i] = sum_j ENDVALS[e][j] q[line i, node j] along axis d; i runs over
+ * the N^(ndim-1) transverse nodes in row-major order */
+static void endpts(const ora_tables *T, const double *q, long rstride,
+                   double *ret, long ostride, int d, int e, int ndim, int V) {
+  int N = T->N, Nd_ = ipow(N, ndim - 1);
+  int sd = ipow(N, ndim - d - 1);
+  for (int ind = 0; ind < Nd_; ind++) {
+    int hi = ind / sd, lo = ind % sd; /* zero_index, evaluations.cpp:4-21 */
+    int base = hi * sd * N + lo;
+    for (int v = 0; v < V; v++) {
+      double s = 0;
+      for (int j = 0; j < N; j++)
+        s += T->endvals[e * N + j] * q[(base + j * sd) * rstride + v];
+      ret[ind * ostride + v] = s;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Eigenvalues of a general real matrix (a4's max|eig|)                */
+/* Householder reduction to Hessenberg form, then the Francis implicit  */
+/* double-shift QR iteration with Wilkinson's deflation test            */
+/* (Golub & Van Loan, Matrix Computations, 4th ed., Alg. 7.4.2, 7.5.1). */
+/* ------------------------------------------------------------------ */
+#define A_(i, j) a[(i) * n + (j)]
+
+static void hessenberg(double *a, int n, double *q /* may be NULL */) {
+  if (q)
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++)
+        q[i * n + j] = (i == j);
+  for (int k = 0; k < n - 2; k++) {
+    double v[ORA_MAXV], alpha = 0, scale = 0;
+    for (int i = k + 1; i < n; i++)
+      scale += fabs(A_(i, k));
+    if (scale == 0.0)
+      continue;
+    for (int i = k + 1; i < n; i++) {
+      v[i] = A_(i, k) / scale;
+      alpha += v[i] * v[i];
+    }
+    double g = sqrt(alpha);
+    if (v[k + 1] > 0)
+      g = -g;
+    double h = alpha - v[k + 1] * g; /* = |v|^2 / 2 after v[k+1] -= g */
+    v[k + 1] -= g;
+    /* A <- P A, P = I - v v^T / h */
+    for (int j = k; j < n; j++) {
+      double s = 0;
+      for (int i = k + 1; i < n; i++)
+        s += v[i] * A_(i, j);
+      s /= h;
+      for (int i = k + 1; i < n; i++)
+        A_(i, j) -= s * v[i];
+    }
+    /* A <- A P */
+    for (int i = 0; i < n; i++) {
+      double s = 0;
+      for (int j = k + 1; j < n; j++)
+        s += A_(i, j) * v[j];
+      s /= h;
+      for (int j = k + 1; j < n; j++)
+        A_(i, j) -= s * v[j];
+    }
+    if (q)
+      for (int i = 0; i < n; i++) {
+        double s = 0;
+        for (int j = k + 1; j < n; j++)
+          s += q[i * n + j] * v[j];
+        s /= h;
+        for (int j = k + 1; j < n; j++)
+          q[i * n + j] -= s * v[j];
+      }
+    A_(k + 1, k) = g * scale;
+    for (int i = k + 2; i < n; i++)
+      A_(i, k) = 0.0;
+  }
+}
+
+/* Francis QR on upper Hessenberg a.  wantt: keep the full quasi-triangular
+ * T (and accumulate into z if non-NULL); otherwise only the active window is
+ * updated.  Returns 0 on success, -1 if an eigenvalue failed to converge. */
+static int francis(double *a, int n, double *wr, double *wi, int wantt,
+                   double *z) {
+  double norm = 0;
+  for (int i = 0; i < n; i++)
+    for (int j = (i > 0 ? i - 1 : 0); j < n; j++)
+      norm += fabs(A_(i, j));
+  int hi = n - 1, its = 0, total = 0;
+  double exshift = 0.0;
+  while (hi >= 0) {
+    int l;
+    for (l = hi; l > 0; l--) { /* deflation */
+      double s = fabs(A_(l - 1, l - 1)) + fabs(A_(l, l));
+      if (s == 0.0)
+        s = norm;
+      if (fabs(A_(l, l - 1)) <= DBL_EPSILON * s) {
+        A_(l, l - 1) = 0.0;
+        break;
+      }
+    }
+    if (l == hi) { /* 1x1 block */
+      wr[hi] = A_(hi, hi) + exshift;
+      wi[hi] = 0.0;
+      if (wantt)
+        A_(hi, hi) = wr[hi];
+      hi--;
+      its = 0;
+      continue;
+    }
+    if (l == hi - 1) { /* 2x2 block */
+      double p = 0.5 * (A_(hi - 1, hi - 1) - A_(hi, hi));
+      double qq = p * p + A_(hi, hi - 1) * A_(hi - 1, hi);
+      double zz = sqrt(fabs(qq));
+      double x = A_(hi, hi) + exshift;
+      if (wantt) {
+        A_(hi, hi) += exshift;
+        A_(hi - 1, hi - 1) += exshift;
+      }
+      if (qq >= 0.0) { /* real pair */
+        zz = (p >= 0) ? p + zz : p - zz;
+        wr[hi - 1] = x + zz;
+        wr[hi] = (zz != 0.0) ? x - A_(hi, hi - 1) * A_(hi - 1, hi) / zz
+                             : x + zz;
+        wi[hi - 1] = wi[hi] = 0.0;
+        if (wantt) { /* rotate the block to upper triangular form */
+          double xx = A_(hi, hi - 1);
+          double s = fabs(xx) + fabs(zz);
+          double pp = xx / s, q2 = zz / s;
+          double r = sqrt(pp * pp + q2 * q2);
+          pp /= r;
+          q2 /= r;
+          for (int j = hi - 1; j < n; j++) {
+            double t = A_(hi - 1, j);
+            A_(hi - 1, j) = q2 * t + pp * A_(hi, j);
+            A_(hi, j) = q2 * A_(hi, j) - pp * t;
+          }
+          for (int i = 0; i <= hi; i++) {
+            double t = A_(i, hi - 1);
+            A_(i, hi - 1) = q2 * t + pp * A_(i, hi);
+            A_(i, hi) = q2 * A_(i, hi) - pp * t;
+          }
+          if (z)
+            for (int i = 0; i < n; i++) {
+              double t = z[i * n + hi - 1];
+              z[i * n + hi - 1] = q2 * t + pp * z[i * n + hi];
+              z[i * n + hi] = q2 * z[i * n + hi] - pp * t;
+            }
+          A_(hi, hi - 1) = 0.0;
+          A_(hi - 1, hi - 1) = wr[hi - 1];
+          A_(hi, hi) = wr[hi];
+        }
+      } else { /* complex pair */
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = zz;
+        wi[hi] = -zz;
+      }
+      hi -= 2;
+      its = 0;
+      continue;
+    }
+    /* shifts */
+    double x = A_(hi, hi), y = A_(hi - 1, hi - 1);
+    double w = A_(hi, hi - 1) * A_(hi - 1, hi);
+    if (its == 10 || its == 20) { /* exceptional shift */
+      exshift += x;
+      for (int i = 0; i <= hi; i++)
+        A_(i, i) -= x;
+      double s = fabs(A_(hi, hi - 1)) + fabs(A_(hi - 1, hi - 2));
+      x = y = 0.75 * s;
+      w = -0.4375 * s * s;
+    }
+    its++;
+    if (++total > 40 * n)
+      return -1;
+    /* look for two consecutive small subdiagonals (start row m) */
+    int m;
+    double p = 0, q = 0, r = 0;
+    for (m = hi - 2; m >= l; m--) {
+      double zz = A_(m, m);
+      double rr = x - zz, ss = y - zz;
+      p = (rr * ss - w) / A_(m + 1, m) + A_(m, m + 1);
+      q = A_(m + 1, m + 1) - zz - rr - ss;
+      r = A_(m + 2, m + 1);
+      double s = fabs(p) + fabs(q) + fabs(r);
+      p /= s;
+      q /= s;
+      r /= s;
+      if (m == l)
+        break;
+      double u = fabs(A_(m, m - 1)) * (fabs(q) + fabs(r));
+      double vv = fabs(p) * (fabs(A_(m - 1, m - 1)) + fabs(zz) +
+                             fabs(A_(m + 1, m + 1)));
+      if (u <= DBL_EPSILON * vv)
+        break;
+    }
+    for (int i = m + 2; i <= hi; i++) {
+      A_(i, i - 2) = 0.0;
+      if (i > m + 2)
+        A_(i, i - 3) = 0.0;
+    }
+    /* double-shift sweep rows/cols m..hi */
+    for (int k = m; k <= hi - 1; k++) {
+      int notlast = (k != hi - 1);
+      if (k != m) {
+        p = A_(k, k - 1);
+        q = A_(k + 1, k - 1);
+        r = notlast ? A_(k + 2, k - 1) : 0.0;
+        x = fabs(p) + fabs(q) + fabs(r);
+        if (x == 0.0)
+          continue;
+        p /= x;
+        q /= x;
+        r /= x;
+      }
+      double s = sqrt(p * p + q * q + r * r);
+      if (p < 0)
+        s = -s;
+      if (k != m)
+        A_(k, k - 1) = -s * x;
+      else if (l != m)
+        A_(k, k - 1) = -A_(k, k - 1);
+      p += s;
+      x = p / s;
+      y = q / s;
+      double zz = r / s;
+      q /= p;
+      r /= p;
+      int jlo = k, jhi = wantt ? n - 1 : hi;
+      for (int j = jlo; j <= jhi; j++) { /* row update */
+        double pp = A_(k, j) + q * A_(k + 1, j);
+        if (notlast) {
+          pp += r * A_(k + 2, j);
+          A_(k + 2, j) -= pp * zz;
+        }
+        A_(k + 1, j) -= pp * y;
+        A_(k, j) -= pp * x;
+      }
+      int ilo = wantt ? 0 : l;
+      int ihi = (hi < k + 3) ? hi : k + 3;
+      for (int i = ilo; i <= ihi; i++) { /* column update */
+        double pp = x * A_(i, k) + y * A_(i, k + 1);
+        if (notlast) {
+          pp += zz * A_(i, k + 2);
+          A_(i, k + 2) -= pp * r;
+        }
+        A_(i, k + 1) -= pp * q;
+        A_(i, k) -= pp;
+      }
+      if (z)
+        for (int i = 0; i < n; i++) {
+          double pp = x * z[i * n + k] + y * z[i * n + k + 1];
+          if (notlast) {
+            pp += zz * z[i * n + k + 2];
+            z[i * n + k + 2] -= pp * r;
+          }
+          z[i * n + k + 1] -= pp * q;
+          z[i * n + k] -= pp;
+        }
+    }
+  }
+  return 0;
+}
+
+double ora_max_abs_eig(double *a, int n) {
+  double wr[ORA_MAXV], wi[ORA_MAXV];
+  if (n == 1)
+    return fabs(a[0]);
+  hessenberg(a, n, NULL);
+  if (francis(a, n, wr, wi, 0, NULL) != 0)
+    return NAN;
+  double m = 0;
+  for (int i = 0; i < n; i++) {
+    double r = (wi[i] == 0.0) ? fabs(wr[i]) : sqrt(wr[i] * wr[i] + wi[i] * wi[i]);
+    if (r > m)
+      m = r;
+  }
+  return m;
+}
+
+/* Eigenvectors of the quasi-triangular T by back substitution, then
+ * V = Z X.  Complex arithmetic via C99 complex is avoided for portability:
+ * (re, im) pairs. */
+int ora_eig(const double *ain, int n, double *wr, double *wi, double *vr,
+            double *vi) {
+  double a[ORA_MAXV * ORA_MAXV], z[ORA_MAXV * ORA_MAXV];
+  memcpy(a, ain, sizeof(double) * n * n);
+  hessenberg(a, n, z);
+  if (francis(a, n, wr, wi, 1, z) != 0)
+    return -1;
+  double norm = 0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      norm += fabs(A_(i, j));
+  double smin = DBL_EPSILON * (norm > 0 ? norm : 1.0);
+  double xr[ORA_MAXV], xi[ORA_MAXV];
+  for (int k = 0; k < n; k++) {
+    double lr = wr[k], li = wi[k];
+    for (int i = 0; i < n; i++)
+      xr[i] = xi[i] = 0.0;
+    int top;
+    if (li == 0.0) {
+      xr[k] = 1.0;
+      top = k - 1;
+    } else if (li > 0.0) { /* first of a pair: block (k, k+1) */
+      /* eigenvector of the 2x2 block [[a b],[c d]] for lambda = lr + i li:
+       * x_{k+1} = 1, x_k = (lambda - d) / c ... use the row with larger
+       * coefficient for stability */
+      double b = A_(k, k + 1), c = A_(k + 1, k);
+      if (fabs(b) >= fabs(c)) {
+        xr[k] = 1.0;
+        xi[k] = 0.0;
+        /* (a - lambda) x_k + b x_{k+1} = 0 */
+        xr[k + 1] = -(A_(k, k) - lr) / b;
+        xi[k + 1] = li / b;
+      } else {
+        xr[k + 1] = 1.0;
+        xi[k + 1] = 0.0;
+        /* c x_k + (d - lambda) x_{k+1} = 0 */
+        xr[k] = -(A_(k + 1, k + 1) - lr) / c;
+        xi[k] = li / c;
+      }
+      top = k - 1;
+    } else { /* second of a pair: conjugate of the first */
+      for (int i = 0; i < n; i++) {
+        vr[i * n + k] = vr[i * n + k - 1];
+        vi[i * n + k] = -vi[i * n + k - 1];
+      }
+      continue;
+    }
+    int last = (li > 0.0) ? k + 1 : k;
+    for (int i = top; i >= 0; i--) {
+      int blk2 = (i > 0 && A_(i, i - 1) != 0.0);
+      if (!blk2) {
+        double sr = 0, si = 0;
+        for (int j = i + 1; j <= last; j++) {
+          sr += A_(i, j) * xr[j];
+          si += A_(i, j) * xi[j];
+        }
+        double dr = A_(i, i) - lr, di = -li;
+        if (fabs(dr) + fabs(di) < smin)
+          dr = smin;
+        double den = dr * dr + di * di; /* x = -s / (dr + i di) */
+        xr[i] = -(sr * dr + si * di) / den;
+        xi[i] = -(si * dr - sr * di) / den;
+      } else { /* 2x2 block rows i-1, i */
+        double s1r = 0, s1i = 0, s2r = 0, s2i = 0;
+        for (int j = i + 1; j <= last; j++) {
+          s1r += A_(i - 1, j) * xr[j];
+          s1i += A_(i - 1, j) * xi[j];
+          s2r += A_(i, j) * xr[j];
+          s2i += A_(i, j) * xi[j];
+        }
+        /* [[a-l, b],[c, d-l]] [x1;x2] = -[s1; s2], complex l */
+        double ar = A_(i - 1, i - 1) - lr, ai = -li, b = A_(i - 1, i);
+        double c = A_(i, i - 1), dr = A_(i, i) - lr, di = -li;
+        /* det = (ar + i ai)(dr + i di) - b c */
+        double detr = ar * dr - ai * di - b * c, deti = ar * di + ai * dr;
+        if (fabs(detr) + fabs(deti) < smin)
+          detr = smin;
+        double dd = detr * detr + deti * deti;
+        /* x1 = (-(d-l) s1 + b s2) / det ; x2 = (c s1 - (a-l) s2) / det */
+        double n1r = -(dr * s1r - di * s1i) + b * s2r;
+        double n1i = -(dr * s1i + di * s1r) + b * s2i;
+        double n2r = c * s1r - (ar * s2r - ai * s2i);
+        double n2i = c * s1i - (ar * s2i + ai * s2r);
+        xr[i - 1] = (n1r * detr + n1i * deti) / dd;
+        xi[i - 1] = (n1i * detr - n1r * deti) / dd;
+        xr[i] = (n2r * detr + n2i * deti) / dd;
+        xi[i] = (n2i * detr - n2r * deti) / dd;
+        i--;
+      }
+    }
+    /* v = Z x, normalised to unit 2-norm */
+    double nrm = 0;
+    for (int i = 0; i < n; i++) {
+      double sr = 0, si = 0;
+      for (int j = 0; j <= last; j++) {
+        sr += z[i * n + j] * xr[j];
+        si += z[i * n + j] * xi[j];
+      }
+      vr[i * n + k] = sr;
+      vi[i * n + k] = si;
+      nrm += sr * sr + si * si;
+    }
+    nrm = sqrt(nrm);
+    for (int i = 0; i < n; i++) {
+      vr[i * n + k] /= nrm;
+      vi[i * n + k] /= nrm;
+    }
+  }
+  return 0;
+}
+#undef A_
+
+/* Solve the complex system (R) x = b (n x n, partial pivoting). */
+static int csolve(int n, double *mr, double *mi, double *br, double *bi) {
+  for (int c = 0; c < n; c++) {
+    int piv = c;
+    double best = sqrt(mr[c * n + c] * mr[c * n + c] + mi[c * n + c] * mi[c * n + c]);
+    for (int r = c + 1; r < n; r++) {
+      double v = sqrt(mr[r * n + c] * mr[r * n + c] + mi[r * n + c] * mi[r * n + c]);
+      if (v > best) {
+        best = v;
+        piv = r;
+      }
+    }
+    if (best == 0.0)
+      return -1;
+    if (piv != c) {
+      for (int j = 0; j < n; j++) {
+        double t = mr[c * n + j];
+        mr[c * n + j] = mr[piv * n + j];
+        mr[piv * n + j] = t;
+        t = mi[c * n + j];
+        mi[c * n + j] = mi[piv * n + j];
+        mi[piv * n + j] = t;
+      }
+      double t = br[c];
+      br[c] = br[piv];
+      br[piv] = t;
+      t = bi[c];
+      bi[c] = bi[piv];
+      bi[piv] = t;
+    }
+    double pr = mr[c * n + c], pi = mi[c * n + c], pd = pr * pr + pi * pi;
+    for (int r = c + 1; r < n; r++) {
+      double fr = (mr[r * n + c] * pr + mi[r * n + c] * pi) / pd;
+      double fi = (mi[r * n + c] * pr - mr[r * n + c] * pi) / pd;
+      for (int j = c; j < n; j++) {
+        mr[r * n + j] -= fr * mr[c * n + j] - fi * mi[c * n + j];
+        mi[r * n + j] -= fr * mi[c * n + j] + fi * mr[c * n + j];
+      }
+      br[r] -= fr * br[c] - fi * bi[c];
+      bi[r] -= fr * bi[c] + fi * br[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    double sr = br[r], si = bi[r];
+    for (int j = r + 1; j < n; j++) {
+      sr -= mr[r * n + j] * br[j] - mi[r * n + j] * bi[j];
+      si -= mr[r * n + j] * bi[j] + mi[r * n + j] * br[j];
+    }
+    double pr = mr[r * n + r], pi = mi[r * n + r], pd = pr * pr + pi * pi;
+    br[r] = (sr * pr + si * pi) / pd;
+    bi[r] = (si * pr - sr * pi) / pd;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* a4: FD Jacobian + B (eigs/NumericalDiff.h:6-44, eigs/system.cpp)    */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  ora_flux_fn F;
+  ora_ncp_fn B;
+  ora_src_fn S;
+  int ndim, N, V, Nd, secondOrder;
+  const double *dX;
+  ora_tables T;
+  double wprod[ORA_MAXN * ORA_MAXN * ORA_MAXN]; /* prod_d W[i_d] per node */
+} ctx_t;
+
+static void ctx_init(ctx_t *c, ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                     int ndim, int N, int V, const double *dX, int so) {
+  c->F = F;
+  c->B = B;
+  c->S = S;
+  c->ndim = ndim;
+  c->N = N;
+  c->V = V;
+  c->Nd = ipow(N, ndim);
+  c->dX = dX;
+  c->secondOrder = so;
+  ora_make_tables(N, &c->T);
+  for (int idx = 0; idx < c->Nd; idx++) { /* stepper.cpp:24-32 */
+    double p = 1.0;
+    int r = idx;
+    int digs[3] = {0, 0, 0};
+    for (int d = ndim - 1; d >= 0; d--) {
+      digs[d] = r % N;
+      r /= N;
+    }
+    for (int d = 0; d < ndim; d++)
+      p *= c->T.wghts[digs[d]];
+    c->wprod[idx] = p;
+  }
+}
+
+/* Forward-difference Jacobian of F (eigs/NumericalDiff.h:6-44).  Both of
+ * the reference's call sites use forwardMode=true, its default:
+ * system.cpp:15 passes only secondOrder=false (perturb q), system.cpp:58
+ * secondOrder=true (perturb dq_d).  h = max(sqrt(eps)|x|, sqrt(eps)). */
+static void fd_jacobian(const ctx_t *c, double *jac, double *q, double *dq,
+                        int d, int wrt_dq) {
+  int V = c->V;
+  double v1[ORA_MAXV], v2[ORA_MAXV];
+  c->F(v1, q, dq, d);
+  for (int i = 0; i < V; i++) {
+    double *qi = wrt_dq ? dq + d * V + i : q + i;
+    double qi0 = *qi;
+    double h = fmax(SQRT_EPS * fabs(qi0), SQRT_EPS);
+    *qi += h;
+    c->F(v2, q, dq, d);
+    *qi = qi0;
+    for (int r = 0; r < V; r++)
+      jac[r * V + i] = (v2[r] - v1[r]) / h;
+  }
+}
+
+static void system_matrix(const ctx_t *c, double *M, double *q, double *dq,
+                          int d) { /* system.cpp:6-26 */
+  int V = c->V;
+  if (c->F)
+    fd_jacobian(c, M, q, dq, d, 0);
+  else
+    for (int i = 0; i < V * V; i++)
+      M[i] = 0.0;
+  if (c->B) {
+    double b[ORA_MAXV * ORA_MAXV];
+    c->B(b, q, d);
+    for (int i = 0; i < V * V; i++)
+      M[i] += b[i];
+  }
+}
+
+static double max_abs_eigs(const ctx_t *c, double *q, double *dq, int d) {
+  double M[ORA_MAXV * ORA_MAXV];
+  system_matrix(c, M, q, dq, d);
+  return ora_max_abs_eig(M, c->V);
+}
+
+static double max_abs_eigs_2nd(const ctx_t *c, double *q, double *dq, int d) {
+  double M[ORA_MAXV * ORA_MAXV]; /* system.cpp:53-61 */
+  fd_jacobian(c, M, q, dq, d, 1);
+  return 2 * (c->N + 1) / c->dX[d] * ora_max_abs_eig(M, c->V);
+}
+
+/* ------------------------------------------------------------------ */
+/* a3: CFL timestep, solvers/stepper.cpp:35-76                         */
+/* ------------------------------------------------------------------ */
+/* The quadrature averages of stepper.cpp:49,53 are Eigen row-vector x
+ * matrix products; the reference build evaluates them with Eigen's
+ * column-major GEMV kernel, whose summation order is: blocks of four nodes,
+ * summed pairwise ((a0+a1)+(a2+a3)) into the running total for result
+ * lanes that fall in a 2-double packet (v < V & ~1) and left to right for
+ * the odd last lane, then the leftover nodes left to right.  The order is
+ * restated here because the FD Jacobian that follows amplifies a one-ulp
+ * change of its input state ~1e8-fold. */
+static double wavg(const double *wp, const double *x, long stride, int n,
+                   int packet) {
+  double s = 0;
+  int k = 0;
+  for (; k + 3 < n; k += 4) {
+    double a0 = wp[k] * x[k * stride], a1 = wp[k + 1] * x[(k + 1) * stride];
+    double a2 = wp[k + 2] * x[(k + 2) * stride];
+    double a3 = wp[k + 3] * x[(k + 3) * stride];
+    if (packet)
+      s = s + ((a0 + a1) + (a2 + a3));
+    else
+      s = (((s + a0) + a1) + a2) + a3;
+  }
+  for (; k < n; k++)
+    s += wp[k] * x[k * stride];
+  return s;
+}
+
+static double cfl_max(const ctx_t *c, const double *w, long c0, long c1) {
+  int V = c->V, Nd = c->Nd, ndim = c->ndim;
+  double MAX = 0.0;
+  double dw[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  for (long cell = c0; cell < c1; cell++) {
+    const double *w0 = w + cell * Nd * V;
+    double q[ORA_MAXV], dq[3 * ORA_MAXV];
+    for (int v = 0; v < V; v++)
+      q[v] = wavg(c->wprod, w0 + v, V, Nd, v < (V & ~1));
+    for (int d = 0; d < ndim; d++) {
+      derivs(&c->T, w0, V, dw, V, d, ndim, V, c->dX[d]);
+      for (int v = 0; v < V; v++)
+        dq[d * V + v] = wavg(c->wprod, dw + v, V, Nd, v < (V & ~1));
+    }
+    double tmp = 0.0;
+    for (int d = 0; d < ndim; d++) {
+      double lam = max_abs_eigs(c, q, dq, d);
+      if (c->secondOrder)
+        lam += max_abs_eigs_2nd(c, q, dq, d);
+      tmp += lam / c->dX[d];
+    }
+    MAX = fmax(MAX, tmp);
+  }
+  return MAX;
+}
+
+static double dt_from_max(double MAX, double CFL, double tf, double t,
+                          long count) {
+  double dt = CFL / MAX;
+  if (count <= 5)
+    dt *= 0.2;
+  if (t + dt > tf)
+    return tf - t;
+  return dt;
+}
+
+double ora_timestep(ora_flux_fn F, ora_ncp_fn B, const double *w, long nrows,
+                    const double *dX, int ndim, int N, int V, double CFL,
+                    double tf, double t, long count, int secondOrder) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, NULL, ndim, N, V, dX, secondOrder);
+  double MAX = cfl_max(c, w, 0, nrows / c->Nd);
+  free(c);
+  return dt_from_max(MAX, CFL, tf, t, count);
+}
+
+/* ------------------------------------------------------------------ */
+/* a5/a6/a7: DG predictor, solvers/dg/dg.cpp                           */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  double dq[ORA_MAXN * ORA_MAXN * ORA_MAXN * 3 * ORA_MAXV];
+  double f[ORA_MAXN * ORA_MAXN * ORA_MAXN * 3 * ORA_MAXV];
+  double df[ORA_MAXN * ORA_MAXN * ORA_MAXN * 3 * ORA_MAXV];
+  double tmp[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  double fd[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+} dg_scratch;
+
+/* rhs(q) = Ww + dt * c_{t,idx} (S - sum_d B_d dq_d - sum_d dF_d/dx_d),
+ * dg.cpp:50-126.  q, ret: (N*Nd) x V. */
+static void dg_rhs(const ctx_t *c, const double *q, const double *Ww,
+                   double dt, double *ret, dg_scratch *s) {
+  int N = c->N, V = c->V, Nd = c->Nd, ndim = c->ndim;
+  for (int t = 0; t < N; t++) {
+    const double *qt = q + t * Nd * V;
+    double *rt = ret + t * Nd * V;
+    for (int d = 0; d < ndim; d++)
+      derivs(&c->T, qt, V, s->dq + d * V, ndim * V, d, ndim, V, c->dX[d]);
+    if (c->F) {
+      for (int idx = 0; idx < Nd; idx++)
+        for (int d = 0; d < ndim; d++)
+          c->F(s->f + (idx * ndim + d) * V, (double *)qt + idx * V,
+               s->dq + idx * ndim * V, d);
+      for (int d = 0; d < ndim; d++) {
+        for (int idx = 0; idx < Nd; idx++)
+          memcpy(s->fd + idx * V, s->f + (idx * ndim + d) * V,
+                 sizeof(double) * V);
+        derivs(&c->T, s->fd, V, s->df + d * V, ndim * V, d, ndim, V,
+               c->dX[d]);
+      }
+    }
+    for (int idx = 0; idx < Nd; idx++) {
+      double *r = rt + idx * V;
+      if (c->S)
+        c->S(r, (double *)qt + idx * V);
+      else
+        for (int v = 0; v < V; v++)
+          r[v] = 0.0;
+      double cc = c->T.wghts[t];
+      int rem = idx, digs[3] = {0, 0, 0};
+      for (int d = ndim - 1; d >= 0; d--) {
+        digs[d] = rem % N;
+        rem /= N;
+      }
+      for (int d = 0; d < ndim; d++) {
+        if (c->B) {
+          double b[ORA_MAXV * ORA_MAXV];
+          c->B(b, (double *)qt + idx * V, d);
+          const double *dqd = s->dq + (idx * ndim + d) * V;
+          for (int i = 0; i < V; i++) {
+            double acc = 0;
+            for (int j = 0; j < V; j++)
+              acc += b[i * V + j] * dqd[j];
+            r[i] -= acc;
+          }
+        }
+        if (c->F)
+          for (int v = 0; v < V; v++)
+            r[v] -= s->df[(idx * ndim + d) * V + v];
+        cc *= c->T.wghts[digs[d]];
+      }
+      for (int v = 0; v < V; v++)
+        r[v] *= cc;
+    }
+  }
+  for (int i = 0; i < N * Nd * V; i++)
+    ret[i] = ret[i] * dt + Ww[i];
+}
+
+/* Ww and the initial guess, dg.cpp:12-20, 156-171 */
+static void dg_init(const ctx_t *c, const double *w, double *Ww, double *q0) {
+  int N = c->N, V = c->V, Nd = c->Nd;
+  for (int t = 0; t < N; t++)
+    for (int idx = 0; idx < Nd; idx++) {
+      double cc = c->T.endvals[t] * c->wprod[idx];
+      /* the reference multiplies ENDVALS(0,t) by each W[i_d] in turn */
+      int rem = idx, digs[3] = {0, 0, 0};
+      for (int d = c->ndim - 1; d >= 0; d--) {
+        digs[d] = rem % N;
+        rem /= N;
+      }
+      cc = c->T.endvals[t];
+      for (int d = 0; d < c->ndim; d++)
+        cc *= c->T.wghts[digs[d]];
+      for (int v = 0; v < V; v++) {
+        Ww[(t * Nd + idx) * V + v] = cc * w[idx * V + v];
+        q0[(t * Nd + idx) * V + v] = w[idx * V + v];
+      }
+    }
+}
+
+/* q1 = DG_U^{-1} r with DG_U = kron(DG_MAT, diag W, ...), dg.cpp:40-47 */
+static void dg_usolve(const ctx_t *c, const double *r, double *q1) {
+  int N = c->N, V = c->V, Nd = c->Nd;
+  for (int t = 0; t < N; t++)
+    for (int idx = 0; idx < Nd; idx++)
+      for (int v = 0; v < V; v++) {
+        double s = 0;
+        for (int k = 0; k < N; k++)
+          s += c->T.dgmat_inv[t * N + k] * r[(k * Nd + idx) * V + v];
+        q1[(t * Nd + idx) * V + v] = s / c->wprod[idx];
+      }
+}
+
+/* Picard iteration, dg.cpp:187-202 */
+static int dg_picard(const ctx_t *c, double *q0, const double *Ww, double dt,
+                     double *q1, dg_scratch *s) {
+  int n = c->N * c->Nd * c->V;
+  double r[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  int it;
+  for (it = 0; it < DG_IT; it++) {
+    dg_rhs(c, q0, Ww, dt, r, s);
+    dg_usolve(c, r, q1);
+    int again = 0;
+    for (int i = 0; i < n; i++)
+      if (fabs(q1[i] - q0[i]) > DG_TOL * (1. + fabs(q0[i]))) {
+        again = 1;
+        break;
+      }
+    if (!again)
+      return it + 1;
+    memcpy(q0, q1, sizeof(double) * n);
+  }
+  return it;
+}
+
+/* LU with partial pivoting, in place (n <= 64) */
+static int lu_factor(double *a, int n, int *piv) {
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    for (int i = k + 1; i < n; i++)
+      if (fabs(a[i * n + k]) > fabs(a[p * n + k]))
+        p = i;
+    piv[k] = p;
+    if (a[p * n + k] == 0.0)
+      return -1;
+    if (p != k)
+      for (int j = 0; j < n; j++) {
+        double t = a[k * n + j];
+        a[k * n + j] = a[p * n + j];
+        a[p * n + j] = t;
+      }
+    for (int i = k + 1; i < n; i++) {
+      double f = a[i * n + k] / a[k * n + k];
+      a[i * n + k] = f;
+      for (int j = k + 1; j < n; j++)
+        a[i * n + j] -= f * a[k * n + j];
+    }
+  }
+  return 0;
+}
+static void lu_solve(const double *a, int n, const int *piv, double *b) {
+  for (int k = 0; k < n; k++) {
+    if (piv[k] != k) {
+      double t = b[k];
+      b[k] = b[piv[k]];
+      b[piv[k]] = t;
+    }
+    for (int i = k + 1; i < n; i++)
+      b[i] -= a[i * n + k] * b[k];
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double s = b[i];
+    for (int j = i + 1; j < n; j++)
+      s -= a[i * n + j] * b[j];
+    b[i] = s / a[i * n + i];
+  }
+}
+
+/* Locally implicit Newton iteration for stiff S: solve obj(q) = rhs(q) -
+ * DG_U q = 0 (dg.cpp:128-154).  Each iteration linearises the source term
+ * exactly at every space-time node and keeps the flux terms explicit:
+ *   per spatial node idx, A[(t,v),(k,w)] = dt W_t dS_v/dq_w(q_t) d_tk
+ *                                          - DG_MAT[t,k] d_vw
+ *   q <- q - A^{-1} obj(q) / prod W_idx
+ * Stops when ||obj(q)||_inf <= tol (or at the rounding floor of obj). */
+static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
+                     double tol, dg_scratch *s) {
+  int N = c->N, V = c->V, Nd = c->Nd;
+  int n = N * Nd * V, nl = N * V;
+  double r[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  double A[ORA_MAXN * ORA_MAXV * ORA_MAXN * ORA_MAXV], b[ORA_MAXN * ORA_MAXV];
+  int piv[ORA_MAXN * ORA_MAXV];
+  for (int it = 0; it < NEWTON_MAXIT; it++) {
+    dg_rhs(c, q, Ww, dt, r, s);
+    double res = 0, scale = 0;
+    for (int t = 0; t < N; t++)
+      for (int idx = 0; idx < Nd; idx++)
+        for (int v = 0; v < V; v++) {
+          double uq = 0;
+          for (int k = 0; k < N; k++)
+            uq += c->T.dgmat[t * N + k] * q[(k * Nd + idx) * V + v];
+          uq *= c->wprod[idx];
+          int i = (t * Nd + idx) * V + v;
+          double rr = r[i];
+          r[i] = rr - uq;
+          res = fmax(res, fabs(r[i]));
+          scale = fmax(scale, fmax(fabs(rr), fabs(uq)));
+        }
+    if (res <= tol || res <= 16 * DBL_EPSILON * scale)
+      return it;
+    for (int idx = 0; idx < Nd; idx++) {
+      for (int i = 0; i < nl * nl; i++)
+        A[i] = 0.0;
+      for (int t = 0; t < N; t++) {
+        double *qn = q + (t * Nd + idx) * V;
+        if (c->S) { /* forward FD Jacobian of S at this node */
+          double s0[ORA_MAXV], s1[ORA_MAXV];
+          c->S(s0, qn);
+          for (int wv = 0; wv < V; wv++) {
+            double q0 = qn[wv];
+            double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
+            qn[wv] = q0 + h;
+            c->S(s1, qn);
+            qn[wv] = q0;
+            for (int v = 0; v < V; v++)
+              A[(t * V + v) * nl + t * V + wv] =
+                  dt * c->T.wghts[t] * ((s1[v] - s0[v]) / h);
+          }
+        }
+        for (int k = 0; k < N; k++)
+          for (int v = 0; v < V; v++)
+            A[(t * V + v) * nl + k * V + v] -= c->T.dgmat[t * N + k];
+      }
+      if (lu_factor(A, nl, piv) != 0)
+        return -1;
+      for (int t = 0; t < N; t++)
+        for (int v = 0; v < V; v++)
+          b[t * V + v] = r[(t * Nd + idx) * V + v] / c->wprod[idx];
+      lu_solve(A, nl, piv, b);
+      for (int t = 0; t < N; t++)
+        for (int v = 0; v < V; v++)
+          q[(t * Nd + idx) * V + v] -= b[t * V + v];
+    }
+  }
+  (void)n;
+  return NEWTON_MAXIT;
+}
+
+static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
+                            int stiff, double dt, double tol, double *qh,
+                            int *maxit) {
+  int N = c->N, V = c->V, Nd = c->Nd;
+  int n = N * Nd * V;
+  dg_scratch *s = malloc(sizeof(dg_scratch));
+  double *Ww = malloc(sizeof(double) * n * 3);
+  double *q0 = Ww + n, *q1 = Ww + 2 * n;
+  long total = 0;
+  int mx = 0;
+  for (long cell = c0; cell < c1; cell++) {
+    dg_init(c, w + cell * Nd * V, Ww, q0);
+    int it;
+    if (stiff) {
+      it = dg_newton(c, q0, Ww, dt, tol, s);
+      memcpy(qh + cell * n, q0, sizeof(double) * n);
+    } else {
+      it = dg_picard(c, q0, Ww, dt, q1, s);
+      memcpy(qh + cell * n, q1, sizeof(double) * n);
+    }
+    total += it;
+    if (it > mx)
+      mx = it;
+  }
+  free(s);
+  free(Ww);
+  if (maxit && mx > *maxit)
+    *maxit = mx;
+  return total;
+}
+
+long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
+                   long nrows, const double *dX, int ndim, int N, int V,
+                   int stiff, double dt, double newton_tol, double *qh,
+                   int *maxit) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, 0);
+  if (maxit)
+    *maxit = 0;
+  long r = predictor_range(c, w, 0, nrows / c->Nd, stiff, dt, newton_tol, qh,
+                           maxit);
+  free(c);
+  return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* a8-a12: FV corrector, solvers/fv/fv.cpp and fluxes.cpp              */
+/* ------------------------------------------------------------------ */
+static void d_rus(const ctx_t *c, double *ret, double *qL, double *qR,
+                  double *dqL, double *dqR, int d) { /* fluxes.cpp:72-78 */
+  double m1 = max_abs_eigs(c, qL, dqL, d);
+  double m2 = max_abs_eigs(c, qR, dqR, d);
+  double m = fmax(m1, m2);
+  for (int v = 0; v < c->V; v++)
+    ret[v] = m * (qL[v] - qR[v]);
+}
+
+/* |A| (qL - qR) from an eigen-decomposition of A (fluxes.cpp:36-41) */
+static void abs_apply(int V, const double *M, const double *Dq, double *out,
+                      double weight, int accumulate) {
+  double wr[ORA_MAXV], wi[ORA_MAXV], vr[ORA_MAXV * ORA_MAXV],
+      vi[ORA_MAXV * ORA_MAXV];
+  ora_eig(M, V, wr, wi, vr, vi);
+  double mr[ORA_MAXV * ORA_MAXV], mi[ORA_MAXV * ORA_MAXV];
+  double br[ORA_MAXV], bi[ORA_MAXV];
+  memcpy(mr, vr, sizeof(double) * V * V);
+  memcpy(mi, vi, sizeof(double) * V * V);
+  for (int i = 0; i < V; i++) {
+    br[i] = Dq[i];
+    bi[i] = 0.0;
+  }
+  csolve(V, mr, mi, br, bi);
+  for (int i = 0; i < V; i++) {
+    double l = sqrt(wr[i] * wr[i] + wi[i] * wi[i]);
+    br[i] *= l;
+    bi[i] *= l;
+  }
+  for (int i = 0; i < V; i++) {
+    double s = 0;
+    for (int j = 0; j < V; j++)
+      s += vr[i * V + j] * br[j] - vi[i * V + j] * bi[j];
+    out[i] = accumulate ? out[i] + weight * s : weight * s;
+  }
+}
+
+static void d_osh(const ctx_t *c, double *ret, double *qL, double *qR,
+                  double *dqL, double *dqR, int d) { /* fluxes.cpp:20-45 */
+  int V = c->V, N = c->N;
+  double Dq[ORA_MAXV], q[ORA_MAXV], dq[3 * ORA_MAXV],
+      M[ORA_MAXV * ORA_MAXV];
+  for (int v = 0; v < V; v++) {
+    Dq[v] = qL[v] - qR[v];
+    ret[v] = 0.0;
+  }
+  for (int i = 0; i < N; i++) {
+    for (int v = 0; v < V; v++)
+      q[v] = qR[v] + c->T.nodes[i] * Dq[v];
+    for (int k = 0; k < c->ndim * V; k++)
+      dq[k] = dqR[k] + c->T.nodes[i] * (dqL[k] - dqR[k]);
+    system_matrix(c, M, q, dq, d);
+    abs_apply(V, M, Dq, ret, c->T.wghts[i], 1);
+  }
+}
+
+static void d_roe(const ctx_t *c, double *ret, double *qL, double *qR,
+                  double *dqL, double *dqR, int d) { /* fluxes.cpp:47-70 */
+  int V = c->V, N = c->N;
+  double Dq[ORA_MAXV], q[ORA_MAXV], dq[3 * ORA_MAXV],
+      M[ORA_MAXV * ORA_MAXV], Mi[ORA_MAXV * ORA_MAXV];
+  for (int v = 0; v < V; v++)
+    Dq[v] = qL[v] - qR[v];
+  for (int i = 0; i < V * V; i++)
+    M[i] = 0.0;
+  for (int i = 0; i < N; i++) {
+    for (int v = 0; v < V; v++)
+      q[v] = qR[v] + c->T.nodes[i] * Dq[v];
+    for (int k = 0; k < c->ndim * V; k++)
+      dq[k] = dqR[k] + c->T.nodes[i] * (dqL[k] - dqR[k]);
+    system_matrix(c, Mi, q, dq, d);
+    for (int k = 0; k < V * V; k++)
+      M[k] += c->T.wghts[i] * Mi[k];
+  }
+  abs_apply(V, M, Dq, ret, 1.0, 0);
+}
+
+static void num_flux(const ctx_t *c, int flux, double *ret, double *qL,
+                     double *qR, double *dqL, double *dqR, int d) {
+  int V = c->V;
+  if (flux == 0)
+    d_rus(c, ret, qL, qR, dqL, dqR, d);
+  else if (flux == 1)
+    d_roe(c, ret, qL, qR, dqL, dqR, d);
+  else
+    d_osh(c, ret, qL, qR, dqL, dqR, d);
+  double fL[ORA_MAXV], fR[ORA_MAXV];
+  c->F(fL, qL, dqL, d);
+  c->F(fR, qR, dqR, d);
+  for (int v = 0; v < V; v++)
+    ret[v] += fL[v] + fR[v];
+  if (c->secondOrder) { /* fluxes.cpp:96-100 */
+    double m1 = max_abs_eigs_2nd(c, qL, dqL, d);
+    double m2 = max_abs_eigs_2nd(c, qR, dqR, d);
+    double m = fmax(m1, m2);
+    for (int v = 0; v < V; v++)
+      ret[v] += m * (qL[v] - qR[v]);
+  }
+}
+
+static void bint(const ctx_t *c, double *ret, const double *qL,
+                 const double *qR, int d) { /* fluxes.cpp:103-117 */
+  int V = c->V, N = c->N;
+  double Dq[ORA_MAXV], q[ORA_MAXV], b[ORA_MAXV * ORA_MAXV],
+      M[ORA_MAXV * ORA_MAXV];
+  for (int v = 0; v < V; v++)
+    Dq[v] = qR[v] - qL[v];
+  for (int i = 0; i < V * V; i++)
+    M[i] = 0.0;
+  for (int i = 0; i < N; i++) {
+    for (int v = 0; v < V; v++)
+      q[v] = qL[v] + c->T.nodes[i] * Dq[v];
+    c->B(b, q, d);
+    for (int k = 0; k < V * V; k++)
+      M[k] += c->T.wghts[i] * b[k];
+  }
+  for (int r = 0; r < V; r++) {
+    double s = 0;
+    for (int j = 0; j < V; j++)
+      s += M[r * V + j] * Dq[j];
+    ret[r] = s;
+  }
+}
+
+/* FV update restricted to u-cells with axis-0 index in [a0, b0): the slab
+ * decomposition of iterator.cpp:68-84.  u is the full array; qh the full
+ * w-grid predictor. */
+static void fv_range(const ctx_t *c, double *u, const double *qh,
+                     const int *nX, double dt, int flux, int a0, int b0) {
+  int N = c->N, V = c->V, Nd = c->Nd, ndim = c->ndim;
+  int Nd_ = ipow(N, ndim - 1);
+  int nX2[3], nX1[3];
+  for (int d = 0; d < ndim; d++) {
+    nX2[d] = nX[d] + 2;
+    nX1[d] = nX[d] + 1;
+  }
+  long qrow = (long)N * Nd * V; /* doubles per w-cell in qh */
+  double *dqh_cell = NULL;      /* second order: per-cell gradients */
+  if (c->B || c->S) { /* centers, fv.cpp:33-85 */
+    double dq[3][ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+    int inds[3] = {0, 0, 0};
+    long ncell = 1;
+    for (int d = 0; d < ndim; d++)
+      ncell *= nX[d];
+    for (long uc = 0; uc < ncell; uc++) {
+      for (int d = ndim - 1; d >= 0; d--) {
+        /* inds kept in sync below */
+      }
+      if (inds[0] >= a0 && inds[0] < b0) {
+        long rc = 0;
+        for (int d = 0; d < ndim; d++)
+          rc = rc * nX2[d] + inds[d] + 1;
+        for (int t = 0; t < N; t++) {
+          const double *qt = qh + rc * qrow + (long)t * Nd * V;
+          for (int d = 0; d < ndim; d++)
+            derivs(&c->T, qt, V, dq[d], V, d, ndim, V, c->dX[d]);
+          for (int idx = 0; idx < Nd; idx++) {
+            double s[ORA_MAXV];
+            if (c->S)
+              c->S(s, (double *)qt + idx * V);
+            else
+              for (int v = 0; v < V; v++)
+                s[v] = 0.0;
+            if (c->B)
+              for (int d = 0; d < ndim; d++) {
+                double b[ORA_MAXV * ORA_MAXV];
+                c->B(b, (double *)qt + idx * V, d);
+                for (int i = 0; i < V; i++) {
+                  double acc = 0;
+                  for (int j = 0; j < V; j++)
+                    acc += b[i * V + j] * dq[d][idx * V + j];
+                  s[i] -= acc;
+                }
+              }
+            double tmp = dt * c->T.wghts[t];
+            int rem = idx, digs[3] = {0, 0, 0};
+            for (int d = ndim - 1; d >= 0; d--) {
+              digs[d] = rem % N;
+              rem /= N;
+            }
+            for (int d = 0; d < ndim; d++)
+              tmp *= c->T.wghts[digs[d]];
+            for (int v = 0; v < V; v++)
+              u[uc * V + v] += tmp * s[v];
+          }
+        }
+      }
+      for (int d = ndim - 1; d >= 0; d--) {
+        if (++inds[d] < nX[d])
+          break;
+        inds[d] = 0;
+      }
+    }
+  }
+  if (!(c->F || c->B))
+    return;
+  /* interfaces, fv.cpp:124-198 */
+  double q0[ORA_MAXN * ORA_MAXN * ORA_MAXV], q1[ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  double dq0[ORA_MAXN * ORA_MAXN * 3 * ORA_MAXV],
+      dq1[ORA_MAXN * ORA_MAXN * 3 * ORA_MAXV];
+  double tmpd[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  memset(dq0, 0, sizeof(dq0));
+  memset(dq1, 0, sizeof(dq1));
+  if (c->secondOrder)
+    dqh_cell = malloc(sizeof(double) * 3 * ORA_MAXN * ORA_MAXN * ORA_MAXN *
+                      ORA_MAXV * 2);
+  int inds[3] = {0, 0, 0};
+  long nfc = 1;
+  for (int d = 0; d < ndim; d++)
+    nfc *= nX1[d];
+  double f[ORA_MAXV], b[ORA_MAXV];
+  for (long fc = 0; fc < nfc; fc++) {
+    /* faces of w-cell `inds` with its +e_d neighbour; u index = inds - 1.
+     * Only faces touching the slab [a0, b0) matter. */
+    int touch = (inds[0] - 1 >= a0 - 1) && (inds[0] - 1 < b0);
+    if (touch) {
+      long qc0 = 0;
+      int valid0 = 1;
+      long u0 = 0;
+      for (int d = 0; d < ndim; d++) {
+        qc0 = qc0 * nX2[d] + inds[d];
+        u0 = u0 * nX[d] + (inds[d] - 1);
+        if (inds[d] - 1 < 0 || inds[d] - 1 >= nX[d])
+          valid0 = 0;
+      }
+      if (valid0 && (inds[0] - 1 < a0 || inds[0] - 1 >= b0))
+        valid0 = 0;
+      for (int t = 0; t < N; t++) {
+        const double *qh0 = qh + qc0 * qrow + (long)t * Nd * V;
+        for (int d = 0; d < ndim; d++) {
+          double cc = dt * c->T.wghts[t] / (2. * c->dX[d]);
+          long qc1 = 0, u1 = 0;
+          int valid1 = 1;
+          for (int e = 0; e < ndim; e++) {
+            int ie = inds[e] + (e == d);
+            qc1 = qc1 * nX2[e] + ie;
+            u1 = u1 * nX[e] + (ie - 1);
+            if (ie - 1 < 0 || ie - 1 >= nX[e])
+              valid1 = 0;
+          }
+          int i1_0 = inds[0] + (d == 0) - 1;
+          if (valid1 && (i1_0 < a0 || i1_0 >= b0))
+            valid1 = 0;
+          if (!valid0 && !valid1)
+            continue;
+          const double *qh1 = qh + qc1 * qrow + (long)t * Nd * V;
+          endpts(&c->T, qh0, V, q0, V, d, 1, ndim, V);
+          endpts(&c->T, qh1, V, q1, V, d, 0, ndim, V);
+          if (c->secondOrder)
+            for (int d_ = 0; d_ < ndim; d_++) {
+              derivs(&c->T, qh0, V, tmpd, V, d_, ndim, V, c->dX[d_]);
+              endpts(&c->T, tmpd, V, dq0 + d_ * V, ndim * V, d, 1, ndim, V);
+              derivs(&c->T, qh1, V, tmpd, V, d_, ndim, V, c->dX[d_]);
+              endpts(&c->T, tmpd, V, dq1 + d_ * V, ndim * V, d, 0, ndim, V);
+            }
+          for (int idx = 0; idx < Nd_; idx++) {
+            for (int v = 0; v < V; v++)
+              f[v] = b[v] = 0.0;
+            if (c->F)
+              num_flux(c, flux, f, q0 + idx * V, q1 + idx * V,
+                       dq0 + idx * ndim * V, dq1 + idx * ndim * V, d);
+            if (c->B)
+              bint(c, b, q0 + idx * V, q1 + idx * V, d);
+            double tmp = cc;
+            int rem = idx, digs[3] = {0, 0, 0};
+            for (int e = ndim - 2; e >= 0; e--) {
+              digs[e] = rem % N;
+              rem /= N;
+            }
+            for (int e = 0; e < ndim - 1; e++)
+              tmp *= c->T.wghts[digs[e]];
+            if (valid0)
+              for (int v = 0; v < V; v++)
+                u[u0 * V + v] -= tmp * (b[v] + f[v]);
+            if (valid1)
+              for (int v = 0; v < V; v++)
+                u[u1 * V + v] -= tmp * (b[v] - f[v]);
+          }
+        }
+      }
+    }
+    for (int d = ndim - 1; d >= 0; d--) {
+      if (++inds[d] < nX1[d])
+        break;
+      inds[d] = 0;
+    }
+  }
+  free(dqh_cell);
+}
+
+void ora_fv(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
+            const double *qh, const int *nX, const double *dX, int ndim,
+            int N, int V, int flux, int secondOrder, double dt) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  fv_range(c, u, qh, nX, dt, flux, 0, nX[0]);
+  free(c);
+}
+
+/* ------------------------------------------------------------------ */
+/* a14: the step loop, solvers/iterator.cpp:38-151, with the reference's */
+/* x-slab thread decomposition (iterator.cpp:68-84).                    */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  const ctx_t *c;
+  int phase; /* 0: dt max, 1: predictor + FV */
+  const double *w;
+  double *qh, *u;
+  const int *nX;
+  int stiff, flux;
+  double dt, tol;
+  long wcells_per_slab_row; /* w-cells per axis-0 index */
+  int a0, b0;               /* u slab along axis 0 */
+  double out_max;
+  long iters;
+  int maxit;
+} job_t;
+
+static void *job_run(void *arg) {
+  job_t *j = arg;
+  /* w-cells of this slab: axis-0 indices a0 .. b0+1 of the w grid */
+  long c0 = (long)j->a0 * j->wcells_per_slab_row;
+  long c1 = (long)(j->b0 + 2) * j->wcells_per_slab_row;
+  if (j->phase == 0) {
+    j->out_max = cfl_max(j->c, j->w, c0, c1);
+  } else {
+    j->iters = predictor_range(j->c, j->w, c0, c1, j->stiff, j->dt, j->tol,
+                               j->qh, &j->maxit);
+    fv_range(j->c, j->u, j->qh, j->nX, j->dt, j->flux, j->a0, j->b0);
+  }
+  return NULL;
+}
+
+static int any_nan(const double *u, long n) {
+  for (long i = 0; i < n; i++)
+    if (isnan(u[i]))
+      return 1;
+  return 0;
+}
+
+long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
+                    double tf, const int *nX, int ndim, const double *dX,
+                    double CFL, const int *bt, int stiff, int flux, int N,
+                    int V, int ndt, int secondOrder, double *ret, int nThreads,
+                    long maxsteps, double newton_tol, double *t_out) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  if (nThreads < 1)
+    nThreads = (int)sysconf(_SC_NPROCESSORS_ONLN);
+  if (nThreads > nX[0])
+    nThreads = nX[0];
+  int nXb[3], nXw[3];
+  long ncell = 1, ncb = 1, ncw = 1;
+  for (int d = 0; d < ndim; d++) {
+    nXb[d] = nX[d] + 2 * N;
+    nXw[d] = nX[d] + 2;
+    ncell *= nX[d];
+    ncb *= nXb[d];
+    ncw *= nXw[d];
+  }
+  long usz = ncell * V;
+  double *ub = malloc(sizeof(double) * ncb * V);
+  double *w = malloc(sizeof(double) * ncw * c->Nd * V);
+  double *qh = malloc(sizeof(double) * ncw * N * c->Nd * V);
+  double *uprev = malloc(sizeof(double) * usz);
+  memcpy(uprev, u, sizeof(double) * usz);
+  long wrow = ncw / nXw[0];
+  job_t *jobs = calloc(nThreads, sizeof(job_t));
+  pthread_t *th = calloc(nThreads, sizeof(pthread_t));
+  for (int i = 0; i < nThreads; i++) {
+    jobs[i].c = c;
+    jobs[i].a0 = (int)((long)i * nX[0] / nThreads);
+    jobs[i].b0 = (int)((long)(i + 1) * nX[0] / nThreads);
+    jobs[i].wcells_per_slab_row = wrow;
+    jobs[i].nX = nX;
+    jobs[i].stiff = stiff;
+    jobs[i].flux = flux;
+    jobs[i].tol = newton_tol;
+  }
+  double t = 0.0;
+  long count = 0;
+  int push = 0;
+  while (t < tf && (maxsteps < 0 || count < maxsteps)) {
+    ora_boundaries(u, nX, ndim, bt, N, V, ub);
+    ora_weno(ub, nXb, ndim, N, V, w);
+    double MAX = 0.0;
+    for (int i = 0; i < nThreads; i++) {
+      jobs[i].phase = 0;
+      jobs[i].w = w;
+      if (nThreads > 1)
+        pthread_create(&th[i], NULL, job_run, &jobs[i]);
+      else
+        job_run(&jobs[i]);
+    }
+    for (int i = 0; i < nThreads; i++) {
+      if (nThreads > 1)
+        pthread_join(th[i], NULL);
+      MAX = fmax(MAX, jobs[i].out_max);
+    }
+    double dt = dt_from_max(MAX, CFL, tf, t, count);
+    for (int i = 0; i < nThreads; i++) {
+      jobs[i].phase = 1;
+      jobs[i].dt = dt;
+      jobs[i].qh = qh;
+      jobs[i].u = u;
+      if (nThreads > 1)
+        pthread_create(&th[i], NULL, job_run, &jobs[i]);
+      else
+        job_run(&jobs[i]);
+    }
+    if (nThreads > 1)
+      for (int i = 0; i < nThreads; i++)
+        pthread_join(th[i], NULL);
+    t += dt;
+    count += 1;
+    if (ret && push < ndt && t >= (double)(push + 1) / (double)ndt * tf) {
+      memcpy(ret + (long)push * usz, u, sizeof(double) * usz);
+      push += 1;
+    }
+    if (any_nan(u, usz)) { /* iterator.cpp:141-145, bounded */
+      if (ret && push < ndt)
+        memcpy(ret + (long)push * usz, uprev, sizeof(double) * usz);
+      if (ret && push + 1 < ndt)
+        memcpy(ret + (long)(push + 1) * usz, u, sizeof(double) * usz);
+    }
+    memcpy(uprev, u, sizeof(double) * usz);
+  }
+  if (ret && ndt > 0)
+    memcpy(ret + (long)(ndt - 1) * usz, u, sizeof(double) * usz);
+  if (t_out)
+    *t_out = t;
+  free(ub);
+  free(w);
+  free(qh);
+  free(uprev);
+  free(jobs);
+  free(th);
+  free(c);
+  return count;
+}

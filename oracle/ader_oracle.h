@@ -1,0 +1,93 @@
+/*
+ * ader_oracle.h -- CPU restatement of PyPDE's ADER-WENO time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker, never the product: only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
+ * it.  The GPU library must not link, include or call anything here.
+ *
+ * Every function restates the algorithm of haranjackson/PyPDE src/ (paths
+ * below are relative to that project) in plain C11 with row-major float64
+ * arrays (the reference's Mat is row-major, src/types.h:21-22).  Parity of
+ * this port with the reference itself is pinned by tests/golden/, whose
+ * vectors are produced by the reference C++ compiled from its own sources
+ * (oracle/Makefile target `ref`, driver oracle/ref_driver.cpp).
+ */
+#ifndef ADER_ORACLE_H
+#define ADER_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Callback signatures of the reference (pypde/cfuncs.py:6-8, src/api.h:4-10) */
+typedef void (*ora_flux_fn)(double *out, double *Q, double *dQ, int d);
+typedef void (*ora_ncp_fn)(double *out, double *Q, int d);
+typedef void (*ora_src_fn)(double *out, double *Q);
+
+#define ORA_MAXN 8
+#define ORA_MAXV 24
+
+/* Built-in test systems (oracle_systems.c).  Returns 0 on success. */
+int ora_system_lookup(const char *name, int ndim, int *V, ora_flux_fn *F,
+                      ora_ncp_fn *B, ora_src_fn *S, int *secondOrder);
+
+/* Constant tables of one (ndim, N) solver (src/poly/basis.cpp,
+ * src/solvers/weno/weno_matrices.cpp, src/solvers/dg/dg_matrices.cpp). */
+typedef struct {
+  int N;
+  double nodes[ORA_MAXN];             /* GL nodes on [0,1] */
+  double wghts[ORA_MAXN];             /* GL weights on [0,1] */
+  double dervals[ORA_MAXN * ORA_MAXN];/* DERVALS[i*N+j] = psi_j'(x_i) */
+  double endvals[2 * ORA_MAXN];       /* ENDVALS[e*N+j] = psi_j(e) */
+  double dgmat[ORA_MAXN * ORA_MAXN];  /* DG_MAT = psi psi^T(1) - <psi,psi'>^T */
+  double dgmat_inv[ORA_MAXN * ORA_MAXN];
+  double weno_inv[4][ORA_MAXN * ORA_MAXN]; /* inverses of mL, mR, mCL, mCR */
+  double sig[ORA_MAXN * ORA_MAXN];    /* oscillation indicator matrix */
+} ora_tables;
+
+void ora_make_tables(int N, ora_tables *T);
+
+/* Step stages.  Arrays are row-major (rows, V) float64. */
+void ora_boundaries(const double *u, const int *nX, int ndim, const int *bt,
+                    int N, int V, double *ub);
+/* WENO reconstruction of an already padded array of shape nXb (weno_solver).
+ * Output rows: prod(nXb - 2(N-1)) * N^ndim, each of V values. */
+void ora_weno(const double *ub, const int *nXb, int ndim, int N, int V,
+              double *w);
+/* CFL timestep over nrows/Nd w-cells (TimeStepper::step). */
+double ora_timestep(ora_flux_fn F, ora_ncp_fn B, const double *w, long nrows,
+                    const double *dX, int ndim, int N, int V, double CFL,
+                    double tf, double t, long count, int secondOrder);
+/* Predictor over nrows/Nd w-cells; qh gets N*nrows rows.  Returns the total
+ * number of Picard / Newton iterations; *maxit gets the per-cell maximum. */
+long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
+                   long nrows, const double *dX, int ndim, int N, int V,
+                   int stiff, double dt, double newton_tol, double *qh,
+                   int *maxit);
+/* FV corrector (FVSolver::apply) on u (prod(nX) rows) using qh over the
+ * w-grid nX+2. */
+void ora_fv(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
+            const double *qh, const int *nX, const double *dX, int ndim,
+            int N, int V, int flux, int secondOrder, double dt);
+
+/* Whole solver (pde_solver, src/api.cpp:5-30 and src/solvers/iterator.cpp).
+ * maxsteps < 0: run to tf.  Returns the number of steps taken; *t_out gets
+ * the final time.  nThreads < 1 means "all host cores".  newton_tol is the
+ * stiff residual tolerance (the reference uses 6e-6, dg.h:9). */
+long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
+                    double tf, const int *nX, int ndim, const double *dX,
+                    double CFL, const int *bt, int stiff, int flux, int N,
+                    int V, int ndt, int secondOrder, double *ret, int nThreads,
+                    long maxsteps, double newton_tol, double *t_out);
+
+/* max |eigenvalue| of a general real n x n row-major matrix (destroys a). */
+double ora_max_abs_eig(double *a, int n);
+/* Real eigen-decomposition: wr/wi eigenvalues, vr/vi eigenvectors (columns,
+ * row-major n x n).  Returns 0 on success. */
+int ora_eig(const double *a, int n, double *wr, double *wi, double *vr,
+            double *vi);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,156 @@
+/*
+ * oracle_systems.c -- C callbacks F/B/S of the test systems, with the
+ * reference's callback signatures (src/api.h:4-10, pypde/cfuncs.py:6-8).
+ *
+ * TEST INFRASTRUCTURE ONLY (see ader_oracle.h).  They play the part of the
+ * user's numba-compiled cfuncs: the reference C++ build (through
+ * ref_driver.cpp) and the C port both call these same functions, so the
+ * two checkers see bit-identical flux values.  The GPU library carries its
+ * own device implementations of the same formulas, written in the same
+ * operation order (pypde_gb300/csrc/systems.cuh).
+ *
+ * Systems:
+ *   euler     V = ndim+2   Q = (rho, m_0..m_{ndim-1}, E), gamma = 1.4.  F only.
+ *   cattaneo  V = 2ndim+3  Euler + relaxing heat flux q_0..q_{ndim-1} + a
+ *             passive s = log10(tau).  T = p/rho, kappa = 1e-2,
+ *             1/tau = 10^-s by pow10_portable.
+ *             F_d adds q_d to the energy flux and kappa*T/tau to q_d;
+ *             S_q = -q/tau.  F and S.
+ *   ncp       V = 3, a non-conservative test system with F, B and S:
+ *             F_d = a_d (Q0^2/2, Q0 Q1, Q0 Q2),
+ *             B_d = a_d [[0,0,0],[0,Q0,0.2],[0,0.2,Q0]],
+ *             S   = (0, 0.1(Q2-Q1), -0.1(Q1+Q2)),  a = (1, 0.5, 0.25).
+ *   burgers2  V = 1, viscous Burgers in the second-order form F(Q, DQ, d):
+ *             F_d = a_d Q0^2/2 - 0.01 DQ[d].
+ */
+#include "ader_oracle.h"
+
+#include <math.h>
+#include <string.h>
+
+#define GAMMA 1.4
+#define KAPPA 1e-2
+
+static int g_ndim = 1;
+
+/* 10^x as 2^(x log2 10): y = n + r with n = round(y), 2^r = e^(r ln 2) by
+ * its Taylor series (Horner, 18 terms), scaled by 2^n.  Built only from
+ * IEEE +, *, /, floor and ldexp, so the host and the device evaluate it to
+ * the same bits (a libm exp/pow may differ between the two in the last
+ * place). */
+static double pow10_portable(double x) {
+  double y = x * 3.321928094887362;
+  double n = floor(y + 0.5);
+  double r = (y - n) * 0.6931471805599453;
+  double p = 1.0;
+  for (int k = 18; k >= 1; k--)
+    p = 1.0 + p * r / k;
+  return ldexp(p, (int)n);
+}
+
+static void euler_core(double *out, const double *Q, int ndim, int d,
+                       double *p_out) {
+  double r = Q[0];
+  double ke = 0.0;
+  for (int i = 0; i < ndim; i++)
+    ke += Q[1 + i] * Q[1 + i];
+  double p = (GAMMA - 1.0) * (Q[ndim + 1] - 0.5 * ke / r);
+  double ud = Q[1 + d] / r;
+  out[0] = Q[1 + d];
+  for (int i = 0; i < ndim; i++)
+    out[1 + i] = Q[1 + i] * ud;
+  out[1 + d] += p;
+  out[ndim + 1] = (Q[ndim + 1] + p) * ud;
+  *p_out = p;
+}
+
+static void euler_F(double *out, double *Q, double *dQ, int d) {
+  (void)dQ;
+  double p;
+  euler_core(out, Q, g_ndim, d, &p);
+}
+
+static void cattaneo_F(double *out, double *Q, double *dQ, int d) {
+  (void)dQ;
+  int nd = g_ndim;
+  double p;
+  euler_core(out, Q, nd, d, &p);
+  double inv_tau = pow10_portable(-Q[2 * nd + 2]);
+  double T = p / Q[0];
+  out[nd + 1] += Q[nd + 2 + d];
+  for (int i = 0; i < nd; i++)
+    out[nd + 2 + i] = 0.0;
+  out[nd + 2 + d] = KAPPA * T * inv_tau;
+  out[2 * nd + 2] = 0.0;
+}
+
+static void cattaneo_S(double *out, double *Q) {
+  int nd = g_ndim;
+  double inv_tau = pow10_portable(-Q[2 * nd + 2]);
+  for (int i = 0; i < nd + 2; i++)
+    out[i] = 0.0;
+  for (int i = 0; i < nd; i++)
+    out[nd + 2 + i] = -Q[nd + 2 + i] * inv_tau;
+  out[2 * nd + 2] = 0.0;
+}
+
+static const double NCP_A[3] = {1.0, 0.5, 0.25};
+
+static void ncp_F(double *out, double *Q, double *dQ, int d) {
+  (void)dQ;
+  double a = NCP_A[d];
+  out[0] = a * (0.5 * Q[0] * Q[0]);
+  out[1] = a * (Q[0] * Q[1]);
+  out[2] = a * (Q[0] * Q[2]);
+}
+
+static void ncp_B(double *out, double *Q, int d) {
+  double a = NCP_A[d];
+  for (int i = 0; i < 9; i++)
+    out[i] = 0.0;
+  out[4] = a * Q[0];
+  out[5] = a * 0.2;
+  out[7] = a * 0.2;
+  out[8] = a * Q[0];
+}
+
+static void ncp_S(double *out, double *Q) {
+  out[0] = 0.0;
+  out[1] = 0.1 * (Q[2] - Q[1]);
+  out[2] = -0.1 * (Q[1] + Q[2]);
+}
+
+static void burgers2_F(double *out, double *Q, double *dQ, int d) {
+  out[0] = NCP_A[d] * (0.5 * Q[0] * Q[0]) - 0.01 * dQ[d];
+}
+
+int ora_system_lookup(const char *name, int ndim, int *V, ora_flux_fn *F,
+                      ora_ncp_fn *B, ora_src_fn *S, int *secondOrder) {
+  if (ndim < 1 || ndim > 3)
+    return -1;
+  g_ndim = ndim;
+  *F = 0;
+  *B = 0;
+  *S = 0;
+  *secondOrder = 0;
+  if (!strcmp(name, "euler")) {
+    *V = ndim + 2;
+    *F = euler_F;
+  } else if (!strcmp(name, "cattaneo")) {
+    *V = 2 * ndim + 3;
+    *F = cattaneo_F;
+    *S = cattaneo_S;
+  } else if (!strcmp(name, "ncp")) {
+    *V = 3;
+    *F = ncp_F;
+    *B = ncp_B;
+    *S = ncp_S;
+  } else if (!strcmp(name, "burgers2")) {
+    *V = 1;
+    *F = burgers2_F;
+    *secondOrder = 1;
+  } else {
+    return -2;
+  }
+  return 0;
+}
