@@ -1,0 +1,167 @@
+/*
+ * pypde_gb300.h -- C ABI of the GB300 ADER-WENO library
+ * (pypde_gb300/libpypde_gb300.so).
+ *
+ * Drop-in for the C ABI of haranjackson/PyPDE (src/api.h), the boundary its
+ * Python front end binds over ctypes (pypde/utils.py:9-16, 83-91).  All
+ * buffers are the caller's host memory; the library copies them to the GPU,
+ * runs every stage of the time step there and copies results back.  There
+ * is no CPU fallback: without a usable GPU every entry point returns
+ * PYPDE_ERR_CUDA.
+ *
+ * Callbacks.  The reference takes three host function pointers F, B, S
+ * (numba cfuncs).  Device code cannot call host functions, so here F, B and
+ * S are handles to one compiled device callback system (pypde_system): a
+ * built-in system, or user source compiled at run time.  The ctypes
+ * argument list is unchanged (three c_void_p), and each non-NULL handle
+ * must name the same system.
+ *
+ * Return values: the reference's functions return void; these return a
+ * status (PYPDE_OK = 0).  A ctypes binding with restype None ignores it.
+ * pypde_last_error() gives a message for the last failure of this thread.
+ */
+#ifndef PYPDE_GB300_H
+#define PYPDE_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYPDE_OK 0
+#define PYPDE_ERR_ARG 1         /* invalid argument or shape */
+#define PYPDE_ERR_CUDA 2        /* CUDA error, or no GPU */
+#define PYPDE_ERR_UNSUPPORTED 3 /* combination not built */
+#define PYPDE_NAN_FOUND 4       /* NaN in the state; see pde_solver */
+#define PYPDE_ERR_COMPILE 5     /* run-time compilation of callbacks failed */
+
+typedef struct pypde_system pypde_system;
+
+/* Options and statistics of pde_solver_ex (extensions; no reference
+ * counterpart).  Zero-initialise and set what you need. */
+typedef struct {
+  long long max_steps;   /* stop after this many steps; <= 0: run to tf */
+  double newton_tol;     /* stiff form: ||obj||_inf tolerance; 0 -> 1e-12 */
+  int device;            /* CUDA device ordinal */
+  int steps_per_graph;   /* steps per CUDA graph launch; 0 -> automatic */
+  int profile_stages;    /* 1: launch eagerly and time every stage with CUDA
+                            events (fills pypde_stats.stage_seconds) */
+} pypde_options;
+
+/* Stages timed by pypde_options.profile_stages, in this order. */
+#define PYPDE_STAGE_BOUNDARIES 0
+#define PYPDE_STAGE_WENO 1
+#define PYPDE_STAGE_CFL 2
+#define PYPDE_STAGE_PREDICTOR 3
+#define PYPDE_STAGE_FACES 4
+#define PYPDE_STAGE_CENTERS 5
+#define PYPDE_STAGE_GATHER 6
+#define PYPDE_STAGE_OTHER 7
+#define PYPDE_NSTAGES 8
+
+typedef struct {
+  long long steps;                 /* time steps taken */
+  double t_final;                  /* time reached */
+  unsigned long long pred_iters;   /* predictor iterations, summed over cells */
+  int pred_max_iters;              /* largest per-cell iteration count */
+  int pred_fail;                   /* cells whose Newton hit its cap */
+  int nan_found;                   /* a NaN appeared in the state */
+  double device_seconds;           /* time of the stepping loop on the GPU */
+  long long kernel_launches;       /* kernels of this library launched */
+  double stage_seconds[8];         /* per stage, with profile_stages */
+} pypde_stats;
+
+/* ---------------- callback systems ---------------- */
+
+/* Built-in systems ("euler", "cattaneo", "ncp", "burgers2") for ndim 1-3.
+ * No reference counterpart: stands in for pypde/cfuncs.py:30-75. */
+int pypde_system_builtin(const char *name, int ndim, pypde_system **out);
+
+/* Compile user callbacks given as CUDA C++ device code (see
+ * pypde_gb300/callbacks.py, which translates Python F/B/S into this form).
+ * src must define `struct UserSystem` with V, NDIM, HAS_F, HAS_B, HAS_S,
+ * SECOND_ORDER and static __device__ F, B, S with the signatures of
+ * pypde/cfuncs.py:6-8.  Stands in for pypde/cfuncs.py:30-75. */
+int pypde_system_compile(const char *src, const char *name, int ndim, int V,
+                         int has_F, int has_B, int has_S, int second_order,
+                         pypde_system **out);
+
+int pypde_system_info(const pypde_system *s, int *V, int *ndim, int *has_F,
+                      int *has_B, int *has_S, int *second_order);
+void pypde_system_free(pypde_system *s);
+
+/* ---------------- the reference's entry points ---------------- */
+
+/* Replaces pde_solver of src/api.h:4-10 / src/api.cpp:5-30.
+ * u (in/out, prod(nX) x V) is advanced to tf, like the reference, which
+ * writes the final state into the caller's array (api.cpp:18,
+ * iterator.cpp:129).  ret (ndt x prod(nX) x V, caller-allocated) receives
+ * the snapshots of iterator.cpp:136-150: row k when t first reaches
+ * (k+1) tf / ndt, and row ndt-1 the final state.  STIFF selects the
+ * locally implicit Newton predictor (else Picard, dg.cpp:187-202); FLUX
+ * 0 Rusanov, 1 Roe, 2 Osher.  nThreads is accepted and ignored (one GPU).
+ * On NaN the run stops; rows push and push+1 receive the last finite and
+ * the first non-finite state (the reference writes them at
+ * iterator.cpp:141-145 and keeps stepping) and PYPDE_NAN_FOUND is
+ * returned. */
+int pde_solver(const pypde_system *F, const pypde_system *B,
+               const pypde_system *S, bool useF, bool useB, bool useS,
+               double *u, double tf, int *nX, int ndim, double *dX, double CFL,
+               int *boundaryTypes, bool STIFF, int FLUX, int N, int V, int ndt,
+               bool secondOrder, double *ret, int nThreads);
+
+/* pde_solver with options and statistics (extension). */
+int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
+                  double *u, double tf, const int *nX, int ndim,
+                  const double *dX, double CFL, const int *boundaryTypes,
+                  bool STIFF, int FLUX, int N, int ndt, double *ret,
+                  const pypde_options *opt, pypde_stats *stats);
+
+/* Replaces weno_solver of src/api.h:12-13 / src/api.cpp:32-48: WENO
+ * reconstruction of an already padded u (nX cells per axis) into ret,
+ * shape (nX - 2(N-1)) x N^ndim x V. */
+int weno_solver(double *ret, double *u, int *nX, int ndim, int N, int V);
+
+/* ---------------- single stages (for checking each kernel) ------------ */
+
+/* Ghost fill (src/grid/boundaries.cpp:25-53): u (prod nX x V) ->
+ * ub (prod(nX+2N) x V). */
+int pypde_boundaries(const double *u, const int *nX, int ndim,
+                     const int *boundaryTypes, int N, int V, double *ub);
+
+/* CFL timestep over the w-cells of w (TimeStepper::step,
+ * src/solvers/stepper.cpp:35-76).  nrows = cells * N^ndim. */
+int pypde_timestep(const pypde_system *sys, const double *w, long long nrows,
+                   const double *dX, int ndim, int N, double CFL, double tf,
+                   double t, long long count, double *dt_out);
+
+/* Space-time predictor (DGSolver::predictor, src/solvers/dg/dg.cpp:204-224)
+ * of every cell of w; qh gets N*nrows rows. */
+int pypde_predictor(const pypde_system *sys, const double *w, long long nrows,
+                    const double *dX, int ndim, int N, bool STIFF, double dt,
+                    double newton_tol, double *qh, pypde_stats *stats);
+
+/* Finite-volume corrector (FVSolver::apply, src/solvers/fv/fv.cpp:200-207):
+ * u (prod nX x V) updated in place from qh over the (nX+2) grid. */
+int pypde_fv(const pypde_system *sys, double *u, const double *qh,
+             const int *nX, const double *dX, int ndim, int N, int FLUX,
+             double dt);
+
+/* Constant tables of order N, in the order nodes[N], wghts[N],
+ * dervals[N*N], endvals[2N], dgmat[N*N], dgmat_inv[N*N], weno_inv[4][N*N],
+ * sig[N*N] (4N + 8N^2 doubles).  Host-only; needs no GPU. */
+int pypde_tables(int N, double *out);
+
+/* FP64 FMA throughput of the device in TFLOP/s, measured by a dependent-
+ * chain FMA loop: the roofline denominator of the FP64-bound kernels.
+ * Bench support; no reference counterpart. */
+int pypde_measure_fp64_peak(int device, double *tflops);
+
+const char *pypde_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

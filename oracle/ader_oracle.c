@@ -1783,3 +1783,33 @@ long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
   free(c);
   return count;
 }
+
+/* Test hooks: the FD Jacobian + B and its max|eig| at one state. */
+double ora_system_max_abs_eigs(ora_flux_fn F, ora_ncp_fn B, int ndim, int V,
+                               double *q, double *dq, int d, double *M) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  double dX[3] = {1, 1, 1};
+  ctx_init(c, F, B, NULL, ndim, 2, V, dX, 0);
+  system_matrix(c, M, q, dq, d);
+  double Mc[ORA_MAXV * ORA_MAXV];
+  memcpy(Mc, M, sizeof(double) * V * V);
+  double r = ora_max_abs_eig(Mc, V);
+  free(c);
+  return r;
+}
+
+/* Test hook: numerical flux and B path integral at one face point. */
+void ora_face_flux(ora_flux_fn F, ora_ncp_fn B, int ndim, int N, int V,
+                   int secondOrder, double *qL, double *qR, double *dqL,
+                   double *dqR, int d, int flux, double *f, double *b) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  double dX[3] = {1, 1, 1};
+  ctx_init(c, F, B, NULL, ndim, N, V, dX, secondOrder);
+  for (int v = 0; v < V; v++)
+    f[v] = b[v] = 0.0;
+  if (F)
+    num_flux(c, flux, f, qL, qR, dqL, dqR, d);
+  if (B)
+    bint(c, b, qL, qR, d);
+  free(c);
+}

@@ -21,6 +21,8 @@
 #include "api.h"
 #include "grid/boundaries.h"
 #include "poly/basis.h"
+#include "eigs/system.h"
+#include "solvers/fv/fluxes.h"
 #include "solvers/fv/fv.h"
 #include "solvers/stepper.h"
 #include "solvers/weno/weno.h"
@@ -216,6 +218,58 @@ int ref_step_times(const char *sys, const double *u0, int *nX, int ndim,
     fv.apply(u, qh, dt);
     t += dt;
     times[k] = t;
+  }
+  return 0;
+}
+}
+
+extern "C" {
+// max |eig| of the FD Jacobian + B at one state (src/eigs/system.cpp:45-51)
+double ref_max_abs_eigs(const char *sys, int ndim, double *q, double *dq,
+                        int d) {
+  Sys s;
+  if (lookup(sys, ndim, &s))
+    return -1;
+  Eigen::Map<Vec> qv(q, s.V);
+  Eigen::Map<Mat> dqm(dq, ndim, s.V);
+  return max_abs_eigs(s.F, s.B, qv, dqm, d);
+}
+// the FD Jacobian + B itself (src/eigs/system.cpp:6-26)
+int ref_system_matrix(const char *sys, int ndim, double *q, double *dq, int d,
+                      double *M) {
+  Sys s;
+  if (lookup(sys, ndim, &s))
+    return -1;
+  Eigen::Map<Vec> qv(q, s.V);
+  Eigen::Map<Mat> dqm(dq, ndim, s.V);
+  Mat m = system_matrix(s.F, s.B, qv, dqm, d);
+  memcpy(M, m.data(), sizeof(double) * m.size());
+  return 0;
+}
+}
+
+extern "C" {
+// Numerical flux D(qL,qR)+F(qL)+F(qR) of src/solvers/fv/fluxes.cpp:80-101
+// (flux 0 Rusanov, 1 Roe, 2 Osher) and the B path integral of :103-117, at
+// one face point, through the reference's FluxGenerator.
+int ref_flux(const char *sys, int ndim, int N, double *qL, double *qR,
+             double *dqL, double *dqR, int d, int flux, double *f, double *b) {
+  Sys s;
+  if (lookup(sys, ndim, &s))
+    return -1;
+  Vec nodes = scaled_nodes(N), wghts = scaled_weights(N);
+  Vec dx = Vec::Ones(ndim);
+  FluxGenerator fg(s.F, s.B, nodes, wghts, dx, s.V, flux, ndim);
+  Eigen::Map<Vec> ql(qL, s.V), qr(qR, s.V);
+  Eigen::Map<Mat> dql(dqL, ndim, s.V), dqr(dqR, ndim, s.V);
+  Vec fv = Vec::Zero(s.V), bv = Vec::Zero(s.V);
+  if (s.F)
+    fg.flux(fv, ql, qr, dql, dqr, d, s.so);
+  if (s.B)
+    fg.Bint(bv, ql, qr, d);
+  for (int i = 0; i < s.V; i++) {
+    f[i] = fv(i);
+    b[i] = bv(i);
   }
   return 0;
 }

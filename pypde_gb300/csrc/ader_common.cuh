@@ -1,0 +1,329 @@
+// ader_common.cuh -- constants, per-(ndim,N) tables and the FP64 numerics
+// shared by the ADER-WENO kernels.
+//
+// Plain-form arithmetic is bit-faithful to the reference algorithm as
+// restated on the host: every sum below keeps the operation order of the
+// reference's Eigen expressions as the reference build evaluates them
+// (cited per function; paths relative to haranjackson/PyPDE), and the
+// translation units are compiled with --fmad=false so that no multiply-add
+// is contracted.  This matters more than usual here: the Rusanov and CFL
+// eigenvalues come from a forward-difference Jacobian with step
+// h = 2^-26 max(|q|, 1) (src/eigs/NumericalDiff.h:6-44), which turns any
+// last-bit change of its input state into a ~1e-8 relative change of the
+// Jacobian.
+#pragma once
+
+#ifndef __CUDACC_RTC__
+#include <cstdint>
+#endif
+
+namespace pypde {
+
+constexpr int MAXN = 8;
+constexpr double SQRT_EPS = 1.4901161193847656e-08; // sqrt(2^-52) = 2^-26
+constexpr double DBL_EPS = 2.220446049250313e-16;
+constexpr double WENO_LAMS = 1.0;  // weno.h:8
+constexpr double WENO_LAMC = 1e5;  // weno.h:9
+constexpr double WENO_EPS = 1e-14; // weno.h:10
+constexpr int DG_IT = 50;          // dg.h:8
+constexpr double DG_TOL = 6e-6;    // dg.h:9
+
+// Constant tables of one order N (src/poly/basis.cpp,
+// src/solvers/weno/weno_matrices.cpp, src/solvers/dg/dg_matrices.cpp).
+struct Tables {
+  int N;
+  double nodes[MAXN];
+  double wghts[MAXN];
+  double dervals[MAXN * MAXN]; // DERVALS[i*N+j] = psi_j'(x_i)
+  double endvals[2 * MAXN];    // ENDVALS[e*N+j] = psi_j(e)
+  double dgmat[MAXN * MAXN];
+  double dgmat_inv[MAXN * MAXN];
+  double weno_inv[4][MAXN * MAXN];
+  double sig[MAXN * MAXN];
+};
+
+template <int B, int E> struct IPow {
+  static constexpr int value = B * IPow<B, E - 1>::value;
+};
+template <int B> struct IPow<B, 0> {
+  static constexpr int value = 1;
+};
+
+// ---------------------------------------------------------------------
+// Eigenvalues of a general real V x V matrix: Householder reduction to
+// Hessenberg form, then the Francis implicit double-shift QR iteration
+// with Wilkinson's deflation test (Golub & Van Loan, Matrix Computations,
+// Alg. 7.4.2 and 7.5.1).  Replaces Eigen::EigenSolver / Spectra
+// (src/eigs/system.cpp:28-43).  Same operation order as the host
+// restatement.  Returns max |lambda|, NaN if the iteration fails.
+// ---------------------------------------------------------------------
+template <int V>
+__device__ __forceinline__ void hessenberg_inplace(double *a) {
+#define A_(i, j) a[(i) * V + (j)]
+  for (int k = 0; k < V - 2; k++) {
+    double v[V];
+    double alpha = 0, scale = 0;
+    for (int i = k + 1; i < V; i++)
+      scale += fabs(A_(i, k));
+    if (scale == 0.0)
+      continue;
+    for (int i = k + 1; i < V; i++) {
+      v[i] = A_(i, k) / scale;
+      alpha += v[i] * v[i];
+    }
+    double g = sqrt(alpha);
+    if (v[k + 1] > 0)
+      g = -g;
+    double h = alpha - v[k + 1] * g;
+    v[k + 1] -= g;
+    for (int j = k; j < V; j++) {
+      double s = 0;
+      for (int i = k + 1; i < V; i++)
+        s += v[i] * A_(i, j);
+      s /= h;
+      for (int i = k + 1; i < V; i++)
+        A_(i, j) -= s * v[i];
+    }
+    for (int i = 0; i < V; i++) {
+      double s = 0;
+      for (int j = k + 1; j < V; j++)
+        s += A_(i, j) * v[j];
+      s /= h;
+      for (int j = k + 1; j < V; j++)
+        A_(i, j) -= s * v[j];
+    }
+    A_(k + 1, k) = g * scale;
+    for (int i = k + 2; i < V; i++)
+      A_(i, k) = 0.0;
+  }
+}
+
+template <int V>
+__device__ __noinline__ double max_abs_eig(double *a) {
+  if (V == 1)
+    return fabs(a[0]);
+  hessenberg_inplace<V>(a);
+  double wr[V], wi[V];
+  double norm = 0;
+  for (int i = 0; i < V; i++)
+    for (int j = (i > 0 ? i - 1 : 0); j < V; j++)
+      norm += fabs(A_(i, j));
+  int hi = V - 1, its = 0, total = 0;
+  double exshift = 0.0;
+  while (hi >= 0) {
+    int l;
+    for (l = hi; l > 0; l--) {
+      double s = fabs(A_(l - 1, l - 1)) + fabs(A_(l, l));
+      if (s == 0.0)
+        s = norm;
+      if (fabs(A_(l, l - 1)) <= DBL_EPS * s) {
+        A_(l, l - 1) = 0.0;
+        break;
+      }
+    }
+    if (l == hi) {
+      wr[hi] = A_(hi, hi) + exshift;
+      wi[hi] = 0.0;
+      hi--;
+      its = 0;
+      continue;
+    }
+    if (l == hi - 1) {
+      double p = 0.5 * (A_(hi - 1, hi - 1) - A_(hi, hi));
+      double qq = p * p + A_(hi, hi - 1) * A_(hi - 1, hi);
+      double zz = sqrt(fabs(qq));
+      double x = A_(hi, hi) + exshift;
+      if (qq >= 0.0) {
+        zz = (p >= 0) ? p + zz : p - zz;
+        wr[hi - 1] = x + zz;
+        wr[hi] = (zz != 0.0) ? x - A_(hi, hi - 1) * A_(hi - 1, hi) / zz
+                             : x + zz;
+        wi[hi - 1] = wi[hi] = 0.0;
+      } else {
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = zz;
+        wi[hi] = -zz;
+      }
+      hi -= 2;
+      its = 0;
+      continue;
+    }
+    double x = A_(hi, hi), y = A_(hi - 1, hi - 1);
+    double w = A_(hi, hi - 1) * A_(hi - 1, hi);
+    if (its == 10 || its == 20) {
+      exshift += x;
+      for (int i = 0; i <= hi; i++)
+        A_(i, i) -= x;
+      double s = fabs(A_(hi, hi - 1)) + fabs(A_(hi - 1, hi - 2));
+      x = y = 0.75 * s;
+      w = -0.4375 * s * s;
+    }
+    its++;
+    if (++total > 40 * V)
+      return __longlong_as_double(0x7ff8000000000000ULL);
+    int m;
+    double p = 0, q = 0, r = 0;
+    for (m = hi - 2; m >= l; m--) {
+      double zz = A_(m, m);
+      double rr = x - zz, ss = y - zz;
+      p = (rr * ss - w) / A_(m + 1, m) + A_(m, m + 1);
+      q = A_(m + 1, m + 1) - zz - rr - ss;
+      r = A_(m + 2, m + 1);
+      double s = fabs(p) + fabs(q) + fabs(r);
+      p /= s;
+      q /= s;
+      r /= s;
+      if (m == l)
+        break;
+      double u = fabs(A_(m, m - 1)) * (fabs(q) + fabs(r));
+      double vv = fabs(p) * (fabs(A_(m - 1, m - 1)) + fabs(zz) +
+                             fabs(A_(m + 1, m + 1)));
+      if (u <= DBL_EPS * vv)
+        break;
+    }
+    for (int i = m + 2; i <= hi; i++) {
+      A_(i, i - 2) = 0.0;
+      if (i > m + 2)
+        A_(i, i - 3) = 0.0;
+    }
+    for (int k = m; k <= hi - 1; k++) {
+      bool notlast = (k != hi - 1);
+      if (k != m) {
+        p = A_(k, k - 1);
+        q = A_(k + 1, k - 1);
+        r = notlast ? A_(k + 2, k - 1) : 0.0;
+        x = fabs(p) + fabs(q) + fabs(r);
+        if (x == 0.0)
+          continue;
+        p /= x;
+        q /= x;
+        r /= x;
+      }
+      double s = sqrt(p * p + q * q + r * r);
+      if (p < 0)
+        s = -s;
+      if (k != m)
+        A_(k, k - 1) = -s * x;
+      else if (l != m)
+        A_(k, k - 1) = -A_(k, k - 1);
+      p += s;
+      x = p / s;
+      y = q / s;
+      double zz = r / s;
+      q /= p;
+      r /= p;
+      for (int j = k; j <= hi; j++) {
+        double pp = A_(k, j) + q * A_(k + 1, j);
+        if (notlast) {
+          pp += r * A_(k + 2, j);
+          A_(k + 2, j) -= pp * zz;
+        }
+        A_(k + 1, j) -= pp * y;
+        A_(k, j) -= pp * x;
+      }
+      int ihi = (hi < k + 3) ? hi : k + 3;
+      for (int i = l; i <= ihi; i++) {
+        double pp = x * A_(i, k) + y * A_(i, k + 1);
+        if (notlast) {
+          pp += zz * A_(i, k + 2);
+          A_(i, k + 2) -= pp * r;
+        }
+        A_(i, k + 1) -= pp * q;
+        A_(i, k) -= pp;
+      }
+    }
+  }
+  double mx = 0;
+  for (int i = 0; i < V; i++) {
+    double rr = (wi[i] == 0.0) ? fabs(wr[i])
+                               : sqrt(wr[i] * wr[i] + wi[i] * wi[i]);
+    if (rr > mx)
+      mx = rr;
+  }
+  return mx;
+#undef A_
+}
+
+// Forward-difference Jacobian of F (NumericalDiff.h:6-44 with its default
+// forwardMode=true, which both call sites use: system.cpp:15, :58).
+// wrt_dq: perturb dq[d*V+i] (second-order form) instead of q[i].
+template <class Sys>
+__device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
+                                            int d, bool wrt_dq) {
+  constexpr int V = Sys::V;
+  double v1[V], v2[V];
+  Sys::F(v1, q, dq, d);
+  for (int i = 0; i < V; i++) {
+    double *qi = wrt_dq ? dq + d * V + i : q + i;
+    double qi0 = *qi;
+    double h = fmax(SQRT_EPS * fabs(qi0), SQRT_EPS);
+    *qi += h;
+    Sys::F(v2, q, dq, d);
+    *qi = qi0;
+    for (int r = 0; r < V; r++)
+      jac[r * V + i] = (v2[r] - v1[r]) / h;
+  }
+}
+
+// system_matrix + max|eig| (src/eigs/system.cpp:6-51)
+template <class Sys>
+__device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d) {
+  constexpr int V = Sys::V;
+  double M[V * V];
+  if (Sys::HAS_F)
+    fd_jacobian<Sys>(M, q, dq, d, false);
+  else
+    for (int i = 0; i < V * V; i++)
+      M[i] = 0.0;
+  if (Sys::HAS_B) {
+    double b[V * V];
+    Sys::B(b, q, d);
+    for (int i = 0; i < V * V; i++)
+      M[i] += b[i];
+  }
+  return max_abs_eig<V>(M);
+}
+
+// 2 (N+1) / dX_d * max|eig(dF/d(dq_d))| (src/eigs/system.cpp:53-61)
+template <class Sys>
+__device__ __forceinline__ double max_abs_eigs_2nd(double *q, double *dq, int d,
+                                                   int N, double dXd) {
+  constexpr int V = Sys::V;
+  double M[V * V];
+  fd_jacobian<Sys>(M, q, dq, d, true);
+  return 2 * (N + 1) / dXd * max_abs_eig<V>(M);
+}
+
+// Quadrature average in the summation order of the reference build's
+// Eigen column-major GEMV (stepper.cpp:49,53): blocks of four nodes summed
+// pairwise into the running total for packet lanes (v < V & ~1), left to
+// right for the odd last lane; leftover nodes left to right.
+__device__ __forceinline__ double wavg(const double *wp, const double *x,
+                                       int stride, int n, bool packet) {
+  double s = 0;
+  int k = 0;
+  for (; k + 3 < n; k += 4) {
+    double a0 = wp[k] * x[k * stride], a1 = wp[k + 1] * x[(k + 1) * stride];
+    double a2 = wp[k + 2] * x[(k + 2) * stride];
+    double a3 = wp[k + 3] * x[(k + 3) * stride];
+    if (packet)
+      s = s + ((a0 + a1) + (a2 + a3));
+    else
+      s = (((s + a0) + a1) + a2) + a3;
+  }
+  for (; k < n; k++)
+    s += wp[k] * x[k * stride];
+  return s;
+}
+
+// Non-negative doubles order like their bit patterns: max via integer
+// atomics.  NaN is skipped, as std::max(MAX, NaN) keeps MAX
+// (stepper.cpp:65).
+__device__ __forceinline__ void atomic_max_pos(double *addr, double v) {
+  if (!(v == v))
+    return;
+  atomicMax(reinterpret_cast<unsigned long long *>(addr),
+            static_cast<unsigned long long>(__double_as_longlong(v)));
+}
+
+} // namespace pypde

@@ -1,0 +1,42 @@
+// kernel_set.cuh -- turns a (system, order) pair into its KernelSet and a
+// SystemDesc; included by the per-system instantiation units.
+#pragma once
+
+#include "runtime.h"
+#include "systems.cuh"
+
+namespace pypde {
+
+template <class Sys, int N> KernelSet make_kernel_set() {
+  using Cfg = PredCfg<Sys, N>;
+  KernelSet k;
+  k.cfl.aot = (const void *)&k_cfl<Sys, N>;
+  k.predictor.aot = (const void *)&k_predictor<Sys, N>;
+  k.faces.aot = (const void *)&k_faces<Sys, N>;
+  k.centers.aot = (const void *)&k_centers<Sys, N>;
+  k.gather.aot = (const void *)&k_gather<Sys, N>;
+  k.pred_threads = Cfg::THREADS;
+  k.pred_cpb = Cfg::CPB;
+  k.pred_smem = (size_t)Cfg::SMEM_DOUBLES * sizeof(double);
+  return k;
+}
+
+template <class Sys, int... Ns> SystemDesc describe(const char *name) {
+  SystemDesc d;
+  d.name = name;
+  d.ndim = Sys::NDIM;
+  d.V = Sys::V;
+  d.has_F = Sys::HAS_F;
+  d.has_B = Sys::HAS_B;
+  d.has_S = Sys::HAS_S;
+  d.second_order = Sys::SECOND_ORDER;
+  int ns[] = {Ns...};
+  KernelSet ks[] = {make_kernel_set<Sys, Ns>()...};
+  for (unsigned i = 0; i < sizeof(ns) / sizeof(ns[0]); i++) {
+    d.sets[ns[i]] = ks[i];
+    d.have[ns[i]] = true;
+  }
+  return d;
+}
+
+} // namespace pypde

@@ -1,0 +1,752 @@
+// kernels.cuh -- the ADER-WENO step as CUDA kernels for sm_103a.
+//
+// One step (src/solvers/iterator.cpp:99-148 of haranjackson/PyPDE):
+//   k_boundaries      ghost fill u -> ub                 (a1)
+//   k_weno_pass x d   reconstruction ub -> w             (a2)
+//   k_cfl + k_dt      max|eig| reduction -> dt            (a3, a4)
+//   k_predictor       space-time DG predictor w -> qh     (a5, a6)
+//   k_faces           face fluxes (Rusanov, B path int.)  (a9, a10, a12)
+//   k_centers         volume terms S - B grad q           (a8)
+//   k_gather          u update in the reference's order   (a8, a9)
+//   k_step_end        t, count, snapshot slot             (a14)
+// Everything is FP64.  Data layout in HBM (row-major, V innermost, as the
+// reference's Mat, src/types.h:21-22):
+//   u  [C][V]                 C   = prod n_i
+//   ub [Cb][V]                Cb  = prod (n_i + 2N)
+//   w  [Cw][Nd][V]            Cw  = prod (n_i + 2), node index k_0 outermost
+//   qh [Cw][N][Nd][V]         time node outermost inside a cell
+//   face contributions [d][face][N][Nd_][2][V]
+//   centre contributions [C][N][Nd][V]
+// Device state (t, dt, count, flags) lives in a small struct in device
+// memory so a whole run of steps can be captured in one CUDA graph; every
+// kernel returns at once when the step is inactive (t >= tf or the step
+// cap is reached).
+#pragma once
+
+#include "ader_common.cuh"
+
+namespace pypde {
+
+struct DevState {
+  double t, dt, tf, cfl;
+  double max_speed;  // CFL reduction target (non-negative doubles)
+  long long count;   // steps taken
+  long long max_steps;
+  int active;        // current step runs
+  int push;          // snapshots taken (ndt semantics)
+  int snap_slot;     // ring slot written this step, or -1
+  int nan_found;     // NaN seen in u after some step
+  int nan_now;       // NaN seen in u after this step
+  int ndt;
+  unsigned long long pred_iters; // sum over cells of predictor iterations
+  int pred_max_iters;
+  int pred_fail;     // cells whose Newton iteration hit its cap
+};
+
+// Geometry of one problem, passed by value.
+struct Geom {
+  int ndim;
+  int nX[3];  // interior cells
+  int nXb[3]; // ghost-padded (n + 2N)
+  int nXw[3]; // reconstruction grid (n + 2)
+  int bt[3];  // 0 transmissive, 1 periodic
+  double dX[3];
+  long long C, Cb, Cw;
+};
+
+__device__ __forceinline__ bool step_active(const DevState *st) {
+  return st->active != 0;
+}
+
+// ---------------------------------------------------------------------
+// a1: ghost fill, grid/boundaries.cpp:7-53
+// ---------------------------------------------------------------------
+__device__ __forceinline__ int renorm_index(int ind, int N, int type,
+                                            int bound) {
+  int r = ind - N;
+  if (r < 0)
+    return type == 0 ? 0 : bound + r;
+  if (r >= bound)
+    return type == 0 ? bound - 1 : r - bound;
+  return r;
+}
+
+// ---------------------------------------------------------------------
+// a2: one WENO pass along axis d (weno.cpp:26-121).  in has shape
+// m[0..ndim) x n4 nodes x V, out has m_d reduced by 2(N-1) and N*n4 nodes.
+// One thread per (output cell, existing node, variable): the N nodal
+// values of its 1-D reconstruction.
+// ---------------------------------------------------------------------
+template <int N>
+__global__ void k_weno_pass(const double *__restrict__ in,
+                            double *__restrict__ out, long long n1, int md,
+                            long long n3, int n4, int V, Tables T,
+                            const DevState *st) {
+  if (!step_active(st))
+    return;
+  constexpr int FN2 = (N - 1) / 2, CN2 = N / 2;
+  constexpr int NST = (N > 2) ? ((N % 2 == 0) ? 4 : 3) : 2;
+  const int n2 = md - 2 * (N - 1);
+  long long total = n1 * n2 * n3 * (long long)n4 * V;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long r = e;
+    int v = (int)(r % V);
+    r /= V;
+    int i4 = (int)(r % n4);
+    r /= n4;
+    long long i3 = r % n3;
+    r /= n3;
+    int i = (int)(r % n2);
+    long long i1 = r / n2;
+    const long long stride = n3 * n4 * (long long)V;
+    const double *data =
+        in + ((i1 * md + i) * n3 + i3) * n4 * (long long)V + i4 * V + v;
+    double dat[2 * N - 1];
+#pragma unroll
+    for (int j = 0; j < 2 * N - 1; j++)
+      dat[j] = data[j * stride];
+    double num[N], den = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++)
+      num[k] = 0;
+    const int starts[4] = {0, N - 1, FN2, CN2};
+    const double lams[4] = {WENO_LAMS, WENO_LAMS, WENO_LAMC, WENO_LAMC};
+#pragma unroll
+    for (int k = 0; k < NST; k++) {
+      double c[N];
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        double s = 0;
+#pragma unroll
+        for (int j = 0; j < N; j++)
+          s += T.weno_inv[k][a * N + j] * dat[starts[k] + j];
+        c[a] = s;
+      }
+      double p = 0;
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        double rr = 0;
+#pragma unroll
+        for (int a = 0; a < N; a++)
+          rr += c[a] * T.sig[a * N + j];
+        p += rr * c[j];
+      }
+      p += WENO_EPS;
+      double p2 = p * p, p4 = p2 * p2, p8 = p4 * p4;
+      double o = lams[k] / p8;
+#pragma unroll
+      for (int a = 0; a < N; a++)
+        num[a] += o * c[a];
+      den += o;
+    }
+    double *o = out + ((i1 * n2 + i) * n3 + i3) * (long long)n4 * N * V +
+                (long long)i4 * N * V + v;
+#pragma unroll
+    for (int a = 0; a < N; a++)
+      o[a * V] = num[a] / den;
+  }
+}
+
+// ---------------------------------------------------------------------
+// a3/a4: CFL reduction, stepper.cpp:35-76.  One thread per w-cell.
+// ---------------------------------------------------------------------
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    k_cfl(const double *__restrict__ w, Geom g, Tables T,
+          const double *__restrict__ wprod_g, DevState *st) {
+  if (!step_active(st))
+    return;
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  constexpr int Nd = IPow<N, D>::value;
+  __shared__ double wprod[Nd];
+  __shared__ double dervals[N * N];
+  for (int i = threadIdx.x; i < Nd; i += blockDim.x)
+    wprod[i] = wprod_g[i];
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x)
+    dervals[i] = T.dervals[i];
+  __syncthreads();
+  double local_max = 0.0;
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       cell < g.Cw; cell += (long long)gridDim.x * blockDim.x) {
+    const double *w0 = w + cell * Nd * V;
+    double q[V], dq[D * V];
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      q[v] = wavg(wprod, w0 + v, V, Nd, v < (V & ~1));
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      int stride_d = 1;
+      for (int e = d + 1; e < D; e++)
+        stride_d *= N;
+      for (int v = 0; v < V; v++) {
+        double dw[Nd];
+        for (int idx = 0; idx < Nd; idx++) {
+          int id = (idx / stride_d) % N;
+          int base = idx - id * stride_d;
+          double s = 0;
+#pragma unroll
+          for (int j = 0; j < N; j++)
+            s += dervals[id * N + j] * w0[(base + j * stride_d) * V + v];
+          dw[idx] = s / g.dX[d];
+        }
+        dq[d * V + v] = wavg(wprod, dw, 1, Nd, v < (V & ~1));
+      }
+    }
+    double tmp = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      double lam = max_abs_eigs<Sys>(q, dq, d);
+      if (Sys::SECOND_ORDER)
+        lam += max_abs_eigs_2nd<Sys>(q, dq, d, N, g.dX[d]);
+      tmp += lam / g.dX[d];
+    }
+    local_max = fmax(local_max, tmp);
+  }
+  // warp max, then one atomic per warp
+  for (int off = 16; off > 0; off >>= 1)
+    local_max = fmax(local_max, __shfl_down_sync(0xffffffffu, local_max, off));
+  if ((threadIdx.x & 31) == 0)
+    atomic_max_pos(&st->max_speed, local_max);
+}
+
+// ---------------------------------------------------------------------
+// a5/a6: space-time DG predictor, Picard form (dg.cpp:50-126, 156-224).
+// A team of NT = N*Nd threads per cell, one per space-time node (t, idx);
+// CPB cells per block.  Shared memory per cell: q0, r (NT x V) and the
+// fluxes f (NT x D x V).
+// ---------------------------------------------------------------------
+template <class Sys, int N> struct PredCfg {
+  static constexpr int V = Sys::V, D = Sys::NDIM;
+  static constexpr int Nd = IPow<N, D>::value;
+  static constexpr int NT = N * Nd;
+  static constexpr int CPB_RAW = (NT >= 256) ? 1 : (256 / NT);
+  static constexpr int CPB = CPB_RAW < 1 ? 1 : CPB_RAW;
+  static constexpr int THREADS = CPB * NT;
+  static constexpr int SMEM_DOUBLES = CPB * NT * V * (2 + D);
+};
+
+template <class Sys, int N>
+__global__ void k_predictor(const double *__restrict__ w,
+                            double *__restrict__ qh, Geom g, Tables T,
+                            const double *__restrict__ wprod_g,
+                            DevState *st) {
+  using Cfg = PredCfg<Sys, N>;
+  constexpr int V = Cfg::V, D = Cfg::D, Nd = Cfg::Nd, NT = Cfg::NT;
+  constexpr int CPB = Cfg::CPB;
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  extern __shared__ double smem[];
+  double *s_q = smem;                    // [CPB][NT][V]
+  double *s_r = s_q + CPB * NT * V;      // [CPB][NT][V]
+  double *s_f = s_r + CPB * NT * V;      // [CPB][NT][D][V]
+  __shared__ double wprod[Nd];
+  __shared__ double dervals[N * N];
+  __shared__ double dginv[N * N];
+  __shared__ double wg[N];
+  __shared__ int again[CPB];
+  for (int i = threadIdx.x; i < Nd; i += blockDim.x)
+    wprod[i] = wprod_g[i];
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    dervals[i] = T.dervals[i];
+    dginv[i] = T.dgmat_inv[i];
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    wg[i] = T.wghts[i];
+
+  const int lc = threadIdx.x / NT;   // local cell
+  const int node = threadIdx.x % NT; // t * Nd + idx
+  const int t = node / Nd, idx = node % Nd;
+  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const bool valid = (lc < CPB) && (cell < g.Cw);
+  int digs[D > 0 ? D : 1];
+  {
+    int rem = idx;
+    for (int d = D - 1; d >= 0; d--) {
+      digs[d] = rem % N;
+      rem /= N;
+    }
+  }
+  double *q0 = s_q + (lc * NT) * V;
+  double *rr = s_r + (lc * NT) * V;
+  double *ff = s_f + (lc * NT) * D * V;
+  double Ww[V], q1[V];
+  __syncthreads();
+  if (valid) {
+    // Ww[t,idx] = ENDVALS(0,t) prod W[i_d] w[idx]; q0[t,idx] = w[idx]
+    // (dg.cpp:12-20, 156-171)
+    double cc = T.endvals[t];
+    for (int d = 0; d < D; d++)
+      cc *= wg[digs[d]];
+    const double *wc = w + (cell * Nd + idx) * V;
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      double x = wc[v];
+      Ww[v] = cc * x;
+      q0[node * V + v] = x;
+    }
+  }
+  bool done = !valid;
+  int iters = 0;
+  for (int it = 0; it < DG_IT; it++) {
+    __syncthreads();
+    double dq[D * V];
+    if (!done) {
+      // derivatives of q_t along each axis (evaluations.cpp:23-47)
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        int sd = 1;
+        for (int e = d + 1; e < D; e++)
+          sd *= N;
+        int base = idx - digs[d] * sd;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+          double s = 0;
+#pragma unroll
+          for (int j = 0; j < N; j++)
+            s += dervals[digs[d] * N + j] *
+                 q0[(t * Nd + base + j * sd) * V + v];
+          dq[d * V + v] = s / g.dX[d];
+        }
+      }
+      if (Sys::HAS_F) {
+#pragma unroll
+        for (int d = 0; d < D; d++)
+          Sys::F(ff + (node * D + d) * V, q0 + node * V, dq, d);
+      }
+    }
+    __syncthreads();
+    if (!done) {
+      double r[V];
+      if (Sys::HAS_S)
+        Sys::S(r, q0 + node * V);
+      else
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          r[v] = 0.0;
+      double cc = wg[t];
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        if (Sys::HAS_B) {
+          double b[V * V];
+          Sys::B(b, q0 + node * V, d);
+#pragma unroll
+          for (int i = 0; i < V; i++) {
+            double acc = 0;
+#pragma unroll
+            for (int j = 0; j < V; j++)
+              acc += b[i * V + j] * dq[d * V + j];
+            r[i] -= acc;
+          }
+        }
+        if (Sys::HAS_F) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          int base = idx - digs[d] * sd;
+#pragma unroll
+          for (int v = 0; v < V; v++) {
+            double s = 0;
+#pragma unroll
+            for (int j = 0; j < N; j++)
+              s += dervals[digs[d] * N + j] *
+                   ff[((t * Nd + base + j * sd) * D + d) * V + v];
+            r[v] -= s / g.dX[d];
+          }
+        }
+        cc *= wg[digs[d]];
+      }
+#pragma unroll
+      for (int v = 0; v < V; v++)
+        rr[node * V + v] = (r[v] * cc) * dt + Ww[v];
+    }
+    __syncthreads();
+    if (lc < CPB && node == 0)
+      again[lc] = 0;
+    __syncthreads();
+    if (!done) {
+      // q1 = DG_U^{-1} r with DG_U = kron(DG_MAT, diag W, ...)
+      bool more = false;
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        double s = 0;
+#pragma unroll
+        for (int k = 0; k < N; k++)
+          s += dginv[t * N + k] * rr[(k * Nd + idx) * V + v];
+        q1[v] = s / wprod[idx];
+        double a = q0[node * V + v];
+        if (fabs(q1[v] - a) > DG_TOL * (1. + fabs(a)))
+          more = true;
+      }
+      if (more)
+        again[lc] = 1;
+    }
+    __syncthreads();
+    if (!done) {
+      iters = it + 1;
+      if (again[lc]) {
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          q0[node * V + v] = q1[v];
+      } else {
+        done = true;
+      }
+    }
+    if (__syncthreads_and(done))
+      break;
+  }
+  if (valid) {
+    double *o = qh + (cell * NT + node) * V;
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      o[v] = q1[v];
+    if (node == 0) {
+      atomicAdd(&st->pred_iters, (unsigned long long)iters);
+      atomicMax(&st->pred_max_iters, iters);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
+// a9/a10/a12: face fluxes (fv.cpp:124-198, fluxes.cpp:72-117).  One
+// thread per face point (direction d, face, time node t, transverse node
+// idx).  Faces of direction d are indexed by their low-side w-cell O with
+// O_d in [0, n_d] and O_e in [1, n_e] for e != d.  Writes
+// tmp (b + f) and tmp (b - f), the amounts the reference subtracts from
+// the low and high cell (fv.cpp:189-193).
+// ---------------------------------------------------------------------
+template <class Sys, int N>
+__device__ __forceinline__ void endpoints(const double *qhc, const Tables &T,
+                                          int d, int e, int idx, double *out) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  int sd = 1;
+  for (int k = d + 1; k < D; k++)
+    sd *= N;
+  int hi = idx / sd, lo = idx % sd; // zero_index, evaluations.cpp:4-21
+  int base = hi * sd * N + lo;
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      s += T.endvals[e * N + j] * qhc[(base + j * sd) * V + v];
+    out[v] = s;
+  }
+}
+
+template <class Sys, int N>
+__device__ __forceinline__ void rusanov_flux(double *f, double *qL,
+                                             double *qR, double *dqL,
+                                             double *dqR, int d, double dXd) {
+  constexpr int V = Sys::V;
+  double m1 = max_abs_eigs<Sys>(qL, dqL, d);
+  double m2 = max_abs_eigs<Sys>(qR, dqR, d);
+  double m = fmax(m1, m2);
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    f[v] = m * (qL[v] - qR[v]);
+  double fL[V], fR[V];
+  Sys::F(fL, qL, dqL, d);
+  Sys::F(fR, qR, dqR, d);
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    f[v] += fL[v] + fR[v];
+  if (Sys::SECOND_ORDER) { // fluxes.cpp:96-100
+    double a1 = max_abs_eigs_2nd<Sys>(qL, dqL, d, N, dXd);
+    double a2 = max_abs_eigs_2nd<Sys>(qR, dqR, d, N, dXd);
+    double mm = fmax(a1, a2);
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      f[v] += mm * (qL[v] - qR[v]);
+  }
+}
+
+template <class Sys, int N>
+__device__ __forceinline__ void bint(double *ret, const double *qL,
+                                     const double *qR, int d,
+                                     const Tables &T) {
+  constexpr int V = Sys::V;
+  double Dq[V], q[V], M[V * V], b[V * V];
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    Dq[v] = qR[v] - qL[v];
+#pragma unroll
+  for (int i = 0; i < V * V; i++)
+    M[i] = 0.0;
+  for (int i = 0; i < N; i++) {
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      q[v] = qL[v] + T.nodes[i] * Dq[v];
+    Sys::B(b, q, d);
+#pragma unroll
+    for (int k = 0; k < V * V; k++)
+      M[k] += T.wghts[i] * b[k];
+  }
+#pragma unroll
+  for (int r = 0; r < V; r++) {
+    double s = 0;
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      s += M[r * V + j] * Dq[j];
+    ret[r] = s;
+  }
+}
+
+struct FaceIndex {
+  long long off[4];   // first face point of each direction (off[D] = total)
+  long long nface[3]; // faces per direction
+};
+
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    k_faces(const double *__restrict__ qh, double *__restrict__ contrib,
+            Geom g, Tables T, FaceIndex fi, DevState *st) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       p < fi.off[D]; p += (long long)gridDim.x * blockDim.x) {
+    int d = 0;
+    while (d + 1 < D && p >= fi.off[d + 1])
+      d++;
+    long long r = p - fi.off[d];
+    int idx = (int)(r % Nd_);
+    r /= Nd_;
+    int t = (int)(r % N);
+    long long face = r / N;
+    // low-side w-cell O from the face index (row-major over the face box)
+    int O[3];
+    long long rem = face;
+    for (int e = D - 1; e >= 0; e--) {
+      int ext = (e == d) ? g.nX[e] + 1 : g.nX[e];
+      int i = (int)(rem % ext);
+      rem /= ext;
+      O[e] = (e == d) ? i : i + 1;
+    }
+    long long qc0 = 0, qc1 = 0;
+    for (int e = 0; e < D; e++) {
+      qc0 = qc0 * g.nXw[e] + O[e];
+      qc1 = qc1 * g.nXw[e] + O[e] + (e == d);
+    }
+    const double *qh0 = qh + (qc0 * N + t) * (long long)Nd * V;
+    const double *qh1 = qh + (qc1 * N + t) * (long long)Nd * V;
+    double q0[V], q1[V], dq0[D * V], dq1[D * V];
+    endpoints<Sys, N>(qh0, T, d, 1, idx, q0);
+    endpoints<Sys, N>(qh1, T, d, 0, idx, q1);
+#pragma unroll
+    for (int k = 0; k < D * V; k++)
+      dq0[k] = dq1[k] = 0.0;
+    if (Sys::SECOND_ORDER) {
+      // gradients at the face point: endpoints of derivs of qh
+      // (fv.cpp:87-122)
+      double tmpd[Nd * V];
+      for (int d_ = 0; d_ < D; d_++) {
+        for (int side = 0; side < 2; side++) {
+          const double *src = side ? qh1 : qh0;
+          int sd = 1;
+          for (int e = d_ + 1; e < D; e++)
+            sd *= N;
+          for (int n = 0; n < Nd; n++) {
+            int id = (n / sd) % N;
+            int base = n - id * sd;
+            for (int v = 0; v < V; v++) {
+              double s = 0;
+              for (int j = 0; j < N; j++)
+                s += T.dervals[id * N + j] * src[(base + j * sd) * V + v];
+              tmpd[n * V + v] = s / g.dX[d_];
+            }
+          }
+          double e_out[V];
+          endpoints<Sys, N>(tmpd, T, d, side ? 0 : 1, idx, e_out);
+          for (int v = 0; v < V; v++)
+            (side ? dq1 : dq0)[d_ * V + v] = e_out[v];
+        }
+      }
+    }
+    double f[V], b[V];
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      f[v] = b[v] = 0.0;
+    if (Sys::HAS_F)
+      rusanov_flux<Sys, N>(f, q0, q1, dq0, dq1, d, g.dX[d]);
+    if (Sys::HAS_B)
+      bint<Sys, N>(b, q0, q1, d, T);
+    double tmp = dt * T.wghts[t] / (2. * g.dX[d]);
+    {
+      int rm = idx;
+      int dg[3] = {0, 0, 0};
+      for (int e = D - 2; e >= 0; e--) {
+        dg[e] = rm % N;
+        rm /= N;
+      }
+      for (int e = 0; e < D - 1; e++)
+        tmp *= T.wghts[dg[e]];
+    }
+    double *o = contrib + p * 2 * V;
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      o[v] = tmp * (b[v] + f[v]);
+      o[V + v] = tmp * (b[v] - f[v]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
+// a8: centre (volume) terms, fv.cpp:33-85.  One thread per (u-cell,
+// space-time node): dt W_t prod W (S(qh) - sum_d B_d dqh_d).
+// ---------------------------------------------------------------------
+template <class Sys, int N>
+__global__ void k_centers(const double *__restrict__ qh,
+                          double *__restrict__ cen, Geom g, Tables T,
+                          DevState *st) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  constexpr int Nd = IPow<N, D>::value, NT = N * Nd;
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  long long total = g.C * NT;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long uc = e / NT;
+    int node = (int)(e % NT);
+    int t = node / Nd, idx = node % Nd;
+    long long rem = uc, rc = 0, mul = 1;
+    for (int d = D - 1; d >= 0; d--) {
+      int i = (int)(rem % g.nX[d]);
+      rem /= g.nX[d];
+      rc += mul * (i + 1);
+      mul *= g.nXw[d];
+    }
+    const double *qt = qh + (rc * N + t) * (long long)Nd * V;
+    int digs[3] = {0, 0, 0};
+    {
+      int rm = idx;
+      for (int d = D - 1; d >= 0; d--) {
+        digs[d] = rm % N;
+        rm /= N;
+      }
+    }
+    double s[V];
+    if (Sys::HAS_S)
+      Sys::S(s, qt + idx * V);
+    else
+#pragma unroll
+      for (int v = 0; v < V; v++)
+        s[v] = 0.0;
+    if (Sys::HAS_B) {
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        int sd = 1;
+        for (int k = d + 1; k < D; k++)
+          sd *= N;
+        int base = idx - digs[d] * sd;
+        double dq[V], b[V * V];
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+          double a = 0;
+#pragma unroll
+          for (int j = 0; j < N; j++)
+            a += T.dervals[digs[d] * N + j] * qt[(base + j * sd) * V + v];
+          dq[v] = a / g.dX[d];
+        }
+        Sys::B(b, qt + idx * V, d);
+#pragma unroll
+        for (int i = 0; i < V; i++) {
+          double acc = 0;
+#pragma unroll
+          for (int j = 0; j < V; j++)
+            acc += b[i * V + j] * dq[j];
+          s[i] -= acc;
+        }
+      }
+    }
+    double tmp = dt * T.wghts[t];
+    for (int d = 0; d < D; d++)
+      tmp *= T.wghts[digs[d]];
+    double *o = cen + e * V;
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      o[v] = tmp * s[v];
+  }
+}
+
+// ---------------------------------------------------------------------
+// Apply centre and face contributions to u in the order the reference's
+// loops do (fv.cpp:200-207: centres first, then the face loop over the
+// low-side w-cell O in row-major order with t, then d, then idx inside):
+// for u-cell c at w-index C, the faces with O = C - e_0, ..., C - e_{D-1}
+// (c is their high side) come before O = C (c is the low side of all D).
+// One thread per (u-cell, variable).  Also flags NaN (iterator.cpp:141).
+// ---------------------------------------------------------------------
+template <class Sys, int N>
+__global__ void k_gather(double *__restrict__ u, const double *__restrict__ cen,
+                         const double *__restrict__ contrib, Geom g,
+                         FaceIndex fi, int use_centers, int use_faces,
+                         DevState *st) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
+  if (!step_active(st))
+    return;
+  long long total = g.C * V;
+  bool nan_seen = false;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long uc = e / V;
+    int v = (int)(e % V);
+    double val = u[e];
+    if (use_centers) {
+      const double *c = cen + uc * (N * Nd) * V + v;
+      for (int k = 0; k < N * Nd; k++)
+        val += c[k * V];
+    }
+    if (use_faces) {
+      int ic[3];
+      long long rem = uc;
+      for (int d = D - 1; d >= 0; d--) {
+        ic[d] = (int)(rem % g.nX[d]);
+        rem /= g.nX[d];
+      }
+      // as the high side of the face with O = C - e_dd, for dd = 0..D-1
+      for (int dd = 0; dd < D; dd++) {
+        long long face = 0;
+        for (int e2 = 0; e2 < D; e2++) {
+          int ext = (e2 == dd) ? g.nX[e2] + 1 : g.nX[e2];
+          int oi = (e2 == dd) ? ic[e2] : ic[e2]; // O_e - (e != dd ? 1 : 0)
+          face = face * ext + oi;
+        }
+        const double *c = contrib + (fi.off[dd] + face * N * Nd_) * 2 * V;
+        for (int t = 0; t < N; t++)
+          for (int idx = 0; idx < Nd_; idx++)
+            val -= c[((t * Nd_ + idx) * 2 + 1) * V + v];
+      }
+      // as the low side (O = C) of all D faces, t outer, d inner
+      long long facel[3];
+      for (int dd = 0; dd < D; dd++) {
+        long long face = 0;
+        for (int e2 = 0; e2 < D; e2++) {
+          int ext = (e2 == dd) ? g.nX[e2] + 1 : g.nX[e2];
+          int oi = (e2 == dd) ? ic[e2] + 1 : ic[e2];
+          face = face * ext + oi;
+        }
+        facel[dd] = face;
+      }
+      for (int t = 0; t < N; t++)
+        for (int dd = 0; dd < D; dd++) {
+          const double *c =
+              contrib + (fi.off[dd] + (facel[dd] * N + t) * Nd_) * 2 * V;
+          for (int idx = 0; idx < Nd_; idx++)
+            val -= c[(idx * 2) * V + v];
+        }
+    }
+    u[e] = val;
+    if (!(val == val))
+      nan_seen = true;
+  }
+  if (__syncthreads_or(nan_seen) && threadIdx.x == 0)
+    atomicOr(&st->nan_now, 1);
+}
+
+} // namespace pypde

@@ -1,0 +1,948 @@
+// runtime.cu -- host driver of the ADER-WENO step on one GPU.
+//
+// Replaces the reference's time loop and thread pool
+// (haranjackson/PyPDE src/solvers/iterator.cpp:38-151,
+// include/ThreadPool.h): the whole grid is resident in HBM, every stage is
+// a kernel, and runs of steps are captured in one CUDA graph so the host
+// only synchronises between graph launches (to drain snapshots and to see
+// whether t reached tf; kernels of steps past the end return at once).
+#include "runtime.h"
+#include "step_kernels.cuh"
+#include "../../include/pypde_gb300.h"
+
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+namespace pypde {
+
+static thread_local std::string g_err;
+void set_error(const std::string &m) { g_err = m; }
+const char *last_error() { return g_err.c_str(); }
+
+#define CK(x)                                                                  \
+  do {                                                                         \
+    cudaError_t e_ = (x);                                                      \
+    if (e_ != cudaSuccess) {                                                   \
+      set_error(std::string(#x) + ": " + cudaGetErrorString(e_));             \
+      return PYPDE_ERR_CUDA;                                                   \
+    }                                                                          \
+  } while (0)
+
+// ------------------------------------------------------------------
+// registry of built-in systems
+// ------------------------------------------------------------------
+static std::vector<SystemDesc> &builtins() {
+  static std::vector<SystemDesc> v;
+  return v;
+}
+void register_builtin(const SystemDesc &d) { builtins().push_back(d); }
+const SystemDesc *find_builtin(const std::string &name, int ndim) {
+  for (auto &d : builtins())
+    if (d.name == name && d.ndim == ndim)
+      return &d;
+  return nullptr;
+}
+
+// ------------------------------------------------------------------
+// launching AOT or run-time compiled kernels
+// ------------------------------------------------------------------
+typedef int (*cuLaunchKernel_t)(void *, unsigned, unsigned, unsigned,
+                                unsigned, unsigned, unsigned, unsigned,
+                                cudaStream_t, void **, void **);
+static cuLaunchKernel_t driver_launch() {
+  static cuLaunchKernel_t fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuLaunchKernel", &p, 12000,
+                                         cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (cuLaunchKernel_t)p;
+  }
+  return fn;
+}
+
+static cudaError_t launch(const KFunc &f, dim3 grid, dim3 block, size_t smem,
+                          cudaStream_t s, void **args) {
+  if (f.aot)
+    return cudaLaunchKernel(f.aot, grid, block, args, smem, s);
+  cuLaunchKernel_t fn = driver_launch();
+  if (!fn || !f.jit)
+    return cudaErrorInvalidDeviceFunction;
+  int r = fn(f.jit, grid.x, grid.y, grid.z, block.x, block.y, block.z,
+             (unsigned)smem, s, args, nullptr);
+  return r == 0 ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+static cudaError_t set_smem(const KFunc &f, size_t bytes) {
+  if (bytes <= 48 * 1024)
+    return cudaSuccess;
+  if (f.aot)
+    return cudaFuncSetAttribute(f.aot,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)bytes);
+  typedef int (*cuFuncSetAttribute_t)(void *, int, int);
+  void *p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuFuncSetAttribute", &p, 12000,
+                                       cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return cudaErrorInvalidDeviceFunction;
+  // CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES = 8
+  return ((cuFuncSetAttribute_t)p)(f.jit, 8, (int)bytes) == 0
+             ? cudaSuccess
+             : cudaErrorInvalidValue;
+}
+
+static unsigned grid_for(long long work, int threads, int cap_blocks) {
+  long long b = (work + threads - 1) / threads;
+  if (b < 1)
+    b = 1;
+  if (b > cap_blocks)
+    b = cap_blocks;
+  return (unsigned)b;
+}
+
+// ------------------------------------------------------------------
+// device memory: grow-only buffers per device, reused across calls
+// ------------------------------------------------------------------
+struct Buf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+static cudaError_t ensure(Buf &b, size_t bytes) {
+  if (bytes == 0)
+    bytes = 8;
+  if (b.cap >= bytes)
+    return cudaSuccess;
+  if (b.p)
+    cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e == cudaSuccess)
+    b.cap = bytes;
+  return e;
+}
+struct Arena {
+  Buf u, uprev, ub, tmpA, tmpB, w, qh, contrib, cen, ring, state, wprod;
+  DevState *host_state = nullptr; // pinned
+  cudaStream_t stream = nullptr;
+};
+static std::mutex g_mu;
+static std::map<int, Arena> g_arena;
+
+static int arena_for(int device, Arena **out) {
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) {
+    set_error("invalid CUDA device ordinal");
+    return PYPDE_ERR_ARG;
+  }
+  CK(cudaSetDevice(device));
+  Arena &a = g_arena[device];
+  if (!a.stream)
+    CK(cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking));
+  if (!a.host_state)
+    CK(cudaMallocHost(&a.host_state, sizeof(DevState)));
+  *out = &a;
+  return PYPDE_OK;
+}
+
+// ------------------------------------------------------------------
+// geometry
+// ------------------------------------------------------------------
+static void fill_geom(Geom &g, int ndim, const int *nX, const int *bt,
+                      const double *dX, int N) {
+  std::memset(&g, 0, sizeof(g));
+  g.ndim = ndim;
+  g.C = g.Cb = g.Cw = 1;
+  for (int d = 0; d < 3; d++) {
+    bool in = d < ndim;
+    g.nX[d] = in ? nX[d] : 1;
+    g.nXb[d] = in ? nX[d] + 2 * N : 1;
+    g.nXw[d] = in ? nX[d] + 2 : 1;
+    g.bt[d] = in && bt ? bt[d] : 0;
+    g.dX[d] = in && dX ? dX[d] : 1.0;
+    if (in) {
+      g.C *= g.nX[d];
+      g.Cb *= g.nXb[d];
+      g.Cw *= g.nXw[d];
+    }
+  }
+}
+
+static FaceIndex face_index(const Geom &g, int N) {
+  FaceIndex fi;
+  std::memset(&fi, 0, sizeof(fi));
+  long long Nd_ = 1;
+  for (int d = 0; d < g.ndim - 1; d++)
+    Nd_ *= N;
+  for (int d = 0; d < 3; d++) {
+    if (d < g.ndim) {
+      long long nf = g.nX[d] + 1;
+      for (int e = 0; e < g.ndim; e++)
+        if (e != d)
+          nf *= g.nX[e];
+      fi.nface[d] = nf;
+      fi.off[d + 1] = fi.off[d] + nf * N * Nd_;
+    } else {
+      fi.off[d + 1] = fi.off[d];
+    }
+  }
+  return fi;
+}
+
+static int ipow(int b, int e) {
+  int r = 1;
+  while (e-- > 0)
+    r *= b;
+  return r;
+}
+
+// ------------------------------------------------------------------
+// WENO passes (generic in V, templated on N)
+// ------------------------------------------------------------------
+static const void *weno_kernel(int N) {
+  switch (N) {
+  case 1: return (const void *)&k_weno_pass<1>;
+  case 2: return (const void *)&k_weno_pass<2>;
+  case 3: return (const void *)&k_weno_pass<3>;
+  case 4: return (const void *)&k_weno_pass<4>;
+  case 5: return (const void *)&k_weno_pass<5>;
+  case 6: return (const void *)&k_weno_pass<6>;
+  default: return nullptr;
+  }
+}
+
+// Enqueue the ndim passes: in has shape m (ndim dims) with one node per
+// cell; the last pass writes w.  tmpA/tmpB hold intermediate passes.
+static cudaError_t enqueue_weno(const double *in, const int *m_in, int ndim,
+                                int N, int V, const Tables &T, double *tmpA,
+                                double *tmpB, double *w, const DevState *st,
+                                cudaStream_t s) {
+  const void *fn = weno_kernel(N);
+  if (!fn)
+    return cudaErrorInvalidValue;
+  int m[3];
+  for (int d = 0; d < ndim; d++)
+    m[d] = m_in[d];
+  const double *src = in;
+  int n4 = 1;
+  for (int d = 0; d < ndim; d++) {
+    long long n1 = 1, n3 = 1;
+    for (int e = 0; e < d; e++)
+      n1 *= m[e];
+    for (int e = d + 1; e < ndim; e++)
+      n3 *= m[e];
+    int md = m[d];
+    double *dst = (d == ndim - 1) ? w : ((d % 2 == 0) ? tmpA : tmpB);
+    long long total = n1 * (md - 2 * (N - 1)) * n3 * (long long)n4 * V;
+    Tables Tc = T;
+    void *args[] = {(void *)&src, (void *)&dst, (void *)&n1, (void *)&md,
+                    (void *)&n3,  (void *)&n4,  (void *)&V,  (void *)&Tc,
+                    (void *)&st};
+    cudaError_t e = cudaLaunchKernel(fn, dim3(grid_for(total, 128, 152 * 64)),
+                                     dim3(128), args, 0, s);
+    if (e != cudaSuccess)
+      return e;
+    src = dst;
+    m[d] -= 2 * (N - 1);
+    n4 *= N;
+  }
+  return cudaSuccess;
+}
+
+static long long weno_tmp_doubles(const int *nXb, int ndim, int N, int V) {
+  // largest intermediate pass output (all but the last)
+  long long best = 0;
+  int m[3];
+  for (int d = 0; d < ndim; d++)
+    m[d] = nXb[d];
+  long long n4 = 1;
+  for (int d = 0; d < ndim - 1; d++) {
+    m[d] -= 2 * (N - 1);
+    n4 *= N;
+    long long sz = n4 * V;
+    for (int e = 0; e < ndim; e++)
+      sz *= m[e];
+    if (sz > best)
+      best = sz;
+  }
+  return best;
+}
+
+// ------------------------------------------------------------------
+// one step, enqueued on a stream (captured into the graph)
+// ------------------------------------------------------------------
+struct StepCtx {
+  const SystemDesc *sys;
+  const KernelSet *ks;
+  Geom g;
+  FaceIndex fi;
+  Tables T;
+  int N, V, ring;
+  bool stiff, faces, centers;
+  double *u, *uprev, *ub, *tmpA, *tmpB, *w, *qh, *contrib, *cen, *ringbuf,
+      *wprod;
+  DevState *st;
+};
+
+static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
+  const KernelSet &k = *c.ks;
+  Geom g = c.g;
+  Tables T = c.T;
+  void *args[] = {(void *)&c.w, (void *)&c.qh, (void *)&g, (void *)&T,
+                  (void *)&c.wprod, (void *)&c.st};
+  if (c.stiff) {
+    unsigned blocks = (unsigned)((g.Cw + k.newton_cpb - 1) / k.newton_cpb);
+    return launch(k.newton, dim3(blocks), dim3(k.newton_threads),
+                  k.newton_smem, s, args);
+  }
+  unsigned blocks = (unsigned)((g.Cw + k.pred_cpb - 1) / k.pred_cpb);
+  return launch(k.predictor, dim3(blocks), dim3(k.pred_threads), k.pred_smem,
+                s, args);
+}
+
+static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
+  const KernelSet &k = *c.ks;
+  Geom g = c.g;
+  Tables T = c.T;
+  FaceIndex fi = c.fi;
+  cudaError_t e;
+  if (c.faces) {
+    void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
+                 (void *)&fi,   (void *)&c.st};
+    e = launch(k.faces, dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)),
+               dim3(128), 0, s, a);
+    if (e != cudaSuccess)
+      return e;
+  }
+  if (c.centers) {
+    long long nn = (long long)c.N * ipow(c.N, c.g.ndim);
+    void *a[] = {(void *)&c.qh, (void *)&c.cen, (void *)&g, (void *)&T,
+                 (void *)&c.st};
+    e = launch(k.centers, dim3(grid_for(g.C * nn, 128, 152 * 256)),
+               dim3(128), 0, s, a);
+    if (e != cudaSuccess)
+      return e;
+  }
+  int uc = c.centers ? 1 : 0, uf = c.faces ? 1 : 0;
+  void *a[] = {(void *)&c.u, (void *)&c.cen, (void *)&c.contrib, (void *)&g,
+               (void *)&fi,  (void *)&uc,    (void *)&uf,        (void *)&c.st};
+  return launch(k.gather, dim3(grid_for(g.C * c.V, 256, 152 * 64)), dim3(256),
+                0, s, a);
+}
+
+// Kernels one step launches (the count reported as kernel_launches).
+static int kernels_per_step(const StepCtx &c) {
+  return 10 + c.g.ndim + (c.faces ? 1 : 0) + (c.centers ? 1 : 0);
+}
+
+// One step.  With ev non-null, events are recorded between the stages
+// (ev[0..8]: start, after ghost fill, WENO, CFL+dt, predictor, faces,
+// centres, gather, end) for the profiling mode.
+static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
+                                cudaEvent_t *ev = nullptr) {
+  cudaError_t e;
+  auto mark = [&](int i) {
+    if (ev)
+      cudaEventRecord(ev[i], s);
+  };
+  k_step_begin<<<1, 1, 0, s>>>(c.st);
+  long long n = c.g.C * c.V;
+  k_copy_prev<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(c.u, c.uprev, n,
+                                                         c.st);
+  mark(0);
+  k_boundaries<<<grid_for(c.g.Cb * c.V, 256, 152 * 32), 256, 0, s>>>(
+      c.u, c.ub, c.g, c.N, c.V, c.st);
+  mark(1);
+  e = enqueue_weno(c.ub, c.g.nXb, c.g.ndim, c.N, c.V, c.T, c.tmpA, c.tmpB,
+                   c.w, c.st, s);
+  if (e != cudaSuccess)
+    return e;
+  mark(2);
+  {
+    Geom g = c.g;
+    Tables T = c.T;
+    void *a[] = {(void *)&c.w, (void *)&g, (void *)&T, (void *)&c.wprod,
+                 (void *)&c.st};
+    e = launch(c.ks->cfl, dim3(grid_for(c.g.Cw, 128, 152 * 64)), dim3(128), 0,
+               s, a);
+    if (e != cudaSuccess)
+      return e;
+  }
+  k_dt<<<1, 1, 0, s>>>(c.st);
+  mark(3);
+  e = enqueue_predictor(c, s);
+  if (e != cudaSuccess)
+    return e;
+  mark(4);
+  {
+    StepCtx f = c;
+    f.centers = false;
+    if (c.faces) {
+      // faces only (the gather is launched below)
+      const KernelSet &k = *c.ks;
+      Geom g = c.g;
+      Tables T = c.T;
+      FaceIndex fi = c.fi;
+      void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
+                   (void *)&fi,   (void *)&c.st};
+      e = launch(k.faces, dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)),
+                 dim3(128), 0, s, a);
+      if (e != cudaSuccess)
+        return e;
+    }
+    mark(5);
+    if (c.centers) {
+      long long nn = (long long)c.N * ipow(c.N, c.g.ndim);
+      Geom g = c.g;
+      Tables T = c.T;
+      void *a[] = {(void *)&c.qh, (void *)&c.cen, (void *)&g, (void *)&T,
+                   (void *)&c.st};
+      e = launch(c.ks->centers, dim3(grid_for(g.C * nn, 128, 152 * 256)),
+                 dim3(128), 0, s, a);
+      if (e != cudaSuccess)
+        return e;
+    }
+    mark(6);
+    Geom g = c.g;
+    FaceIndex fi = c.fi;
+    int uc = c.centers ? 1 : 0, uf = c.faces ? 1 : 0;
+    void *a[] = {(void *)&c.u, (void *)&c.cen, (void *)&c.contrib,
+                 (void *)&g,   (void *)&fi,    (void *)&uc,
+                 (void *)&uf,  (void *)&c.st};
+    e = launch(c.ks->gather, dim3(grid_for(g.C * c.V, 256, 152 * 64)),
+               dim3(256), 0, s, a);
+    if (e != cudaSuccess)
+      return e;
+  }
+  mark(7);
+  k_step_end<<<1, 1, 0, s>>>(c.st, c.ring);
+  k_snapshot<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(c.u, c.ringbuf, n,
+                                                        c.st);
+  mark(8);
+  return cudaGetLastError();
+}
+
+static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
+                        int flux) {
+  if (sys.ndim != ndim) {
+    set_error("system was built for another number of dimensions");
+    return PYPDE_ERR_ARG;
+  }
+  if (N < 1 || N > MAXN || !sys.have[N]) {
+    set_error("order N=" + std::to_string(N) + " is not built for system " +
+              sys.name);
+    return PYPDE_ERR_UNSUPPORTED;
+  }
+  if (stiff && !sys.sets[N].newton.valid()) {
+    set_error("stiff predictor not built for system " + sys.name);
+    return PYPDE_ERR_UNSUPPORTED;
+  }
+  if (flux != 0) {
+    set_error("only the Rusanov flux (FLUX=0) is built");
+    return PYPDE_ERR_UNSUPPORTED;
+  }
+  return PYPDE_OK;
+}
+
+// ------------------------------------------------------------------
+// the solver (pde_solver)
+// ------------------------------------------------------------------
+int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
+  if (a.ndim < 1 || a.ndim > 3 || !a.u || a.tf < 0 || a.ndt < 1) {
+    set_error("invalid arguments");
+    return PYPDE_ERR_ARG;
+  }
+  for (int d = 0; d < a.ndim; d++)
+    if (a.nX[d] < 1 || !(a.dX[d] > 0)) {
+      set_error("invalid grid");
+      return PYPDE_ERR_ARG;
+    }
+  int rc = check_system(sys, a.ndim, a.N, a.stiff, a.flux);
+  if (rc)
+    return rc;
+  if ((a.useF != sys.has_F) || (a.useB != sys.has_B) ||
+      (a.useS != sys.has_S)) {
+    set_error("useF/useB/useS do not match the callbacks of system " +
+              sys.name);
+    return PYPDE_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  rc = arena_for(a.device, &ar);
+  if (rc)
+    return rc;
+  cudaStream_t s = ar->stream;
+  StepCtx c;
+  c.sys = &sys;
+  c.ks = &sys.sets[a.N];
+  c.N = a.N;
+  c.V = sys.V;
+  fill_geom(c.g, a.ndim, a.nX, a.bt, a.dX, a.N);
+  c.fi = face_index(c.g, a.N);
+  if (make_tables(a.N, &c.T)) {
+    set_error("bad order");
+    return PYPDE_ERR_ARG;
+  }
+  c.stiff = a.stiff;
+  c.faces = sys.has_F || sys.has_B;
+  c.centers = sys.has_B || sys.has_S;
+  const int V = c.V, N = c.N, Nd = ipow(N, a.ndim);
+  long long usz = c.g.C * V;
+  int K = a.steps_per_graph;
+  if (K <= 0) {
+    long long k = (1LL << 21) / (c.g.C * N * Nd);
+    K = (int)(k < 1 ? 1 : (k > 32 ? 32 : k));
+  }
+  c.ring = K + 1;
+  CK(ensure(ar->u, usz * 8));
+  CK(ensure(ar->uprev, usz * 8));
+  CK(ensure(ar->ub, c.g.Cb * V * 8));
+  long long tmpn = weno_tmp_doubles(c.g.nXb, a.ndim, N, V);
+  CK(ensure(ar->tmpA, tmpn * 8));
+  CK(ensure(ar->tmpB, tmpn * 8));
+  CK(ensure(ar->w, c.g.Cw * Nd * V * 8));
+  CK(ensure(ar->qh, c.g.Cw * N * Nd * V * 8));
+  CK(ensure(ar->contrib, (c.faces ? c.fi.off[a.ndim] : 1) * 2 * V * 8));
+  CK(ensure(ar->cen, (c.centers ? c.g.C * N * Nd : 1) * V * 8));
+  CK(ensure(ar->ring, c.ring * usz * 8));
+  CK(ensure(ar->state, sizeof(DevState)));
+  CK(ensure(ar->wprod, Nd * 8));
+  c.u = (double *)ar->u.p;
+  c.uprev = (double *)ar->uprev.p;
+  c.ub = (double *)ar->ub.p;
+  c.tmpA = (double *)ar->tmpA.p;
+  c.tmpB = (double *)ar->tmpB.p;
+  c.w = (double *)ar->w.p;
+  c.qh = (double *)ar->qh.p;
+  c.contrib = (double *)ar->contrib.p;
+  c.cen = (double *)ar->cen.p;
+  c.ringbuf = (double *)ar->ring.p;
+  c.wprod = (double *)ar->wprod.p;
+  c.st = (DevState *)ar->state.p;
+  {
+    std::vector<double> wp(Nd);
+    make_wprod(c.T, a.ndim, wp.data());
+    CK(cudaMemcpyAsync(c.wprod, wp.data(), Nd * 8, cudaMemcpyHostToDevice,
+                       s));
+  }
+  CK(set_smem(c.ks->predictor, c.ks->pred_smem));
+  if (c.stiff)
+    CK(set_smem(c.ks->newton, c.ks->newton_smem));
+  DevState hs;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.tf = a.tf;
+  hs.cfl = a.cfl;
+  hs.max_steps = a.max_steps > 0 ? a.max_steps : -1;
+  hs.ndt = a.ndt;
+  hs.snap_slot = -1;
+  *ar->host_state = hs;
+  CK(cudaMemcpyAsync(c.st, ar->host_state, sizeof(DevState),
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c.u, a.u, usz * 8, cudaMemcpyHostToDevice, s));
+
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (!a.profile) { // capture K steps into one graph
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaSuccess;
+    for (int k = 0; k < K && ce == cudaSuccess; k++)
+      ce = enqueue_step(c, s);
+    cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) {
+      set_error(std::string("enqueue step: ") + cudaGetErrorString(ce));
+      return PYPDE_ERR_CUDA;
+    }
+    CK(ee);
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+  }
+  cudaEvent_t pev[9];
+  if (a.profile)
+    for (int i = 0; i < 9; i++)
+      CK(cudaEventCreate(&pev[i]));
+  double stage_s[8] = {};
+  long long launches = 0;
+
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, s));
+  int drained = 0;
+  rc = PYPDE_OK;
+  for (;;) {
+    if (a.profile) {
+      CK(enqueue_step(c, s, pev));
+      launches += kernels_per_step(c);
+    } else {
+      CK(cudaGraphLaunch(exec, s));
+      launches += (long long)K * kernels_per_step(c);
+    }
+    CK(cudaMemcpyAsync(ar->host_state, c.st, sizeof(DevState),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    DevState h = *ar->host_state;
+    if (a.profile && h.active) {
+      // stage i spans events (i, i+1); ghost fill .. gather are stages 0-6,
+      // the bookkeeping kernels count as "other"
+      for (int i = 0; i < 7; i++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, pev[i], pev[i + 1]);
+        stage_s[i] += ms * 1e-3;
+      }
+      float ms = 0;
+      cudaEventElapsedTime(&ms, pev[7], pev[8]);
+      stage_s[7] += ms * 1e-3;
+    }
+    // snapshots taken during this launch: ring slot p % ring holds row p
+    for (; drained < h.push; drained++)
+      if (a.ret)
+        CK(cudaMemcpyAsync(a.ret + (long long)drained * usz,
+                           c.ringbuf + (long long)(drained % c.ring) * usz,
+                           usz * 8, cudaMemcpyDeviceToHost, s));
+    bool more = (h.t < h.tf) && (h.max_steps < 0 || h.count < h.max_steps) &&
+                !h.nan_found;
+    if (h.nan_found) {
+      if (a.ret && h.push < a.ndt)
+        CK(cudaMemcpyAsync(a.ret + (long long)h.push * usz, c.uprev, usz * 8,
+                           cudaMemcpyDeviceToHost, s));
+      if (a.ret && h.push + 1 < a.ndt)
+        CK(cudaMemcpyAsync(a.ret + (long long)(h.push + 1) * usz, c.u,
+                           usz * 8, cudaMemcpyDeviceToHost, s));
+      rc = PYPDE_NAN_FOUND;
+    }
+    if (!more)
+      break;
+  }
+  CK(cudaEventRecord(e1, s));
+  CK(cudaMemcpyAsync(a.u, c.u, usz * 8, cudaMemcpyDeviceToHost, s));
+  if (a.ret)
+    CK(cudaMemcpyAsync(a.ret + (long long)(a.ndt - 1) * usz, c.u, usz * 8,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (exec)
+    cudaGraphExecDestroy(exec);
+  if (graph)
+    cudaGraphDestroy(graph);
+  if (a.profile)
+    for (int i = 0; i < 9; i++)
+      cudaEventDestroy(pev[i]);
+  DevState h = *ar->host_state;
+  if (out) {
+    out->steps = h.count;
+    out->t_final = h.t;
+    out->pred_iters = h.pred_iters;
+    out->pred_max_iters = h.pred_max_iters;
+    out->pred_fail = h.pred_fail;
+    out->nan_found = h.nan_found;
+    out->device_seconds = ms * 1e-3;
+    out->kernel_launches = launches;
+    for (int i = 0; i < 8; i++)
+      out->stage_seconds[i] = stage_s[i];
+  }
+  return rc;
+}
+
+// ------------------------------------------------------------------
+// single stages
+// ------------------------------------------------------------------
+static int put_state(Arena *ar, DevState **dst, double t, double tf,
+                     double cfl, long long count, double dt) {
+  CK(ensure(ar->state, sizeof(DevState)));
+  DevState hs;
+  std::memset(&hs, 0, sizeof(hs));
+  hs.active = 1;
+  hs.t = t;
+  hs.tf = tf;
+  hs.cfl = cfl;
+  hs.count = count;
+  hs.dt = dt;
+  hs.max_steps = -1;
+  hs.snap_slot = -1;
+  *ar->host_state = hs;
+  CK(cudaMemcpyAsync(ar->state.p, ar->host_state, sizeof(DevState),
+                     cudaMemcpyHostToDevice, ar->stream));
+  *dst = (DevState *)ar->state.p;
+  return PYPDE_OK;
+}
+
+int stage_boundaries(const double *u, const int *nX, int ndim, const int *bt,
+                     int N, int V, double *ub) {
+  if (ndim < 1 || ndim > 3 || N < 1 || V < 1) {
+    set_error("invalid arguments");
+    return PYPDE_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  int rc = arena_for(0, &ar);
+  if (rc)
+    return rc;
+  Geom g;
+  fill_geom(g, ndim, nX, bt, nullptr, N);
+  DevState *st;
+  if ((rc = put_state(ar, &st, 0, 1, 1, 0, 0)))
+    return rc;
+  CK(ensure(ar->u, g.C * V * 8));
+  CK(ensure(ar->ub, g.Cb * V * 8));
+  cudaStream_t s = ar->stream;
+  CK(cudaMemcpyAsync(ar->u.p, u, g.C * V * 8, cudaMemcpyHostToDevice, s));
+  k_boundaries<<<grid_for(g.Cb * V, 256, 152 * 32), 256, 0, s>>>(
+      (double *)ar->u.p, (double *)ar->ub.p, g, N, V, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ub, ar->ub.p, g.Cb * V * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return PYPDE_OK;
+}
+
+int stage_weno(const double *ubh, const int *nXb, int ndim, int N, int V,
+               double *wh) {
+  if (ndim < 1 || ndim > 3 || N < 1 || N > 6 || V < 1) {
+    set_error("invalid arguments (WENO is built for N <= 6)");
+    return PYPDE_ERR_ARG;
+  }
+  long long cin = 1, cout = 1;
+  for (int d = 0; d < ndim; d++) {
+    if (nXb[d] - 2 * (N - 1) < 1) {
+      set_error("grid too small for this order");
+      return PYPDE_ERR_ARG;
+    }
+    cin *= nXb[d];
+    cout *= nXb[d] - 2 * (N - 1);
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  int rc = arena_for(0, &ar);
+  if (rc)
+    return rc;
+  DevState *st;
+  if ((rc = put_state(ar, &st, 0, 1, 1, 0, 0)))
+    return rc;
+  long long nout = cout * ipow(N, ndim) * V;
+  long long tmpn = weno_tmp_doubles(nXb, ndim, N, V);
+  CK(ensure(ar->ub, cin * V * 8));
+  CK(ensure(ar->w, nout * 8));
+  CK(ensure(ar->tmpA, tmpn * 8));
+  CK(ensure(ar->tmpB, tmpn * 8));
+  Tables T;
+  make_tables(N, &T);
+  cudaStream_t s = ar->stream;
+  CK(cudaMemcpyAsync(ar->ub.p, ubh, cin * V * 8, cudaMemcpyHostToDevice, s));
+  CK(enqueue_weno((double *)ar->ub.p, nXb, ndim, N, V, T,
+                  (double *)ar->tmpA.p, (double *)ar->tmpB.p,
+                  (double *)ar->w.p, st, s));
+  CK(cudaMemcpyAsync(wh, ar->w.p, nout * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return PYPDE_OK;
+}
+
+int stage_timestep(const SystemDesc &sys, const double *w, long long nrows,
+                   const double *dX, int ndim, int N, double cfl, double tf,
+                   double t, long long count, double *dt) {
+  int rc = check_system(sys, ndim, N, false, 0);
+  if (rc)
+    return rc;
+  int Nd = ipow(N, ndim);
+  if (nrows < 1 || nrows % Nd) {
+    set_error("nrows must be a positive multiple of N^ndim");
+    return PYPDE_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  if ((rc = arena_for(0, &ar)))
+    return rc;
+  DevState *st;
+  if ((rc = put_state(ar, &st, t, tf, cfl, count, 0)))
+    return rc;
+  Geom g;
+  int ones[3] = {1, 1, 1};
+  fill_geom(g, ndim, ones, nullptr, dX, N);
+  g.Cw = nrows / Nd;
+  Tables T;
+  make_tables(N, &T);
+  std::vector<double> wp(Nd);
+  make_wprod(T, ndim, wp.data());
+  CK(ensure(ar->w, nrows * sys.V * 8));
+  CK(ensure(ar->wprod, Nd * 8));
+  cudaStream_t s = ar->stream;
+  CK(cudaMemcpyAsync(ar->w.p, w, nrows * sys.V * 8, cudaMemcpyHostToDevice,
+                     s));
+  CK(cudaMemcpyAsync(ar->wprod.p, wp.data(), Nd * 8, cudaMemcpyHostToDevice,
+                     s));
+  double *wd = (double *)ar->w.p, *wpd = (double *)ar->wprod.p;
+  void *a[] = {(void *)&wd, (void *)&g, (void *)&T, (void *)&wpd,
+               (void *)&st};
+  CK(launch(sys.sets[N].cfl, dim3(grid_for(g.Cw, 128, 152 * 64)), dim3(128),
+            0, s, a));
+  k_dt<<<1, 1, 0, s>>>(st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ar->host_state, st, sizeof(DevState),
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *dt = ar->host_state->dt;
+  return PYPDE_OK;
+}
+
+int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
+                    const double *dX, int ndim, int N, bool stiff, double dt,
+                    double tol, double *qh, Stats *out) {
+  int rc = check_system(sys, ndim, N, stiff, 0);
+  if (rc)
+    return rc;
+  int Nd = ipow(N, ndim);
+  if (nrows < 1 || nrows % Nd) {
+    set_error("nrows must be a positive multiple of N^ndim");
+    return PYPDE_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  if ((rc = arena_for(0, &ar)))
+    return rc;
+  DevState *st;
+  if ((rc = put_state(ar, &st, 0, 1, 1, 0, dt)))
+    return rc;
+  (void)tol;
+  StepCtx c;
+  std::memset(&c, 0, sizeof(c));
+  c.sys = &sys;
+  c.ks = &sys.sets[N];
+  int ones[3] = {1, 1, 1};
+  fill_geom(c.g, ndim, ones, nullptr, dX, N);
+  c.g.Cw = nrows / Nd;
+  make_tables(N, &c.T);
+  c.N = N;
+  c.V = sys.V;
+  c.stiff = stiff;
+  std::vector<double> wp(Nd);
+  make_wprod(c.T, ndim, wp.data());
+  CK(ensure(ar->w, nrows * sys.V * 8));
+  CK(ensure(ar->qh, nrows * N * sys.V * 8));
+  CK(ensure(ar->wprod, Nd * 8));
+  cudaStream_t s = ar->stream;
+  CK(cudaMemcpyAsync(ar->w.p, w, nrows * sys.V * 8, cudaMemcpyHostToDevice,
+                     s));
+  CK(cudaMemcpyAsync(ar->wprod.p, wp.data(), Nd * 8, cudaMemcpyHostToDevice,
+                     s));
+  c.w = (double *)ar->w.p;
+  c.qh = (double *)ar->qh.p;
+  c.wprod = (double *)ar->wprod.p;
+  c.st = st;
+  CK(set_smem(stiff ? c.ks->newton : c.ks->predictor,
+              stiff ? c.ks->newton_smem : c.ks->pred_smem));
+  CK(enqueue_predictor(c, s));
+  CK(cudaMemcpyAsync(qh, c.qh, nrows * N * sys.V * 8, cudaMemcpyDeviceToHost,
+                     s));
+  CK(cudaMemcpyAsync(ar->host_state, st, sizeof(DevState),
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (out) {
+    out->pred_iters = ar->host_state->pred_iters;
+    out->pred_max_iters = ar->host_state->pred_max_iters;
+    out->pred_fail = ar->host_state->pred_fail;
+  }
+  return PYPDE_OK;
+}
+
+int stage_fv(const SystemDesc &sys, double *u, const double *qh,
+             const int *nX, const double *dX, int ndim, int N, int flux,
+             double dt) {
+  int rc = check_system(sys, ndim, N, false, flux);
+  if (rc)
+    return rc;
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  if ((rc = arena_for(0, &ar)))
+    return rc;
+  DevState *st;
+  if ((rc = put_state(ar, &st, 0, 1, 1, 0, dt)))
+    return rc;
+  StepCtx c;
+  std::memset(&c, 0, sizeof(c));
+  c.sys = &sys;
+  c.ks = &sys.sets[N];
+  fill_geom(c.g, ndim, nX, nullptr, dX, N);
+  c.fi = face_index(c.g, N);
+  make_tables(N, &c.T);
+  c.N = N;
+  c.V = sys.V;
+  c.faces = sys.has_F || sys.has_B;
+  c.centers = sys.has_B || sys.has_S;
+  int Nd = ipow(N, ndim);
+  long long usz = c.g.C * c.V, qsz = c.g.Cw * N * Nd * c.V;
+  CK(ensure(ar->u, usz * 8));
+  CK(ensure(ar->qh, qsz * 8));
+  CK(ensure(ar->contrib, (c.faces ? c.fi.off[ndim] : 1) * 2 * c.V * 8));
+  CK(ensure(ar->cen, (c.centers ? c.g.C * N * Nd : 1) * c.V * 8));
+  cudaStream_t s = ar->stream;
+  CK(cudaMemcpyAsync(ar->u.p, u, usz * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ar->qh.p, qh, qsz * 8, cudaMemcpyHostToDevice, s));
+  c.u = (double *)ar->u.p;
+  c.qh = (double *)ar->qh.p;
+  c.contrib = (double *)ar->contrib.p;
+  c.cen = (double *)ar->cen.p;
+  c.st = st;
+  CK(enqueue_fv(c, s));
+  CK(cudaMemcpyAsync(u, ar->u.p, usz * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return PYPDE_OK;
+}
+
+// ------------------------------------------------------------------
+// FP64 throughput of this GPU: the roofline denominator of the FP64-bound
+// kernels (independent FMA chains, 8 per thread, 8 blocks per SM).
+// ------------------------------------------------------------------
+__global__ void k_dfma_peak(double *out, double a, double b, int iters) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b);
+    x3 = fma(x3, a, b); x4 = fma(x4, a, b); x5 = fma(x5, a, b);
+    x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] =
+      x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+int measure_fp64(int device, double *tflops) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  int rc = arena_for(device, &ar);
+  if (rc)
+    return rc;
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  Buf out;
+  CK(ensure(out, (size_t)blocks * threads * 8));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; rep++) {
+    CK(cudaEventRecord(e0, ar->stream));
+    k_dfma_peak<<<blocks, threads, 0, ar->stream>>>((double *)out.p, 0.999,
+                                                     1e-3, iters);
+    CK(cudaEventRecord(e1, ar->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best)
+      best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out.p);
+  *tflops = 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return PYPDE_OK;
+}
+
+} // namespace pypde

@@ -1,0 +1,94 @@
+// step_kernels.cuh -- the kernels that are not templated on a system:
+// ghost fill, dt and the step bookkeeping.  Included by runtime.cu only.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace pypde {
+
+__global__ void k_boundaries(const double *__restrict__ u,
+                             double *__restrict__ ub, Geom g, int N, int V,
+                             const DevState *st) {
+  if (!step_active(st))
+    return;
+  long long total = g.Cb * V;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)gridDim.x * blockDim.x) {
+    long long idx = e / V;
+    int v = (int)(e - idx * V);
+    long long rem = idx, src = 0, mul = 1;
+    for (int d = g.ndim - 1; d >= 0; d--) {
+      int i = (int)(rem % g.nXb[d]);
+      rem /= g.nXb[d];
+      src += mul * renorm_index(i, N, g.bt[d], g.nX[d]);
+      mul *= g.nX[d];
+    }
+    ub[e] = u[src * V + v];
+  }
+}
+
+// dt from the reduced maximum (stepper.cpp:67-75)
+__global__ void k_dt(DevState *st) {
+  if (!step_active(st))
+    return;
+  double dt = st->cfl / st->max_speed;
+  if (st->count <= 5)
+    dt *= 0.2;
+  if (st->t + dt > st->tf)
+    dt = st->tf - st->t;
+  st->dt = dt;
+}
+
+// ---------------------------------------------------------------------
+// Step bookkeeping (iterator.cpp:99-148).
+// ---------------------------------------------------------------------
+__global__ void k_step_begin(DevState *st) {
+  st->active = (st->t < st->tf) &&
+               (st->max_steps < 0 || st->count < st->max_steps) &&
+               !st->nan_found;
+  st->max_speed = 0.0;
+  st->snap_slot = -1;
+  st->nan_now = 0;
+}
+
+// t += dt, count += 1, and the snapshot decision of iterator.cpp:136-139.
+// Snapshots go to a ring of device slots the host drains between graph
+// launches: slot = push % ring.
+__global__ void k_step_end(DevState *st, int ring) {
+  if (!step_active(st))
+    return;
+  st->t += st->dt;
+  st->count += 1;
+  if (st->push < st->ndt &&
+      st->t >= double(st->push + 1) / double(st->ndt) * st->tf) {
+    st->snap_slot = st->push % ring;
+    st->push += 1;
+  }
+  if (st->nan_now)
+    st->nan_found = 1;
+}
+
+// Keep the state of the previous step (the NaN rows of iterator.cpp:141-145).
+__global__ void k_copy_prev(const double *__restrict__ u,
+                            double *__restrict__ uprev, long long n,
+                            const DevState *st) {
+  if (!step_active(st))
+    return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    uprev[i] = u[i];
+}
+
+// Copy u into its snapshot slot when k_step_end chose one.
+__global__ void k_snapshot(const double *__restrict__ u,
+                           double *__restrict__ ring, long long n,
+                           const DevState *st) {
+  if (!step_active(st) || st->snap_slot < 0)
+    return;
+  double *dst = ring + (long long)st->snap_slot * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = u[i];
+}
+
+} // namespace pypde

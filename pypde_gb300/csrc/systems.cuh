@@ -1,0 +1,145 @@
+// systems.cuh -- built-in device callback systems (the user's F/B/S of
+// pypde's pde_solver, src/api.h:4-10, compiled ahead of time).
+//
+// A system is a struct with
+//   static constexpr int V, NDIM; HAS_F, HAS_B, HAS_S, SECOND_ORDER flags
+//   F(out[V], Q[V], dQ[NDIM*V], d)   flux in direction d
+//   B(out[V*V] row-major, Q[V], d)   non-conservative matrix
+//   S(out[V], Q[V])                  source
+// exactly the reference callback signatures (pypde/cfuncs.py:6-8).  User
+// systems compiled at run time (NVRTC) provide the same struct.
+//
+// Formulas and operation order match the host test callbacks, so host and
+// device produce the same bits (the kernels are compiled without FMA
+// contraction):
+//   Euler<D>     V = D+2   (rho, m_0..m_{D-1}, E), gamma = 1.4
+//   Cattaneo<D>  V = 2D+3  Euler + relaxing heat flux q + passive
+//                s = log10(tau); T = p/rho, kappa = 1e-2, 1/tau = 10^-s;
+//                F_d adds q_d to the energy flux and kappa T/tau to q_d;
+//                S_q = -q/tau
+//   Ncp<D>       V = 3, F, B and S (a non-conservative test system)
+//   Burgers2     V = 1, D = 1, second-order form F(Q, dQ, d)
+#pragma once
+
+namespace pypde {
+
+// 10^x from IEEE +, *, /, floor and ldexp only (2^(x log2 10), Taylor
+// series of 2^r on |r| <= 1/2), so that host and device agree bitwise.
+__device__ __forceinline__ double pow10_portable(double x) {
+  double y = x * 3.321928094887362;
+  double n = floor(y + 0.5);
+  double r = (y - n) * 0.6931471805599453;
+  double p = 1.0;
+#pragma unroll
+  for (int k = 18; k >= 1; k--)
+    p = 1.0 + p * r / k;
+  return ldexp(p, (int)n);
+}
+
+template <int D> struct EulerCore {
+  static __device__ __forceinline__ double flux(double *out, const double *Q,
+                                                int d) {
+    double r = Q[0];
+    double ke = 0.0;
+#pragma unroll
+    for (int i = 0; i < D; i++)
+      ke += Q[1 + i] * Q[1 + i];
+    double p = (1.4 - 1.0) * (Q[D + 1] - 0.5 * ke / r);
+    double ud = Q[1 + d] / r;
+    out[0] = Q[1 + d];
+#pragma unroll
+    for (int i = 0; i < D; i++)
+      out[1 + i] = Q[1 + i] * ud;
+    out[1 + d] += p;
+    out[D + 1] = (Q[D + 1] + p) * ud;
+    return p;
+  }
+};
+
+template <int D> struct Euler {
+  static constexpr int V = D + 2, NDIM = D;
+  static constexpr bool HAS_F = true, HAS_B = false, HAS_S = false;
+  static constexpr bool SECOND_ORDER = false;
+  static __device__ __forceinline__ void F(double *out, const double *Q,
+                                           const double *, int d) {
+    EulerCore<D>::flux(out, Q, d);
+  }
+  static __device__ __forceinline__ void B(double *, const double *, int) {}
+  static __device__ __forceinline__ void S(double *, const double *) {}
+};
+
+template <int D> struct Cattaneo {
+  static constexpr int V = 2 * D + 3, NDIM = D;
+  static constexpr bool HAS_F = true, HAS_B = false, HAS_S = true;
+  static constexpr bool SECOND_ORDER = false;
+  static __device__ __forceinline__ void F(double *out, const double *Q,
+                                           const double *, int d) {
+    double p = EulerCore<D>::flux(out, Q, d);
+    double inv_tau = pow10_portable(-Q[2 * D + 2]);
+    double T = p / Q[0];
+    out[D + 1] += Q[D + 2 + d];
+#pragma unroll
+    for (int i = 0; i < D; i++)
+      out[D + 2 + i] = 0.0;
+    out[D + 2 + d] = 1e-2 * T * inv_tau;
+    out[2 * D + 2] = 0.0;
+  }
+  static __device__ __forceinline__ void B(double *, const double *, int) {}
+  static __device__ __forceinline__ void S(double *out, const double *Q) {
+    double inv_tau = pow10_portable(-Q[2 * D + 2]);
+#pragma unroll
+    for (int i = 0; i < D + 2; i++)
+      out[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < D; i++)
+      out[D + 2 + i] = -Q[D + 2 + i] * inv_tau;
+    out[2 * D + 2] = 0.0;
+  }
+};
+
+__device__ __forceinline__ double ncp_a(int d) {
+  return d == 0 ? 1.0 : (d == 1 ? 0.5 : 0.25);
+}
+
+template <int D> struct Ncp {
+  static constexpr int V = 3, NDIM = D;
+  static constexpr bool HAS_F = true, HAS_B = true, HAS_S = true;
+  static constexpr bool SECOND_ORDER = false;
+  static __device__ __forceinline__ void F(double *out, const double *Q,
+                                           const double *, int d) {
+    double a = ncp_a(d);
+    out[0] = a * (0.5 * Q[0] * Q[0]);
+    out[1] = a * (Q[0] * Q[1]);
+    out[2] = a * (Q[0] * Q[2]);
+  }
+  static __device__ __forceinline__ void B(double *out, const double *Q,
+                                           int d) {
+    double a = ncp_a(d);
+#pragma unroll
+    for (int i = 0; i < 9; i++)
+      out[i] = 0.0;
+    out[4] = a * Q[0];
+    out[5] = a * 0.2;
+    out[7] = a * 0.2;
+    out[8] = a * Q[0];
+  }
+  static __device__ __forceinline__ void S(double *out, const double *Q) {
+    out[0] = 0.0;
+    out[1] = 0.1 * (Q[2] - Q[1]);
+    out[2] = -0.1 * (Q[1] + Q[2]);
+  }
+};
+
+struct Burgers2 {
+  static constexpr int V = 1, NDIM = 1;
+  static constexpr bool HAS_F = true, HAS_B = false, HAS_S = false;
+  static constexpr bool SECOND_ORDER = true;
+  static __device__ __forceinline__ void F(double *out, const double *Q,
+                                           const double *dQ, int d) {
+    out[0] = ncp_a(d) * (0.5 * Q[0] * Q[0]) - 0.01 * dQ[d];
+  }
+  static __device__ __forceinline__ void B(double *, const double *, int) {}
+  static __device__ __forceinline__ void S(double *, const double *) {}
+};
+
+} // namespace pypde

@@ -1,0 +1,85 @@
+"""pde_solver and weno_solver with the reference's Python API
+(haranjackson/PyPDE pypde/solvers.py:13-244), run on the GPU.
+
+Differences from the reference, all at the callback boundary:
+  * F, B and S must be callbacks the GPU can run: the built-in systems of
+    pypde_gb300.systems, or Python functions that pypde_gb300.callbacks can
+    translate to device code (the reference compiles them with numba into
+    host cfuncs, pypde/cfuncs.py:30-75).
+  * ``nThreads`` is accepted and ignored (one GPU does the work of the
+    reference's CPU thread pool).
+  * Extensions (keyword-only): ``max_steps``, ``newton_tol``, ``device``,
+    ``stats`` (a dict filled with step and iteration counts).
+"""
+import numpy as np
+
+from . import _lib
+from .callbacks import resolve_system
+from .utils import nargs, parse_boundary_types
+
+FLUXES = {"rusanov": 0, "roe": 1, "osher": 2}
+
+
+def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cfl=0.9,
+               order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *,
+               max_steps=None, newton_tol=None, device=0, stats=None):
+    """Solve dQ/dt + div F(Q, grad Q) + B(Q) . grad Q = S(Q) on [0, L] (see
+    pypde/solvers.py:28-175 for the full description of the arguments).
+
+    Returns an array of shape (ndt,) + Q0.shape: row k holds the state when t
+    first reaches (k+1) tf / ndt, row ndt-1 the state at tf.  Like the
+    reference, the final state is also written into Q0 when Q0 is a
+    contiguous float64 array.
+    """
+    nX = np.array(Q0.shape[:-1], dtype="int32")
+    ndim = len(nX)
+    V = Q0.shape[-1]
+    dX = np.array([L[i] / nX[i] for i in range(len(L))], dtype="float64")
+
+    bt = parse_boundary_types(boundaryTypes, ndim)
+
+    useF, useB, useS = F is not None, B is not None, S is not None
+    secondOrder = useF and nargs(F) == 3
+    system = resolve_system(F, B, S, ndim, V, secondOrder)
+
+    ret = np.zeros(ndt * Q0.size)
+    ur = Q0.ravel()
+    if ur.dtype != np.float64:
+        print("invalid array type")
+        raise TypeError("Q0 must be a float64 array")
+
+    opt = _lib.Options()
+    opt.max_steps = int(max_steps) if max_steps else -1
+    opt.newton_tol = float(newton_tol) if newton_tol else 0.0
+    opt.device = int(device)
+    st = _lib.Stats()
+    lib = _lib.lib()
+    code = lib.pde_solver_ex(system.handle, useF, useB, useS, _lib.c_ptr(ur), float(tf),
+                             _lib.c_ptr(nX), ndim, _lib.c_ptr(dX), float(cfl), _lib.c_ptr(bt),
+                             bool(stiff), FLUXES[flux], int(order), int(ndt), _lib.c_ptr(ret),
+                             opt, st)
+    _lib.check(code)
+    if code == _lib.PYPDE_NAN_FOUND:
+        print("NaNs found")
+    if stats is not None:
+        stats.update(st.as_dict())
+    return ret.reshape((ndt,) + Q0.shape)
+
+
+# The name used by the GB300 build's documentation; same function.
+ader_solver = pde_solver
+
+
+def weno_solver(u, order=2):
+    """WENO reconstruction of an already padded array u of shape
+    (n_1..n_d, V) (pypde/solvers.py:217-244).  Returns shape
+    (n_1-2(order-1), ..., order, ..., order, V)."""
+    nX = np.array(u.shape[:-1], dtype=np.int32)
+    ndim = len(nX)
+    V = u.shape[-1]
+    nXret = nX - 2 * (order - 1)
+    ret = np.zeros(int(nXret.prod()) * order ** ndim * V)
+    ur = np.ascontiguousarray(u, dtype=np.float64).ravel()
+    _lib.check(_lib.lib().weno_solver(_lib.c_ptr(ret), _lib.c_ptr(ur), _lib.c_ptr(nX), ndim,
+                                      order, V))
+    return ret.reshape(np.concatenate([nXret, [order] * ndim, [V]]))

@@ -1,0 +1,130 @@
+"""Built-in callback systems.
+
+Each system exposes Python callables F, B, S with the reference's callback
+signatures (pypde/solvers.py:80-119): ``F(Q, d)`` (or ``F(Q, DQ, d)`` for
+the second-order form), ``B(Q, d)``, ``S(Q)``.  They are plain numpy
+functions, usable on their own, and each carries the name of its compiled
+device twin (pypde_gb300/csrc/systems.cuh) so that ``pde_solver`` runs the
+device code.  Both evaluate the same formulas in the same operation order.
+
+    euler(ndim)     V = ndim+2, Q = (rho, m_0..m_{ndim-1}, E), gamma = 1.4
+    cattaneo(ndim)  V = 2 ndim+3: Euler + relaxing heat flux q + passive
+                    s = log10(tau); T = p/rho, kappa = 1e-2; S_q = -q/tau
+    ncp(ndim)       V = 3, a non-conservative test system with F, B and S
+    burgers2()      V = 1, viscous Burgers F(Q, DQ, d) (second order)
+"""
+from dataclasses import dataclass
+from typing import Callable, Optional
+
+import numpy as np
+
+GAMMA = 1.4
+KAPPA = 1e-2
+
+
+def pow10_portable(x):
+    """10^x from +, *, /, floor and ldexp (bitwise equal on host and device)."""
+    y = x * 3.321928094887362
+    n = np.floor(y + 0.5)
+    r = (y - n) * 0.6931471805599453
+    p = 1.0
+    for k in range(18, 0, -1):
+        p = 1.0 + p * r / k
+    return np.ldexp(p, int(n))
+
+
+@dataclass
+class System:
+    name: str
+    ndim: int
+    V: int
+    F: Optional[Callable]
+    B: Optional[Callable]
+    S: Optional[Callable]
+    second_order: bool = False
+
+
+def _tag(fn, name, ndim, role):
+    fn._pypde_builtin = (name, ndim)
+    fn._pypde_role = role
+    return fn
+
+
+def _euler_flux(Q, ndim, d):
+    r = Q[0]
+    ke = 0.0
+    for i in range(ndim):
+        ke += Q[1 + i] * Q[1 + i]
+    p = (GAMMA - 1.0) * (Q[ndim + 1] - 0.5 * ke / r)
+    ud = Q[1 + d] / r
+    out = np.empty(len(Q))
+    out[0] = Q[1 + d]
+    for i in range(ndim):
+        out[1 + i] = Q[1 + i] * ud
+    out[1 + d] += p
+    out[ndim + 1] = (Q[ndim + 1] + p) * ud
+    return out, p
+
+
+def euler(ndim):
+    def F(Q, d):
+        return _euler_flux(Q, ndim, d)[0][:ndim + 2]
+
+    return System("euler", ndim, ndim + 2, _tag(F, "euler", ndim, "F"), None, None)
+
+
+def cattaneo(ndim):
+    V = 2 * ndim + 3
+
+    def F(Q, d):
+        out, p = _euler_flux(Q, ndim, d)
+        inv_tau = pow10_portable(-Q[2 * ndim + 2])
+        T = p / Q[0]
+        out[ndim + 1] += Q[ndim + 2 + d]
+        out[ndim + 2:2 * ndim + 2] = 0.0
+        out[ndim + 2 + d] = KAPPA * T * inv_tau
+        out[2 * ndim + 2] = 0.0
+        return out
+
+    def S(Q):
+        inv_tau = pow10_portable(-Q[2 * ndim + 2])
+        out = np.zeros(V)
+        out[ndim + 2:2 * ndim + 2] = -Q[ndim + 2:2 * ndim + 2] * inv_tau
+        return out
+
+    return System("cattaneo", ndim, V, _tag(F, "cattaneo", ndim, "F"), None,
+                  _tag(S, "cattaneo", ndim, "S"))
+
+
+_NCP_A = (1.0, 0.5, 0.25)
+
+
+def ncp(ndim):
+    def F(Q, d):
+        a = _NCP_A[d]
+        return np.array([a * (0.5 * Q[0] * Q[0]), a * (Q[0] * Q[1]), a * (Q[0] * Q[2])])
+
+    def B(Q, d):
+        a = _NCP_A[d]
+        out = np.zeros((3, 3))
+        out[1, 1] = a * Q[0]
+        out[1, 2] = a * 0.2
+        out[2, 1] = a * 0.2
+        out[2, 2] = a * Q[0]
+        return out
+
+    def S(Q):
+        return np.array([0.0, 0.1 * (Q[2] - Q[1]), -0.1 * (Q[1] + Q[2])])
+
+    return System("ncp", ndim, 3, _tag(F, "ncp", ndim, "F"), _tag(B, "ncp", ndim, "B"),
+                  _tag(S, "ncp", ndim, "S"))
+
+
+def burgers2():
+    def F(Q, DQ, d):
+        return np.array([_NCP_A[d] * (0.5 * Q[0] * Q[0]) - 0.01 * DQ[d][0]])
+
+    return System("burgers2", 1, 1, _tag(F, "burgers2", 1, "F"), None, None, True)
+
+
+BUILTINS = {"euler": euler, "cattaneo": cattaneo, "ncp": ncp}

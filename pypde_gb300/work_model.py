@@ -1,0 +1,135 @@
+"""Algorithmic work of the ADER-WENO step: FP64 flops and HBM bytes per unit.
+
+The counts follow the reference algorithm (haranjackson/PyPDE src/), not
+this implementation: they are what `roofline.achieved` divides by kernel
+time.  Flops count +, -, *, / and sqrt as one each; a callback counts the
+operations of its formula (F_FLOPS); max|eig| of a V x V matrix counts the
+nominal 10 V^3 of a Hessenberg reduction plus Francis QR.
+
+Units:
+  face point   one (face, time node, transverse node) of fv.cpp:144-196
+  w-cell       one cell of the reconstruction grid (n+2)^d
+  cell-update  one interior cell advanced by one step
+"""
+
+# flops of one callback evaluation, counted from the formulas of
+# pypde_gb300/csrc/systems.cuh (identical to the test callbacks)
+def f_flops(system, ndim):
+    if system == "euler":
+        return 3 * ndim + 8
+    if system == "cattaneo":
+        return 3 * ndim + 8 + 58 + 4  # + 10^-s (Horner, 18 terms) + T, q, kappa T/tau
+    if system == "ncp":
+        return 8
+    if system == "burgers2":
+        return 5
+    raise ValueError(system)
+
+
+def b_flops(system):
+    return 4 if system == "ncp" else 0
+
+
+def s_flops(system, ndim):
+    return {"cattaneo": 58 + ndim, "ncp": 4}.get(system, 0)
+
+
+def eig_flops(V):
+    return 10 * V ** 3
+
+
+def max_abs_eigs_flops(system, ndim, V):
+    """FD Jacobian (V+1 callbacks, V columns of V differences and V
+    divisions, step h) + B + max|eig| (src/eigs/system.cpp:6-51)."""
+    jac = (V + 1) * f_flops(system, ndim) + V * (2 + 2 * V)
+    return jac + (V * V if b_flops(system) else 0) + eig_flops(V)
+
+
+def face_point_flops(system, ndim, V, N):
+    """k_faces: endpoints, Rusanov flux, B path integral, weights, outputs."""
+    ends = 2 * V * 2 * N
+    rus = 2 * max_abs_eigs_flops(system, ndim, V) + 2 * V + 2 * f_flops(system, ndim) + 2 * V
+    bint = N * (2 * V + b_flops(system) + 2 * V * V) + 2 * V * V + V if b_flops(system) else 0
+    return ends + rus + bint + 3 + (ndim - 1) + 4 * V
+
+
+def face_points(nX, N):
+    ndim = len(nX)
+    total = 0
+    for d in range(ndim):
+        nf = nX[d] + 1
+        for e in range(ndim):
+            if e != d:
+                nf *= nX[e]
+        total += nf * N * N ** (ndim - 1)
+    return total
+
+
+def weno_flops_per_output(N):
+    """One 1-D reconstruction (N nodal values of one variable)."""
+    nst = 2 if N <= 2 else (4 if N % 2 == 0 else 3)
+    per_stencil = 2 * N * N + 2 * N * N + 1 + 3 + 1 + 2 * N + 1
+    return nst * per_stencil + N
+
+
+def cfl_flops_per_wcell(system, ndim, V, N):
+    Nd = N ** ndim
+    avg = V * 2 * Nd
+    grads = ndim * V * (Nd * (2 * N + 1) + 2 * Nd)
+    return avg + grads + ndim * (max_abs_eigs_flops(system, ndim, V) + 2)
+
+
+def predictor_flops_per_iteration(system, ndim, V, N):
+    """One Picard iteration of one cell (dg.cpp:50-126, 192-199)."""
+    Nd = N ** ndim
+    nodes = N * Nd
+    per_node = (ndim * V * (2 * N + 1) + ndim * f_flops(system, ndim)
+                + ndim * V * (2 * N + 1) + s_flops(system, ndim)
+                + ndim * (V + (2 * V * V + b_flops(system) if b_flops(system) else 0))
+                + 3 * V + V * (2 * N + 1) + 3 * V)
+    return nodes * per_node
+
+
+def step_flops(system, nX, V, N, pred_iters_per_cell):
+    """Whole-step algorithmic flops, per stage."""
+    ndim = len(nX)
+    C = 1
+    Cw = 1
+    for n in nX:
+        C *= n
+        Cw *= n + 2
+    out = {}
+    # WENO: pass d produces (cells of that pass) x N^d nodes x V outputs
+    shape = [n + 2 * N for n in nX]
+    weno = 0
+    n4 = 1
+    for d in range(ndim):
+        shape[d] -= 2 * (N - 1)
+        cells = 1
+        for m in shape:
+            cells *= m
+        weno += cells * n4 * V * weno_flops_per_output(N)
+        n4 *= N
+    out["weno"] = weno
+    out["cfl"] = Cw * cfl_flops_per_wcell(system, ndim, V, N)
+    out["predictor"] = Cw * pred_iters_per_cell * predictor_flops_per_iteration(system, ndim, V, N)
+    out["faces"] = face_points(nX, N) * face_point_flops(system, ndim, V, N)
+    return out
+
+
+def bytes_per_cell_update(nX, V, N):
+    """Unfused algorithmic HBM bytes per cell-update, per stage (FP64)."""
+    ndim = len(nX)
+    C = Cb = Cw = 1
+    for n in nX:
+        C *= n
+        Cb *= n + 2 * N
+        Cw *= n + 2
+    Nd = N ** ndim
+    return {
+        "ghost": 8 * V * (1 + Cb / C),
+        "weno": 8 * V * (Cb / C) + 8 * V * Nd * Cw / C,
+        "cfl": 8 * V * Nd * Cw / C,
+        "predictor": 8 * V * Nd * (1 + N) * Cw / C,
+        "fv": 8 * V * N * Nd * Cw / C + 16 * V,
+    }

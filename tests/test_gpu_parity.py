@@ -1,0 +1,168 @@
+"""GPU kernels against the CPU restatement (oracle/) and the reference's
+golden vectors, through the C ABI.
+
+The plain FP64 form is built to be bit-identical to the restatement: same
+algorithms, same summation orders, no contracted multiply-adds.  So every
+stage is compared for exact equality, and full runs must agree to well
+inside the 1e-10 relative L1 bar (they are expected to agree exactly).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, l1, load
+from oracle import ora
+from pypde_gb300 import stages, systems, workloads
+from pypde_gb300.solvers import pde_solver
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("euler", (40,), 2, [0]), ("euler", (40,), 3, [1]), ("euler", (17,), 1, [1]),
+         ("euler", (12, 10), 2, [1, 0]), ("euler", (12, 10), 3, [1, 1]),
+         ("euler", (5, 6, 4), 2, [1, 0, 1]), ("euler", (4, 3, 5), 3, [0, 1, 1]),
+         ("cattaneo", (10, 8), 2, [1, 1]), ("ncp", (16,), 3, [0]), ("ncp", (9, 8), 2, [1, 0]),
+         ("burgers2", (24,), 2, [1]), ("euler", (1,), 2, [1]), ("euler", (2, 1), 2, [1, 1])]
+
+
+def _ids(c):
+    return f"{c[0]}-{'x'.join(map(str, c[1]))}-N{c[2]}"
+
+
+def _state(system, shape, seed=1):
+    u = workloads.random_state(system, shape, seed)
+    if system == "cattaneo":
+        u[..., -1] = np.random.default_rng(seed).uniform(-1, 0, shape)
+    return u
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+def test_stages_bitwise(gpu_lib, case):
+    system, shape, N, bt = case
+    u = _state(system, shape)
+    dX = [1.0 / n for n in shape]
+    ub_o = ora.boundaries(u, N, bt)
+    ub_g = stages.boundaries(u, N, bt)
+    assert np.array_equal(ub_g, ub_o)
+    w_o = ora.weno(ub_o, N)
+    w_g = stages.weno(ub_o, N)
+    assert np.array_equal(w_g, w_o)
+    for count in (0, 9):
+        dt_o = ora.timestep(system, w_o, dX, N, 0.9, 1.0, 0.0, count)
+        dt_g = stages.timestep(system, w_o, dX, N, 0.9, 1.0, 0.0, count)
+        assert dt_g == dt_o
+    qh_o, its_o, mx_o = ora.predictor(system, w_o, dX, N, False, dt_o)
+    qh_g, st = stages.predictor(system, w_o, dX, N, False, dt_o)
+    assert np.array_equal(qh_g, qh_o)
+    assert st["pred_iters"] == its_o and st["pred_max_iters"] == mx_o
+    u_o = ora.fv(system, u, qh_o, dX, N, dt_o)
+    u_g = stages.fv(system, u, qh_o, dX, N, dt_o)
+    assert np.array_equal(u_g, u_o)
+
+
+def test_dt_clipped_to_tf(gpu_lib):
+    u = _state("euler", (12, 10))
+    w = ora.weno(ora.boundaries(u, 2, [1, 1]), 2)
+    dt_full = stages.timestep("euler", w, [0.1, 0.1], 2, 0.9, 1.0, 0.0, 9)
+    t = 1.0 - 0.25 * dt_full
+    assert stages.timestep("euler", w, [0.1, 0.1], 2, 0.9, 1.0, t, 9) == 1.0 - t
+
+
+@pytest.mark.parametrize("fixture", sorted(os.path.basename(f) for f in
+                                           glob.glob(os.path.join(GOLDEN, "stages_*.npz"))))
+def test_weno_against_reference_golden(gpu_lib, fixture):
+    z = load(fixture)
+    w = stages.weno(z["ub"], int(z["N"]))
+    assert np.abs(w - z["w"]).max() <= 1e-10 * np.abs(z["w"]).max()
+    assert np.array_equal(stages.boundaries(z["u"], int(z["N"]), z["bt"]).ravel(),
+                          z["ub"].ravel())
+
+
+RUNS = [("euler", workloads.sod(400), 2, [0], 0.9, 30, "sod400"),
+        ("euler", workloads.shear(32), 3, [1, 1], 0.8, 10, "shear32"),
+        ("euler", workloads.shear(16), 2, [1, 0], 0.8, 10, "shear16"),
+        ("ncp", workloads.random_state("ncp", (12, 10), 4), 2, [1, 1], 0.5, 6, "ncp12x10"),
+        ("burgers2", workloads.random_state("burgers2", (32,), 5), 3, [1], 0.5, 6, "burgers32"),
+        ("euler", workloads.random_state("euler", (6, 5, 7), 6), 2, [1, 1, 0], 0.5, 4, "euler3d")]
+
+
+@pytest.mark.parametrize("run", RUNS, ids=[r[-1] for r in RUNS])
+def test_full_run_matches_port(gpu_lib, run):
+    system, u0, N, bt, cfl, K, _ = run
+    ndim = u0.ndim - 1
+    L = [1.0] * ndim
+    u_o, ret_o, steps_o, t_o = ora.pde_solver(system, u0, 10.0, L, bt, cfl, N, ndt=4,
+                                              max_steps=K)
+    sysobj = {"euler": systems.euler, "ncp": systems.ncp}.get(system)
+    s = sysobj(ndim) if sysobj else systems.burgers2()
+    q = u0.copy()
+    st = {}
+    ret = pde_solver(q, 10.0, L, F=s.F, B=s.B, S=s.S,
+                     boundaryTypes=[("transitive", "periodic")[b] for b in bt], cfl=cfl,
+                     order=N, ndt=4, stiff=False, max_steps=K, stats=st)
+    assert st["steps"] == steps_o == K
+    assert st["t_final"] == t_o
+    err = l1(q, u_o)
+    assert np.all(err <= 1e-10), err
+    assert np.array_equal(q, u_o)               # expected bit-identical
+    assert np.array_equal(ret[-1], q)
+
+
+@pytest.mark.parametrize("fixture", sorted(os.path.basename(f) for f in
+                                           glob.glob(os.path.join(GOLDEN, "run_*.npz"))))
+def test_full_run_within_reference_band(gpu_lib, fixture):
+    z = load(fixture)
+    ndim = z["u0"].ndim - 1
+    s = systems.euler(ndim)
+    q = z["u0"].copy()
+    st = {}
+    bt = [("transitive", "periodic")[b] for b in z["bt"]]
+    pde_solver(q, float(z["tf"]), [float(z["L"])] * ndim, F=s.F, boundaryTypes=bt,
+               cfl=float(z["cfl"]), order=int(z["N"]), ndt=1, stiff=False,
+               max_steps=int(z["K"]), stats=st)
+    assert st["steps"] == int(z["K"])
+    err = l1(q, z["uK"])
+    assert np.all(err <= np.maximum(20 * z["band"], 1e-13)), (err, z["band"])
+
+
+def test_snapshots_follow_reference_rule(gpu_lib):
+    """ret[k] is the state when t first reaches (k+1) tf / ndt
+    (iterator.cpp:136-139); ret[ndt-1] the final state."""
+    u0 = workloads.sod(200)
+    s = systems.euler(1)
+    tf, ndt = 0.05, 5
+    u_o, ret_o, steps, t = ora.pde_solver("euler", u0, tf, [1.0], [0], 0.9, 2, ndt=ndt)
+    q = u0.copy()
+    ret = pde_solver(q, tf, [1.0], F=s.F, cfl=0.9, order=2, ndt=ndt, stiff=False)
+    assert np.array_equal(ret, ret_o)
+    assert np.array_equal(q, u_o)
+    assert abs(t - tf) <= 1e-15
+
+
+def test_in_place_final_state(gpu_lib):
+    u0 = workloads.sod(64)
+    q = u0.copy()
+    s = systems.euler(1)
+    ret = pde_solver(q, 0.01, [1.0], F=s.F, order=2, ndt=2, stiff=False)
+    assert not np.array_equal(q, u0)
+    assert np.array_equal(q, ret[-1])
+
+
+def test_nan_stops_with_reference_rows(gpu_lib):
+    u0 = workloads.sod(32)
+    u0[5, 0] = np.nan
+    q = u0.copy()
+    s = systems.euler(1)
+    st = {}
+    ret = pde_solver(q, 0.05, [1.0], F=s.F, order=2, ndt=3, stiff=False, stats=st)
+    assert st["nan_found"] == 1
+    assert np.isnan(ret[-1]).any()
+
+
+def test_weno_solver_api_shape(gpu_lib):
+    from pypde_gb300 import weno_solver
+    u = workloads.random_state("euler", (9, 8))
+    r = weno_solver(u, order=3)
+    assert r.shape == (5, 4, 3, 3, 4)
+    assert np.array_equal(r.reshape(-1, 4), ora.weno(u, 3))

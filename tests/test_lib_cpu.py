@@ -1,0 +1,77 @@
+"""CPU-only checks of the library and the host-side API: the C-ABI library
+loads without a GPU and exports every entry point of include/pypde_gb300.h;
+the host-side tables are bit-identical to the CPU restatement's; argument
+handling follows the reference (pypde/utils.py, pypde/solvers.py)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import ora
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "pypde_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_exports_header(gpu_lib):
+    names = header_functions()
+    assert "pde_solver" in names and "weno_solver" in names
+    for n in names:
+        assert hasattr(gpu_lib, n), n
+
+
+def test_library_loads_without_gpu_and_fails_loudly(gpu_lib):
+    """No CPU fallback: without a usable GPU the solver reports a CUDA error."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from pypde_gb300 import _lib, systems
+    from pypde_gb300.solvers import pde_solver
+    s = systems.euler(1)
+    with pytest.raises(_lib.PyPDEError) as e:
+        pde_solver(np.ones((8, 3)), 0.1, [1.0], F=s.F, stiff=False)
+    assert e.value.code == _lib.PYPDE_ERR_CUDA
+
+
+@pytest.mark.parametrize("N", range(1, 7))
+def test_tables_bitwise_equal_to_port(gpu_lib, N):
+    from pypde_gb300 import stages
+    assert np.array_equal(stages.tables(N), ora.tables(N))
+
+
+def test_boundary_parsing_matches_reference():
+    from pypde_gb300.utils import parse_boundary_types
+    assert list(parse_boundary_types("periodic", 2)) == [1, 1]
+    assert list(parse_boundary_types(["transitive", "periodic"], 2)) == [0, 1]
+    for bad in ("wall", ["periodic"], 3):
+        with pytest.raises(SystemExit):
+            parse_boundary_types(bad, 2)
+
+
+def test_builtin_python_callbacks_match_c_callbacks():
+    """The numpy twins of the built-in systems equal the C callbacks."""
+    from pypde_gb300 import systems, workloads
+    P = ora.port()
+    for name, ndim in (("euler", 1), ("euler", 2), ("euler", 3), ("cattaneo", 2), ("ncp", 2)):
+        s = getattr(systems, name)(ndim)
+        ps = ora.PortSystem(name, ndim)
+        fn = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.c_int)(ps.F.value)
+        q = workloads.random_state(name, (1,) * ndim, 3).reshape(-1)
+        for d in range(ndim):
+            out = np.zeros(s.V)
+            fn(ora.ptr(out), ora.ptr(q.copy()), ora.ptr(np.zeros(ndim * s.V)), d)
+            assert np.array_equal(out, s.F(q, d))
+
+
+def test_unknown_callback_is_rejected():
+    from pypde_gb300.solvers import pde_solver
+    with pytest.raises(NotImplementedError):
+        pde_solver(np.ones((8, 3)), 0.1, [1.0], F=lambda Q, d: Q, stiff=False)

@@ -1,0 +1,123 @@
+"""The CPU restatement (oracle/ader_oracle.c) against golden vectors produced
+by the reference itself (tests/golden/make_golden.py).
+
+Where a stage's output feeds the reference's forward-difference Jacobian
+(step 2^-26 max(|q|,1), src/eigs/NumericalDiff.h:6-44), a last-bit
+difference of the input state becomes a ~1e-8 relative difference of the
+eigenvalue.  The reference's Eigen kernels sum in an order that depends on
+memory alignment and solve its small systems by QR, so no restatement is
+bit-identical to it everywhere; the tolerances below say, per stage, how
+close a restatement can be, and full runs are checked against the
+reference's own sensitivity `band` (its L1 change when the initial state is
+perturbed by +-1 ulp).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, l1, load
+from oracle import ora
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("N", range(1, 7))
+def test_tables_match_reference(N):
+    z = load("tables.npz")
+    t = ora.tables(N)
+    nodes, wghts = t[:N], t[N:2 * N]
+    dervals, endvals = t[2 * N:2 * N + N * N], t[2 * N + N * N:2 * N + N * N + 2 * N]
+    if N <= 3:  # bit-identical where the configs live
+        for a, b in ((nodes, z[f"nodes{N}"]), (wghts, z[f"wghts{N}"]),
+                     (dervals, z[f"dervals{N}"]), (endvals, z[f"endvals{N}"])):
+            assert np.array_equal(a, b)
+    else:
+        np.testing.assert_allclose(nodes, z[f"nodes{N}"], rtol=1e-14)
+        np.testing.assert_allclose(wghts, z[f"wghts{N}"], rtol=1e-13)
+        np.testing.assert_allclose(dervals, z[f"dervals{N}"], rtol=1e-11, atol=1e-11)
+        np.testing.assert_allclose(endvals, z[f"endvals{N}"], rtol=1e-11, atol=1e-11)
+
+
+STAGES = sorted(os.path.basename(f) for f in glob.glob(os.path.join(GOLDEN, "stages_*.npz")))
+
+
+@pytest.mark.parametrize("fixture", STAGES)
+def test_stages_match_reference(fixture):
+    z = load(fixture)
+    system = fixture.split("_")[1]
+    N = int(z["N"])
+    ub = ora.boundaries(z["u"], N, z["bt"])
+    assert np.array_equal(ub.ravel(), z["ub"].ravel())  # copies only
+    w = ora.weno(z["ub"], N)
+    assert rel(w, z["w"]) < 1e-10  # precomputed inverses vs per-call QR
+    if "dt" not in z:
+        return
+    for count, key in ((7, "dt"), (3, "dt_count3")):
+        dt = ora.timestep(system, z["w"], z["dX"], N, 0.9, 1.0, 0.0, count)
+        assert abs(dt - z[key]) <= 1e-13 * z[key]
+    qh, its, _ = ora.predictor(system, z["w"], z["dX"], N, False, float(z["dt"]))
+    assert rel(qh, z["qh"]) < 1e-13
+    u1 = ora.fv(system, z["u"], z["qh"], z["dX"], N, float(z["dt"]))
+    # relative to the size of the update; FD-amplified alignment effects
+    assert rel(u1 - z["u"], z["u_fv"] - z["u"]) < 1e-8
+
+
+@pytest.mark.parametrize("fixture", ["cfl_ncp_16_N3.npz", "cfl_ncp_9x8_N2.npz"])
+def test_cfl_with_ncp_terms(fixture):
+    z = load(fixture)
+    dt = ora.timestep("ncp", z["w"], z["dX"], int(z["N"]), 0.9, 1.0, 0.0, 7)
+    assert abs(dt - z["dt"]) <= 1e-13 * z["dt"]
+
+
+RUNS = sorted(os.path.basename(f) for f in glob.glob(os.path.join(GOLDEN, "run_*.npz")))
+
+
+@pytest.mark.parametrize("fixture", RUNS)
+def test_runs_within_reference_band(fixture):
+    z = load(fixture)
+    ndim = z["u0"].ndim - 1
+    u, ret, steps, t = ora.pde_solver(str(z["system"]), z["u0"], float(z["tf"]),
+                                      [float(z["L"])] * ndim, z["bt"], float(z["cfl"]),
+                                      int(z["N"]), max_steps=int(z["K"]))
+    assert steps == int(z["K"])
+    # dt = CFL / max|eig| inherits the state's FD-amplified differences
+    assert abs(t - float(z["tf"])) <= 1e-8 * float(z["tf"])
+    err = l1(u, z["uK"])
+    band = z["band"]
+    assert np.all(err <= np.maximum(20 * band, 1e-13)), (err, band)
+
+
+def test_stiff_predictor_matches_tight_reference():
+    """Newton to ||obj||_inf <= 1e-12 against the reference's Newton-Krylov
+    predictor built with DG_TOL = 1e-12 (same fixed point)."""
+    z = load("stiff_cattaneo_6x5_N2.npz")
+    qh, its, mx = ora.predictor("cattaneo", z["w"], z["dX"], int(z["N"]), True, float(z["dt"]),
+                                1e-12)
+    assert rel(qh, z["qh"]) < 1e-10
+    assert mx < 50
+
+
+def test_eigen_solver_against_numpy():
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 3, 4, 5, 7, 9):
+        for _ in range(50):
+            a = rng.standard_normal((n, n))
+            if rng.random() < 0.3:
+                a = a + a.T
+            want = np.abs(np.linalg.eigvals(a)).max()
+            got = ora.port().ora_max_abs_eig(ora.ptr(a.copy()), n)
+            assert abs(got - want) <= 1e-12 * max(1.0, want)
+
+
+def test_slab_count_invariance():
+    """The reference's x-slab threading is bit-invariant (iterator.cpp:68-84);
+    so is the port's."""
+    from pypde_gb300 import workloads
+    u0 = workloads.shear(16)
+    a = ora.pde_solver("euler", u0, 1.0, [1.0, 1.0], [1, 1], 0.8, 2, max_steps=3, nthreads=1)
+    b = ora.pde_solver("euler", u0, 1.0, [1.0, 1.0], [1, 1], 0.8, 2, max_steps=3, nthreads=5)
+    assert np.array_equal(a[0], b[0])
