@@ -308,6 +308,12 @@ static int renorm_index(int ind, int N, int type, int bound) {
 void ora_boundaries(const double *u, const int *nX, int ndim, const int *bt,
                     int N, int V, double *ub) {
   int nb[3], inds[3] = {0, 0, 0};
+  for (int d = 0; d < ndim; d++)
+    if (bt[d] == 1 && nX[d] < N) { /* periodic wrap needs n >= N */
+      fprintf(stderr, "ora_boundaries: periodic axis %d has %d < N cells\n",
+              d, nX[d]);
+      abort();
+    }
   long ncell = 1;
   for (int d = 0; d < ndim; d++) {
     nb[d] = nX[d] + 2 * N;

@@ -15,6 +15,10 @@ template <class Sys, int N> KernelSet make_kernel_set() {
   k.faces.aot = (const void *)&k_faces<Sys, N>;
   k.centers.aot = (const void *)&k_centers<Sys, N>;
   k.gather.aot = (const void *)&k_gather<Sys, N>;
+  k.newton.aot = (const void *)&k_newton<Sys, N>;
+  k.newton_threads = NewtonCfg<Sys, N>::THREADS;
+  k.newton_cpb = NewtonCfg<Sys, N>::CPB;
+  k.newton_smem = NewtonCfg<Sys, N>::SMEM_BYTES;
   k.pred_threads = Cfg::THREADS;
   k.pred_cpb = Cfg::CPB;
   k.pred_smem = (size_t)Cfg::SMEM_DOUBLES * sizeof(double);

@@ -409,6 +409,314 @@ __global__ void k_predictor(const double *__restrict__ w,
 }
 
 // ---------------------------------------------------------------------
+// a7: stiff predictor.  Locally implicit Newton iteration on
+// obj(q) = rhs(q) - DG_U q (dg.cpp:128-154): the source is linearised
+// exactly at every space-time node, the fluxes are kept explicit.  Per
+// spatial node idx the (N V) x (N V) system
+//   A[(t,v),(k,w)] = dt W_t dS_v/dq_w(q_t) [t = k] - DG_MAT[t,k] [v = w]
+// is factored (LU, partial pivoting) and q <- q - A^{-1} obj(q) / prod W_idx.
+// Stops at ||obj||_inf <= tol, or at the rounding floor of obj
+// (16 eps max(|rhs|, |DG_U q|)).  Same operation order as the host
+// restatement's dg_newton.  Replaces the reference's Newton-Krylov
+// (dg.cpp:173-185, scipy/algos/newton_krylov.cpp), whose absolute
+// tolerance is 6e-6, by an iteration to tol (default 1e-12).
+// ---------------------------------------------------------------------
+constexpr int NEWTON_MAXIT = 200;
+
+template <class Sys, int N> struct NewtonCfg {
+  static constexpr int V = Sys::V, D = Sys::NDIM;
+  static constexpr int Nd = IPow<N, D>::value;
+  static constexpr int NT = N * Nd;
+  static constexpr int NL = N * V; // size of one spatial node's system
+  static constexpr int CELL_DOUBLES = NT * V * (2 + D) + Nd * NL * NL;
+  static constexpr int CELL_BYTES = CELL_DOUBLES * 8 + Nd * NL * 4;
+  static constexpr int BY_THREADS = (NT >= 128) ? 1 : 128 / NT;
+  static constexpr int BY_SMEM = (100 * 1024) / CELL_BYTES;
+  static constexpr int CPB_RAW = BY_THREADS < BY_SMEM ? BY_THREADS : BY_SMEM;
+  static constexpr int CPB = CPB_RAW < 1 ? 1 : CPB_RAW;
+  static constexpr int THREADS = CPB * NT;
+  static constexpr size_t SMEM_BYTES = (size_t)CPB * CELL_BYTES;
+};
+
+template <class Sys, int N>
+__global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
+                         Geom g, Tables T, const double *__restrict__ wprod_g,
+                         DevState *st, double tol) {
+  using Cfg = NewtonCfg<Sys, N>;
+  constexpr int V = Cfg::V, D = Cfg::D, Nd = Cfg::Nd, NT = Cfg::NT;
+  constexpr int NL = Cfg::NL, CPB = Cfg::CPB;
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  extern __shared__ double smem[];
+  double *s_q = smem;                        // [CPB][NT][V]
+  double *s_r = s_q + CPB * NT * V;          // [CPB][NT][V]
+  double *s_f = s_r + CPB * NT * V;          // [CPB][NT][D][V]
+  double *s_A = s_f + CPB * NT * D * V;      // [CPB][Nd][NL][NL]
+  int *s_piv = (int *)(s_A + CPB * Nd * NL * NL); // [CPB][Nd][NL]
+  __shared__ double wprod[Nd];
+  __shared__ double dervals[N * N];
+  __shared__ double dgmat[N * N];
+  __shared__ double wg[N];
+  __shared__ unsigned long long res_bits[CPB], scale_bits[CPB];
+  __shared__ int cell_done[CPB];
+  for (int i = threadIdx.x; i < Nd; i += blockDim.x)
+    wprod[i] = wprod_g[i];
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    dervals[i] = T.dervals[i];
+    dgmat[i] = T.dgmat[i];
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    wg[i] = T.wghts[i];
+
+  const int lc = threadIdx.x / NT;
+  const int node = threadIdx.x % NT;
+  const int t = node / Nd, idx = node % Nd;
+  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const bool valid = (lc < CPB) && (cell < g.Cw);
+  int digs[D > 0 ? D : 1];
+  {
+    int rem = idx;
+    for (int d = D - 1; d >= 0; d--) {
+      digs[d] = rem % N;
+      rem /= N;
+    }
+  }
+  double *q = s_q + (lc * NT) * V;
+  double *rr = s_r + (lc * NT) * V;
+  double *ff = s_f + (lc * NT) * D * V;
+  double Ww[V];
+  if (threadIdx.x < CPB)
+    cell_done[threadIdx.x] = 0;
+  __syncthreads();
+  if (valid) {
+    double cc = T.endvals[t];
+    for (int d = 0; d < D; d++)
+      cc *= wg[digs[d]];
+    const double *wc = w + (cell * Nd + idx) * V;
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      double x = wc[v];
+      Ww[v] = cc * x;
+      q[node * V + v] = x;
+    }
+  } else if (lc < CPB && node == 0) {
+    cell_done[lc] = 1;
+  }
+  int iters = 0;
+  bool failed = false;
+  for (int it = 0; it < NEWTON_MAXIT; it++) {
+    if (lc < CPB && node == 0) {
+      res_bits[lc] = 0ULL;
+      scale_bits[lc] = 0ULL;
+    }
+    __syncthreads();
+    const bool active = valid && !cell_done[lc];
+    double dq[D * V];
+    if (active) {
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        int sd = 1;
+        for (int e = d + 1; e < D; e++)
+          sd *= N;
+        int base = idx - digs[d] * sd;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+          double s = 0;
+#pragma unroll
+          for (int j = 0; j < N; j++)
+            s += dervals[digs[d] * N + j] * q[(t * Nd + base + j * sd) * V + v];
+          dq[d * V + v] = s / g.dX[d];
+        }
+      }
+      if (Sys::HAS_F) {
+#pragma unroll
+        for (int d = 0; d < D; d++)
+          Sys::F(ff + (node * D + d) * V, q + node * V, dq, d);
+      }
+    }
+    __syncthreads();
+    if (active) {
+      double r[V];
+      if (Sys::HAS_S)
+        Sys::S(r, q + node * V);
+      else
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          r[v] = 0.0;
+      double cc = wg[t];
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        if (Sys::HAS_B) {
+          double b[V * V];
+          Sys::B(b, q + node * V, d);
+#pragma unroll
+          for (int i = 0; i < V; i++) {
+            double acc = 0;
+#pragma unroll
+            for (int j = 0; j < V; j++)
+              acc += b[i * V + j] * dq[d * V + j];
+            r[i] -= acc;
+          }
+        }
+        if (Sys::HAS_F) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          int base = idx - digs[d] * sd;
+#pragma unroll
+          for (int v = 0; v < V; v++) {
+            double s = 0;
+#pragma unroll
+            for (int j = 0; j < N; j++)
+              s += dervals[digs[d] * N + j] *
+                   ff[((t * Nd + base + j * sd) * D + d) * V + v];
+            r[v] -= s / g.dX[d];
+          }
+        }
+        cc *= wg[digs[d]];
+      }
+      double res = 0, scale = 0;
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        double rv = (r[v] * cc) * dt + Ww[v];
+        double uq = 0;
+#pragma unroll
+        for (int k = 0; k < N; k++)
+          uq += dgmat[t * N + k] * q[(k * Nd + idx) * V + v];
+        uq *= wprod[idx];
+        double ov = rv - uq;
+        rr[node * V + v] = ov;
+        res = fmax(res, fabs(ov));
+        scale = fmax(scale, fmax(fabs(rv), fabs(uq)));
+      }
+      atomicMax(&res_bits[lc], (unsigned long long)__double_as_longlong(res));
+      atomicMax(&scale_bits[lc], (unsigned long long)__double_as_longlong(scale));
+    }
+    __syncthreads();
+    bool conv = false;
+    if (active) {
+      double res = __longlong_as_double((long long)res_bits[lc]);
+      double scale = __longlong_as_double((long long)scale_bits[lc]);
+      conv = (res <= tol || res <= 16 * DBL_EPS * scale);
+      if (!conv) {
+        // row block t of A for spatial node idx: the FD Jacobian of S
+        double *A = s_A + ((lc * Nd) + idx) * NL * NL;
+        double *qn = q + node * V;
+        double s0[V], s1[V];
+        if (Sys::HAS_S)
+          Sys::S(s0, qn);
+        for (int wv = 0; wv < V; wv++) {
+          if (Sys::HAS_S) {
+            double q0 = qn[wv];
+            double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
+            qn[wv] = q0 + h;
+            Sys::S(s1, qn);
+            qn[wv] = q0;
+          }
+          for (int v = 0; v < V; v++)
+            for (int k = 0; k < N; k++) {
+              double a = 0.0;
+              if (k == t && Sys::HAS_S)
+                a = dt * wg[t] * ((s1[v] - s0[v]) / (fmax(SQRT_EPS * fabs(qn[wv]),
+                                                           SQRT_EPS)));
+              A[(t * V + v) * NL + k * V + wv] = a;
+            }
+        }
+        for (int k = 0; k < N; k++)
+          for (int v = 0; v < V; v++)
+            A[(t * V + v) * NL + k * V + v] -= dgmat[t * N + k];
+      }
+    }
+    __syncthreads();
+    if (active && !conv && t == 0) {
+      // LU with partial pivoting of A, then solve for the update of node
+      // idx at every time node (lu_factor / lu_solve of the restatement)
+      double *A = s_A + ((lc * Nd) + idx) * NL * NL;
+      int *piv = s_piv + ((lc * Nd) + idx) * NL;
+      bool ok = true;
+      for (int k = 0; k < NL && ok; k++) {
+        int p = k;
+        for (int i = k + 1; i < NL; i++)
+          if (fabs(A[i * NL + k]) > fabs(A[p * NL + k]))
+            p = i;
+        piv[k] = p;
+        if (A[p * NL + k] == 0.0) {
+          ok = false;
+          break;
+        }
+        if (p != k)
+          for (int j = 0; j < NL; j++) {
+            double tmp = A[k * NL + j];
+            A[k * NL + j] = A[p * NL + j];
+            A[p * NL + j] = tmp;
+          }
+        for (int i = k + 1; i < NL; i++) {
+          double f = A[i * NL + k] / A[k * NL + k];
+          A[i * NL + k] = f;
+          for (int j = k + 1; j < NL; j++)
+            A[i * NL + j] -= f * A[k * NL + j];
+        }
+      }
+      if (!ok) {
+        failed = true;
+      } else {
+        double b[NL];
+        for (int tt = 0; tt < N; tt++)
+          for (int v = 0; v < V; v++)
+            b[tt * V + v] = rr[(tt * Nd + idx) * V + v] / wprod[idx];
+        for (int k = 0; k < NL; k++) {
+          if (piv[k] != k) {
+            double tmp = b[k];
+            b[k] = b[piv[k]];
+            b[piv[k]] = tmp;
+          }
+          for (int i = k + 1; i < NL; i++)
+            b[i] -= A[i * NL + k] * b[k];
+        }
+        for (int i = NL - 1; i >= 0; i--) {
+          double sacc = b[i];
+          for (int j = i + 1; j < NL; j++)
+            sacc -= A[i * NL + j] * b[j];
+          b[i] = sacc / A[i * NL + i];
+        }
+        for (int tt = 0; tt < N; tt++)
+          for (int v = 0; v < V; v++)
+            q[(tt * Nd + idx) * V + v] -= b[tt * V + v];
+      }
+    }
+    if (failed)
+      atomicOr(&cell_done[lc], 2);
+    __syncthreads();
+    if (active && node == 0) {
+      if (conv)
+        cell_done[lc] |= 1;
+      else
+        iters = it + 1;
+    }
+    if (active && conv && node == 0)
+      iters = it;
+    bool all_done = true;
+    if (node == 0 && lc < CPB)
+      all_done = cell_done[lc] != 0;
+    if (__syncthreads_and(all_done))
+      break;
+  }
+  if (valid) {
+    double *o = qh + (cell * NT + node) * V;
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      o[v] = q[node * V + v];
+    if (node == 0) {
+      atomicAdd(&st->pred_iters, (unsigned long long)iters);
+      atomicMax(&st->pred_max_iters, iters);
+      if (cell_done[lc] != 1)
+        atomicAdd(&st->pred_fail, 1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
 // a9/a10/a12: face fluxes (fv.cpp:124-198, fluxes.cpp:72-117).  One
 // thread per face point (direction d, face, time node t, transverse node
 // idx).  Faces of direction d are indexed by their low-side w-cell O with

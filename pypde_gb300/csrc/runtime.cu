@@ -286,6 +286,7 @@ struct StepCtx {
   FaceIndex fi;
   Tables T;
   int N, V, ring;
+  double tol;
   bool stiff, faces, centers;
   double *u, *uprev, *ub, *tmpA, *tmpB, *w, *qh, *contrib, *cen, *ringbuf,
       *wprod;
@@ -296,8 +297,9 @@ static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
   const KernelSet &k = *c.ks;
   Geom g = c.g;
   Tables T = c.T;
-  void *args[] = {(void *)&c.w, (void *)&c.qh, (void *)&g, (void *)&T,
-                  (void *)&c.wprod, (void *)&c.st};
+  double tol = c.tol;
+  void *args[] = {(void *)&c.w, (void *)&c.qh, (void *)&g,   (void *)&T,
+                  (void *)&c.wprod, (void *)&c.st, (void *)&tol};
   if (c.stiff) {
     unsigned blocks = (unsigned)((g.Cw + k.newton_cpb - 1) / k.newton_cpb);
     return launch(k.newton, dim3(blocks), dim3(k.newton_threads),
@@ -430,6 +432,23 @@ static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
   return cudaGetLastError();
 }
 
+// A periodic axis wraps ghost cells around once (boundaries.cpp:7-23), which
+// needs at least N cells on it; a transmissive axis has no such limit.
+static int check_grid(int ndim, const int *nX, const int *bt, int N) {
+  for (int d = 0; d < ndim; d++) {
+    if (nX[d] < 1) {
+      set_error("grid sizes must be positive");
+      return PYPDE_ERR_ARG;
+    }
+    if (bt && bt[d] == 1 && nX[d] < N) {
+      set_error("a periodic axis needs at least N cells (axis " +
+                std::to_string(d) + " has " + std::to_string(nX[d]) + ")");
+      return PYPDE_ERR_ARG;
+    }
+  }
+  return PYPDE_OK;
+}
+
 static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
                         int flux) {
   if (sys.ndim != ndim) {
@@ -468,6 +487,8 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   int rc = check_system(sys, a.ndim, a.N, a.stiff, a.flux);
   if (rc)
     return rc;
+  if ((rc = check_grid(a.ndim, a.nX, a.bt, a.N)))
+    return rc;
   if ((a.useF != sys.has_F) || (a.useB != sys.has_B) ||
       (a.useS != sys.has_S)) {
     set_error("useF/useB/useS do not match the callbacks of system " +
@@ -492,6 +513,7 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
     return PYPDE_ERR_ARG;
   }
   c.stiff = a.stiff;
+  c.tol = a.newton_tol;
   c.faces = sys.has_F || sys.has_B;
   c.centers = sys.has_B || sys.has_S;
   const int V = c.V, N = c.N, Nd = ipow(N, a.ndim);
@@ -682,9 +704,12 @@ int stage_boundaries(const double *u, const int *nX, int ndim, const int *bt,
     set_error("invalid arguments");
     return PYPDE_ERR_ARG;
   }
+  int rc = check_grid(ndim, nX, bt, N);
+  if (rc)
+    return rc;
   std::lock_guard<std::mutex> lock(g_mu);
   Arena *ar;
-  int rc = arena_for(0, &ar);
+  rc = arena_for(0, &ar);
   if (rc)
     return rc;
   Geom g;
@@ -810,7 +835,6 @@ int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
   DevState *st;
   if ((rc = put_state(ar, &st, 0, 1, 1, 0, dt)))
     return rc;
-  (void)tol;
   StepCtx c;
   std::memset(&c, 0, sizeof(c));
   c.sys = &sys;
@@ -822,6 +846,7 @@ int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
   c.N = N;
   c.V = sys.V;
   c.stiff = stiff;
+  c.tol = tol;
   std::vector<double> wp(Nd);
   make_wprod(c.T, ndim, wp.data());
   CK(ensure(ar->w, nrows * sys.V * 8));

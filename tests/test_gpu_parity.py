@@ -23,7 +23,8 @@ CASES = [("euler", (40,), 2, [0]), ("euler", (40,), 3, [1]), ("euler", (17,), 1,
          ("euler", (12, 10), 2, [1, 0]), ("euler", (12, 10), 3, [1, 1]),
          ("euler", (5, 6, 4), 2, [1, 0, 1]), ("euler", (4, 3, 5), 3, [0, 1, 1]),
          ("cattaneo", (10, 8), 2, [1, 1]), ("ncp", (16,), 3, [0]), ("ncp", (9, 8), 2, [1, 0]),
-         ("burgers2", (24,), 2, [1]), ("euler", (1,), 2, [1]), ("euler", (2, 1), 2, [1, 1])]
+         ("burgers2", (24,), 2, [1]), ("euler", (1,), 2, [0]), ("euler", (2, 1), 2, [1, 0]),
+         ("euler", (2, 3), 2, [1, 1])]
 
 
 def _ids(c):
@@ -59,6 +60,20 @@ def test_stages_bitwise(gpu_lib, case):
     u_o = ora.fv(system, u, qh_o, dX, N, dt_o)
     u_g = stages.fv(system, u, qh_o, dX, N, dt_o)
     assert np.array_equal(u_g, u_o)
+
+
+def test_periodic_axis_shorter_than_order_is_rejected(gpu_lib):
+    """The periodic ghost fill wraps once (boundaries.cpp:7-23): an axis
+    with fewer than N cells cannot be padded and is refused before any
+    device work."""
+    from pypde_gb300 import _lib
+    with pytest.raises(_lib.PyPDEError) as e:
+        stages.boundaries(np.ones((1, 4)), 2, [1])
+    assert e.value.code == _lib.PYPDE_ERR_ARG
+    s = systems.euler(1)
+    with pytest.raises(_lib.PyPDEError):
+        pde_solver(np.ones((2, 3)), 0.1, [1.0], F=s.F, boundaryTypes="periodic", order=3,
+                   stiff=False)
 
 
 def test_dt_clipped_to_tf(gpu_lib):
@@ -166,3 +181,51 @@ def test_weno_solver_api_shape(gpu_lib):
     r = weno_solver(u, order=3)
     assert r.shape == (5, 4, 3, 3, 4)
     assert np.array_equal(r.reshape(-1, 4), ora.weno(u, 3))
+
+
+STIFF_CASES = [("cattaneo", (10, 8), 2), ("cattaneo", (6, 5, 4), 2), ("cattaneo", (9, 7), 3),
+               ("ncp", (12,), 2), ("euler", (8, 6), 2)]
+
+
+@pytest.mark.parametrize("case", STIFF_CASES, ids=[f"{c[0]}-{len(c[1])}d-N{c[2]}"
+                                                   for c in STIFF_CASES])
+def test_newton_predictor_bitwise(gpu_lib, case):
+    """The locally implicit Newton predictor equals the restatement's bit for
+    bit, iteration counts included; stiff relaxation times 1e-4..1e-2."""
+    system, shape, N = case
+    u = workloads.random_state(system, shape, 2)
+    dX = [1.0 / n for n in shape]
+    bt = [1] * len(shape)
+    w = ora.weno(ora.boundaries(u, N, bt), N)
+    dt = ora.timestep(system, w, dX, N, 0.9, 1.0, 0.0, 9)
+    qh_o, its_o, mx_o = ora.predictor(system, w, dX, N, True, dt, 1e-12)
+    qh_g, st = stages.predictor(system, w, dX, N, True, dt, 1e-12)
+    assert np.array_equal(qh_g, qh_o)
+    assert st["pred_iters"] == its_o and st["pred_max_iters"] == mx_o
+    assert st["pred_fail"] == 0
+
+
+def test_newton_against_tight_reference(gpu_lib):
+    """Same fixed point as the reference's Newton-Krylov predictor built with
+    DG_TOL = 1e-12 (tests/golden/make_golden.py)."""
+    z = load("stiff_cattaneo_6x5_N2.npz")
+    qh, st = stages.predictor("cattaneo", z["w"], z["dX"], int(z["N"]), True, float(z["dt"]),
+                              1e-12)
+    assert np.abs(qh - z["qh"]).max() <= 1e-10 * np.abs(z["qh"]).max()
+
+
+def test_stiff_run_matches_port(gpu_lib):
+    """The stiff relaxation workload (tau down to 1e-7, dt/tau >> 1): GPU and
+    restatement bit-identical after K steps."""
+    u0 = workloads.relaxation(24, 2, seed=3)
+    s = systems.cattaneo(2)
+    K = 4
+    u_o, _, steps, t_o = ora.pde_solver("cattaneo", u0, 10.0, [1.0, 1.0], [1, 1], 0.8, 2,
+                                        stiff=True, max_steps=K)
+    q = u0.copy()
+    st = {}
+    pde_solver(q, 10.0, [1.0, 1.0], F=s.F, S=s.S, boundaryTypes="periodic", cfl=0.8, order=2,
+               ndt=1, stiff=True, max_steps=K, stats=st)
+    assert st["steps"] == steps == K and st["pred_fail"] == 0
+    assert st["t_final"] == t_o
+    assert np.array_equal(q, u_o)
