@@ -1245,6 +1245,7 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
   double r[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
   double A[ORA_MAXN * ORA_MAXV * ORA_MAXN * ORA_MAXV], b[ORA_MAXN * ORA_MAXV];
   int piv[ORA_MAXN * ORA_MAXV];
+  int failed = 0;
   for (int it = 0; it < NEWTON_MAXIT; it++) {
     dg_rhs(c, q, Ww, dt, r, s);
     double res = 0, scale = 0;
@@ -1286,8 +1287,10 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
           for (int v = 0; v < V; v++)
             A[(t * V + v) * nl + k * V + v] -= c->T.dgmat[t * N + k];
       }
-      if (lu_factor(A, nl, piv) != 0)
-        return -1;
+      if (lu_factor(A, nl, piv) != 0) { /* singular: keep this node, */
+        failed = 1;                        /* finish the others, stop    */
+        continue;
+      }
       for (int t = 0; t < N; t++)
         for (int v = 0; v < V; v++)
           b[t * V + v] = r[(t * Nd + idx) * V + v] / c->wprod[idx];
@@ -1296,6 +1299,8 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
         for (int v = 0; v < V; v++)
           q[(t * Nd + idx) * V + v] -= b[t * V + v];
     }
+    if (failed)
+      return -1;
   }
   (void)n;
   return NEWTON_MAXIT;

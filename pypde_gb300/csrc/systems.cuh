@@ -14,9 +14,9 @@
 // contraction):
 //   Euler<D>     V = D+2   (rho, m_0..m_{D-1}, E), gamma = 1.4
 //   Cattaneo<D>  V = 2D+3  Euler + relaxing heat flux q + passive
-//                s = log10(tau); T = p/rho, kappa = 1e-2, 1/tau = 10^-s;
-//                F_d adds q_d to the energy flux and kappa T/tau to q_d;
-//                S_q = -q/tau
+//                s = log10(tau); T = p/rho; F_d adds q_d to the energy flux
+//                and kappa_h T to q_d (kappa_h = kappa/tau_ref = 1); the
+//                local tau (1/tau = 10^-s) enters only S_q = -q/tau
 //   Ncp<D>       V = 3, F, B and S (a non-conservative test system)
 //   Burgers2     V = 1, D = 1, second-order form F(Q, dQ, d)
 #pragma once
@@ -75,13 +75,12 @@ template <int D> struct Cattaneo {
   static __device__ __forceinline__ void F(double *out, const double *Q,
                                            const double *, int d) {
     double p = EulerCore<D>::flux(out, Q, d);
-    double inv_tau = pow10_portable(-Q[2 * D + 2]);
     double T = p / Q[0];
     out[D + 1] += Q[D + 2 + d];
 #pragma unroll
     for (int i = 0; i < D; i++)
       out[D + 2 + i] = 0.0;
-    out[D + 2 + d] = 1e-2 * T * inv_tau;
+    out[D + 2 + d] = 1.0 * T;
     out[2 * D + 2] = 0.0;
   }
   static __device__ __forceinline__ void B(double *, const double *, int) {}

@@ -9,7 +9,8 @@ device code.  Both evaluate the same formulas in the same operation order.
 
     euler(ndim)     V = ndim+2, Q = (rho, m_0..m_{ndim-1}, E), gamma = 1.4
     cattaneo(ndim)  V = 2 ndim+3: Euler + relaxing heat flux q + passive
-                    s = log10(tau); T = p/rho, kappa = 1e-2; S_q = -q/tau
+                    s = log10(tau); T = p/rho; heat-flux flux kappa_h T with
+                    kappa_h = kappa/tau_ref = 1e-2/1e-2; S_q = -q/tau
     ncp(ndim)       V = 3, a non-conservative test system with F, B and S
     burgers2()      V = 1, viscous Burgers F(Q, DQ, d) (second order)
 """
@@ -19,7 +20,7 @@ from typing import Callable, Optional
 import numpy as np
 
 GAMMA = 1.4
-KAPPA = 1e-2
+KAPPA_H = 1.0  # kappa / tau_ref = 1e-2 / 1e-2
 
 
 def pow10_portable(x):
@@ -78,11 +79,10 @@ def cattaneo(ndim):
 
     def F(Q, d):
         out, p = _euler_flux(Q, ndim, d)
-        inv_tau = pow10_portable(-Q[2 * ndim + 2])
         T = p / Q[0]
         out[ndim + 1] += Q[ndim + 2 + d]
         out[ndim + 2:2 * ndim + 2] = 0.0
-        out[ndim + 2 + d] = KAPPA * T * inv_tau
+        out[ndim + 2 + d] = KAPPA_H * T
         out[2 * ndim + 2] = 0.0
         return out
 
