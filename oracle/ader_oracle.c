@@ -710,7 +710,7 @@ static int francis(double *a, int n, double *wr, double *wi, int wantt,
   return 0;
 }
 
-double ora_max_abs_eig(double *a, int n) {
+double ora_max_abs_eig_qr(double *a, int n) {
   double wr[ORA_MAXV], wi[ORA_MAXV];
   if (n == 1)
     return fabs(a[0]);
@@ -724,6 +724,313 @@ double ora_max_abs_eig(double *a, int n) {
       m = r;
   }
   return m;
+}
+
+
+/* ---- FP32 eigenvalues: the shifts of the FP64 refinement below.  Same
+ * Householder + Francis algorithm as the FP64 version, in float. ---- */
+#define AF(i, j) a[(i) * n + (j)]
+static void hessenberg_f(float *a, int n) {
+  for (int k = 0; k < n - 2; k++) {
+    float v[ORA_MAXV], alpha = 0, scale = 0;
+    for (int i = k + 1; i < n; i++)
+      scale += fabsf(AF(i, k));
+    if (scale == 0.0f)
+      continue;
+    for (int i = k + 1; i < n; i++) {
+      v[i] = AF(i, k) / scale;
+      alpha += v[i] * v[i];
+    }
+    float g = sqrtf(alpha);
+    if (v[k + 1] > 0)
+      g = -g;
+    float h = alpha - v[k + 1] * g;
+    v[k + 1] -= g;
+    for (int j = k; j < n; j++) {
+      float s = 0;
+      for (int i = k + 1; i < n; i++)
+        s += v[i] * AF(i, j);
+      s /= h;
+      for (int i = k + 1; i < n; i++)
+        AF(i, j) -= s * v[i];
+    }
+    for (int i = 0; i < n; i++) {
+      float s = 0;
+      for (int j = k + 1; j < n; j++)
+        s += AF(i, j) * v[j];
+      s /= h;
+      for (int j = k + 1; j < n; j++)
+        AF(i, j) -= s * v[j];
+    }
+    AF(k + 1, k) = g * scale;
+    for (int i = k + 2; i < n; i++)
+      AF(i, k) = 0.0f;
+  }
+}
+
+static int francis_vals_f(float *a, int n, float *wr, float *wi) {
+  const float eps = 1.1920929e-07f;
+  float norm = 0;
+  for (int i = 0; i < n; i++)
+    for (int j = (i > 0 ? i - 1 : 0); j < n; j++)
+      norm += fabsf(AF(i, j));
+  int hi = n - 1, its = 0, total = 0;
+  float exshift = 0.0f;
+  while (hi >= 0) {
+    int l;
+    for (l = hi; l > 0; l--) {
+      float s = fabsf(AF(l - 1, l - 1)) + fabsf(AF(l, l));
+      if (s == 0.0f)
+        s = norm;
+      if (fabsf(AF(l, l - 1)) <= eps * s) {
+        AF(l, l - 1) = 0.0f;
+        break;
+      }
+    }
+    if (l == hi) {
+      wr[hi] = AF(hi, hi) + exshift;
+      wi[hi] = 0.0f;
+      hi--;
+      its = 0;
+      continue;
+    }
+    if (l == hi - 1) {
+      float p = 0.5f * (AF(hi - 1, hi - 1) - AF(hi, hi));
+      float qq = p * p + AF(hi, hi - 1) * AF(hi - 1, hi);
+      float zz = sqrtf(fabsf(qq));
+      float x = AF(hi, hi) + exshift;
+      if (qq >= 0.0f) {
+        zz = (p >= 0) ? p + zz : p - zz;
+        wr[hi - 1] = x + zz;
+        wr[hi] = (zz != 0.0f) ? x - AF(hi, hi - 1) * AF(hi - 1, hi) / zz
+                              : x + zz;
+        wi[hi - 1] = wi[hi] = 0.0f;
+      } else {
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = zz;
+        wi[hi] = -zz;
+      }
+      hi -= 2;
+      its = 0;
+      continue;
+    }
+    float x = AF(hi, hi), y = AF(hi - 1, hi - 1);
+    float w = AF(hi, hi - 1) * AF(hi - 1, hi);
+    if (its == 10 || its == 20) {
+      exshift += x;
+      for (int i = 0; i <= hi; i++)
+        AF(i, i) -= x;
+      float s = fabsf(AF(hi, hi - 1)) + fabsf(AF(hi - 1, hi - 2));
+      x = y = 0.75f * s;
+      w = -0.4375f * s * s;
+    }
+    its++;
+    if (++total > 40 * n)
+      return -1;
+    int m;
+    float p = 0, q = 0, r = 0;
+    for (m = hi - 2; m >= l; m--) {
+      float zz = AF(m, m);
+      float rr = x - zz, ss = y - zz;
+      p = (rr * ss - w) / AF(m + 1, m) + AF(m, m + 1);
+      q = AF(m + 1, m + 1) - zz - rr - ss;
+      r = AF(m + 2, m + 1);
+      float s = fabsf(p) + fabsf(q) + fabsf(r);
+      p /= s;
+      q /= s;
+      r /= s;
+      if (m == l)
+        break;
+      float u = fabsf(AF(m, m - 1)) * (fabsf(q) + fabsf(r));
+      float vv = fabsf(p) * (fabsf(AF(m - 1, m - 1)) + fabsf(zz) +
+                             fabsf(AF(m + 1, m + 1)));
+      if (u <= eps * vv)
+        break;
+    }
+    for (int i = m + 2; i <= hi; i++) {
+      AF(i, i - 2) = 0.0f;
+      if (i > m + 2)
+        AF(i, i - 3) = 0.0f;
+    }
+    for (int k = m; k <= hi - 1; k++) {
+      int notlast = (k != hi - 1);
+      if (k != m) {
+        p = AF(k, k - 1);
+        q = AF(k + 1, k - 1);
+        r = notlast ? AF(k + 2, k - 1) : 0.0f;
+        x = fabsf(p) + fabsf(q) + fabsf(r);
+        if (x == 0.0f)
+          continue;
+        p /= x;
+        q /= x;
+        r /= x;
+      }
+      float s = sqrtf(p * p + q * q + r * r);
+      if (p < 0)
+        s = -s;
+      if (k != m)
+        AF(k, k - 1) = -s * x;
+      else if (l != m)
+        AF(k, k - 1) = -AF(k, k - 1);
+      p += s;
+      x = p / s;
+      y = q / s;
+      float zz = r / s;
+      q /= p;
+      r /= p;
+      for (int j = k; j <= hi; j++) {
+        float pp = AF(k, j) + q * AF(k + 1, j);
+        if (notlast) {
+          pp += r * AF(k + 2, j);
+          AF(k + 2, j) -= pp * zz;
+        }
+        AF(k + 1, j) -= pp * y;
+        AF(k, j) -= pp * x;
+      }
+      int ihi = (hi < k + 3) ? hi : k + 3;
+      for (int i = l; i <= ihi; i++) {
+        float pp = x * AF(i, k) + y * AF(i, k + 1);
+        if (notlast) {
+          pp += zz * AF(i, k + 2);
+          AF(i, k + 2) -= pp * r;
+        }
+        AF(i, k + 1) -= pp * q;
+        AF(i, k) -= pp;
+      }
+    }
+  }
+  return 0;
+}
+#undef AF
+
+/* One real eigenvalue of M refined in FP64 from the FP32 shift lam0:
+ * LU (partial pivoting, FMA) of M - lam0 I, five inverse-iteration steps
+ * from x = (1, ..., 1) with max-normalisation, then the Rayleigh quotient
+ * lam0 + x.(M - lam0 I)x / x.x.  Returns 0, or -1 on an exactly singular
+ * pivot (the caller then falls back to the FP64 QR). */
+static int refine_real(const double *M, int n, double lam0, double *lam) {
+  double A[ORA_MAXV * ORA_MAXV], ud[ORA_MAXV], x[ORA_MAXV];
+  int piv[ORA_MAXV];
+  for (int i = 0; i < n * n; i++)
+    A[i] = M[i];
+  for (int i = 0; i < n; i++)
+    A[i * n + i] = M[i * n + i] - lam0;
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    for (int i = k + 1; i < n; i++)
+      if (fabs(A[i * n + k]) > fabs(A[p * n + k]))
+        p = i;
+    piv[k] = p;
+    if (A[p * n + k] == 0.0)
+      return -1;
+    if (p != k)
+      for (int j = 0; j < n; j++) {
+        double t = A[k * n + j];
+        A[k * n + j] = A[p * n + j];
+        A[p * n + j] = t;
+      }
+    ud[k] = 1.0 / A[k * n + k];
+    for (int i = k + 1; i < n; i++) {
+      double f = A[i * n + k] * ud[k];
+      A[i * n + k] = f;
+      for (int j = k + 1; j < n; j++)
+        A[i * n + j] = fma(-f, A[k * n + j], A[i * n + j]);
+    }
+  }
+  for (int i = 0; i < n; i++)
+    x[i] = 1.0;
+  for (int it = 0; it < 5; it++) {
+    /* rows were swapped whole (L included): permute first, then solve */
+    for (int k = 0; k < n; k++)
+      if (piv[k] != k) {
+        double t = x[k];
+        x[k] = x[piv[k]];
+        x[piv[k]] = t;
+      }
+    for (int k = 0; k < n; k++)
+      for (int i = k + 1; i < n; i++)
+        x[i] = fma(-A[i * n + k], x[k], x[i]);
+    double mx = 0;
+    for (int i = n - 1; i >= 0; i--) {
+      double s = x[i];
+      for (int j = i + 1; j < n; j++)
+        s = fma(-A[i * n + j], x[j], s);
+      x[i] = s * ud[i];
+      mx = fmax(mx, fabs(x[i]));
+    }
+    if (!(mx > 0.0) || mx != mx)
+      return -1;
+    double inv = 1.0 / mx;
+    for (int i = 0; i < n; i++)
+      x[i] *= inv;
+  }
+  double num = 0, den = 0;
+  for (int i = 0; i < n; i++) {
+    double r = -lam0 * x[i];
+    for (int j = 0; j < n; j++)
+      r = fma(M[i * n + j], x[j], r);
+    num = fma(x[i], r, num);
+    den = fma(x[i], x[i], den);
+  }
+  *lam = lam0 + num / den;
+  return 0;
+}
+
+/* max |eigenvalue| of a general real matrix (a4).  FP32 eigenvalues pick
+ * the candidates of largest modulus (within 2^-10 of the largest); each is
+ * refined in FP64 (refine_real).  Complex or nearly coincident candidates,
+ * a failed FP32 iteration, a singular shift or a refinement that moves the
+ * shift by more than 1e-5 relative (an ill-conditioned FP32 spectrum)
+ * fall back to the FP64
+ * Francis QR (ora_max_abs_eig_qr).  Result accurate to ~1e-15 relative for
+ * well-conditioned eigenvalues, like a backward-stable QR. */
+double ora_max_abs_eig(double *a, int n) {
+  if (n == 1)
+    return fabs(a[0]);
+  float af[ORA_MAXV * ORA_MAXV], wr[ORA_MAXV], wi[ORA_MAXV];
+  double M[ORA_MAXV * ORA_MAXV];
+  for (int i = 0; i < n * n; i++) {
+    M[i] = a[i];
+    af[i] = (float)a[i];
+  }
+  hessenberg_f(af, n);
+  if (francis_vals_f(af, n, wr, wi) != 0)
+    return ora_max_abs_eig_qr(a, n);
+  float mf = 0;
+  for (int i = 0; i < n; i++) {
+    float m = (wi[i] == 0.0f) ? fabsf(wr[i]) : sqrtf(wr[i] * wr[i] + wi[i] * wi[i]);
+    if (m > mf)
+      mf = m;
+  }
+  if (!(mf > 0.0f) || mf != mf || mf > 3.0e38f)
+    return ora_max_abs_eig_qr(a, n);
+  float thr = mf - mf * 0.0009765625f;
+  int cand[ORA_MAXV], nc = 0;
+  for (int i = 0; i < n; i++) {
+    float m = (wi[i] == 0.0f) ? fabsf(wr[i]) : sqrtf(wr[i] * wr[i] + wi[i] * wi[i]);
+    if (m >= thr) {
+      if (wi[i] != 0.0f)
+        return ora_max_abs_eig_qr(a, n);
+      cand[nc++] = i;
+    }
+  }
+  for (int i = 0; i < nc; i++)
+    for (int j = i + 1; j < nc; j++)
+      if (fabsf(wr[cand[i]] - wr[cand[j]]) <= 1e-4f * mf)
+        return ora_max_abs_eig_qr(a, n);
+  double best = 0;
+  for (int i = 0; i < nc; i++) {
+    double lam;
+    double lam0 = (double)wr[cand[i]];
+    if (refine_real(M, n, lam0, &lam) != 0)
+      return ora_max_abs_eig_qr(a, n);
+    /* a shift that moved by more than ~80 float ulps came from an
+     * ill-conditioned FP32 spectrum: its ranking cannot be trusted */
+    if (!(fabs(lam - lam0) <= 1e-5 * fabs(lam0)))
+      return ora_max_abs_eig_qr(a, n);
+    best = fmax(best, fabs(lam));
+  }
+  return best;
 }
 
 /* Eigenvectors of the quasi-triangular T by back substitution, then
@@ -951,8 +1258,9 @@ static void fd_jacobian(const ctx_t *c, double *jac, double *q, double *dq,
     *qi += h;
     c->F(v2, q, dq, d);
     *qi = qi0;
+    double ih = 1.0 / h; /* one division per column */
     for (int r = 0; r < V; r++)
-      jac[r * V + i] = (v2[r] - v1[r]) / h;
+      jac[r * V + i] = (v2[r] - v1[r]) * ih;
   }
 }
 
@@ -1213,16 +1521,18 @@ static int lu_factor(double *a, int n, int *piv) {
   }
   return 0;
 }
+/* lu_factor swaps whole rows (L included), so the permutation is applied
+ * to b first, then the unit-lower and upper triangular solves. */
 static void lu_solve(const double *a, int n, const int *piv, double *b) {
-  for (int k = 0; k < n; k++) {
+  for (int k = 0; k < n; k++)
     if (piv[k] != k) {
       double t = b[k];
       b[k] = b[piv[k]];
       b[piv[k]] = t;
     }
+  for (int k = 0; k < n; k++)
     for (int i = k + 1; i < n; i++)
       b[i] -= a[i * n + k] * b[k];
-  }
   for (int i = n - 1; i >= 0; i--) {
     double s = b[i];
     for (int j = i + 1; j < n; j++)

@@ -80,8 +80,11 @@ long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
                     int V, int ndt, int secondOrder, double *ret, int nThreads,
                     long maxsteps, double newton_tol, double *t_out);
 
-/* max |eigenvalue| of a general real n x n row-major matrix (destroys a). */
+/* max |eigenvalue| of a general real n x n row-major matrix: FP32
+ * eigenvalues refined in FP64 (ora_max_abs_eig), or the FP64 Francis QR
+ * (ora_max_abs_eig_qr, destroys a). */
 double ora_max_abs_eig(double *a, int n);
+double ora_max_abs_eig_qr(double *a, int n);
 /* Real eigen-decomposition: wr/wi eigenvalues, vr/vi eigenvectors (columns,
  * row-major n x n).  Returns 0 on success. */
 int ora_eig(const double *a, int n, double *wr, double *wi, double *vr,

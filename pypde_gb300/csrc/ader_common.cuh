@@ -99,7 +99,7 @@ __device__ __forceinline__ void hessenberg_inplace(double *a) {
 }
 
 template <int V>
-__device__ __noinline__ double max_abs_eig(double *a) {
+__device__ __noinline__ double max_abs_eig_qr(double *a) {
   if (V == 1)
     return fabs(a[0]);
   hessenberg_inplace<V>(a);
@@ -244,8 +244,321 @@ __device__ __noinline__ double max_abs_eig(double *a) {
 #undef A_
 }
 
+// ---------------------------------------------------------------------
+// FP32 eigenvalues (Householder + Francis, same algorithm in float): the
+// shifts of the FP64 refinement.  FP32 runs on this part at ~70x the FP64
+// rate, so the QR sweeps cost next to nothing; only the refinement below
+// uses the FP64 pipe.  Returns 0, or -1 if the iteration fails.
+// ---------------------------------------------------------------------
+template <int V>
+__device__ __noinline__ int eig_vals_f(float *a, float *wr, float *wi) {
+#define AF(i, j) a[(i) * V + (j)]
+  for (int k = 0; k < V - 2; k++) {
+    float v[V];
+    float alpha = 0, scale = 0;
+    for (int i = k + 1; i < V; i++)
+      scale += fabsf(AF(i, k));
+    if (scale == 0.0f)
+      continue;
+    for (int i = k + 1; i < V; i++) {
+      v[i] = AF(i, k) / scale;
+      alpha += v[i] * v[i];
+    }
+    float g = sqrtf(alpha);
+    if (v[k + 1] > 0)
+      g = -g;
+    float h = alpha - v[k + 1] * g;
+    v[k + 1] -= g;
+    for (int j = k; j < V; j++) {
+      float s = 0;
+      for (int i = k + 1; i < V; i++)
+        s += v[i] * AF(i, j);
+      s /= h;
+      for (int i = k + 1; i < V; i++)
+        AF(i, j) -= s * v[i];
+    }
+    for (int i = 0; i < V; i++) {
+      float s = 0;
+      for (int j = k + 1; j < V; j++)
+        s += AF(i, j) * v[j];
+      s /= h;
+      for (int j = k + 1; j < V; j++)
+        AF(i, j) -= s * v[j];
+    }
+    AF(k + 1, k) = g * scale;
+    for (int i = k + 2; i < V; i++)
+      AF(i, k) = 0.0f;
+  }
+  const float eps = 1.1920929e-07f;
+  float norm = 0;
+  for (int i = 0; i < V; i++)
+    for (int j = (i > 0 ? i - 1 : 0); j < V; j++)
+      norm += fabsf(AF(i, j));
+  int hi = V - 1, its = 0, total = 0;
+  float exshift = 0.0f;
+  while (hi >= 0) {
+    int l;
+    for (l = hi; l > 0; l--) {
+      float s = fabsf(AF(l - 1, l - 1)) + fabsf(AF(l, l));
+      if (s == 0.0f)
+        s = norm;
+      if (fabsf(AF(l, l - 1)) <= eps * s) {
+        AF(l, l - 1) = 0.0f;
+        break;
+      }
+    }
+    if (l == hi) {
+      wr[hi] = AF(hi, hi) + exshift;
+      wi[hi] = 0.0f;
+      hi--;
+      its = 0;
+      continue;
+    }
+    if (l == hi - 1) {
+      float p = 0.5f * (AF(hi - 1, hi - 1) - AF(hi, hi));
+      float qq = p * p + AF(hi, hi - 1) * AF(hi - 1, hi);
+      float zz = sqrtf(fabsf(qq));
+      float x = AF(hi, hi) + exshift;
+      if (qq >= 0.0f) {
+        zz = (p >= 0) ? p + zz : p - zz;
+        wr[hi - 1] = x + zz;
+        wr[hi] = (zz != 0.0f) ? x - AF(hi, hi - 1) * AF(hi - 1, hi) / zz
+                              : x + zz;
+        wi[hi - 1] = wi[hi] = 0.0f;
+      } else {
+        wr[hi - 1] = wr[hi] = x + p;
+        wi[hi - 1] = zz;
+        wi[hi] = -zz;
+      }
+      hi -= 2;
+      its = 0;
+      continue;
+    }
+    float x = AF(hi, hi), y = AF(hi - 1, hi - 1);
+    float w = AF(hi, hi - 1) * AF(hi - 1, hi);
+    if (its == 10 || its == 20) {
+      exshift += x;
+      for (int i = 0; i <= hi; i++)
+        AF(i, i) -= x;
+      float s = fabsf(AF(hi, hi - 1)) + fabsf(AF(hi - 1, hi - 2));
+      x = y = 0.75f * s;
+      w = -0.4375f * s * s;
+    }
+    its++;
+    if (++total > 40 * V)
+      return -1;
+    int m;
+    float p = 0, q = 0, r = 0;
+    for (m = hi - 2; m >= l; m--) {
+      float zz = AF(m, m);
+      float rr = x - zz, ss = y - zz;
+      p = (rr * ss - w) / AF(m + 1, m) + AF(m, m + 1);
+      q = AF(m + 1, m + 1) - zz - rr - ss;
+      r = AF(m + 2, m + 1);
+      float s = fabsf(p) + fabsf(q) + fabsf(r);
+      p /= s;
+      q /= s;
+      r /= s;
+      if (m == l)
+        break;
+      float u = fabsf(AF(m, m - 1)) * (fabsf(q) + fabsf(r));
+      float vv = fabsf(p) * (fabsf(AF(m - 1, m - 1)) + fabsf(zz) +
+                             fabsf(AF(m + 1, m + 1)));
+      if (u <= eps * vv)
+        break;
+    }
+    for (int i = m + 2; i <= hi; i++) {
+      AF(i, i - 2) = 0.0f;
+      if (i > m + 2)
+        AF(i, i - 3) = 0.0f;
+    }
+    for (int k = m; k <= hi - 1; k++) {
+      bool notlast = (k != hi - 1);
+      if (k != m) {
+        p = AF(k, k - 1);
+        q = AF(k + 1, k - 1);
+        r = notlast ? AF(k + 2, k - 1) : 0.0f;
+        x = fabsf(p) + fabsf(q) + fabsf(r);
+        if (x == 0.0f)
+          continue;
+        p /= x;
+        q /= x;
+        r /= x;
+      }
+      float s = sqrtf(p * p + q * q + r * r);
+      if (p < 0)
+        s = -s;
+      if (k != m)
+        AF(k, k - 1) = -s * x;
+      else if (l != m)
+        AF(k, k - 1) = -AF(k, k - 1);
+      p += s;
+      x = p / s;
+      y = q / s;
+      float zz = r / s;
+      q /= p;
+      r /= p;
+      for (int j = k; j <= hi; j++) {
+        float pp = AF(k, j) + q * AF(k + 1, j);
+        if (notlast) {
+          pp += r * AF(k + 2, j);
+          AF(k + 2, j) -= pp * zz;
+        }
+        AF(k + 1, j) -= pp * y;
+        AF(k, j) -= pp * x;
+      }
+      int ihi = (hi < k + 3) ? hi : k + 3;
+      for (int i = l; i <= ihi; i++) {
+        float pp = x * AF(i, k) + y * AF(i, k + 1);
+        if (notlast) {
+          pp += zz * AF(i, k + 2);
+          AF(i, k + 2) -= pp * r;
+        }
+        AF(i, k + 1) -= pp * q;
+        AF(i, k) -= pp;
+      }
+    }
+  }
+  return 0;
+#undef AF
+}
+
+// One real eigenvalue refined in FP64 from the FP32 shift lam0: LU with
+// partial pivoting (whole-row swaps) of M - lam0 I, five inverse-iteration
+// steps from x = 1 with max-normalisation, then lam0 + x.(M - lam0 I)x/x.x.
+// Returns -1 on an exactly singular pivot or a degenerate vector.
+template <int V>
+__device__ __forceinline__ int refine_real(const double *M, double lam0,
+                                           double *lam) {
+  double A[V * V], ud[V], x[V];
+  int piv[V];
+#pragma unroll
+  for (int i = 0; i < V * V; i++)
+    A[i] = M[i];
+#pragma unroll
+  for (int i = 0; i < V; i++)
+    A[i * V + i] = M[i * V + i] - lam0;
+  for (int k = 0; k < V; k++) {
+    int p = k;
+    for (int i = k + 1; i < V; i++)
+      if (fabs(A[i * V + k]) > fabs(A[p * V + k]))
+        p = i;
+    piv[k] = p;
+    if (A[p * V + k] == 0.0)
+      return -1;
+    if (p != k)
+      for (int j = 0; j < V; j++) {
+        double t = A[k * V + j];
+        A[k * V + j] = A[p * V + j];
+        A[p * V + j] = t;
+      }
+    ud[k] = 1.0 / A[k * V + k];
+    for (int i = k + 1; i < V; i++) {
+      double f = A[i * V + k] * ud[k];
+      A[i * V + k] = f;
+      for (int j = k + 1; j < V; j++)
+        A[i * V + j] = fma(-f, A[k * V + j], A[i * V + j]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < V; i++)
+    x[i] = 1.0;
+  for (int it = 0; it < 5; it++) {
+    for (int k = 0; k < V; k++)
+      if (piv[k] != k) {
+        double t = x[k];
+        x[k] = x[piv[k]];
+        x[piv[k]] = t;
+      }
+    for (int k = 0; k < V; k++)
+      for (int i = k + 1; i < V; i++)
+        x[i] = fma(-A[i * V + k], x[k], x[i]);
+    double mx = 0;
+    for (int i = V - 1; i >= 0; i--) {
+      double s = x[i];
+      for (int j = i + 1; j < V; j++)
+        s = fma(-A[i * V + j], x[j], s);
+      x[i] = s * ud[i];
+      mx = fmax(mx, fabs(x[i]));
+    }
+    if (!(mx > 0.0) || mx != mx)
+      return -1;
+    double inv = 1.0 / mx;
+#pragma unroll
+    for (int i = 0; i < V; i++)
+      x[i] *= inv;
+  }
+  double num = 0, den = 0;
+#pragma unroll
+  for (int i = 0; i < V; i++) {
+    double r = -lam0 * x[i];
+#pragma unroll
+    for (int j = 0; j < V; j++)
+      r = fma(M[i * V + j], x[j], r);
+    num = fma(x[i], r, num);
+    den = fma(x[i], x[i], den);
+  }
+  *lam = lam0 + num / den;
+  return 0;
+}
+
+// max |eigenvalue| (a4): FP32 eigenvalues choose the candidates of largest
+// modulus (within 2^-10 of the largest); each is refined in FP64.  Complex
+// or nearly coincident candidates, a failed FP32 iteration, a singular
+// shift, or a refinement that moves its shift by more than 1e-5 relative
+// fall back to the FP64 Francis QR.  Same algorithm and operation order as
+// the host restatement, so both give the same bits.
+template <int V>
+__device__ __noinline__ double max_abs_eig(double *a) {
+  if (V == 1)
+    return fabs(a[0]);
+  float af[V * V], wr[V], wi[V];
+#pragma unroll
+  for (int i = 0; i < V * V; i++)
+    af[i] = (float)a[i];
+  if (eig_vals_f<V>(af, wr, wi) != 0)
+    return max_abs_eig_qr<V>(a);
+  float mf = 0;
+  for (int i = 0; i < V; i++) {
+    float m = (wi[i] == 0.0f) ? fabsf(wr[i])
+                              : sqrtf(wr[i] * wr[i] + wi[i] * wi[i]);
+    if (m > mf)
+      mf = m;
+  }
+  if (!(mf > 0.0f) || mf != mf || mf > 3.0e38f)
+    return max_abs_eig_qr<V>(a);
+  float thr = mf - mf * 0.0009765625f;
+  int cand[V], nc = 0;
+  for (int i = 0; i < V; i++) {
+    float m = (wi[i] == 0.0f) ? fabsf(wr[i])
+                              : sqrtf(wr[i] * wr[i] + wi[i] * wi[i]);
+    if (m >= thr) {
+      if (wi[i] != 0.0f)
+        return max_abs_eig_qr<V>(a);
+      cand[nc++] = i;
+    }
+  }
+  for (int i = 0; i < nc; i++)
+    for (int j = i + 1; j < nc; j++)
+      if (fabsf(wr[cand[i]] - wr[cand[j]]) <= 1e-4f * mf)
+        return max_abs_eig_qr<V>(a);
+  double best = 0;
+  for (int i = 0; i < nc; i++) {
+    double lam;
+    double lam0 = (double)wr[cand[i]];
+    if (refine_real<V>(a, lam0, &lam) != 0)
+      return max_abs_eig_qr<V>(a);
+    if (!(fabs(lam - lam0) <= 1e-5 * fabs(lam0)))
+      return max_abs_eig_qr<V>(a);
+    best = fmax(best, fabs(lam));
+  }
+  return best;
+}
+
 // Forward-difference Jacobian of F (NumericalDiff.h:6-44 with its default
-// forwardMode=true, which both call sites use: system.cpp:15, :58).
+// forwardMode=true, which both call sites use: system.cpp:15, :58).  The
+// quotient uses one reciprocal of h per column instead of V divisions; the
+// F values themselves, the part the step h amplifies, are unchanged.
 // wrt_dq: perturb dq[d*V+i] (second-order form) instead of q[i].
 template <class Sys>
 __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
@@ -260,8 +573,9 @@ __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
     *qi += h;
     Sys::F(v2, q, dq, d);
     *qi = qi0;
+    double ih = 1.0 / h; // one division per column
     for (int r = 0; r < V; r++)
-      jac[r * V + i] = (v2[r] - v1[r]) / h;
+      jac[r * V + i] = (v2[r] - v1[r]) * ih;
   }
 }
 

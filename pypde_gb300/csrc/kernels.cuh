@@ -665,15 +665,16 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         for (int tt = 0; tt < N; tt++)
           for (int v = 0; v < V; v++)
             b[tt * V + v] = rr[(tt * Nd + idx) * V + v] / wprod[idx];
-        for (int k = 0; k < NL; k++) {
+        // rows were swapped whole (L included): permute b first
+        for (int k = 0; k < NL; k++)
           if (piv[k] != k) {
             double tmp = b[k];
             b[k] = b[piv[k]];
             b[piv[k]] = tmp;
           }
+        for (int k = 0; k < NL; k++)
           for (int i = k + 1; i < NL; i++)
             b[i] -= A[i * NL + k] * b[k];
-        }
         for (int i = NL - 1; i >= 0; i--) {
           double sacc = b[i];
           for (int j = i + 1; j < NL; j++)
