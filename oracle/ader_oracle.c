@@ -355,7 +355,7 @@ static void weno_coeffs(const ora_tables *T, const double *data, long dstride,
       for (int v = 0; v < V; v++) {
         double s = 0;
         for (int j = 0; j < N; j++)
-          s += Mi[i * N + j] * data[(starts[k] + j) * dstride + v];
+          s = fma(Mi[i * N + j], data[(starts[k] + j) * dstride + v], s);
         c[i * V + v] = s;
       }
     for (int v = 0; v < V; v++) {
@@ -363,20 +363,22 @@ static void weno_coeffs(const ora_tables *T, const double *data, long dstride,
       for (int j = 0; j < N; j++) {
         double r = 0;
         for (int i = 0; i < N; i++)
-          r += c[i * V + v] * T->sig[i * N + j];
-        p += r * c[j * V + v];
+          r = fma(c[i * V + v], T->sig[i * N + j], r);
+        p = fma(r, c[j * V + v], p);
       }
       p += WENO_EPS;
       double p2 = p * p, p4 = p2 * p2, p8 = p4 * p4;
       double o = lams[k] / p8;
       for (int i = 0; i < N; i++)
-        num[i * V + v] += o * c[i * V + v];
+        num[i * V + v] = fma(o, c[i * V + v], num[i * V + v]);
       den[v] += o;
     }
   }
-  for (int i = 0; i < N; i++)
-    for (int v = 0; v < V; v++)
-      out[i * V + v] = num[i * V + v] / den[v];
+  for (int v = 0; v < V; v++) {
+    double rden = 1.0 / den[v];
+    for (int i = 0; i < N; i++)
+      out[i * V + v] = num[i * V + v] * rden;
+  }
 }
 
 void ora_weno(const double *ub, const int *nXb, int ndim, int N, int V,
@@ -428,20 +430,23 @@ void ora_weno(const double *ub, const int *nXb, int ndim, int N, int V,
 /* Node-block helpers, poly/evaluations.cpp:23-70                      */
 /* ------------------------------------------------------------------ */
 /* ret[idx] = (sum_j DERVALS[i_d][j] q[idx with i_d=j]) / dX  over an Nd x V
- * block (rows strided by rstride doubles) */
+ * block (rows strided by rstride doubles).  Fused multiply-adds and one
+ * reciprocal of dX: the reference sums with Eigen products and divides
+ * (evaluations.cpp:23-47); the difference is at rounding level. */
 static void derivs(const ora_tables *T, const double *q, long rstride,
                    double *ret, long ostride, int d, int ndim, int V,
                    double dXd) {
   int N = T->N, Nd = ipow(N, ndim);
   int sd = ipow(N, ndim - d - 1);
+  double rdx = 1.0 / dXd;
   for (int idx = 0; idx < Nd; idx++) {
     int id = (idx / sd) % N;
     int base = idx - id * sd;
     for (int v = 0; v < V; v++) {
       double s = 0;
       for (int j = 0; j < N; j++)
-        s += T->dervals[id * N + j] * q[(base + j * sd) * rstride + v];
-      ret[idx * ostride + v] = s / dXd;
+        s = fma(T->dervals[id * N + j], q[(base + j * sd) * rstride + v], s);
+      ret[idx * ostride + v] = s * rdx;
     }
   }
 }
@@ -458,7 +463,7 @@ static void endpts(const ora_tables *T, const double *q, long rstride,
     for (int v = 0; v < V; v++) {
       double s = 0;
       for (int j = 0; j < N; j++)
-        s += T->endvals[e * N + j] * q[(base + j * sd) * rstride + v];
+        s = fma(T->endvals[e * N + j], q[(base + j * sd) * rstride + v], s);
       ret[ind * ostride + v] = s;
     }
   }
@@ -1214,6 +1219,7 @@ typedef struct {
   const double *dX;
   ora_tables T;
   double wprod[ORA_MAXN * ORA_MAXN * ORA_MAXN]; /* prod_d W[i_d] per node */
+  double rwprod[ORA_MAXN * ORA_MAXN * ORA_MAXN]; /* 1 / wprod */
 } ctx_t;
 
 static void ctx_init(ctx_t *c, ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
@@ -1239,6 +1245,7 @@ static void ctx_init(ctx_t *c, ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
     for (int d = 0; d < ndim; d++)
       p *= c->T.wghts[digs[d]];
     c->wprod[idx] = p;
+    c->rwprod[idx] = 1.0 / p;
   }
 }
 
@@ -1247,10 +1254,13 @@ static void ctx_init(ctx_t *c, ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
  * system.cpp:15 passes only secondOrder=false (perturb q), system.cpp:58
  * secondOrder=true (perturb dq_d).  h = max(sqrt(eps)|x|, sqrt(eps)). */
 static void fd_jacobian(const ctx_t *c, double *jac, double *q, double *dq,
-                        int d, int wrt_dq) {
+                        int d, int wrt_dq, double *f0) {
   int V = c->V;
   double v1[ORA_MAXV], v2[ORA_MAXV];
   c->F(v1, q, dq, d);
+  if (f0) /* F(q) itself, reused by the Rusanov flux */
+    for (int r = 0; r < V; r++)
+      f0[r] = v1[r];
   for (int i = 0; i < V; i++) {
     double *qi = wrt_dq ? dq + d * V + i : q + i;
     double qi0 = *qi;
@@ -1265,10 +1275,10 @@ static void fd_jacobian(const ctx_t *c, double *jac, double *q, double *dq,
 }
 
 static void system_matrix(const ctx_t *c, double *M, double *q, double *dq,
-                          int d) { /* system.cpp:6-26 */
+                          int d, double *f0) { /* system.cpp:6-26 */
   int V = c->V;
   if (c->F)
-    fd_jacobian(c, M, q, dq, d, 0);
+    fd_jacobian(c, M, q, dq, d, 0, f0);
   else
     for (int i = 0; i < V * V; i++)
       M[i] = 0.0;
@@ -1280,15 +1290,16 @@ static void system_matrix(const ctx_t *c, double *M, double *q, double *dq,
   }
 }
 
-static double max_abs_eigs(const ctx_t *c, double *q, double *dq, int d) {
+static double max_abs_eigs(const ctx_t *c, double *q, double *dq, int d,
+                           double *f0) {
   double M[ORA_MAXV * ORA_MAXV];
-  system_matrix(c, M, q, dq, d);
+  system_matrix(c, M, q, dq, d, f0);
   return ora_max_abs_eig(M, c->V);
 }
 
 static double max_abs_eigs_2nd(const ctx_t *c, double *q, double *dq, int d) {
   double M[ORA_MAXV * ORA_MAXV]; /* system.cpp:53-61 */
-  fd_jacobian(c, M, q, dq, d, 1);
+  fd_jacobian(c, M, q, dq, d, 1, NULL);
   return 2 * (c->N + 1) / c->dX[d] * ora_max_abs_eig(M, c->V);
 }
 
@@ -1330,14 +1341,19 @@ static double cfl_max(const ctx_t *c, const double *w, long c0, long c1) {
     double q[ORA_MAXV], dq[3 * ORA_MAXV];
     for (int v = 0; v < V; v++)
       q[v] = wavg(c->wprod, w0 + v, V, Nd, v < (V & ~1));
-    for (int d = 0; d < ndim; d++) {
+    for (int d = 0; d < ndim; d++) { /* F sees dQ only in the 2nd-order form */
+      if (!c->secondOrder) {
+        for (int v = 0; v < V; v++)
+          dq[d * V + v] = 0.0;
+        continue;
+      }
       derivs(&c->T, w0, V, dw, V, d, ndim, V, c->dX[d]);
       for (int v = 0; v < V; v++)
         dq[d * V + v] = wavg(c->wprod, dw + v, V, Nd, v < (V & ~1));
     }
     double tmp = 0.0;
     for (int d = 0; d < ndim; d++) {
-      double lam = max_abs_eigs(c, q, dq, d);
+      double lam = max_abs_eigs(c, q, dq, d, NULL);
       if (c->secondOrder)
         lam += max_abs_eigs_2nd(c, q, dq, d);
       tmp += lam / c->dX[d];
@@ -1386,8 +1402,9 @@ static void dg_rhs(const ctx_t *c, const double *q, const double *Ww,
   for (int t = 0; t < N; t++) {
     const double *qt = q + t * Nd * V;
     double *rt = ret + t * Nd * V;
-    for (int d = 0; d < ndim; d++)
-      derivs(&c->T, qt, V, s->dq + d * V, ndim * V, d, ndim, V, c->dX[d]);
+    if (c->secondOrder || c->B) /* dQ reaches only B and 2nd-order F */
+      for (int d = 0; d < ndim; d++)
+        derivs(&c->T, qt, V, s->dq + d * V, ndim * V, d, ndim, V, c->dX[d]);
     if (c->F) {
       for (int idx = 0; idx < Nd; idx++)
         for (int d = 0; d < ndim; d++)
@@ -1422,7 +1439,7 @@ static void dg_rhs(const ctx_t *c, const double *q, const double *Ww,
           for (int i = 0; i < V; i++) {
             double acc = 0;
             for (int j = 0; j < V; j++)
-              acc += b[i * V + j] * dqd[j];
+              acc = fma(b[i * V + j], dqd[j], acc);
             r[i] -= acc;
           }
         }
@@ -1436,7 +1453,7 @@ static void dg_rhs(const ctx_t *c, const double *q, const double *Ww,
     }
   }
   for (int i = 0; i < N * Nd * V; i++)
-    ret[i] = ret[i] * dt + Ww[i];
+    ret[i] = fma(ret[i], dt, Ww[i]);
 }
 
 /* Ww and the initial guess, dg.cpp:12-20, 156-171 */
@@ -1469,8 +1486,8 @@ static void dg_usolve(const ctx_t *c, const double *r, double *q1) {
       for (int v = 0; v < V; v++) {
         double s = 0;
         for (int k = 0; k < N; k++)
-          s += c->T.dgmat_inv[t * N + k] * r[(k * Nd + idx) * V + v];
-        q1[(t * Nd + idx) * V + v] = s / c->wprod[idx];
+          s = fma(c->T.dgmat_inv[t * N + k], r[(k * Nd + idx) * V + v], s);
+        q1[(t * Nd + idx) * V + v] = s * c->rwprod[idx];
       }
 }
 
@@ -1512,11 +1529,12 @@ static int lu_factor(double *a, int n, int *piv) {
         a[k * n + j] = a[p * n + j];
         a[p * n + j] = t;
       }
+    double rp = 1.0 / a[k * n + k];
     for (int i = k + 1; i < n; i++) {
-      double f = a[i * n + k] / a[k * n + k];
+      double f = a[i * n + k] * rp;
       a[i * n + k] = f;
       for (int j = k + 1; j < n; j++)
-        a[i * n + j] -= f * a[k * n + j];
+        a[i * n + j] = fma(-f, a[k * n + j], a[i * n + j]);
     }
   }
   return 0;
@@ -1532,11 +1550,11 @@ static void lu_solve(const double *a, int n, const int *piv, double *b) {
     }
   for (int k = 0; k < n; k++)
     for (int i = k + 1; i < n; i++)
-      b[i] -= a[i * n + k] * b[k];
+      b[i] = fma(-a[i * n + k], b[k], b[i]);
   for (int i = n - 1; i >= 0; i--) {
     double s = b[i];
     for (int j = i + 1; j < n; j++)
-      s -= a[i * n + j] * b[j];
+      s = fma(-a[i * n + j], b[j], s);
     b[i] = s / a[i * n + i];
   }
 }
@@ -1564,7 +1582,7 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
         for (int v = 0; v < V; v++) {
           double uq = 0;
           for (int k = 0; k < N; k++)
-            uq += c->T.dgmat[t * N + k] * q[(k * Nd + idx) * V + v];
+            uq = fma(c->T.dgmat[t * N + k], q[(k * Nd + idx) * V + v], uq);
           uq *= c->wprod[idx];
           int i = (t * Nd + idx) * V + v;
           double rr = r[i];
@@ -1588,9 +1606,10 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
             qn[wv] = q0 + h;
             c->S(s1, qn);
             qn[wv] = q0;
+            double ih = 1.0 / h;
             for (int v = 0; v < V; v++)
               A[(t * V + v) * nl + t * V + wv] =
-                  dt * c->T.wghts[t] * ((s1[v] - s0[v]) / h);
+                  dt * c->T.wghts[t] * ((s1[v] - s0[v]) * ih);
           }
         }
         for (int k = 0; k < N; k++)
@@ -1603,7 +1622,7 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
       }
       for (int t = 0; t < N; t++)
         for (int v = 0; v < V; v++)
-          b[t * V + v] = r[(t * Nd + idx) * V + v] / c->wprod[idx];
+          b[t * V + v] = r[(t * Nd + idx) * V + v] * c->rwprod[idx];
       lu_solve(A, nl, piv, b);
       for (int t = 0; t < N; t++)
         for (int v = 0; v < V; v++)
@@ -1665,9 +1684,10 @@ long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
 /* a8-a12: FV corrector, solvers/fv/fv.cpp and fluxes.cpp              */
 /* ------------------------------------------------------------------ */
 static void d_rus(const ctx_t *c, double *ret, double *qL, double *qR,
-                  double *dqL, double *dqR, int d) { /* fluxes.cpp:72-78 */
-  double m1 = max_abs_eigs(c, qL, dqL, d);
-  double m2 = max_abs_eigs(c, qR, dqR, d);
+                  double *dqL, double *dqR, int d, double *fL,
+                  double *fR) { /* fluxes.cpp:72-78 */
+  double m1 = max_abs_eigs(c, qL, dqL, d, fL);
+  double m2 = max_abs_eigs(c, qR, dqR, d, fR);
   double m = fmax(m1, m2);
   for (int v = 0; v < c->V; v++)
     ret[v] = m * (qL[v] - qR[v]);
@@ -1715,7 +1735,7 @@ static void d_osh(const ctx_t *c, double *ret, double *qL, double *qR,
       q[v] = qR[v] + c->T.nodes[i] * Dq[v];
     for (int k = 0; k < c->ndim * V; k++)
       dq[k] = dqR[k] + c->T.nodes[i] * (dqL[k] - dqR[k]);
-    system_matrix(c, M, q, dq, d);
+    system_matrix(c, M, q, dq, d, NULL);
     abs_apply(V, M, Dq, ret, c->T.wghts[i], 1);
   }
 }
@@ -1734,7 +1754,7 @@ static void d_roe(const ctx_t *c, double *ret, double *qL, double *qR,
       q[v] = qR[v] + c->T.nodes[i] * Dq[v];
     for (int k = 0; k < c->ndim * V; k++)
       dq[k] = dqR[k] + c->T.nodes[i] * (dqL[k] - dqR[k]);
-    system_matrix(c, Mi, q, dq, d);
+    system_matrix(c, Mi, q, dq, d, NULL);
     for (int k = 0; k < V * V; k++)
       M[k] += c->T.wghts[i] * Mi[k];
   }
@@ -1744,15 +1764,17 @@ static void d_roe(const ctx_t *c, double *ret, double *qL, double *qR,
 static void num_flux(const ctx_t *c, int flux, double *ret, double *qL,
                      double *qR, double *dqL, double *dqR, int d) {
   int V = c->V;
-  if (flux == 0)
-    d_rus(c, ret, qL, qR, dqL, dqR, d);
-  else if (flux == 1)
-    d_roe(c, ret, qL, qR, dqL, dqR, d);
-  else
-    d_osh(c, ret, qL, qR, dqL, dqR, d);
   double fL[ORA_MAXV], fR[ORA_MAXV];
-  c->F(fL, qL, dqL, d);
-  c->F(fR, qR, dqR, d);
+  if (flux == 0) { /* F(qL), F(qR) come out of the FD Jacobians */
+    d_rus(c, ret, qL, qR, dqL, dqR, d, fL, fR);
+  } else {
+    if (flux == 1)
+      d_roe(c, ret, qL, qR, dqL, dqR, d);
+    else
+      d_osh(c, ret, qL, qR, dqL, dqR, d);
+    c->F(fL, qL, dqL, d);
+    c->F(fR, qR, dqR, d);
+  }
   for (int v = 0; v < V; v++)
     ret[v] += fL[v] + fR[v];
   if (c->secondOrder) { /* fluxes.cpp:96-100 */
@@ -1775,15 +1797,15 @@ static void bint(const ctx_t *c, double *ret, const double *qL,
     M[i] = 0.0;
   for (int i = 0; i < N; i++) {
     for (int v = 0; v < V; v++)
-      q[v] = qL[v] + c->T.nodes[i] * Dq[v];
+      q[v] = fma(c->T.nodes[i], Dq[v], qL[v]);
     c->B(b, q, d);
     for (int k = 0; k < V * V; k++)
-      M[k] += c->T.wghts[i] * b[k];
+      M[k] = fma(c->T.wghts[i], b[k], M[k]);
   }
   for (int r = 0; r < V; r++) {
     double s = 0;
     for (int j = 0; j < V; j++)
-      s += M[r * V + j] * Dq[j];
+      s = fma(M[r * V + j], Dq[j], s);
     ret[r] = s;
   }
 }
@@ -1834,7 +1856,7 @@ static void fv_range(const ctx_t *c, double *u, const double *qh,
                 for (int i = 0; i < V; i++) {
                   double acc = 0;
                   for (int j = 0; j < V; j++)
-                    acc += b[i * V + j] * dq[d][idx * V + j];
+                    acc = fma(b[i * V + j], dq[d][idx * V + j], acc);
                   s[i] -= acc;
                 }
               }
@@ -2111,7 +2133,7 @@ double ora_system_max_abs_eigs(ora_flux_fn F, ora_ncp_fn B, int ndim, int V,
   ctx_t *c = malloc(sizeof(ctx_t));
   double dX[3] = {1, 1, 1};
   ctx_init(c, F, B, NULL, ndim, 2, V, dX, 0);
-  system_matrix(c, M, q, dq, d);
+  system_matrix(c, M, q, dq, d, NULL);
   double Mc[ORA_MAXV * ORA_MAXV];
   memcpy(Mc, M, sizeof(double) * V * V);
   double r = ora_max_abs_eig(Mc, V);

@@ -562,10 +562,14 @@ __device__ __noinline__ double max_abs_eig(double *a) {
 // wrt_dq: perturb dq[d*V+i] (second-order form) instead of q[i].
 template <class Sys>
 __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
-                                            int d, bool wrt_dq) {
+                                            int d, bool wrt_dq,
+                                            double *f0 = nullptr) {
   constexpr int V = Sys::V;
   double v1[V], v2[V];
   Sys::F(v1, q, dq, d);
+  if (f0) // F(q) itself, reused by the Rusanov flux
+    for (int r = 0; r < V; r++)
+      f0[r] = v1[r];
   for (int i = 0; i < V; i++) {
     double *qi = wrt_dq ? dq + d * V + i : q + i;
     double qi0 = *qi;
@@ -581,11 +585,12 @@ __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
 
 // system_matrix + max|eig| (src/eigs/system.cpp:6-51)
 template <class Sys>
-__device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d) {
+__device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d,
+                                               double *f0 = nullptr) {
   constexpr int V = Sys::V;
   double M[V * V];
   if (Sys::HAS_F)
-    fd_jacobian<Sys>(M, q, dq, d, false);
+    fd_jacobian<Sys>(M, q, dq, d, false, f0);
   else
     for (int i = 0; i < V * V; i++)
       M[i] = 0.0;

@@ -120,7 +120,7 @@ __global__ void k_weno_pass(const double *__restrict__ in,
         double s = 0;
 #pragma unroll
         for (int j = 0; j < N; j++)
-          s += T.weno_inv[k][a * N + j] * dat[starts[k] + j];
+          s = fma(T.weno_inv[k][a * N + j], dat[starts[k] + j], s);
         c[a] = s;
       }
       double p = 0;
@@ -129,22 +129,23 @@ __global__ void k_weno_pass(const double *__restrict__ in,
         double rr = 0;
 #pragma unroll
         for (int a = 0; a < N; a++)
-          rr += c[a] * T.sig[a * N + j];
-        p += rr * c[j];
+          rr = fma(c[a], T.sig[a * N + j], rr);
+        p = fma(rr, c[j], p);
       }
       p += WENO_EPS;
       double p2 = p * p, p4 = p2 * p2, p8 = p4 * p4;
       double o = lams[k] / p8;
 #pragma unroll
       for (int a = 0; a < N; a++)
-        num[a] += o * c[a];
+        num[a] = fma(o, c[a], num[a]);
       den += o;
     }
     double *o = out + ((i1 * n2 + i) * n3 + i3) * (long long)n4 * N * V +
                 (long long)i4 * N * V + v;
+    const double rden = 1.0 / den;
 #pragma unroll
     for (int a = 0; a < N; a++)
-      o[a * V] = num[a] / den;
+      o[a * V] = num[a] * rden;
   }
 }
 
@@ -176,9 +177,15 @@ __global__ void __launch_bounds__(128)
       q[v] = wavg(wprod, w0 + v, V, Nd, v < (V & ~1));
 #pragma unroll
     for (int d = 0; d < D; d++) {
+      if (!Sys::SECOND_ORDER) { // F sees dQ only in the 2nd-order form
+        for (int v = 0; v < V; v++)
+          dq[d * V + v] = 0.0;
+        continue;
+      }
       int stride_d = 1;
       for (int e = d + 1; e < D; e++)
         stride_d *= N;
+      const double rdx = 1.0 / g.dX[d];
       for (int v = 0; v < V; v++) {
         double dw[Nd];
         for (int idx = 0; idx < Nd; idx++) {
@@ -187,8 +194,8 @@ __global__ void __launch_bounds__(128)
           double s = 0;
 #pragma unroll
           for (int j = 0; j < N; j++)
-            s += dervals[id * N + j] * w0[(base + j * stride_d) * V + v];
-          dw[idx] = s / g.dX[d];
+            s = fma(dervals[id * N + j], w0[(base + j * stride_d) * V + v], s);
+          dw[idx] = s * rdx;
         }
         dq[d * V + v] = wavg(wprod, dw, 1, Nd, v < (V & ~1));
       }
@@ -293,21 +300,25 @@ __global__ void k_predictor(const double *__restrict__ w,
     __syncthreads();
     double dq[D * V];
     if (!done) {
-      // derivatives of q_t along each axis (evaluations.cpp:23-47)
+      // derivatives of q_t along each axis (evaluations.cpp:23-47); only
+      // B and the second-order F read them
+      if (Sys::SECOND_ORDER || Sys::HAS_B) {
 #pragma unroll
-      for (int d = 0; d < D; d++) {
-        int sd = 1;
-        for (int e = d + 1; e < D; e++)
-          sd *= N;
-        int base = idx - digs[d] * sd;
+        for (int d = 0; d < D; d++) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          int base = idx - digs[d] * sd;
+          const double rdx = 1.0 / g.dX[d];
 #pragma unroll
-        for (int v = 0; v < V; v++) {
-          double s = 0;
+          for (int v = 0; v < V; v++) {
+            double s = 0;
 #pragma unroll
-          for (int j = 0; j < N; j++)
-            s += dervals[digs[d] * N + j] *
-                 q0[(t * Nd + base + j * sd) * V + v];
-          dq[d * V + v] = s / g.dX[d];
+            for (int j = 0; j < N; j++)
+              s = fma(dervals[digs[d] * N + j],
+                      q0[(t * Nd + base + j * sd) * V + v], s);
+            dq[d * V + v] = s * rdx;
+          }
         }
       }
       if (Sys::HAS_F) {
@@ -336,7 +347,7 @@ __global__ void k_predictor(const double *__restrict__ w,
             double acc = 0;
 #pragma unroll
             for (int j = 0; j < V; j++)
-              acc += b[i * V + j] * dq[d * V + j];
+              acc = fma(b[i * V + j], dq[d * V + j], acc);
             r[i] -= acc;
           }
         }
@@ -345,21 +356,22 @@ __global__ void k_predictor(const double *__restrict__ w,
           for (int e = d + 1; e < D; e++)
             sd *= N;
           int base = idx - digs[d] * sd;
+          const double rdx = 1.0 / g.dX[d];
 #pragma unroll
           for (int v = 0; v < V; v++) {
             double s = 0;
 #pragma unroll
             for (int j = 0; j < N; j++)
-              s += dervals[digs[d] * N + j] *
-                   ff[((t * Nd + base + j * sd) * D + d) * V + v];
-            r[v] -= s / g.dX[d];
+              s = fma(dervals[digs[d] * N + j],
+                      ff[((t * Nd + base + j * sd) * D + d) * V + v], s);
+            r[v] -= s * rdx;
           }
         }
         cc *= wg[digs[d]];
       }
 #pragma unroll
       for (int v = 0; v < V; v++)
-        rr[node * V + v] = (r[v] * cc) * dt + Ww[v];
+        rr[node * V + v] = fma(r[v] * cc, dt, Ww[v]);
     }
     __syncthreads();
     if (lc < CPB && node == 0)
@@ -368,13 +380,14 @@ __global__ void k_predictor(const double *__restrict__ w,
     if (!done) {
       // q1 = DG_U^{-1} r with DG_U = kron(DG_MAT, diag W, ...)
       bool more = false;
+      const double rwp = 1.0 / wprod[idx];
 #pragma unroll
       for (int v = 0; v < V; v++) {
         double s = 0;
 #pragma unroll
         for (int k = 0; k < N; k++)
-          s += dginv[t * N + k] * rr[(k * Nd + idx) * V + v];
-        q1[v] = s / wprod[idx];
+          s = fma(dginv[t * N + k], rr[(k * Nd + idx) * V + v], s);
+        q1[v] = s * rwp;
         double a = q0[node * V + v];
         if (fabs(q1[v] - a) > DG_TOL * (1. + fabs(a)))
           more = true;
@@ -514,19 +527,23 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
     const bool active = valid && !cell_done[lc];
     double dq[D * V];
     if (active) {
+      if (Sys::SECOND_ORDER || Sys::HAS_B) {
 #pragma unroll
-      for (int d = 0; d < D; d++) {
-        int sd = 1;
-        for (int e = d + 1; e < D; e++)
-          sd *= N;
-        int base = idx - digs[d] * sd;
+        for (int d = 0; d < D; d++) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          int base = idx - digs[d] * sd;
+          const double rdx = 1.0 / g.dX[d];
 #pragma unroll
-        for (int v = 0; v < V; v++) {
-          double s = 0;
+          for (int v = 0; v < V; v++) {
+            double s = 0;
 #pragma unroll
-          for (int j = 0; j < N; j++)
-            s += dervals[digs[d] * N + j] * q[(t * Nd + base + j * sd) * V + v];
-          dq[d * V + v] = s / g.dX[d];
+            for (int j = 0; j < N; j++)
+              s = fma(dervals[digs[d] * N + j],
+                      q[(t * Nd + base + j * sd) * V + v], s);
+            dq[d * V + v] = s * rdx;
+          }
         }
       }
       if (Sys::HAS_F) {
@@ -555,7 +572,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
             double acc = 0;
 #pragma unroll
             for (int j = 0; j < V; j++)
-              acc += b[i * V + j] * dq[d * V + j];
+              acc = fma(b[i * V + j], dq[d * V + j], acc);
             r[i] -= acc;
           }
         }
@@ -564,14 +581,15 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
           for (int e = d + 1; e < D; e++)
             sd *= N;
           int base = idx - digs[d] * sd;
+          const double rdx = 1.0 / g.dX[d];
 #pragma unroll
           for (int v = 0; v < V; v++) {
             double s = 0;
 #pragma unroll
             for (int j = 0; j < N; j++)
-              s += dervals[digs[d] * N + j] *
-                   ff[((t * Nd + base + j * sd) * D + d) * V + v];
-            r[v] -= s / g.dX[d];
+              s = fma(dervals[digs[d] * N + j],
+                      ff[((t * Nd + base + j * sd) * D + d) * V + v], s);
+            r[v] -= s * rdx;
           }
         }
         cc *= wg[digs[d]];
@@ -579,11 +597,11 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
       double res = 0, scale = 0;
 #pragma unroll
       for (int v = 0; v < V; v++) {
-        double rv = (r[v] * cc) * dt + Ww[v];
+        double rv = fma(r[v] * cc, dt, Ww[v]);
         double uq = 0;
 #pragma unroll
         for (int k = 0; k < N; k++)
-          uq += dgmat[t * N + k] * q[(k * Nd + idx) * V + v];
+          uq = fma(dgmat[t * N + k], q[(k * Nd + idx) * V + v], uq);
         uq *= wprod[idx];
         double ov = rv - uq;
         rr[node * V + v] = ov;
@@ -607,19 +625,20 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         if (Sys::HAS_S)
           Sys::S(s0, qn);
         for (int wv = 0; wv < V; wv++) {
+          double ih = 0.0;
           if (Sys::HAS_S) {
             double q0 = qn[wv];
             double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
             qn[wv] = q0 + h;
             Sys::S(s1, qn);
             qn[wv] = q0;
+            ih = 1.0 / h;
           }
           for (int v = 0; v < V; v++)
             for (int k = 0; k < N; k++) {
               double a = 0.0;
               if (k == t && Sys::HAS_S)
-                a = dt * wg[t] * ((s1[v] - s0[v]) / (fmax(SQRT_EPS * fabs(qn[wv]),
-                                                           SQRT_EPS)));
+                a = dt * wg[t] * ((s1[v] - s0[v]) * ih);
               A[(t * V + v) * NL + k * V + wv] = a;
             }
         }
@@ -651,11 +670,12 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
             A[k * NL + j] = A[p * NL + j];
             A[p * NL + j] = tmp;
           }
+        const double rp = 1.0 / A[k * NL + k];
         for (int i = k + 1; i < NL; i++) {
-          double f = A[i * NL + k] / A[k * NL + k];
+          double f = A[i * NL + k] * rp;
           A[i * NL + k] = f;
           for (int j = k + 1; j < NL; j++)
-            A[i * NL + j] -= f * A[k * NL + j];
+            A[i * NL + j] = fma(-f, A[k * NL + j], A[i * NL + j]);
         }
       }
       if (!ok) {
@@ -664,7 +684,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         double b[NL];
         for (int tt = 0; tt < N; tt++)
           for (int v = 0; v < V; v++)
-            b[tt * V + v] = rr[(tt * Nd + idx) * V + v] / wprod[idx];
+            b[tt * V + v] = rr[(tt * Nd + idx) * V + v] * (1.0 / wprod[idx]);
         // rows were swapped whole (L included): permute b first
         for (int k = 0; k < NL; k++)
           if (piv[k] != k) {
@@ -674,11 +694,11 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
           }
         for (int k = 0; k < NL; k++)
           for (int i = k + 1; i < NL; i++)
-            b[i] -= A[i * NL + k] * b[k];
+            b[i] = fma(-A[i * NL + k], b[k], b[i]);
         for (int i = NL - 1; i >= 0; i--) {
           double sacc = b[i];
           for (int j = i + 1; j < NL; j++)
-            sacc -= A[i * NL + j] * b[j];
+            sacc = fma(-A[i * NL + j], b[j], sacc);
           b[i] = sacc / A[i * NL + i];
         }
         for (int tt = 0; tt < N; tt++)
@@ -739,7 +759,7 @@ __device__ __forceinline__ void endpoints(const double *qhc, const Tables &T,
     double s = 0;
 #pragma unroll
     for (int j = 0; j < N; j++)
-      s += T.endvals[e * N + j] * qhc[(base + j * sd) * V + v];
+      s = fma(T.endvals[e * N + j], qhc[(base + j * sd) * V + v], s);
     out[v] = s;
   }
 }
@@ -749,15 +769,13 @@ __device__ __forceinline__ void rusanov_flux(double *f, double *qL,
                                              double *qR, double *dqL,
                                              double *dqR, int d, double dXd) {
   constexpr int V = Sys::V;
-  double m1 = max_abs_eigs<Sys>(qL, dqL, d);
-  double m2 = max_abs_eigs<Sys>(qR, dqR, d);
+  double fL[V], fR[V]; // F(qL), F(qR) come out of the FD Jacobians
+  double m1 = max_abs_eigs<Sys>(qL, dqL, d, fL);
+  double m2 = max_abs_eigs<Sys>(qR, dqR, d, fR);
   double m = fmax(m1, m2);
 #pragma unroll
   for (int v = 0; v < V; v++)
     f[v] = m * (qL[v] - qR[v]);
-  double fL[V], fR[V];
-  Sys::F(fL, qL, dqL, d);
-  Sys::F(fR, qR, dqR, d);
 #pragma unroll
   for (int v = 0; v < V; v++)
     f[v] += fL[v] + fR[v];
@@ -786,18 +804,18 @@ __device__ __forceinline__ void bint(double *ret, const double *qL,
   for (int i = 0; i < N; i++) {
 #pragma unroll
     for (int v = 0; v < V; v++)
-      q[v] = qL[v] + T.nodes[i] * Dq[v];
+      q[v] = fma(T.nodes[i], Dq[v], qL[v]);
     Sys::B(b, q, d);
 #pragma unroll
     for (int k = 0; k < V * V; k++)
-      M[k] += T.wghts[i] * b[k];
+      M[k] = fma(T.wghts[i], b[k], M[k]);
   }
 #pragma unroll
   for (int r = 0; r < V; r++) {
     double s = 0;
 #pragma unroll
     for (int j = 0; j < V; j++)
-      s += M[r * V + j] * Dq[j];
+      s = fma(M[r * V + j], Dq[j], s);
     ret[r] = s;
   }
 }
@@ -858,14 +876,15 @@ __global__ void __launch_bounds__(128)
           int sd = 1;
           for (int e = d_ + 1; e < D; e++)
             sd *= N;
+          const double rdx = 1.0 / g.dX[d_];
           for (int n = 0; n < Nd; n++) {
             int id = (n / sd) % N;
             int base = n - id * sd;
             for (int v = 0; v < V; v++) {
               double s = 0;
               for (int j = 0; j < N; j++)
-                s += T.dervals[id * N + j] * src[(base + j * sd) * V + v];
-              tmpd[n * V + v] = s / g.dX[d_];
+                s = fma(T.dervals[id * N + j], src[(base + j * sd) * V + v], s);
+              tmpd[n * V + v] = s * rdx;
             }
           }
           double e_out[V];
@@ -958,8 +977,8 @@ __global__ void k_centers(const double *__restrict__ qh,
           double a = 0;
 #pragma unroll
           for (int j = 0; j < N; j++)
-            a += T.dervals[digs[d] * N + j] * qt[(base + j * sd) * V + v];
-          dq[v] = a / g.dX[d];
+            a = fma(T.dervals[digs[d] * N + j], qt[(base + j * sd) * V + v], a);
+          dq[v] = a * (1.0 / g.dX[d]);
         }
         Sys::B(b, qt + idx * V, d);
 #pragma unroll
@@ -967,7 +986,7 @@ __global__ void k_centers(const double *__restrict__ qh,
           double acc = 0;
 #pragma unroll
           for (int j = 0; j < V; j++)
-            acc += b[i * V + j] * dq[j];
+            acc = fma(b[i * V + j], dq[j], acc);
           s[i] -= acc;
         }
       }
