@@ -1669,9 +1669,9 @@ static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
 long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
                    long nrows, const double *dX, int ndim, int N, int V,
                    int stiff, double dt, double newton_tol, double *qh,
-                   int *maxit) {
+                   int *maxit, int secondOrder) {
   ctx_t *c = malloc(sizeof(ctx_t));
-  ctx_init(c, F, B, S, ndim, N, V, dX, 0);
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
   if (maxit)
     *maxit = 0;
   long r = predictor_range(c, w, 0, nrows / c->Nd, stiff, dt, newton_tol, qh,

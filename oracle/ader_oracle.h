@@ -63,7 +63,7 @@ double ora_timestep(ora_flux_fn F, ora_ncp_fn B, const double *w, long nrows,
 long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
                    long nrows, const double *dX, int ndim, int N, int V,
                    int stiff, double dt, double newton_tol, double *qh,
-                   int *maxit);
+                   int *maxit, int secondOrder);
 /* FV corrector (FVSolver::apply) on u (prod(nX) rows) using qh over the
  * w-grid nX+2. */
 void ora_fv(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,

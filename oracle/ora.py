@@ -61,7 +61,7 @@ def port():
                                    D, D, c_long, c_int]
         L.ora_predictor.restype = c_long
         L.ora_predictor.argtypes = [c_void_p, c_void_p, c_void_p, dp, c_long, dp, c_int, c_int,
-                                    c_int, c_int, D, D, dp, ip]
+                                    c_int, c_int, D, D, dp, ip, c_int]
         L.ora_fv.restype = None
         L.ora_fv.argtypes = [c_void_p, c_void_p, c_void_p, dp, dp, ip, dp, c_int, c_int, c_int,
                              c_int, c_int, D]
@@ -151,7 +151,8 @@ def predictor(sysname, w, dX, N, stiff, dt, tol=1e-12):
     qh = np.zeros((w.shape[0] * N, s.V))
     mi = c_int()
     its = port().ora_predictor(s.F, s.B, s.S, ptr(w), w.shape[0], ptr(dX), len(dX), N, s.V,
-                               int(stiff), dt, tol, ptr(qh), ctypes.byref(mi))
+                               int(stiff), dt, tol, ptr(qh), ctypes.byref(mi),
+                               s.second_order)
     return qh, its, mi.value
 
 
