@@ -124,6 +124,22 @@ int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
  * shape (nX - 2(N-1)) x N^ndim x V. */
 int weno_solver(double *ret, double *u, int *nX, int ndim, int N, int V);
 
+/* weno_solver on caller-owned DEVICE buffers, for callers that cannot
+ * allocate device memory (code running inside another framework's device
+ * memory budget, or on paths where cudaMalloc's device synchronisation is
+ * not allowed).  No counterpart in the reference.  u_dev (prod(nX) x V) and
+ * ret_dev ((nX - 2(N-1)) x N^ndim x V) are device pointers; stream is a
+ * cudaStream_t (NULL: the default stream); the call is asynchronous on it.
+ * Allocates nothing: the passes between axes use one file-scope __device__
+ * scratch array of 32 MiB (4 Mi doubles) that every GPU loading the library
+ * holds until exit; larger grids are rejected with PYPDE_ERR_ARG.  All calls
+ * share that array, so calls that overlap on the GPU (different streams,
+ * other threads) race; serialise them.  The first call on a device looks up
+ * the array's address (cudaGetSymbolAddress): make it before any stream
+ * capture. */
+int weno_solver_noalloc(double *ret_dev, const double *u_dev, const int *nX,
+                        int ndim, int N, int V, void *stream);
+
 /* ---------------- single stages (for checking each kernel) ------------ */
 
 /* Ghost fill (src/grid/boundaries.cpp:25-53): u (prod nX x V) ->

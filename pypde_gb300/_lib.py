@@ -57,6 +57,7 @@ SIGNATURES = {
                               c_double, ip, c_bool, c_int, c_int, c_int, dp, POINTER(Options),
                               POINTER(Stats)]),
     "weno_solver": (c_int, [dp, dp, ip, c_int, c_int, c_int]),
+    "weno_solver_noalloc": (c_int, [c_void_p, c_void_p, ip, c_int, c_int, c_int, c_void_p]),
     "pypde_boundaries": (c_int, [dp, ip, c_int, ip, c_int, c_int, dp]),
     "pypde_timestep": (c_int, [c_void_p, dp, c_longlong, dp, c_int, c_int, c_double, c_double,
                                c_double, c_longlong, dp]),
