@@ -603,6 +603,24 @@ __device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d,
   return max_abs_eig<V>(M);
 }
 
+// The FD Jacobian + B itself (src/eigs/system.cpp:6-26).
+template <class Sys>
+__device__ __forceinline__ void system_matrix(double *M, double *q, double *dq,
+                                              int d) {
+  constexpr int V = Sys::V;
+  if (Sys::HAS_F)
+    fd_jacobian<Sys>(M, q, dq, d, false);
+  else
+    for (int i = 0; i < V * V; i++)
+      M[i] = 0.0;
+  if (Sys::HAS_B) {
+    double b[V * V];
+    Sys::B(b, q, d);
+    for (int i = 0; i < V * V; i++)
+      M[i] += b[i];
+  }
+}
+
 // 2 (N+1) / dX_d * max|eig(dF/d(dq_d))| (src/eigs/system.cpp:53-61)
 template <class Sys>
 __device__ __forceinline__ double max_abs_eigs_2nd(double *q, double *dq, int d,

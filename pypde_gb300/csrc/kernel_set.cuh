@@ -12,7 +12,10 @@ template <class Sys, int N> KernelSet make_kernel_set() {
   KernelSet k;
   k.cfl.aot = (const void *)&k_cfl<Sys, N>;
   k.predictor.aot = (const void *)&k_predictor<Sys, N>;
-  k.faces.aot = (const void *)&k_faces<Sys, N>;
+  k.faces.aot = (const void *)&k_faces<Sys, N, 0>;
+  k.faces_flux[0].aot = (const void *)&k_faces<Sys, N, 0>;
+  k.faces_flux[1].aot = (const void *)&k_faces<Sys, N, 1>;
+  k.faces_flux[2].aot = (const void *)&k_faces<Sys, N, 2>;
   k.centers.aot = (const void *)&k_centers<Sys, N>;
   k.gather.aot = (const void *)&k_gather<Sys, N>;
   k.newton.aot = (const void *)&k_newton<Sys, N>;

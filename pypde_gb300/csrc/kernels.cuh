@@ -24,6 +24,7 @@
 #pragma once
 
 #include "ader_common.cuh"
+#include "eig_full.cuh"
 
 namespace pypde {
 
@@ -789,6 +790,112 @@ __device__ __forceinline__ void rusanov_flux(double *f, double *qL,
   }
 }
 
+// |A| Dq from an eigen-decomposition A = R Lambda R^-1: solve R b = Dq,
+// scale by |lambda|, multiply by R (fluxes.cpp:36-41, 64-69).  With
+// accumulate, out += weight * that.
+template <int V>
+__device__ __noinline__ void abs_apply(const double *M, const double *Dq,
+                                       double *out, double weight,
+                                       bool accumulate) {
+  double wr[V], wi[V], vr[V * V], vi[V * V];
+  eig_full<V>(M, wr, wi, vr, vi);
+  double mr[V * V], mi[V * V], br[V], bi[V];
+  for (int i = 0; i < V * V; i++) {
+    mr[i] = vr[i];
+    mi[i] = vi[i];
+  }
+  for (int i = 0; i < V; i++) {
+    br[i] = Dq[i];
+    bi[i] = 0.0;
+  }
+  csolve<V>(mr, mi, br, bi);
+  for (int i = 0; i < V; i++) {
+    double l = sqrt(wr[i] * wr[i] + wi[i] * wi[i]);
+    br[i] *= l;
+    bi[i] *= l;
+  }
+  for (int i = 0; i < V; i++) {
+    double s = 0;
+    for (int j = 0; j < V; j++)
+      s += vr[i * V + j] * br[j] - vi[i * V + j] * bi[j];
+    out[i] = accumulate ? out[i] + weight * s : weight * s;
+  }
+}
+
+// Osher: sum_i W_i |A(q_i)| (qL - qR) along the straight path
+// q_i = qR + x_i (qL - qR) (fluxes.cpp:20-45).
+template <class Sys, int N>
+__device__ __forceinline__ void osher_d(double *ret, const double *qL,
+                                        const double *qR, const double *dqL,
+                                        const double *dqR, int d,
+                                        const Tables &T) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  double Dq[V], q[V], dq[D * V], M[V * V];
+  for (int v = 0; v < V; v++) {
+    Dq[v] = qL[v] - qR[v];
+    ret[v] = 0.0;
+  }
+  for (int i = 0; i < N; i++) {
+    for (int v = 0; v < V; v++)
+      q[v] = qR[v] + T.nodes[i] * Dq[v];
+    for (int k = 0; k < D * V; k++)
+      dq[k] = dqR[k] + T.nodes[i] * (dqL[k] - dqR[k]);
+    system_matrix<Sys>(M, q, dq, d);
+    abs_apply<V>(M, Dq, ret, T.wghts[i], true);
+  }
+}
+
+// Roe: |sum_i W_i A(q_i)| (qL - qR) (fluxes.cpp:47-70).
+template <class Sys, int N>
+__device__ __forceinline__ void roe_d(double *ret, const double *qL,
+                                      const double *qR, const double *dqL,
+                                      const double *dqR, int d,
+                                      const Tables &T) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  double Dq[V], q[V], dq[D * V], M[V * V], Mi[V * V];
+  for (int v = 0; v < V; v++)
+    Dq[v] = qL[v] - qR[v];
+  for (int i = 0; i < V * V; i++)
+    M[i] = 0.0;
+  for (int i = 0; i < N; i++) {
+    for (int v = 0; v < V; v++)
+      q[v] = qR[v] + T.nodes[i] * Dq[v];
+    for (int k = 0; k < D * V; k++)
+      dq[k] = dqR[k] + T.nodes[i] * (dqL[k] - dqR[k]);
+    system_matrix<Sys>(Mi, q, dq, d);
+    for (int k = 0; k < V * V; k++)
+      M[k] += T.wghts[i] * Mi[k];
+  }
+  abs_apply<V>(M, Dq, ret, 1.0, false);
+}
+
+// Roe / Osher numerical flux D + F(qL) + F(qR) (+ the second-order term),
+// fluxes.cpp:80-101.
+template <class Sys, int N, int FLUX>
+__device__ __forceinline__ void eig_flux(double *f, double *qL, double *qR,
+                                         double *dqL, double *dqR, int d,
+                                         double dXd, const Tables &T) {
+  constexpr int V = Sys::V;
+  if (FLUX == 1)
+    roe_d<Sys, N>(f, qL, qR, dqL, dqR, d, T);
+  else
+    osher_d<Sys, N>(f, qL, qR, dqL, dqR, d, T);
+  double fL[V], fR[V];
+  Sys::F(fL, qL, dqL, d);
+  Sys::F(fR, qR, dqR, d);
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    f[v] += fL[v] + fR[v];
+  if (Sys::SECOND_ORDER) {
+    double a1 = max_abs_eigs_2nd<Sys>(qL, dqL, d, N, dXd);
+    double a2 = max_abs_eigs_2nd<Sys>(qR, dqR, d, N, dXd);
+    double mm = fmax(a1, a2);
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      f[v] += mm * (qL[v] - qR[v]);
+  }
+}
+
 template <class Sys, int N>
 __device__ __forceinline__ void bint(double *ret, const double *qL,
                                      const double *qR, int d,
@@ -825,7 +932,7 @@ struct FaceIndex {
   long long nface[3]; // faces per direction
 };
 
-template <class Sys, int N>
+template <class Sys, int N, int FLUX = 0>
 __global__ void __launch_bounds__(128)
     k_faces(const double *__restrict__ qh, double *__restrict__ contrib,
             Geom g, Tables T, FaceIndex fi, DevState *st) {
@@ -898,8 +1005,12 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int v = 0; v < V; v++)
       f[v] = b[v] = 0.0;
-    if (Sys::HAS_F)
-      rusanov_flux<Sys, N>(f, q0, q1, dq0, dq1, d, g.dX[d]);
+    if (Sys::HAS_F) {
+      if (FLUX == 0)
+        rusanov_flux<Sys, N>(f, q0, q1, dq0, dq1, d, g.dX[d]);
+      else
+        eig_flux<Sys, N, FLUX>(f, q0, q1, dq0, dq1, d, g.dX[d], T);
+    }
     if (Sys::HAS_B)
       bint<Sys, N>(b, q0, q1, d, T);
     double tmp = dt * T.wghts[t] / (2. * g.dX[d]);

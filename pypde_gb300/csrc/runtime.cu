@@ -285,7 +285,7 @@ struct StepCtx {
   Geom g;
   FaceIndex fi;
   Tables T;
-  int N, V, ring;
+  int N, V, ring, flux;
   double tol;
   bool stiff, faces, centers;
   double *u, *uprev, *ub, *tmpA, *tmpB, *w, *qh, *contrib, *cen, *ringbuf,
@@ -319,8 +319,9 @@ static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
   if (c.faces) {
     void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
                  (void *)&fi,   (void *)&c.st};
-    e = launch(k.faces, dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)),
-               dim3(128), 0, s, a);
+    e = launch(k.faces_flux[c.flux],
+               dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)), dim3(128), 0,
+               s, a);
     if (e != cudaSuccess)
       return e;
   }
@@ -395,8 +396,9 @@ static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
       FaceIndex fi = c.fi;
       void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
                    (void *)&fi,   (void *)&c.st};
-      e = launch(k.faces, dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)),
-                 dim3(128), 0, s, a);
+      e = launch(k.faces_flux[c.flux],
+                 dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)), dim3(128),
+                 0, s, a);
       if (e != cudaSuccess)
         return e;
     }
@@ -464,9 +466,9 @@ static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
     set_error("stiff predictor not built for system " + sys.name);
     return PYPDE_ERR_UNSUPPORTED;
   }
-  if (flux != 0) {
-    set_error("only the Rusanov flux (FLUX=0) is built");
-    return PYPDE_ERR_UNSUPPORTED;
+  if (flux < 0 || flux > 2 || !sys.sets[N].faces_flux[flux].valid()) {
+    set_error("FLUX must be 0 (Rusanov), 1 (Roe) or 2 (Osher)");
+    return PYPDE_ERR_ARG;
   }
   return PYPDE_OK;
 }
@@ -513,6 +515,7 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
     return PYPDE_ERR_ARG;
   }
   c.stiff = a.stiff;
+  c.flux = a.flux;
   c.tol = a.newton_tol;
   c.faces = sys.has_F || sys.has_B;
   c.centers = sys.has_B || sys.has_S;
@@ -901,6 +904,7 @@ int stage_fv(const SystemDesc &sys, double *u, const double *qh,
   c.V = sys.V;
   c.faces = sys.has_F || sys.has_B;
   c.centers = sys.has_B || sys.has_S;
+  c.flux = flux;
   int Nd = ipow(N, ndim);
   long long usz = c.g.C * c.V, qsz = c.g.Cw * N * Nd * c.V;
   CK(ensure(ar->u, usz * 8));

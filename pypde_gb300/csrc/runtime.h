@@ -23,6 +23,7 @@ struct KFunc {
 // Kernels of one (system, order).
 struct KernelSet {
   KFunc cfl, predictor, newton, faces, centers, gather;
+  KFunc faces_flux[3]; // Rusanov, Roe, Osher
   int pred_threads = 0, pred_cpb = 0;
   size_t pred_smem = 0;
   int newton_threads = 0, newton_cpb = 0;

@@ -151,8 +151,41 @@ def ref_stiff_predictor(shape, N, seed, dt):
     return tag
 
 
+def ref_flux_points():
+    """D(qL,qR) + F(qL) + F(qR) and the B path integral at single face
+    points through the reference's FluxGenerator (fluxes.cpp:80-117), for
+    Rusanov (0), Roe (1) and Osher (2)."""
+    R = ora.ref()
+    R.ref_flux.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int] + [ora.dp] * 4 + \
+        [ctypes.c_int, ctypes.c_int, ora.dp, ora.dp]
+    out = {}
+    for name, ndim, N in (("euler", 1, 2), ("euler", 2, 3), ("ncp", 2, 2), ("cattaneo", 2, 2)):
+        u = workloads.random_state(name, (6,) * ndim, 11).reshape(-1, workloads.random_state(
+            name, (1,) * ndim, 0).shape[-1])
+        if name == "cattaneo":
+            u[:, -1] = -3.0
+        V = u.shape[1]
+        qL, qR = u[:-1].copy(), u[1:].copy()
+        for flux in (0, 1, 2):
+            f = np.zeros_like(qL)
+            b = np.zeros_like(qL)
+            for i in range(len(qL)):
+                dq = np.zeros(ndim * V)
+                fi, bi = np.zeros(V), np.zeros(V)
+                R.ref_flux(name.encode(), ndim, N, ora.ptr(qL[i].copy()), ora.ptr(qR[i].copy()),
+                           ora.ptr(dq), ora.ptr(dq.copy()), i % ndim, flux, ora.ptr(fi),
+                           ora.ptr(bi))
+                f[i], b[i] = fi, bi
+            out[f"{name}{ndim}_N{N}_flux{flux}_f"] = f
+            out[f"{name}{ndim}_N{N}_flux{flux}_b"] = b
+        out[f"{name}{ndim}_N{N}_qL"] = qL
+        out[f"{name}{ndim}_N{N}_qR"] = qR
+    np.savez_compressed(os.path.join(OUT, "flux_points.npz"), **out)
+
+
 def main():
     ref_tables()
+    ref_flux_points()
     for system, shape, N, bt in [("euler", (40,), 2, [0]), ("euler", (40,), 3, [1]),
                                  ("euler", (12, 10), 2, [1, 0]), ("euler", (12, 10), 3, [1, 1]),
                                  ("cattaneo", (10, 8), 2, [1, 1])]:

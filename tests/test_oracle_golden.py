@@ -121,3 +121,28 @@ def test_slab_count_invariance():
     a = ora.pde_solver("euler", u0, 1.0, [1.0, 1.0], [1, 1], 0.8, 2, max_steps=3, nthreads=1)
     b = ora.pde_solver("euler", u0, 1.0, [1.0, 1.0], [1, 1], 0.8, 2, max_steps=3, nthreads=5)
     assert np.array_equal(a[0], b[0])
+
+
+@pytest.mark.parametrize("case", [("euler", 1, 2), ("euler", 2, 3), ("ncp", 2, 2),
+                                  ("cattaneo", 2, 2)])
+@pytest.mark.parametrize("flux", [0, 1, 2])
+def test_face_fluxes_match_reference(case, flux):
+    """Rusanov / Roe / Osher (with the B path integral) at single face
+    points against the reference's FluxGenerator."""
+    import ctypes
+    name, ndim, N = case
+    z = load("flux_points.npz")
+    key = f"{name}{ndim}_N{N}"
+    s = ora.PortSystem(name, ndim)
+    P = ora.port()
+    P.ora_face_flux.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_int] * 4 + [ora.dp] * 4 + \
+        [ctypes.c_int, ctypes.c_int, ora.dp, ora.dp]
+    qL, qR = z[key + "_qL"], z[key + "_qR"]
+    for i in range(len(qL)):
+        f, b = np.zeros(s.V), np.zeros(s.V)
+        dq = np.zeros(ndim * s.V)
+        P.ora_face_flux(s.F, s.B, ndim, N, s.V, 0, ora.ptr(qL[i].copy()), ora.ptr(qR[i].copy()),
+                        ora.ptr(dq), ora.ptr(dq.copy()), i % ndim, flux, ora.ptr(f), ora.ptr(b))
+        fr, br = z[f"{key}_flux{flux}_f"][i], z[f"{key}_flux{flux}_b"][i]
+        assert np.abs(f - fr).max() <= 1e-12 * np.abs(fr).max()
+        assert np.abs(b - br).max() <= 1e-12 * max(np.abs(br).max(), 1e-300)
