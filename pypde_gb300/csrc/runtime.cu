@@ -451,12 +451,24 @@ static int check_grid(int ndim, const int *nX, const int *bt, int N) {
   return PYPDE_OK;
 }
 
+int jit_ensure(SystemDesc &d, int N);
+
+// Kernels of a run-time compiled system are built on first use of an order
+// N, on the current device (called after the device is selected).
+static int ensure_kernels(const SystemDesc &sys, int N) {
+  if (N < 1 || N > MAXN || sys.have[N] || !sys.module)
+    return PYPDE_OK;
+  return jit_ensure(const_cast<SystemDesc &>(sys), N);
+}
+
 static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
                         int flux) {
   if (sys.ndim != ndim) {
     set_error("system was built for another number of dimensions");
     return PYPDE_ERR_ARG;
   }
+  if (sys.module && N >= 1 && N <= 3)
+    return PYPDE_OK; // compiled on first use (ensure_kernels)
   if (N < 1 || N > MAXN || !sys.have[N]) {
     set_error("order N=" + std::to_string(N) + " is not built for system " +
               sys.name);
@@ -501,6 +513,8 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   Arena *ar;
   rc = arena_for(a.device, &ar);
   if (rc)
+    return rc;
+  if ((rc = ensure_kernels(sys, a.N)))
     return rc;
   cudaStream_t s = ar->stream;
   StepCtx c;
@@ -788,6 +802,8 @@ int stage_timestep(const SystemDesc &sys, const double *w, long long nrows,
   Arena *ar;
   if ((rc = arena_for(0, &ar)))
     return rc;
+  if ((rc = ensure_kernels(sys, N)))
+    return rc;
   DevState *st;
   if ((rc = put_state(ar, &st, t, tf, cfl, count, 0)))
     return rc;
@@ -834,6 +850,8 @@ int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
   std::lock_guard<std::mutex> lock(g_mu);
   Arena *ar;
   if ((rc = arena_for(0, &ar)))
+    return rc;
+  if ((rc = ensure_kernels(sys, N)))
     return rc;
   DevState *st;
   if ((rc = put_state(ar, &st, 0, 1, 1, 0, dt)))
@@ -889,6 +907,8 @@ int stage_fv(const SystemDesc &sys, double *u, const double *qh,
   std::lock_guard<std::mutex> lock(g_mu);
   Arena *ar;
   if ((rc = arena_for(0, &ar)))
+    return rc;
+  if ((rc = ensure_kernels(sys, N)))
     return rc;
   DevState *st;
   if ((rc = put_state(ar, &st, 0, 1, 1, 0, dt)))

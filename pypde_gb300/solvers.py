@@ -2,10 +2,11 @@
 (haranjackson/PyPDE pypde/solvers.py:13-244), run on the GPU.
 
 Differences from the reference, all at the callback boundary:
-  * F, B and S must be callbacks the GPU can run: the built-in systems of
-    pypde_gb300.systems, or Python functions that pypde_gb300.callbacks can
-    translate to device code (the reference compiles them with numba into
-    host cfuncs, pypde/cfuncs.py:30-75).
+  * F, B and S run on the GPU: the built-in systems of pypde_gb300.systems
+    use kernels compiled ahead of time; other Python callbacks are
+    translated to device code (pypde_gb300.translate) and compiled at run
+    time with NVRTC (the reference compiles them with numba into host
+    cfuncs, pypde/cfuncs.py:30-75).  jit=True forces the run-time path.
   * ``nThreads`` is accepted and ignored (one GPU does the work of the
     reference's CPU thread pool).
   * Extensions (keyword-only): ``max_steps``, ``newton_tol``, ``device``,
@@ -22,7 +23,7 @@ FLUXES = {"rusanov": 0, "roe": 1, "osher": 2}
 
 def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cfl=0.9,
                order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *,
-               max_steps=None, newton_tol=None, device=0, stats=None):
+               max_steps=None, newton_tol=None, device=0, stats=None, jit=False):
     """Solve dQ/dt + div F(Q, grad Q) + B(Q) . grad Q = S(Q) on [0, L] (see
     pypde/solvers.py:28-175 for the full description of the arguments).
 
@@ -40,7 +41,7 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
 
     useF, useB, useS = F is not None, B is not None, S is not None
     secondOrder = useF and nargs(F) == 3
-    system = resolve_system(F, B, S, ndim, V, secondOrder)
+    system = resolve_system(F, B, S, ndim, V, secondOrder, jit=jit)
 
     ret = np.zeros(ndt * Q0.size)
     ur = Q0.ravel()

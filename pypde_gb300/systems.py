@@ -31,7 +31,7 @@ def pow10_portable(x):
     p = 1.0
     for k in range(18, 0, -1):
         p = 1.0 + p * r / k
-    return np.ldexp(p, int(n))
+    return float(np.ldexp(p, int(n)))
 
 
 @dataclass
@@ -51,25 +51,21 @@ def _tag(fn, name, ndim, role):
     return fn
 
 
-def _euler_flux(Q, ndim, d):
-    r = Q[0]
-    ke = 0.0
-    for i in range(ndim):
-        ke += Q[1 + i] * Q[1 + i]
-    p = (GAMMA - 1.0) * (Q[ndim + 1] - 0.5 * ke / r)
-    ud = Q[1 + d] / r
-    out = np.empty(len(Q))
-    out[0] = Q[1 + d]
-    for i in range(ndim):
-        out[1 + i] = Q[1 + i] * ud
-    out[1 + d] += p
-    out[ndim + 1] = (Q[ndim + 1] + p) * ud
-    return out, p
-
-
 def euler(ndim):
     def F(Q, d):
-        return _euler_flux(Q, ndim, d)[0][:ndim + 2]
+        r = Q[0]
+        ke = 0.0
+        for i in range(ndim):
+            ke += Q[1 + i] * Q[1 + i]
+        p = (GAMMA - 1.0) * (Q[ndim + 1] - 0.5 * ke / r)
+        ud = Q[1 + d] / r
+        out = np.zeros(ndim + 2)
+        out[0] = Q[1 + d]
+        for i in range(ndim):
+            out[1 + i] = Q[1 + i] * ud
+        out[1 + d] += p
+        out[ndim + 1] = (Q[ndim + 1] + p) * ud
+        return out
 
     return System("euler", ndim, ndim + 2, _tag(F, "euler", ndim, "F"), None, None)
 
@@ -78,18 +74,28 @@ def cattaneo(ndim):
     V = 2 * ndim + 3
 
     def F(Q, d):
-        out, p = _euler_flux(Q, ndim, d)
+        r = Q[0]
+        ke = 0.0
+        for i in range(ndim):
+            ke += Q[1 + i] * Q[1 + i]
+        p = (GAMMA - 1.0) * (Q[ndim + 1] - 0.5 * ke / r)
+        ud = Q[1 + d] / r
+        out = np.zeros(V)
+        out[0] = Q[1 + d]
+        for i in range(ndim):
+            out[1 + i] = Q[1 + i] * ud
+        out[1 + d] += p
+        out[ndim + 1] = (Q[ndim + 1] + p) * ud
         T = p / Q[0]
         out[ndim + 1] += Q[ndim + 2 + d]
-        out[ndim + 2:2 * ndim + 2] = 0.0
         out[ndim + 2 + d] = KAPPA_H * T
-        out[2 * ndim + 2] = 0.0
         return out
 
     def S(Q):
         inv_tau = pow10_portable(-Q[2 * ndim + 2])
         out = np.zeros(V)
-        out[ndim + 2:2 * ndim + 2] = -Q[ndim + 2:2 * ndim + 2] * inv_tau
+        for i in range(ndim):
+            out[ndim + 2 + i] = -Q[ndim + 2 + i] * inv_tau
         return out
 
     return System("cattaneo", ndim, V, _tag(F, "cattaneo", ndim, "F"), None,

@@ -71,7 +71,14 @@ def test_builtin_python_callbacks_match_c_callbacks():
             assert np.array_equal(out, s.F(q, d))
 
 
-def test_unknown_callback_is_rejected():
+def untranslatable_flux(Q, d):
+    return [q * d for q in Q]
+
+
+def test_untranslatable_callback_is_rejected():
+    """Callbacks outside the translatable subset fail with a message naming
+    the function and line, before any device work."""
     from pypde_gb300.solvers import pde_solver
-    with pytest.raises(NotImplementedError):
-        pde_solver(np.ones((8, 3)), 0.1, [1.0], F=lambda Q, d: Q, stiff=False)
+    from pypde_gb300.translate import TranslateError
+    with pytest.raises(TranslateError, match="untranslatable_flux"):
+        pde_solver(np.ones((8, 3)), 0.1, [1.0], F=untranslatable_flux, stiff=False)

@@ -1,0 +1,166 @@
+"""The Python -> CUDA C++ callback translator (pypde_gb300/translate.py).
+
+Each translated callback is compiled as host C++ (the device qualifiers
+defined away, no FMA contraction) and evaluated on random states against
+the Python function itself: same operation order, so the same bits (a few
+ulp where a libm function and numpy's differ).  A second test compiles the
+full kernel templates for a translated system with NVRTC, which needs no
+GPU.
+"""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from pypde_gb300 import systems, workloads
+from pypde_gb300.translate import TranslateError, translate
+
+GAMMA = 1.4
+RHO_FLOOR = 1e-12
+COEF = (0.3, 0.7, 1.1)
+
+
+def helper_pressure(Q, n):
+    ke = 0.0
+    for i in range(n):
+        ke += Q[1 + i] * Q[1 + i]
+    return (GAMMA - 1.0) * (Q[n + 1] - 0.5 * ke / Q[0])
+
+
+def user_euler2(Q, d):
+    """numpy style: slices, array arithmetic, a helper, a conditional."""
+    r = max(Q[0], RHO_FLOOR)
+    v = Q[1:3] / r
+    p = helper_pressure(Q, 2)
+    ret = v[d] * Q
+    ret[1 + d] += p
+    ret[3] += p * v[d]
+    return ret
+
+
+def user_src(Q):
+    out = np.zeros(4)
+    e = Q[3] / Q[0]
+    out[3] = -0.5 * e if e > 2.0 else 0.25 * e ** 2
+    out[1] = COEF[0] * Q[1] + COEF[1] * Q[2]
+    return out
+
+
+def user_ncp(Q, d):
+    B = np.zeros((4, 4))
+    for i in range(4):
+        B[i, i] = Q[0] * COEF[d]
+    B[1, 2] = 0.1
+    B[2][1] = 0.1
+    return B
+
+
+def user_second_order(Q, DQ, d):
+    a, b = 0.5, 0.01
+    return np.array([a * Q[0] * Q[0] - b * DQ[d][0] + b * DQ[d, 0] * 0.0])
+
+
+CASES = [
+    ("F", user_euler2, 2, 4), ("S", user_src, 2, 4), ("B", user_ncp, 2, 4),
+    ("F", user_second_order, 1, 1),
+    ("F", systems.euler(1).F, 1, 3), ("F", systems.euler(2).F, 2, 4),
+    ("F", systems.euler(3).F, 3, 5), ("F", systems.cattaneo(2).F, 2, 7),
+    ("S", systems.cattaneo(2).S, 2, 7), ("F", systems.ncp(2).F, 2, 3),
+    ("B", systems.ncp(2).B, 2, 3), ("S", systems.ncp(2).S, 2, 3),
+    ("F", systems.burgers2().F, 1, 1),
+]
+
+
+def _host_lib(src, role):
+    d = tempfile.mkdtemp()
+    cpp = os.path.join(d, "cb.cpp")
+    so = os.path.join(d, "cb.so")
+    call = {"F": "UserSystem::F(out, Q, dQ, d);", "B": "UserSystem::B(out, Q, d);",
+            "S": "UserSystem::S(out, Q);"}[role]
+    with open(cpp, "w") as f:
+        f.write("#include <cmath>\nusing namespace std;\n#define __device__\n"
+                "#define __forceinline__ inline\n" + src +
+                "\nextern \"C\" void call(double *out, const double *Q, const double *dQ, int d)"
+                " { (void)dQ; (void)d; " + call + " }\n")
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", cpp, "-o", so],
+                   check=True)
+    lib = ctypes.CDLL(so)
+    lib.call.argtypes = [ctypes.POINTER(ctypes.c_double)] * 3 + [ctypes.c_int]
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}-{c[1].__name__}-{c[2]}d-V{c[3]}"
+                                             for c in CASES])
+def test_translated_callback_matches_python(case):
+    role, fn, ndim, V = case
+    src = translate(fn if role == "F" else None, fn if role == "B" else None,
+                    fn if role == "S" else None, ndim, V)
+    lib = _host_lib(src, role)
+    rng = np.random.default_rng(0)
+    nout = V * V if role == "B" else V
+    for k in range(50):
+        name = "cattaneo" if V == 7 else ("euler" if V == ndim + 2 else "ncp")
+        Q = workloads.random_state(name, (1,) * ndim, k).reshape(-1)[:V].copy() \
+            if name != "ncp" or V == 3 else 0.5 + rng.random(V)
+        if Q.shape[0] != V:
+            Q = 0.5 + rng.random(V)
+        dQ = rng.standard_normal(ndim * V)
+        for d in range(ndim if role != "S" else 1):
+            out = np.zeros(nout)
+            lib.call(_p(out), _p(Q), _p(dQ), d)
+            if role == "S":
+                want = fn(Q)
+            elif fn.__code__.co_argcount == 3:
+                want = fn(Q, dQ.reshape(ndim, V), d)
+            elif fn.__code__.co_argcount == 2:
+                want = fn(Q, d)
+            else:
+                want = fn(Q)
+            want = np.asarray(want, dtype=np.float64).reshape(-1)
+            assert np.array_equal(out, want), (k, d, out, want)
+
+
+def test_unsupported_constructs_are_reported():
+    def bad(Q, d):
+        return [q for q in Q]
+    with pytest.raises(TranslateError):
+        translate(bad, None, None, 1, 3)
+
+
+def test_nvrtc_compiles_the_kernels_for_a_translated_system():
+    try:
+        nv = ctypes.CDLL("libnvrtc.so")
+    except OSError:
+        try:
+            nv = ctypes.CDLL("/usr/local/cuda/lib64/libnvrtc.so")
+        except OSError:
+            pytest.skip("NVRTC not available")
+    here = os.path.join(os.path.dirname(__file__), "..", "pypde_gb300", "csrc")
+    names = ["kernels.cuh", "ader_common.cuh", "eig_full.cuh"]
+    hdrs = [open(os.path.join(here, n)).read().encode() for n in names]
+    src = ('#include "kernels.cuh"\n' + translate(user_euler2, user_ncp, user_src, 2, 4)).encode()
+    prog = ctypes.c_void_p()
+    arr = ctypes.c_char_p * 3
+    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src, b"u.cu", 3, arr(*hdrs),
+                                 arr(*[n.encode() for n in names])) == 0
+    for e in (b"&pypde::k_faces<UserSystem, 2, 0>", b"&pypde::k_newton<UserSystem, 2>"):
+        nv.nvrtcAddNameExpression(prog, e)
+    opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", b"--fmad=false"]
+    rc = nv.nvrtcCompileProgram(prog, len(opts), (ctypes.c_char_p * len(opts))(*opts))
+    n = ctypes.c_size_t()
+    nv.nvrtcGetProgramLogSize(prog, ctypes.byref(n))
+    log = ctypes.create_string_buffer(n.value)
+    nv.nvrtcGetProgramLog(prog, log)
+    assert rc == 0, log.value.decode()[:4000]
+
+
+def test_lambda_callback_translates():
+    src = translate(lambda Q, d: Q * 2.0, None, None, 1, 3)
+    assert "Q[i_] * 2.0" in src
