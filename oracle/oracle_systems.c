@@ -34,18 +34,25 @@
 
 static int g_ndim = 1;
 
-/* 10^x as 2^(x log2 10): y = n + r with n = round(y), 2^r = e^(r ln 2) by
- * its Taylor series (Horner, 18 terms), scaled by 2^n.  Built only from
- * IEEE +, *, /, floor and ldexp, so the host and the device evaluate it to
- * the same bits (a libm exp/pow may differ between the two in the last
- * place). */
+/* 10^x = 2^n e^r with n = round(x log2 10), |r| <= ln2/2, and e^r by its
+ * Taylor polynomial of degree 16 in Horner form (truncation below 1e-22).
+ * Built only from IEEE +, *, floor and ldexp, so the host and the device
+ * evaluate it to the same bits (a libm exp/pow may differ between the two in
+ * the last place).  INV_FACT[k] is the double nearest to 1/k!. */
+static const double INV_FACT[17] = {
+    1.0, 1.0, 0.5, 0.16666666666666666,
+    0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984,
+    2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08,
+    2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13,
+    4.779477332387385e-14};
+
 static double pow10_portable(double x) {
   double y = x * 3.321928094887362;
   double n = floor(y + 0.5);
   double r = (y - n) * 0.6931471805599453;
-  double p = 1.0;
-  for (int k = 18; k >= 1; k--)
-    p = 1.0 + p * r / k;
+  double p = INV_FACT[16];
+  for (int k = 15; k >= 0; k--)
+    p = p * r + INV_FACT[k];
   return ldexp(p, (int)n);
 }
 

@@ -675,6 +675,8 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         for (int i = k + 1; i < NL; i++) {
           double f = A[i * NL + k] * rp;
           A[i * NL + k] = f;
+          if (f == 0.0) // structural zero: the row is unchanged
+            continue;
           for (int j = k + 1; j < NL; j++)
             A[i * NL + j] = fma(-f, A[k * NL + j], A[i * NL + j]);
         }
@@ -695,11 +697,13 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
           }
         for (int k = 0; k < NL; k++)
           for (int i = k + 1; i < NL; i++)
-            b[i] = fma(-A[i * NL + k], b[k], b[i]);
+            if (A[i * NL + k] != 0.0)
+              b[i] = fma(-A[i * NL + k], b[k], b[i]);
         for (int i = NL - 1; i >= 0; i--) {
           double sacc = b[i];
           for (int j = i + 1; j < NL; j++)
-            sacc = fma(-A[i * NL + j], b[j], sacc);
+            if (A[i * NL + j] != 0.0)
+              sacc = fma(-A[i * NL + j], b[j], sacc);
           b[i] = sacc / A[i * NL + i];
         }
         for (int tt = 0; tt < N; tt++)

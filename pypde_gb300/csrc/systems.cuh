@@ -23,16 +23,24 @@
 
 namespace pypde {
 
-// 10^x from IEEE +, *, /, floor and ldexp only (2^(x log2 10), Taylor
-// series of 2^r on |r| <= 1/2), so that host and device agree bitwise.
+// 10^x = 2^n e^r with n = round(x log2 10), |r| <= ln2/2, and e^r by its
+// Taylor polynomial of degree 16 in Horner form (truncation below 1e-22),
+// from IEEE +, *, floor and ldexp only, so that host and device agree
+// bitwise.  The coefficients are the doubles nearest to 1/k!.
 __device__ __forceinline__ double pow10_portable(double x) {
+  constexpr double c[17] = {
+      1.0, 1.0, 0.5, 0.16666666666666666,
+      0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984,
+      2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08,
+      2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13,
+      4.779477332387385e-14};
   double y = x * 3.321928094887362;
   double n = floor(y + 0.5);
   double r = (y - n) * 0.6931471805599453;
-  double p = 1.0;
+  double p = c[16];
 #pragma unroll
-  for (int k = 18; k >= 1; k--)
-    p = 1.0 + p * r / k;
+  for (int k = 15; k >= 0; k--)
+    p = p * r + c[k];
   return ldexp(p, (int)n);
 }
 

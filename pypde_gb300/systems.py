@@ -23,14 +23,21 @@ GAMMA = 1.4
 KAPPA_H = 1.0  # kappa / tau_ref = 1e-2 / 1e-2
 
 
+# 1/k! for k = 0..16, each the double nearest to it
+_INV_FACT = (1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08, 2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13, 4.779477332387385e-14)
+
+
 def pow10_portable(x):
-    """10^x from +, *, /, floor and ldexp (bitwise equal on host and device)."""
+    """10^x from +, *, floor and ldexp only, so that host and device agree
+    bitwise: 10^x = 2^n e^r with n = round(x log2 10), |r| <= ln2/2, and e^r
+    by its Taylor polynomial of degree 16 in Horner form (truncation error
+    below 1e-22)."""
     y = x * 3.321928094887362
     n = np.floor(y + 0.5)
     r = (y - n) * 0.6931471805599453
-    p = 1.0
-    for k in range(18, 0, -1):
-        p = 1.0 + p * r / k
+    p = _INV_FACT[16]
+    for k in range(15, -1, -1):
+        p = p * r + _INV_FACT[k]
     return float(np.ldexp(p, int(n)))
 
 
