@@ -38,6 +38,7 @@ extern "C" {
 #define PYPDE_ERR_COMPILE 5     /* run-time compilation of callbacks failed */
 
 typedef struct pypde_system pypde_system;
+typedef struct pypde_warm_start pypde_warm_start;
 
 /* Options and statistics of pde_solver_ex (extensions; no reference
  * counterpart).  Zero-initialise and set what you need. */
@@ -48,6 +49,8 @@ typedef struct {
   int steps_per_graph;   /* steps per CUDA graph launch; 0 -> automatic */
   int profile_stages;    /* 1: launch eagerly and time every stage with CUDA
                             events (fills pypde_stats.stage_seconds) */
+  const pypde_warm_start *warm_start; /* stiff form: learned initial guess of
+                            the Newton predictor (NULL: plain guess) */
 } pypde_options;
 
 /* Stages timed by pypde_options.profile_stages, in this order. */
@@ -71,6 +74,8 @@ typedef struct {
   double device_seconds;           /* time of the stepping loop on the GPU */
   long long kernel_launches;       /* kernels of this library launched */
   double stage_seconds[8];         /* per stage, with profile_stages */
+  unsigned long long pred_fallbacks; /* warm-started cells that fell back to
+                                      the plain guess */
 } pypde_stats;
 
 /* ---------------- callback systems ---------------- */
@@ -174,6 +179,70 @@ int pypde_tables(int N, double *out);
  * chain FMA loop: the roofline denominator of the FP64-bound kernels.
  * Bench support; no reference counterpart. */
 int pypde_measure_fp64_peak(int device, double *tflops);
+
+/* ---------------- learned warm start (no reference counterpart) ---------
+ * A per-cell MLP maps the WENO coefficients of a cell and log10(dt/tau) to
+ * the initial guess of the stiff predictor's Newton iteration, which then
+ * iterates to the same tolerance and falls back to the plain guess q = w
+ * at the first iteration whose residual does not fall.  Network: feat
+ * features padded to k1 -> 128 -> 128 -> no, SiLU, BF16 weights, FP32
+ * accumulation.  Features of a cell: the V means over its N^ndim nodes,
+ * the N^ndim*V deviations from them, log10(dt) - mean[tau_var] (log10(dt)
+ * when tau_var < 0) and log10(r), all normalised by x_mean/x_scale, after
+ * which the deviations are divided by their RMS r; outputs: the correction
+ * qh - w at the N^(ndim+1)*V space-time values divided by r, padded to
+ * no. */
+
+/* Widths for (sys, N); PYPDE_ERR_UNSUPPORTED when sys has no source. */
+int pypde_warm_start_shape(const pypde_system *sys, int N, int *feat, int *k1,
+                           int *no);
+/* Upload a trained network (FP32 host arrays; weights row-major [out][in]:
+ * W1 128 x k1, W2 128 x 128, W3 no x 128; x = (f - x_mean) * x_scale;
+ * correction = (y * y_scale + y_mean) * r). */
+int pypde_warm_start_create(const pypde_system *sys, int N, int device,
+                            const float *W1, const float *b1, const float *W2,
+                            const float *b2, const float *W3, const float *b3,
+                            const float *x_mean, const float *x_scale,
+                            const float *y_mean, const float *y_scale,
+                            int tau_var, pypde_warm_start **out);
+int pypde_warm_start_free(pypde_warm_start *ws);
+
+/* Stiff predictor started from an initial guess: the host array guess
+ * (N*nrows x V) or, with guess NULL, the network warm. */
+int pypde_predictor_guess(const pypde_system *sys, const double *w,
+                          long long nrows, const double *dX, int ndim, int N,
+                          double dt, double newton_tol, const double *guess,
+                          const pypde_warm_start *warm, double *qh,
+                          pypde_stats *stats);
+
+/* Training pairs: runs pde_solver_ex for at most `steps` steps and, after
+ * the predictor of step k, samples per_step reconstruction cells (every
+ * stride-th, from an offset that changes with k): their WENO coefficients
+ * (w_out, steps*per_step x N^ndim*V), converged predictor (qh_out,
+ * steps*per_step x N^(ndim+1)*V) and dt (dt_out, steps). */
+int pypde_harvest(const pypde_system *sys, double *u, double tf,
+                  const int *nX, int ndim, const double *dX, double CFL,
+                  const int *boundaryTypes, bool STIFF, int N, int steps,
+                  long long per_step, long long stride, double *w_out,
+                  double *qh_out, double *dt_out, const pypde_options *opt,
+                  pypde_stats *stats);
+
+/* Training kernels on device pointers, enqueued on `stream` (a
+ * cudaStream_t; NULL = legacy default stream).
+ * C[M][N] = sum_k A(m,k) B(k,n), A(m,k) = A[m*sam + k*sak],
+ * B(k,n) = B[k*sbk + n*sbn], both rounded to BF16, FP32 accumulation;
+ * then C += bias[n] and act = SiLU(C) when those pointers are non-NULL
+ * (C may be NULL).  splits > 1 splits k, summed in a fixed order through
+ * work (splits*M*N floats). */
+int pypde_mlp_gemm(const float *A, long long sam, long long sak,
+                   const float *B, long long sbk, long long sbn, float *C,
+                   int M, int N, int K, int splits, float *work,
+                   const float *bias, float *act, void *stream);
+/* dZ = dA * SiLU'(Z), n elements. */
+int pypde_mlp_silu_grad(const float *dA, const float *Z, float *dZ,
+                        long long n, void *stream);
+/* out[n] = sum over m of X[m][n] (M x N row-major), fixed order. */
+int pypde_mlp_colsum(const float *X, int M, int N, float *out, void *stream);
 
 const char *pypde_last_error(void);
 

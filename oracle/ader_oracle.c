@@ -1573,17 +1573,26 @@ static void lu_solve(const double *a, int n, const int *piv, double *b) {
  *                                          - DG_MAT[t,k] d_vw
  *   q <- q - A^{-1} obj(q) / prod W_idx
  * Stops when ||obj(q)||_inf <= tol (or at the rounding floor of obj). */
+/* With q_plain non-null, q holds a warm start (a learned guess) and
+ * q_plain the plain guess: the first iteration whose residual does not
+ * fall below the previous one, or has an entry that is not finite, spends
+ * itself resetting q to q_plain, after which the iteration is the plain
+ * one; *fell_back is set. */
 static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
-                     double tol, dg_scratch *s) {
+                     double tol, dg_scratch *s, const double *q_plain,
+                     int *fell_back) {
   int N = c->N, V = c->V, Nd = c->Nd;
   int n = N * Nd * V, nl = N * V;
   double r[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
   double A[ORA_MAXN * ORA_MAXV * ORA_MAXN * ORA_MAXV], b[ORA_MAXN * ORA_MAXV];
   int piv[ORA_MAXN * ORA_MAXV];
   int failed = 0;
+  int on_guess = q_plain != NULL;
+  double prev = INFINITY;
   for (int it = 0; it < NEWTON_MAXIT; it++) {
     dg_rhs(c, q, Ww, dt, r, s);
     double res = 0, scale = 0;
+    int bad = 0; /* a residual entry that is not finite */
     for (int t = 0; t < N; t++)
       for (int idx = 0; idx < Nd; idx++)
         for (int v = 0; v < V; v++) {
@@ -1596,7 +1605,18 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
           r[i] = rr - uq;
           res = fmax(res, fabs(r[i]));
           scale = fmax(scale, fmax(fabs(rr), fabs(uq)));
+          if (!(fabs(r[i]) <= DBL_MAX))
+            bad = 1;
         }
+    if (on_guess) {
+      if (bad || !(res < prev)) {
+        memcpy(q, q_plain, sizeof(double) * n);
+        on_guess = 0;
+        *fell_back = 1;
+        continue;
+      }
+      prev = res;
+    }
     if (res <= tol || res <= 16 * DBL_EPSILON * scale)
       return it;
     for (int idx = 0; idx < Nd; idx++) {
@@ -1644,7 +1664,7 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
 
 static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
                             int stiff, double dt, double tol, double *qh,
-                            int *maxit) {
+                            int *maxit, const double *guess, long *fallbacks) {
   int N = c->N, V = c->V, Nd = c->Nd;
   int n = N * Nd * V;
   dg_scratch *s = malloc(sizeof(dg_scratch));
@@ -1655,8 +1675,16 @@ static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
   for (long cell = c0; cell < c1; cell++) {
     dg_init(c, w + cell * Nd * V, Ww, q0);
     int it;
-    if (stiff) {
-      it = dg_newton(c, q0, Ww, dt, tol, s);
+    if (stiff && guess) {
+      int fb = 0;
+      memcpy(q1, q0, sizeof(double) * n);
+      memcpy(q0, guess + cell * n, sizeof(double) * n);
+      it = dg_newton(c, q0, Ww, dt, tol, s, q1, &fb);
+      memcpy(qh + cell * n, q0, sizeof(double) * n);
+      if (fallbacks)
+        *fallbacks += fb;
+    } else if (stiff) {
+      it = dg_newton(c, q0, Ww, dt, tol, s, NULL, NULL);
       memcpy(qh + cell * n, q0, sizeof(double) * n);
     } else {
       it = dg_picard(c, q0, Ww, dt, q1, s);
@@ -1682,7 +1710,24 @@ long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
   if (maxit)
     *maxit = 0;
   long r = predictor_range(c, w, 0, nrows / c->Nd, stiff, dt, newton_tol, qh,
-                           maxit);
+                           maxit, NULL, NULL);
+  free(c);
+  return r;
+}
+
+long ora_predictor_guess(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                         const double *w, long nrows, const double *dX,
+                         int ndim, int N, int V, double dt, double newton_tol,
+                         const double *guess, double *qh, int *maxit,
+                         long *fallbacks, int secondOrder) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  if (maxit)
+    *maxit = 0;
+  if (fallbacks)
+    *fallbacks = 0;
+  long r = predictor_range(c, w, 0, nrows / c->Nd, 1, dt, newton_tol, qh,
+                           maxit, guess, fallbacks);
   free(c);
   return r;
 }
@@ -2020,7 +2065,7 @@ static void *job_run(void *arg) {
     j->out_max = cfl_max(j->c, j->w, c0, c1);
   } else {
     j->iters = predictor_range(j->c, j->w, c0, c1, j->stiff, j->dt, j->tol,
-                               j->qh, &j->maxit);
+                               j->qh, &j->maxit, NULL, NULL);
     fv_range(j->c, j->u, j->qh, j->nX, j->dt, j->flux, j->a0, j->b0);
   }
   return NULL;

@@ -64,6 +64,15 @@ long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
                    long nrows, const double *dX, int ndim, int N, int V,
                    int stiff, double dt, double newton_tol, double *qh,
                    int *maxit, int secondOrder);
+/* Stiff predictor started from a given guess (nrows/Nd cells x N Nd V,
+ * e.g. a learned warm start), falling back per cell to the plain guess at
+ * the first iteration whose residual does not fall; *fallbacks counts the
+ * cells that fell back.  Not in the reference: the warm-start extension. */
+long ora_predictor_guess(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                         const double *w, long nrows, const double *dX,
+                         int ndim, int N, int V, double dt, double newton_tol,
+                         const double *guess, double *qh, int *maxit,
+                         long *fallbacks, int secondOrder);
 /* FV corrector (FVSolver::apply) on u (prod(nX) rows) using qh over the
  * w-grid nX+2. */
 void ora_fv(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,

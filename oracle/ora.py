@@ -62,6 +62,10 @@ def port():
         L.ora_predictor.restype = c_long
         L.ora_predictor.argtypes = [c_void_p, c_void_p, c_void_p, dp, c_long, dp, c_int, c_int,
                                     c_int, c_int, D, D, dp, ip, c_int]
+        L.ora_predictor_guess.restype = c_long
+        L.ora_predictor_guess.argtypes = [c_void_p, c_void_p, c_void_p, dp, c_long, dp, c_int,
+                                          c_int, c_int, D, D, dp, dp, ip,
+                                          POINTER(ctypes.c_long), c_int]
         L.ora_fv.restype = None
         L.ora_fv.argtypes = [c_void_p, c_void_p, c_void_p, dp, dp, ip, dp, c_int, c_int, c_int,
                              c_int, c_int, D]
@@ -154,6 +158,21 @@ def predictor(sysname, w, dX, N, stiff, dt, tol=1e-12):
                                int(stiff), dt, tol, ptr(qh), ctypes.byref(mi),
                                s.second_order)
     return qh, its, mi.value
+
+
+def predictor_guess(sysname, w, dX, N, dt, guess, tol=1e-12):
+    """Stiff predictor from a warm start; returns (qh, iters, max_iters,
+    cells that fell back to the plain guess)."""
+    dX = np.asarray(dX, dtype=np.float64)
+    s = PortSystem(sysname, len(dX))
+    qh = np.zeros((w.shape[0] * N, s.V))
+    g = np.ascontiguousarray(guess, dtype=np.float64).reshape(qh.shape)
+    mi = c_int()
+    fb = ctypes.c_long()
+    its = port().ora_predictor_guess(s.F, s.B, s.S, ptr(w), w.shape[0], ptr(dX), len(dX), N,
+                                     s.V, dt, tol, ptr(g), ptr(qh), ctypes.byref(mi),
+                                     ctypes.byref(fb), s.second_order)
+    return qh, its, mi.value, fb.value
 
 
 def fv(sysname, u, qh, dX, N, dt, flux=0):

@@ -22,7 +22,8 @@ PYPDE_ERR_COMPILE = 5
 
 class Options(Structure):
     _fields_ = [("max_steps", c_longlong), ("newton_tol", c_double),
-                ("device", c_int), ("steps_per_graph", c_int), ("profile_stages", c_int)]
+                ("device", c_int), ("steps_per_graph", c_int), ("profile_stages", c_int),
+                ("warm_start", c_void_p)]
 
 STAGES = ("boundaries", "weno", "cfl", "predictor", "faces", "centers", "gather", "other")
 
@@ -32,7 +33,7 @@ class Stats(Structure):
                 ("pred_iters", c_ulonglong), ("pred_max_iters", c_int),
                 ("pred_fail", c_int), ("nan_found", c_int),
                 ("device_seconds", c_double), ("kernel_launches", c_longlong),
-                ("stage_seconds", c_double * 8)]
+                ("stage_seconds", c_double * 8), ("pred_fallbacks", c_ulonglong)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_seconds"}
@@ -42,6 +43,7 @@ class Stats(Structure):
 
 dp = POINTER(c_double)
 ip = POINTER(c_int)
+fp = POINTER(ctypes.c_float)
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -66,6 +68,20 @@ SIGNATURES = {
     "pypde_fv": (c_int, [c_void_p, dp, dp, ip, dp, c_int, c_int, c_int, c_double]),
     "pypde_tables": (c_int, [c_int, dp]),
     "pypde_measure_fp64_peak": (c_int, [c_int, dp]),
+    "pypde_warm_start_shape": (c_int, [c_void_p, c_int, ip, ip, ip]),
+    "pypde_warm_start_create": (c_int, [c_void_p, c_int, c_int] + [fp] * 10 +
+                                [c_int, POINTER(c_void_p)]),
+    "pypde_warm_start_free": (c_int, [c_void_p]),
+    "pypde_predictor_guess": (c_int, [c_void_p, dp, c_longlong, dp, c_int, c_int, c_double,
+                                      c_double, dp, c_void_p, dp, POINTER(Stats)]),
+    "pypde_harvest": (c_int, [c_void_p, dp, c_double, ip, c_int, dp, c_double, ip, c_bool,
+                              c_int, c_int, c_longlong, c_longlong, dp, dp, dp,
+                              POINTER(Options), POINTER(Stats)]),
+    "pypde_mlp_gemm": (c_int, [c_void_p, c_longlong, c_longlong, c_void_p, c_longlong,
+                               c_longlong, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
+                               c_void_p, c_void_p, c_void_p]),
+    "pypde_mlp_silu_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_longlong, c_void_p]),
+    "pypde_mlp_colsum": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "pypde_last_error": (c_char_p, []),
 }
 

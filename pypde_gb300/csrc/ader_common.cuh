@@ -22,6 +22,7 @@ namespace pypde {
 constexpr int MAXN = 8;
 constexpr double SQRT_EPS = 1.4901161193847656e-08; // sqrt(2^-52) = 2^-26
 constexpr double DBL_EPS = 2.220446049250313e-16;
+constexpr double DBL_MAX_VAL = 1.7976931348623157e308;
 constexpr double WENO_LAMS = 1.0;  // weno.h:8
 constexpr double WENO_LAMC = 1e5;  // weno.h:9
 constexpr double WENO_EPS = 1e-14; // weno.h:10

@@ -10,6 +10,11 @@ struct pypde_system {
   pypde::SystemDesc *owned; // run-time compiled systems
 };
 
+struct pypde_warm_start {
+  pypde::WarmStart *ws;
+  int N, V, ndim;
+};
+
 namespace pypde {
 int compile_system(const char *src, const char *name, int ndim, int V,
                    int has_F, int has_B, int has_S, int second_order,
@@ -97,6 +102,9 @@ void pypde_system_free(pypde_system *s) {
   delete s;
 }
 
+static int run_ex(const pypde_system *sys, const RunArgs &a,
+                  pypde_stats *stats);
+
 int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
                   double *u, double tf, const int *nX, int ndim,
                   const double *dX, double CFL, const int *boundaryTypes,
@@ -135,7 +143,20 @@ int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
     a.device = opt->device;
     a.steps_per_graph = opt->steps_per_graph;
     a.profile = opt->profile_stages != 0;
+    if (opt->warm_start) {
+      const pypde_warm_start *w = opt->warm_start;
+      if (w->N != N || w->V != sys->desc->V || w->ndim != ndim) {
+        set_error("warm start was built for another system, order or ndim");
+        return PYPDE_ERR_ARG;
+      }
+      a.warm = w->ws;
+    }
   }
+  return run_ex(sys, a, stats);
+}
+
+static int run_ex(const pypde_system *sys, const RunArgs &a,
+                  pypde_stats *stats) {
   Stats st;
   int rc = run_solver(*sys->desc, a, &st);
   if (stats) {
@@ -149,6 +170,7 @@ int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
     stats->kernel_launches = st.kernel_launches;
     for (int i = 0; i < 8; i++)
       stats->stage_seconds[i] = st.stage_seconds[i];
+    stats->pred_fallbacks = st.pred_fallbacks;
   }
   return rc;
 }
@@ -219,6 +241,201 @@ int pypde_predictor(const pypde_system *sys, const double *w, long long nrows,
     stats->pred_fail = st.pred_fail;
   }
   return rc;
+}
+
+// ---------------------------------------------------------------- warm start
+
+static int warm_shape(const pypde_system *sys, int N, int *feat, int *k1,
+                      int *no) {
+  if (!sys || N < 1 || N > MAXN) {
+    set_error("invalid arguments");
+    return PYPDE_ERR_ARG;
+  }
+  const SystemDesc &d = *sys->desc;
+  int Nd = 1;
+  for (int i = 0; i < d.ndim; i++)
+    Nd *= N;
+  int f = d.V + Nd * d.V + 2, k = (f + 15) / 16 * 16,
+      o = (N * Nd * d.V + 7) / 8 * 8;
+  if (feat)
+    *feat = f;
+  if (k1)
+    *k1 = k;
+  if (no)
+    *no = o;
+  if (!d.has_S || k > 128 || o > 256) {
+    set_error("no warm-start network for system " + d.name +
+              " at this order (needs a source term, <= 128 features and "
+              "<= 256 outputs)");
+    return PYPDE_ERR_UNSUPPORTED;
+  }
+  return PYPDE_OK;
+}
+
+int pypde_warm_start_shape(const pypde_system *sys, int N, int *feat, int *k1,
+                           int *no) {
+  return warm_shape(sys, N, feat, k1, no);
+}
+
+int pypde_warm_start_create(const pypde_system *sys, int N, int device,
+                            const float *W1, const float *b1, const float *W2,
+                            const float *b2, const float *W3, const float *b3,
+                            const float *x_mean, const float *x_scale,
+                            const float *y_mean, const float *y_scale,
+                            int tau_var, pypde_warm_start **out) {
+  int k1 = 0, no = 0;
+  int rc = warm_shape(sys, N, nullptr, &k1, &no);
+  if (rc)
+    return rc;
+  if (!W1 || !b1 || !W2 || !b2 || !W3 || !b3 || !x_mean || !x_scale ||
+      !y_mean || !y_scale || !out || tau_var >= sys->desc->V) {
+    set_error("invalid arguments");
+    return PYPDE_ERR_ARG;
+  }
+  WarmStartDesc d;
+  d.device = device;
+  d.k1 = k1;
+  d.no = no;
+  d.tau_var = tau_var < 0 ? -1 : tau_var;
+  d.W1 = W1;
+  d.b1 = b1;
+  d.W2 = W2;
+  d.b2 = b2;
+  d.W3 = W3;
+  d.b3 = b3;
+  d.x_mean = x_mean;
+  d.x_scale = x_scale;
+  d.y_mean = y_mean;
+  d.y_scale = y_scale;
+  WarmStart *ws = nullptr;
+  rc = warm_start_create(d, &ws);
+  if (rc)
+    return rc == -1 ? PYPDE_ERR_ARG : PYPDE_ERR_CUDA;
+  pypde_warm_start *h = new (std::nothrow) pypde_warm_start;
+  if (!h) {
+    warm_start_free(ws);
+    set_error("out of host memory");
+    return PYPDE_ERR_ARG;
+  }
+  h->ws = ws;
+  h->N = N;
+  h->V = sys->desc->V;
+  h->ndim = sys->desc->ndim;
+  *out = h;
+  return PYPDE_OK;
+}
+
+int pypde_warm_start_free(pypde_warm_start *ws) {
+  if (ws) {
+    warm_start_free(ws->ws);
+    delete ws;
+  }
+  return PYPDE_OK;
+}
+
+int pypde_predictor_guess(const pypde_system *sys, const double *w,
+                          long long nrows, const double *dX, int ndim, int N,
+                          double dt, double newton_tol, const double *guess,
+                          const pypde_warm_start *warm, double *qh,
+                          pypde_stats *stats) {
+  if (!sys || !w || !dX || !qh || (!guess && !warm) || (guess && warm)) {
+    set_error("invalid arguments (give exactly one of guess and warm)");
+    return PYPDE_ERR_ARG;
+  }
+  if (warm && (warm->N != N || warm->V != sys->desc->V || warm->ndim != ndim)) {
+    set_error("warm start was built for another system, order or ndim");
+    return PYPDE_ERR_ARG;
+  }
+  Stats st;
+  int rc = stage_predictor(*sys->desc, w, nrows, dX, ndim, N, true, dt,
+                           newton_tol > 0 ? newton_tol : 1e-12, qh, &st, guess,
+                           warm ? warm->ws : nullptr);
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->pred_iters = st.pred_iters;
+    stats->pred_max_iters = st.pred_max_iters;
+    stats->pred_fail = st.pred_fail;
+    stats->pred_fallbacks = st.pred_fallbacks;
+  }
+  return rc;
+}
+
+int pypde_harvest(const pypde_system *sys, double *u, double tf,
+                  const int *nX, int ndim, const double *dX, double CFL,
+                  const int *boundaryTypes, bool STIFF, int N, int steps,
+                  long long per_step, long long stride, double *w_out,
+                  double *qh_out, double *dt_out, const pypde_options *opt,
+                  pypde_stats *stats) {
+  if (!sys || !u || !nX || !dX || !boundaryTypes || ndim < 1 || ndim > 3 ||
+      steps < 1 || per_step < 1 || stride < 1 || !w_out || !qh_out ||
+      !dt_out) {
+    set_error("invalid arguments");
+    return PYPDE_ERR_ARG;
+  }
+  RunArgs a;
+  a.u = u;
+  a.tf = tf;
+  a.ndim = ndim;
+  for (int d = 0; d < ndim; d++) {
+    a.nX[d] = nX[d];
+    a.dX[d] = dX[d];
+    a.bt[d] = boundaryTypes[d];
+  }
+  a.cfl = CFL;
+  a.stiff = STIFF;
+  a.N = N;
+  a.useF = sys->desc->has_F;
+  a.useB = sys->desc->has_B;
+  a.useS = sys->desc->has_S;
+  a.max_steps = steps;
+  if (opt) {
+    if (opt->newton_tol > 0)
+      a.newton_tol = opt->newton_tol;
+    a.device = opt->device;
+  }
+  HarvestArgs h;
+  h.steps = steps;
+  h.per_step = per_step;
+  h.stride = stride;
+  h.w = w_out;
+  h.qh = qh_out;
+  h.dt = dt_out;
+  a.harvest = &h;
+  return run_ex(sys, a, stats);
+}
+
+// ------------------------------------------------------- training kernels
+
+int pypde_mlp_gemm(const float *A, long long sam, long long sak,
+                   const float *B, long long sbk, long long sbn, float *C,
+                   int M, int N, int K, int splits, float *work,
+                   const float *bias, float *act, void *stream) {
+  if (!A || !B) {
+    set_error("null operand");
+    return PYPDE_ERR_ARG;
+  }
+  int rc = mlp_gemm(A, sam, sak, B, sbk, sbn, C, M, N, K, splits, work, bias,
+                    act, (cudaStream_t)stream);
+  return rc == 0 ? PYPDE_OK : (rc == -1 ? PYPDE_ERR_ARG : PYPDE_ERR_CUDA);
+}
+
+int pypde_mlp_silu_grad(const float *dA, const float *Z, float *dZ,
+                        long long n, void *stream) {
+  if (!dA || !Z || !dZ) {
+    set_error("null operand");
+    return PYPDE_ERR_ARG;
+  }
+  int rc = mlp_silu_grad(dA, Z, dZ, n, (cudaStream_t)stream);
+  return rc == 0 ? PYPDE_OK : PYPDE_ERR_CUDA;
+}
+
+int pypde_mlp_colsum(const float *X, int M, int N, float *out, void *stream) {
+  if (!X || !out) {
+    set_error("null operand");
+    return PYPDE_ERR_ARG;
+  }
+  int rc = mlp_colsum(X, M, N, out, (cudaStream_t)stream);
+  return rc == 0 ? PYPDE_OK : (rc == -1 ? PYPDE_ERR_ARG : PYPDE_ERR_CUDA);
 }
 
 int pypde_fv(const pypde_system *sys, double *u, const double *qh,

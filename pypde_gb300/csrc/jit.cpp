@@ -143,8 +143,9 @@ struct JitInfo {
 
 std::mutex g_jit_mu;
 
-const char *KERNELS[] = {"k_cfl", "k_predictor", "k_newton", "k_faces0",
-                         "k_faces1", "k_faces2", "k_centers", "k_gather"};
+const char *KERNELS[] = {"k_cfl",     "k_predictor", "k_newton",
+                         "k_faces0",  "k_faces1",    "k_faces2",
+                         "k_centers", "k_gather",    "k_mlp_guess"};
 
 } // namespace
 
@@ -160,23 +161,29 @@ int jit_ensure(SystemDesc &d, int N) {
     return PYPDE_ERR_ARG;
   }
   std::string dir = lib_dir() + "/csrc/";
-  const char *hdrs[] = {"kernels.cuh", "ader_common.cuh", "eig_full.cuh"};
-  std::vector<std::string> hsrc(3);
-  for (int i = 0; i < 3; i++)
+  const char *hdrs[] = {"kernels.cuh", "ader_common.cuh", "eig_full.cuh",
+                        "mlp.cuh"};
+  const int nh = 4;
+  std::vector<std::string> hsrc(nh);
+  for (int i = 0; i < nh; i++)
     if (!read_file(dir + hdrs[i], &hsrc[i])) {
       set_error("cannot read " + dir + hdrs[i]);
       return PYPDE_ERR_COMPILE;
     }
   std::string ns = std::to_string(N);
-  std::string prog = "#include \"kernels.cuh\"\n" + ji->src +
-                     "\n__constant__ int pypde_cfg[6] = {"
+  std::string sh = "pypde::MlpShape<UserSystem, " + ns + ">";
+  std::string prog = "#include \"mlp.cuh\"\n" + ji->src +
+                     "\n__constant__ int pypde_cfg[11] = {"
                      "pypde::PredCfg<UserSystem, " + ns + ">::THREADS, "
                      "pypde::PredCfg<UserSystem, " + ns + ">::CPB, "
                      "pypde::PredCfg<UserSystem, " + ns + ">::SMEM_DOUBLES * 8, "
                      "pypde::NewtonCfg<UserSystem, " + ns + ">::THREADS, "
                      "pypde::NewtonCfg<UserSystem, " + ns + ">::CPB, "
                      "(int)pypde::NewtonCfg<UserSystem, " + ns +
-                     ">::SMEM_BYTES};\n";
+                     ">::SMEM_BYTES, "
+                     "(" + sh + "::OK && UserSystem::HAS_S) ? 1 : 0, "
+                     "(int)" + sh + "::SMEM, " + sh + "::K1, " + sh + "::NO, " +
+                     sh + "::FEAT};\n";
   std::vector<std::string> exprs = {
       "&pypde::k_cfl<UserSystem, " + ns + ">",
       "&pypde::k_predictor<UserSystem, " + ns + ">",
@@ -185,7 +192,8 @@ int jit_ensure(SystemDesc &d, int N) {
       "&pypde::k_faces<UserSystem, " + ns + ", 1>",
       "&pypde::k_faces<UserSystem, " + ns + ", 2>",
       "&pypde::k_centers<UserSystem, " + ns + ">",
-      "&pypde::k_gather<UserSystem, " + ns + ">"};
+      "&pypde::k_gather<UserSystem, " + ns + ">",
+      "&pypde::k_mlp_guess<UserSystem, " + ns + ">"};
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17",
                         "--fmad=false", "-lineinfo", "-DPYPDE_JIT=1"};
   const int nopts = 5;
@@ -217,8 +225,9 @@ int jit_ensure(SystemDesc &d, int N) {
       std::getline(is, l);
   } else {
     nvrtcProgram p;
-    const char *hp[3] = {hsrc[0].c_str(), hsrc[1].c_str(), hsrc[2].c_str()};
-    if (nv->create(&p, prog.c_str(), "user_system.cu", 3, hp, hdrs) != 0) {
+    const char *hp[nh] = {hsrc[0].c_str(), hsrc[1].c_str(), hsrc[2].c_str(),
+                          hsrc[3].c_str()};
+    if (nv->create(&p, prog.c_str(), "user_system.cu", nh, hp, hdrs) != 0) {
       set_error("nvrtcCreateProgram failed");
       return PYPDE_ERR_COMPILE;
     }
@@ -277,7 +286,8 @@ int jit_ensure(SystemDesc &d, int N) {
   KFunc *slots[] = {&d.sets[N].cfl,           &d.sets[N].predictor,
                     &d.sets[N].newton,        &d.sets[N].faces_flux[0],
                     &d.sets[N].faces_flux[1], &d.sets[N].faces_flux[2],
-                    &d.sets[N].centers,       &d.sets[N].gather};
+                    &d.sets[N].centers,       &d.sets[N].gather,
+                    &d.sets[N].guess};
   for (size_t i = 0; i < exprs.size(); i++) {
     void *f = nullptr;
     if (lowered[i].empty() || getfn(&f, mod, lowered[i].c_str()) != 0) {
@@ -291,7 +301,7 @@ int jit_ensure(SystemDesc &d, int N) {
   d.sets[N].faces = d.sets[N].faces_flux[0];
   unsigned long long gp = 0;
   size_t gsz = 0;
-  int cfg[6];
+  int cfg[11];
   if (getglob(&gp, &gsz, mod, "pypde_cfg") != 0 ||
       cudaMemcpy(cfg, (void *)gp, sizeof(cfg), cudaMemcpyDeviceToHost) !=
           cudaSuccess) {
@@ -304,6 +314,14 @@ int jit_ensure(SystemDesc &d, int N) {
   d.sets[N].newton_threads = cfg[3];
   d.sets[N].newton_cpb = cfg[4];
   d.sets[N].newton_smem = (size_t)cfg[5];
+  if (cfg[6]) {
+    d.sets[N].guess_smem = (size_t)cfg[7];
+    d.sets[N].guess_k1 = cfg[8];
+    d.sets[N].guess_no = cfg[9];
+    d.sets[N].guess_feat = cfg[10];
+  } else {
+    d.sets[N].guess = KFunc();
+  }
   d.have[N] = true;
   return PYPDE_OK;
 }

@@ -22,6 +22,13 @@ template <class Sys, int N> KernelSet make_kernel_set() {
   k.newton_threads = NewtonCfg<Sys, N>::THREADS;
   k.newton_cpb = NewtonCfg<Sys, N>::CPB;
   k.newton_smem = NewtonCfg<Sys, N>::SMEM_BYTES;
+  if constexpr (MlpShape<Sys, N>::OK && Sys::HAS_S) {
+    k.guess.aot = (const void *)&k_mlp_guess<Sys, N>;
+    k.guess_smem = MlpShape<Sys, N>::SMEM;
+    k.guess_k1 = MlpShape<Sys, N>::K1;
+    k.guess_no = MlpShape<Sys, N>::NO;
+    k.guess_feat = MlpShape<Sys, N>::FEAT;
+  }
   k.pred_threads = Cfg::THREADS;
   k.pred_cpb = Cfg::CPB;
   k.pred_smem = (size_t)Cfg::SMEM_DOUBLES * sizeof(double);

@@ -42,6 +42,7 @@ struct DevState {
   unsigned long long pred_iters; // sum over cells of predictor iterations
   int pred_max_iters;
   int pred_fail;     // cells whose Newton iteration hit its cap
+  unsigned long long pred_fallbacks; // warm-started cells reset to the plain guess
 };
 
 // Geometry of one problem, passed by value.
@@ -434,6 +435,12 @@ __global__ void k_predictor(const double *__restrict__ w,
 // restatement's dg_newton.  Replaces the reference's Newton-Krylov
 // (dg.cpp:173-185, scipy/algos/newton_krylov.cpp), whose absolute
 // tolerance is 6e-6, by an iteration to tol (default 1e-12).
+//
+// With guess != 0 the iteration starts from the values already in qh (a
+// learned warm start) instead of the plain guess q = w.  A cell whose
+// residual does not fall below the previous iteration's, or has an entry
+// that is not finite, spends that iteration resetting q to the plain guess
+// and then runs the plain iteration; pred_fallbacks counts those cells.
 // ---------------------------------------------------------------------
 constexpr int NEWTON_MAXIT = 200;
 
@@ -455,7 +462,7 @@ template <class Sys, int N> struct NewtonCfg {
 template <class Sys, int N>
 __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
                          Geom g, Tables T, const double *__restrict__ wprod_g,
-                         DevState *st, double tol) {
+                         DevState *st, double tol, int guess) {
   using Cfg = NewtonCfg<Sys, N>;
   constexpr int V = Cfg::V, D = Cfg::D, Nd = Cfg::Nd, NT = Cfg::NT;
   constexpr int NL = Cfg::NL, CPB = Cfg::CPB;
@@ -474,6 +481,8 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
   __shared__ double wg[N];
   __shared__ unsigned long long res_bits[CPB], scale_bits[CPB];
   __shared__ int cell_done[CPB];
+  __shared__ int on_guess[CPB], bad_res[CPB];
+  __shared__ double prev_res[CPB];
   for (int i = threadIdx.x; i < Nd; i += blockDim.x)
     wprod[i] = wprod_g[i];
   for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
@@ -500,19 +509,23 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
   double *rr = s_r + (lc * NT) * V;
   double *ff = s_f + (lc * NT) * D * V;
   double Ww[V];
-  if (threadIdx.x < CPB)
+  if (threadIdx.x < CPB) {
     cell_done[threadIdx.x] = 0;
+    on_guess[threadIdx.x] = guess != 0;
+    prev_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL); // +inf
+  }
   __syncthreads();
+  const double *wc = w + (cell * Nd + idx) * V;
   if (valid) {
     double cc = T.endvals[t];
     for (int d = 0; d < D; d++)
       cc *= wg[digs[d]];
-    const double *wc = w + (cell * Nd + idx) * V;
+    const double *gq = qh + (cell * NT + node) * V;
 #pragma unroll
     for (int v = 0; v < V; v++) {
       double x = wc[v];
       Ww[v] = cc * x;
-      q[node * V + v] = x;
+      q[node * V + v] = guess ? gq[v] : x;
     }
   } else if (lc < CPB && node == 0) {
     cell_done[lc] = 1;
@@ -523,6 +536,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
     if (lc < CPB && node == 0) {
       res_bits[lc] = 0ULL;
       scale_bits[lc] = 0ULL;
+      bad_res[lc] = 0;
     }
     __syncthreads();
     const bool active = valid && !cell_done[lc];
@@ -596,6 +610,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         cc *= wg[digs[d]];
       }
       double res = 0, scale = 0;
+      bool bad = false;
 #pragma unroll
       for (int v = 0; v < V; v++) {
         double rv = fma(r[v] * cc, dt, Ww[v]);
@@ -608,17 +623,26 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         rr[node * V + v] = ov;
         res = fmax(res, fabs(ov));
         scale = fmax(scale, fmax(fabs(rv), fabs(uq)));
+        bad |= !(fabs(ov) <= DBL_MAX_VAL);
       }
+      if (bad)
+        bad_res[lc] = 1;
       atomicMax(&res_bits[lc], (unsigned long long)__double_as_longlong(res));
       atomicMax(&scale_bits[lc], (unsigned long long)__double_as_longlong(scale));
     }
     __syncthreads();
-    bool conv = false;
+    bool conv = false, reset = false;
+    double res = 0.0;
     if (active) {
-      double res = __longlong_as_double((long long)res_bits[lc]);
+      res = __longlong_as_double((long long)res_bits[lc]);
       double scale = __longlong_as_double((long long)scale_bits[lc]);
-      conv = (res <= tol || res <= 16 * DBL_EPS * scale);
-      if (!conv) {
+      reset = on_guess[lc] && (bad_res[lc] || !(res < prev_res[lc]));
+      conv = !reset && (res <= tol || res <= 16 * DBL_EPS * scale);
+      if (reset) {
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          q[node * V + v] = wc[v];
+      } else if (!conv) {
         // row block t of A for spatial node idx: the FD Jacobian of S
         double *A = s_A + ((lc * Nd) + idx) * NL * NL;
         double *qn = q + node * V;
@@ -649,7 +673,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
       }
     }
     __syncthreads();
-    if (active && !conv && t == 0) {
+    if (active && !conv && !reset && t == 0) {
       // LU with partial pivoting of A, then solve for the update of node
       // idx at every time node (lu_factor / lu_solve of the restatement)
       double *A = s_A + ((lc * Nd) + idx) * NL * NL;
@@ -715,6 +739,12 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
       atomicOr(&cell_done[lc], 2);
     __syncthreads();
     if (active && node == 0) {
+      if (reset) {
+        on_guess[lc] = 0;
+        atomicAdd(&st->pred_fallbacks, 1ULL);
+      } else if (on_guess[lc]) {
+        prev_res[lc] = res;
+      }
       if (conv)
         cell_done[lc] |= 1;
       else

@@ -291,6 +291,12 @@ struct StepCtx {
   double *u, *uprev, *ub, *tmpA, *tmpB, *w, *qh, *contrib, *cen, *ringbuf,
       *wprod;
   DevState *st;
+  const WarmStart *warm; // learned warm start of the Newton predictor
+  const double *guess;   // or a given initial guess already in qh
+  // harvest of training pairs (device buffers)
+  double *hw, *hq, *hdt;
+  long long hstride, hper;
+  int hsteps;
 };
 
 static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
@@ -301,9 +307,27 @@ static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
   void *args[] = {(void *)&c.w, (void *)&c.qh, (void *)&g,   (void *)&T,
                   (void *)&c.wprod, (void *)&c.st, (void *)&tol};
   if (c.stiff) {
+    int guess = 0;
+    if (c.warm) {
+      // qh = w + the network's correction, then Newton from there
+      MlpModel m = c.warm->model;
+      void *ga[] = {(void *)&c.w, (void *)&c.qh, (void *)&g, (void *)&m,
+                    (void *)&c.st};
+      long long tiles = (g.Cw + 127) / 128;
+      unsigned gb = (unsigned)(tiles < 152 * 2 ? tiles : 152 * 2);
+      cudaError_t e = launch(k.guess, dim3(gb), dim3(256), k.guess_smem, s, ga);
+      if (e != cudaSuccess)
+        return e;
+      guess = 1;
+    } else if (c.guess) {
+      guess = 1;
+    }
+    void *na[] = {(void *)&c.w,     (void *)&c.qh, (void *)&g,
+                  (void *)&T,       (void *)&c.wprod, (void *)&c.st,
+                  (void *)&tol,     (void *)&guess};
     unsigned blocks = (unsigned)((g.Cw + k.newton_cpb - 1) / k.newton_cpb);
     return launch(k.newton, dim3(blocks), dim3(k.newton_threads),
-                  k.newton_smem, s, args);
+                  k.newton_smem, s, na);
   }
   unsigned blocks = (unsigned)((g.Cw + k.pred_cpb - 1) / k.pred_cpb);
   return launch(k.predictor, dim3(blocks), dim3(k.pred_threads), k.pred_smem,
@@ -343,7 +367,8 @@ static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
 
 // Kernels one step launches (the count reported as kernel_launches).
 static int kernels_per_step(const StepCtx &c) {
-  return 10 + c.g.ndim + (c.faces ? 1 : 0) + (c.centers ? 1 : 0);
+  return 10 + c.g.ndim + (c.faces ? 1 : 0) + (c.centers ? 1 : 0) +
+         (c.stiff && c.warm ? 1 : 0) + (c.hw ? 1 : 0);
 }
 
 // One step.  With ev non-null, events are recorded between the stages
@@ -384,6 +409,13 @@ static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
   e = enqueue_predictor(c, s);
   if (e != cudaSuccess)
     return e;
+  if (c.hw) {
+    const int Nd = ipow(c.N, c.g.ndim);
+    const int nw = Nd * c.V, nq = c.N * Nd * c.V;
+    k_harvest<<<grid_for(c.hper * (nw + nq), 256, 152 * 8), 256, 0, s>>>(
+        c.w, c.qh, c.g.Cw, nw, nq, c.st, c.hw, c.hq, c.hdt, c.hstride,
+        c.hsteps, c.hper);
+  }
   mark(4);
   {
     StepCtx f = c;
@@ -488,6 +520,46 @@ static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
 // ------------------------------------------------------------------
 // the solver (pde_solver)
 // ------------------------------------------------------------------
+// Device allocations owned by one call (training-data buffers).
+struct DeviceBuffers {
+  std::vector<void *> ptrs;
+  cudaError_t alloc(void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+    if (e == cudaSuccess)
+      ptrs.push_back(*p);
+    return e;
+  }
+  ~DeviceBuffers() {
+    for (void *p : ptrs)
+      cudaFree(p);
+  }
+};
+
+// A warm start fits (system, N) when its layer widths are the ones the
+// system's guess kernel was built for and it lives on the run's device.
+static int check_warm(const SystemDesc &sys, int N, bool stiff, int device,
+                      const WarmStart *w) {
+  const KernelSet &k = sys.sets[N];
+  if (!stiff) {
+    set_error("the learned warm start applies to the stiff (Newton) "
+              "predictor only");
+    return PYPDE_ERR_ARG;
+  }
+  if (!k.guess.valid() || k.guess_k1 == 0) {
+    set_error("no warm-start kernel for system " + sys.name + " at this order");
+    return PYPDE_ERR_ARG;
+  }
+  if (w->model.k1 != k.guess_k1 || w->model.no != k.guess_no ||
+      w->model.tau_var >= sys.V || w->device != device) {
+    set_error("warm start does not fit system " + sys.name + ": expected k1=" +
+              std::to_string(k.guess_k1) + ", no=" +
+              std::to_string(k.guess_no) + " on device " +
+              std::to_string(device));
+    return PYPDE_ERR_ARG;
+  }
+  return PYPDE_OK;
+}
+
 int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   if (a.ndim < 1 || a.ndim > 3 || !a.u || a.tf < 0 || a.ndt < 1) {
     set_error("invalid arguments");
@@ -516,6 +588,8 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
     return rc;
   if ((rc = ensure_kernels(sys, a.N)))
     return rc;
+  if (a.warm && (rc = check_warm(sys, a.N, a.stiff, a.device, a.warm)))
+    return rc;
   cudaStream_t s = ar->stream;
   StepCtx c;
   c.sys = &sys;
@@ -531,6 +605,12 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   c.stiff = a.stiff;
   c.flux = a.flux;
   c.tol = a.newton_tol;
+  c.warm = a.warm;
+  c.guess = nullptr;
+  c.hw = c.hq = c.hdt = nullptr;
+  c.hstride = 1;
+  c.hper = 0;
+  c.hsteps = 0;
   c.faces = sys.has_F || sys.has_B;
   c.centers = sys.has_B || sys.has_S;
   const int V = c.V, N = c.N, Nd = ipow(N, a.ndim);
@@ -575,6 +655,24 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   CK(set_smem(c.ks->predictor, c.ks->pred_smem));
   if (c.stiff)
     CK(set_smem(c.ks->newton, c.ks->newton_smem));
+  if (c.stiff && c.warm)
+    CK(set_smem(c.ks->guess, c.ks->guess_smem));
+  DeviceBuffers hbuf; // harvest buffers, freed on every return
+  if (a.harvest && a.harvest->steps > 0 && a.harvest->per_step > 0) {
+    const HarvestArgs &h = *a.harvest;
+    if (!h.w || !h.qh || !h.dt || h.stride < 1) {
+      set_error("harvest: missing output arrays or bad stride");
+      return PYPDE_ERR_ARG;
+    }
+    long long rows = (long long)h.steps * h.per_step;
+    CK(hbuf.alloc((void **)&c.hw, rows * Nd * V * 8));
+    CK(hbuf.alloc((void **)&c.hq, rows * N * Nd * V * 8));
+    CK(hbuf.alloc((void **)&c.hdt, h.steps * 8));
+    CK(cudaMemsetAsync(c.hdt, 0, h.steps * 8, s));
+    c.hsteps = h.steps;
+    c.hper = h.per_step;
+    c.hstride = h.stride;
+  }
   DevState hs;
   std::memset(&hs, 0, sizeof(hs));
   hs.tf = a.tf;
@@ -661,6 +759,15 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   }
   CK(cudaEventRecord(e1, s));
   CK(cudaMemcpyAsync(a.u, c.u, usz * 8, cudaMemcpyDeviceToHost, s));
+  if (c.hw) {
+    long long rows = (long long)c.hsteps * c.hper;
+    CK(cudaMemcpyAsync(a.harvest->w, c.hw, rows * Nd * V * 8,
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(a.harvest->qh, c.hq, rows * N * Nd * V * 8,
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(a.harvest->dt, c.hdt, c.hsteps * 8,
+                       cudaMemcpyDeviceToHost, s));
+  }
   if (a.ret)
     CK(cudaMemcpyAsync(a.ret + (long long)(a.ndt - 1) * usz, c.u, usz * 8,
                        cudaMemcpyDeviceToHost, s));
@@ -683,6 +790,7 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
     out->pred_iters = h.pred_iters;
     out->pred_max_iters = h.pred_max_iters;
     out->pred_fail = h.pred_fail;
+    out->pred_fallbacks = h.pred_fallbacks;
     out->nan_found = h.nan_found;
     out->device_seconds = ms * 1e-3;
     out->kernel_launches = launches;
@@ -838,10 +946,15 @@ int stage_timestep(const SystemDesc &sys, const double *w, long long nrows,
 
 int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
                     const double *dX, int ndim, int N, bool stiff, double dt,
-                    double tol, double *qh, Stats *out) {
+                    double tol, double *qh, Stats *out, const double *guess,
+                    const WarmStart *warm) {
   int rc = check_system(sys, ndim, N, stiff, 0);
   if (rc)
     return rc;
+  if ((guess || warm) && !stiff) {
+    set_error("an initial guess applies to the stiff predictor only");
+    return PYPDE_ERR_ARG;
+  }
   int Nd = ipow(N, ndim);
   if (nrows < 1 || nrows % Nd) {
     set_error("nrows must be a positive multiple of N^ndim");
@@ -852,6 +965,8 @@ int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
   if ((rc = arena_for(0, &ar)))
     return rc;
   if ((rc = ensure_kernels(sys, N)))
+    return rc;
+  if (warm && (rc = check_warm(sys, N, stiff, 0, warm)))
     return rc;
   DevState *st;
   if ((rc = put_state(ar, &st, 0, 1, 1, 0, dt)))
@@ -882,6 +997,13 @@ int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
   c.qh = (double *)ar->qh.p;
   c.wprod = (double *)ar->wprod.p;
   c.st = st;
+  c.warm = warm;
+  c.guess = guess;
+  if (guess)
+    CK(cudaMemcpyAsync(c.qh, guess, nrows * N * sys.V * 8,
+                       cudaMemcpyHostToDevice, s));
+  if (warm)
+    CK(set_smem(c.ks->guess, c.ks->guess_smem));
   CK(set_smem(stiff ? c.ks->newton : c.ks->predictor,
               stiff ? c.ks->newton_smem : c.ks->pred_smem));
   CK(enqueue_predictor(c, s));
@@ -894,6 +1016,7 @@ int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
     out->pred_iters = ar->host_state->pred_iters;
     out->pred_max_iters = ar->host_state->pred_max_iters;
     out->pred_fail = ar->host_state->pred_fail;
+    out->pred_fallbacks = ar->host_state->pred_fallbacks;
   }
   return PYPDE_OK;
 }

@@ -2,7 +2,7 @@
 // (system, order), the step driver and the stage launchers.
 #pragma once
 
-#include "kernels.cuh"
+#include "mlp.cuh"
 
 #include <cuda_runtime.h>
 #include <string>
@@ -28,6 +28,10 @@ struct KernelSet {
   size_t pred_smem = 0;
   int newton_threads = 0, newton_cpb = 0;
   size_t newton_smem = 0;
+  // learned warm start (k_mlp_guess); guess_k1 == 0: not available
+  KFunc guess;
+  size_t guess_smem = 0;
+  int guess_k1 = 0, guess_no = 0, guess_feat = 0;
 };
 
 struct SystemDesc {
@@ -42,6 +46,40 @@ struct SystemDesc {
 // Built-in systems, registered by the instantiation units.
 void register_builtin(const SystemDesc &d);
 const SystemDesc *find_builtin(const std::string &name, int ndim);
+
+// Host description of a trained warm-start network (FP32 arrays; weights
+// row-major [out][in], W1 [128][k1], W2 [128][128], W3 [no][128]).
+struct WarmStartDesc {
+  int device = 0;
+  int k1 = 0, no = 0, tau_var = -1;
+  const float *W1, *b1, *W2, *b2, *W3, *b3;
+  const float *x_mean, *x_scale, *y_mean, *y_scale;
+};
+
+// A network resident on one device (BF16 weights, FP32 the rest).
+struct WarmStart {
+  int device = 0;
+  void *mem = nullptr;
+  MlpModel model;
+};
+
+int warm_start_create(const WarmStartDesc &d, WarmStart **out);
+void warm_start_free(WarmStart *ws);
+int mlp_gemm(const float *A, long long sam, long long sak, const float *B,
+             long long sbk, long long sbn, float *C, int M, int N, int K,
+             int splits, float *work, const float *bias, float *act,
+             cudaStream_t s);
+int mlp_silu_grad(const float *dA, const float *Z, float *dZ, long long n,
+                  cudaStream_t s);
+int mlp_colsum(const float *X, int M, int N, float *out, cudaStream_t s);
+
+// Sampling of (w, converged qh, dt) from the first `steps` steps of a run,
+// per_step cells per step, every stride-th reconstruction cell.
+struct HarvestArgs {
+  int steps = 0;
+  long long per_step = 0, stride = 1;
+  double *w = nullptr, *qh = nullptr, *dt = nullptr; // host outputs
+};
 
 struct RunArgs {
   double *u = nullptr; // host, in/out
@@ -62,6 +100,8 @@ struct RunArgs {
   int steps_per_graph = 0;
   bool profile = false;
   bool useF = true, useB = true, useS = true;
+  const WarmStart *warm = nullptr;    // learned warm start of the Newton predictor
+  const HarvestArgs *harvest = nullptr;
 };
 
 struct Stats {
@@ -69,6 +109,7 @@ struct Stats {
   double t_final = 0;
   unsigned long long pred_iters = 0;
   int pred_max_iters = 0, pred_fail = 0, nan_found = 0;
+  unsigned long long pred_fallbacks = 0;
   double device_seconds = 0;
   long long kernel_launches = 0;
   double stage_seconds[8] = {};
@@ -87,7 +128,9 @@ int stage_timestep(const SystemDesc &sys, const double *w, long long nrows,
                    double t, long long count, double *dt);
 int stage_predictor(const SystemDesc &sys, const double *w, long long nrows,
                     const double *dX, int ndim, int N, bool stiff, double dt,
-                    double tol, double *qh, Stats *st);
+                    double tol, double *qh, Stats *st,
+                    const double *guess = nullptr,
+                    const WarmStart *warm = nullptr);
 int stage_fv(const SystemDesc &sys, double *u, const double *qh,
              const int *nX, const double *dX, int ndim, int N, int flux,
              double dt);

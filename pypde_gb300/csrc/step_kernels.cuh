@@ -91,4 +91,33 @@ __global__ void k_snapshot(const double *__restrict__ u,
     dst[i] = u[i];
 }
 
+// Training pairs for the warm start: after the predictor of step `count`
+// (< nslots), copy per_slot sampled reconstruction cells' w and converged
+// qh, and dt.  Sample j of slot s is cell (off_s + j stride) mod Cw.
+__global__ void k_harvest(const double *__restrict__ w,
+                          const double *__restrict__ qh, long long Cw, int nw,
+                          int nq, const DevState *st, double *hw, double *hq,
+                          double *hdt, long long stride, int nslots,
+                          long long per_slot) {
+  if (!step_active(st))
+    return;
+  const long long slot = st->count;
+  if (slot >= nslots)
+    return;
+  const long long off = (slot * 7919 + 13) % stride;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    hdt[slot] = st->dt;
+  const long long tot = per_slot * (nw + nq);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long j = e / (nw + nq);
+    const int k = (int)(e - j * (nw + nq));
+    const long long cell = (off + j * stride) % Cw;
+    if (k < nw)
+      hw[(slot * per_slot + j) * nw + k] = w[cell * nw + k];
+    else
+      hq[(slot * per_slot + j) * nq + (k - nw)] = qh[cell * nq + (k - nw)];
+  }
+}
+
 } // namespace pypde

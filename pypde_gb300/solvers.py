@@ -10,7 +10,9 @@ Differences from the reference, all at the callback boundary:
   * ``nThreads`` is accepted and ignored (one GPU does the work of the
     reference's CPU thread pool).
   * Extensions (keyword-only): ``max_steps``, ``newton_tol``, ``device``,
-    ``stats`` (a dict filled with step and iteration counts).
+    ``stats`` (a dict filled with step and iteration counts), ``jit``,
+    ``warm_start`` (a pypde_gb300.warmstart.WarmStart: learned initial guess
+    of the stiff predictor's Newton iteration).
 """
 import numpy as np
 
@@ -23,7 +25,8 @@ FLUXES = {"rusanov": 0, "roe": 1, "osher": 2}
 
 def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cfl=0.9,
                order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *,
-               max_steps=None, newton_tol=None, device=0, stats=None, jit=False):
+               max_steps=None, newton_tol=None, device=0, stats=None, jit=False,
+               warm_start=None):
     """Solve dQ/dt + div F(Q, grad Q) + B(Q) . grad Q = S(Q) on [0, L] (see
     pypde/solvers.py:28-175 for the full description of the arguments).
 
@@ -53,6 +56,10 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
     opt.max_steps = int(max_steps) if max_steps else -1
     opt.newton_tol = float(newton_tol) if newton_tol else 0.0
     opt.device = int(device)
+    if warm_start is not None:
+        if not stiff:
+            raise ValueError("warm_start applies to the stiff (Newton) predictor")
+        opt.warm_start = warm_start.handle
     st = _lib.Stats()
     lib = _lib.lib()
     code = lib.pde_solver_ex(system.handle, useF, useB, useS, _lib.c_ptr(ur), float(tf),

@@ -65,6 +65,22 @@ def predictor(system, w, dX, N, stiff, dt, tol=1e-12):
     return qh, st.as_dict()
 
 
+def predictor_guess(system, w, dX, N, dt, guess=None, warm=None, tol=1e-12):
+    """Stiff predictor from an initial guess: a host array (N rows per row
+    of w) or a WarmStart network.  Returns (qh, stats dict)."""
+    dX = np.asarray(dX, dtype=np.float64)
+    s = builtin_system(system, len(dX)) if isinstance(system, str) else system
+    w = _f64(w)
+    qh = np.zeros((w.shape[0] * N, w.shape[1]))
+    g = None if guess is None else _f64(np.asarray(guess).reshape(qh.shape))
+    st = _lib.Stats()
+    _lib.check(_lib.lib().pypde_predictor_guess(
+        s.handle, _lib.c_ptr(w), w.shape[0], _lib.c_ptr(dX), len(dX), N, dt, tol,
+        _lib.c_ptr(g) if g is not None else None, warm.handle if warm is not None else None,
+        _lib.c_ptr(qh), st))
+    return qh, st.as_dict()
+
+
 def fv(system, u, qh, dX, N, dt, flux="rusanov"):
     dX = np.asarray(dX, dtype=np.float64)
     s = builtin_system(system, len(dX))

@@ -143,14 +143,15 @@ def test_nvrtc_compiles_the_kernels_for_a_translated_system():
         except OSError:
             pytest.skip("NVRTC not available")
     here = os.path.join(os.path.dirname(__file__), "..", "pypde_gb300", "csrc")
-    names = ["kernels.cuh", "ader_common.cuh", "eig_full.cuh"]
+    names = ["kernels.cuh", "ader_common.cuh", "eig_full.cuh", "mlp.cuh"]
     hdrs = [open(os.path.join(here, n)).read().encode() for n in names]
-    src = ('#include "kernels.cuh"\n' + translate(user_euler2, user_ncp, user_src, 2, 4)).encode()
+    src = ('#include "mlp.cuh"\n' + translate(user_euler2, user_ncp, user_src, 2, 4)).encode()
     prog = ctypes.c_void_p()
-    arr = ctypes.c_char_p * 3
-    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src, b"u.cu", 3, arr(*hdrs),
+    arr = ctypes.c_char_p * len(names)
+    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src, b"u.cu", len(names), arr(*hdrs),
                                  arr(*[n.encode() for n in names])) == 0
-    for e in (b"&pypde::k_faces<UserSystem, 2, 0>", b"&pypde::k_newton<UserSystem, 2>"):
+    for e in (b"&pypde::k_faces<UserSystem, 2, 0>", b"&pypde::k_newton<UserSystem, 2>",
+              b"&pypde::k_mlp_guess<UserSystem, 2>"):
         nv.nvrtcAddNameExpression(prog, e)
     opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", b"--fmad=false"]
     rc = nv.nvrtcCompileProgram(prog, len(opts), (ctypes.c_char_p * len(opts))(*opts))
