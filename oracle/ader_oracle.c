@@ -1392,6 +1392,8 @@ typedef struct {
   double df[ORA_MAXN * ORA_MAXN * ORA_MAXN * 3 * ORA_MAXV];
   double tmp[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
   double fd[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
+  double *lu;  /* Newton: LU factors per spatial node, Nd x (N V)^2 */
+  int *piv;    /* Newton: pivots per spatial node, Nd x N V */
 } dg_scratch;
 
 /* rhs(q) = Ww + dt * c_{t,idx} (S - sum_d B_d dq_d - sum_d dF_d/dx_d),
@@ -1567,28 +1569,33 @@ static void lu_solve(const double *a, int n, const int *piv, double *b) {
 }
 
 /* Locally implicit Newton iteration for stiff S: solve obj(q) = rhs(q) -
- * DG_U q = 0 (dg.cpp:128-154).  Each iteration linearises the source term
- * exactly at every space-time node and keeps the flux terms explicit:
+ * DG_U q = 0 (dg.cpp:128-154).  The source term is linearised at every
+ * space-time node and the flux terms are kept explicit:
  *   per spatial node idx, A[(t,v),(k,w)] = dt W_t dS_v/dq_w(q_t) d_tk
  *                                          - DG_MAT[t,k] d_vw
  *   q <- q - A^{-1} obj(q) / prod W_idx
- * Stops when ||obj(q)||_inf <= tol (or at the rounding floor of obj). */
-/* With q_plain non-null, q holds a warm start (a learned guess) and
+ * Simplified Newton: A is built and factored at the first update and
+ * reused; it is rebuilt at the current iterate whenever the residual has
+ * fallen by less than half since the previous iteration.  Stops when
+ * ||obj(q)||_inf <= tol (or at the rounding floor of obj).
+ *
+ * With q_plain non-null, q holds a warm start (a learned guess) and
  * q_plain the plain guess: the first iteration whose residual does not
  * fall below the previous one, or has an entry that is not finite, spends
  * itself resetting q to q_plain, after which the iteration is the plain
- * one; *fell_back is set. */
+ * one (factors discarded); *fell_back is set. */
 static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
                      double tol, dg_scratch *s, const double *q_plain,
                      int *fell_back) {
   int N = c->N, V = c->V, Nd = c->Nd;
   int n = N * Nd * V, nl = N * V;
   double r[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
-  double A[ORA_MAXN * ORA_MAXV * ORA_MAXN * ORA_MAXV], b[ORA_MAXN * ORA_MAXV];
-  int piv[ORA_MAXN * ORA_MAXV];
+  double b[ORA_MAXN * ORA_MAXV];
   int failed = 0;
   int on_guess = q_plain != NULL;
-  double prev = INFINITY;
+  double prev = INFINITY;  /* residual of the previous warm-start iteration */
+  double last = INFINITY;  /* residual at the previous update */
+  int have_lu = 0;
   for (int it = 0; it < NEWTON_MAXIT; it++) {
     dg_rhs(c, q, Ww, dt, r, s);
     double res = 0, scale = 0;
@@ -1613,39 +1620,47 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
         memcpy(q, q_plain, sizeof(double) * n);
         on_guess = 0;
         *fell_back = 1;
+        have_lu = 0;
+        last = INFINITY;
         continue;
       }
       prev = res;
     }
     if (res <= tol || res <= 16 * DBL_EPSILON * scale)
       return it;
+    int refresh = !have_lu || !(res <= 0.5 * last);
+    last = res;
     for (int idx = 0; idx < Nd; idx++) {
-      for (int i = 0; i < nl * nl; i++)
-        A[i] = 0.0;
-      for (int t = 0; t < N; t++) {
-        double *qn = q + (t * Nd + idx) * V;
-        if (c->S) { /* forward FD Jacobian of S at this node */
-          double s0[ORA_MAXV], s1[ORA_MAXV];
-          c->S(s0, qn);
-          for (int wv = 0; wv < V; wv++) {
-            double q0 = qn[wv];
-            double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
-            qn[wv] = q0 + h;
-            c->S(s1, qn);
-            qn[wv] = q0;
-            double ih = 1.0 / h;
-            for (int v = 0; v < V; v++)
-              A[(t * V + v) * nl + t * V + wv] =
-                  dt * c->T.wghts[t] * ((s1[v] - s0[v]) * ih);
+      double *A = s->lu + (size_t)idx * nl * nl;
+      int *piv = s->piv + idx * nl;
+      if (refresh) {
+        for (int i = 0; i < nl * nl; i++)
+          A[i] = 0.0;
+        for (int t = 0; t < N; t++) {
+          double *qn = q + (t * Nd + idx) * V;
+          if (c->S) { /* forward FD Jacobian of S at this node */
+            double s0[ORA_MAXV], s1[ORA_MAXV];
+            c->S(s0, qn);
+            for (int wv = 0; wv < V; wv++) {
+              double q0 = qn[wv];
+              double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
+              qn[wv] = q0 + h;
+              c->S(s1, qn);
+              qn[wv] = q0;
+              double ih = 1.0 / h;
+              for (int v = 0; v < V; v++)
+                A[(t * V + v) * nl + t * V + wv] =
+                    dt * c->T.wghts[t] * ((s1[v] - s0[v]) * ih);
+            }
           }
+          for (int k = 0; k < N; k++)
+            for (int v = 0; v < V; v++)
+              A[(t * V + v) * nl + k * V + v] -= c->T.dgmat[t * N + k];
         }
-        for (int k = 0; k < N; k++)
-          for (int v = 0; v < V; v++)
-            A[(t * V + v) * nl + k * V + v] -= c->T.dgmat[t * N + k];
-      }
-      if (lu_factor(A, nl, piv) != 0) { /* singular: keep this node, */
-        failed = 1;                        /* finish the others, stop    */
-        continue;
+        if (lu_factor(A, nl, piv) != 0) { /* singular: keep this node, */
+          failed = 1;                        /* finish the others, stop    */
+          continue;
+        }
       }
       for (int t = 0; t < N; t++)
         for (int v = 0; v < V; v++)
@@ -1657,6 +1672,7 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
     }
     if (failed)
       return -1;
+    have_lu = 1;
   }
   (void)n;
   return NEWTON_MAXIT;
@@ -1668,6 +1684,8 @@ static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
   int N = c->N, V = c->V, Nd = c->Nd;
   int n = N * Nd * V;
   dg_scratch *s = malloc(sizeof(dg_scratch));
+  s->lu = malloc(sizeof(double) * Nd * (N * V) * (N * V));
+  s->piv = malloc(sizeof(int) * Nd * N * V);
   double *Ww = malloc(sizeof(double) * n * 3);
   double *q0 = Ww + n, *q1 = Ww + 2 * n;
   long total = 0;
@@ -1694,6 +1712,8 @@ static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
     if (it > mx)
       mx = it;
   }
+  free(s->lu);
+  free(s->piv);
   free(s);
   free(Ww);
   if (maxit && mx > *maxit)

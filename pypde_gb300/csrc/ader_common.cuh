@@ -23,6 +23,19 @@ constexpr int MAXN = 8;
 constexpr double SQRT_EPS = 1.4901161193847656e-08; // sqrt(2^-52) = 2^-26
 constexpr double DBL_EPS = 2.220446049250313e-16;
 constexpr double DBL_MAX_VAL = 1.7976931348623157e308;
+constexpr unsigned long long INF_BITS = 0x7ff0000000000000ULL;
+
+// |x| as its bit pattern: for x not NaN, a > b as doubles exactly when
+// mag_bits(a) > mag_bits(b) as integers; zero is 0.
+__host__ __device__ __forceinline__ unsigned long long mag_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+#else
+  unsigned long long u;
+  __builtin_memcpy(&u, &x, 8);
+  return u & 0x7fffffffffffffffULL;
+#endif
+}
 constexpr double WENO_LAMS = 1.0;  // weno.h:8
 constexpr double WENO_LAMC = 1e5;  // weno.h:9
 constexpr double WENO_EPS = 1e-14; // weno.h:10

@@ -481,8 +481,8 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
   __shared__ double wg[N];
   __shared__ unsigned long long res_bits[CPB], scale_bits[CPB];
   __shared__ int cell_done[CPB];
-  __shared__ int on_guess[CPB], bad_res[CPB];
-  __shared__ double prev_res[CPB];
+  __shared__ int on_guess[CPB], bad_res[CPB], have_lu[CPB];
+  __shared__ double prev_res[CPB], last_res[CPB];
   for (int i = threadIdx.x; i < Nd; i += blockDim.x)
     wprod[i] = wprod_g[i];
   for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
@@ -513,6 +513,8 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
     cell_done[threadIdx.x] = 0;
     on_guess[threadIdx.x] = guess != 0;
     prev_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL); // +inf
+    last_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL);
+    have_lu[threadIdx.x] = 0;
   }
   __syncthreads();
   const double *wc = w + (cell * Nd + idx) * V;
@@ -609,7 +611,9 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         }
         cc *= wg[digs[d]];
       }
-      double res = 0, scale = 0;
+      // max |.| over the entries that are not NaN, as integer maxima of
+      // the magnitude bits (the ordering of non-negative doubles)
+      unsigned long long res = 0, scale = 0;
       bool bad = false;
 #pragma unroll
       for (int v = 0; v < V; v++) {
@@ -621,28 +625,37 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         uq *= wprod[idx];
         double ov = rv - uq;
         rr[node * V + v] = ov;
-        res = fmax(res, fabs(ov));
-        scale = fmax(scale, fmax(fabs(rv), fabs(uq)));
-        bad |= !(fabs(ov) <= DBL_MAX_VAL);
+        const unsigned long long a = mag_bits(ov), b = mag_bits(rv),
+                                 c2 = mag_bits(uq);
+        if (a <= INF_BITS && a > res)
+          res = a;
+        if (b <= INF_BITS && b > scale)
+          scale = b;
+        if (c2 <= INF_BITS && c2 > scale)
+          scale = c2;
+        bad |= a >= INF_BITS;
       }
       if (bad)
         bad_res[lc] = 1;
-      atomicMax(&res_bits[lc], (unsigned long long)__double_as_longlong(res));
-      atomicMax(&scale_bits[lc], (unsigned long long)__double_as_longlong(scale));
+      atomicMax(&res_bits[lc], res);
+      atomicMax(&scale_bits[lc], scale);
     }
     __syncthreads();
-    bool conv = false, reset = false;
+    bool conv = false, reset = false, refresh = false;
     double res = 0.0;
     if (active) {
       res = __longlong_as_double((long long)res_bits[lc]);
       double scale = __longlong_as_double((long long)scale_bits[lc]);
       reset = on_guess[lc] && (bad_res[lc] || !(res < prev_res[lc]));
       conv = !reset && (res <= tol || res <= 16 * DBL_EPS * scale);
+      // simplified Newton: factors reused until the residual falls by
+      // less than half in an iteration
+      refresh = !have_lu[lc] || !(res <= 0.5 * last_res[lc]);
       if (reset) {
 #pragma unroll
         for (int v = 0; v < V; v++)
           q[node * V + v] = wc[v];
-      } else if (!conv) {
+      } else if (!conv && refresh) {
         // row block t of A for spatial node idx: the FD Jacobian of S
         double *A = s_A + ((lc * Nd) + idx) * NL * NL;
         double *qn = q + node * V;
@@ -674,18 +687,25 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
     }
     __syncthreads();
     if (active && !conv && !reset && t == 0) {
-      // LU with partial pivoting of A, then solve for the update of node
-      // idx at every time node (lu_factor / lu_solve of the restatement)
+      // LU with partial pivoting of A (when refreshed), then solve for the
+      // update of node idx at every time node (lu_factor / lu_solve of the
+      // restatement).  Magnitude comparisons and zero tests are done on
+      // the bits: the same decisions for every value that is not NaN.
       double *A = s_A + ((lc * Nd) + idx) * NL * NL;
       int *piv = s_piv + ((lc * Nd) + idx) * NL;
       bool ok = true;
-      for (int k = 0; k < NL && ok; k++) {
+      for (int k = 0; k < NL && ok && refresh; k++) {
         int p = k;
-        for (int i = k + 1; i < NL; i++)
-          if (fabs(A[i * NL + k]) > fabs(A[p * NL + k]))
+        unsigned long long pm = mag_bits(A[k * NL + k]);
+        for (int i = k + 1; i < NL; i++) {
+          const unsigned long long m = mag_bits(A[i * NL + k]);
+          if (m > pm) {
             p = i;
+            pm = m;
+          }
+        }
         piv[k] = p;
-        if (A[p * NL + k] == 0.0) {
+        if (pm == 0ULL) {
           ok = false;
           break;
         }
@@ -699,7 +719,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
         for (int i = k + 1; i < NL; i++) {
           double f = A[i * NL + k] * rp;
           A[i * NL + k] = f;
-          if (f == 0.0) // structural zero: the row is unchanged
+          if (mag_bits(f) == 0ULL) // structural zero: the row is unchanged
             continue;
           for (int j = k + 1; j < NL; j++)
             A[i * NL + j] = fma(-f, A[k * NL + j], A[i * NL + j]);
@@ -721,12 +741,12 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
           }
         for (int k = 0; k < NL; k++)
           for (int i = k + 1; i < NL; i++)
-            if (A[i * NL + k] != 0.0)
+            if (mag_bits(A[i * NL + k]) != 0ULL)
               b[i] = fma(-A[i * NL + k], b[k], b[i]);
         for (int i = NL - 1; i >= 0; i--) {
           double sacc = b[i];
           for (int j = i + 1; j < NL; j++)
-            if (A[i * NL + j] != 0.0)
+            if (mag_bits(A[i * NL + j]) != 0ULL)
               sacc = fma(-A[i * NL + j], b[j], sacc);
           b[i] = sacc / A[i * NL + i];
         }
@@ -741,9 +761,17 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
     if (active && node == 0) {
       if (reset) {
         on_guess[lc] = 0;
+        have_lu[lc] = 0;
+        last_res[lc] = __longlong_as_double(0x7ff0000000000000LL);
         atomicAdd(&st->pred_fallbacks, 1ULL);
-      } else if (on_guess[lc]) {
-        prev_res[lc] = res;
+      } else {
+        if (on_guess[lc])
+          prev_res[lc] = res;
+        if (!conv) {
+          last_res[lc] = res;
+          if (refresh)
+            have_lu[lc] = 1;
+        }
       }
       if (conv)
         cell_done[lc] |= 1;
