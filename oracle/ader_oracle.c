@@ -908,76 +908,124 @@ static int francis_vals_f(float *a, int n, float *wr, float *wi) {
 }
 #undef AF
 
-/* One real eigenvalue of M refined in FP64 from the FP32 shift lam0:
- * LU (partial pivoting, FMA) of M - lam0 I, five inverse-iteration steps
- * from x = (1, ..., 1) with max-normalisation, then the Rayleigh quotient
- * lam0 + x.(M - lam0 I)x / x.x.  Returns 0, or -1 on an exactly singular
- * pivot (the caller then falls back to the FP64 QR). */
-static int refine_real(const double *M, int n, double lam0, double *lam) {
-  double A[ORA_MAXV * ORA_MAXV], ud[ORA_MAXV], x[ORA_MAXV];
-  int piv[ORA_MAXV];
-  for (int i = 0; i < n * n; i++)
-    A[i] = M[i];
-  for (int i = 0; i < n; i++)
-    A[i * n + i] = M[i * n + i] - lam0;
+/* FP32 LU with partial pivoting (whole-row swaps) of the n x n matrix A in
+ * place; ud gets the reciprocals of the pivots.  -1 on a zero pivot. */
+static int lu32(float *A, int n, int *piv, float *ud) {
   for (int k = 0; k < n; k++) {
     int p = k;
     for (int i = k + 1; i < n; i++)
-      if (fabs(A[i * n + k]) > fabs(A[p * n + k]))
+      if (fabsf(A[i * n + k]) > fabsf(A[p * n + k]))
         p = i;
     piv[k] = p;
-    if (A[p * n + k] == 0.0)
+    if (A[p * n + k] == 0.0f)
       return -1;
     if (p != k)
       for (int j = 0; j < n; j++) {
-        double t = A[k * n + j];
+        float t = A[k * n + j];
         A[k * n + j] = A[p * n + j];
         A[p * n + j] = t;
       }
-    ud[k] = 1.0 / A[k * n + k];
+    ud[k] = 1.0f / A[k * n + k];
     for (int i = k + 1; i < n; i++) {
-      double f = A[i * n + k] * ud[k];
+      float f = A[i * n + k] * ud[k];
       A[i * n + k] = f;
       for (int j = k + 1; j < n; j++)
-        A[i * n + j] = fma(-f, A[k * n + j], A[i * n + j]);
+        A[i * n + j] = fmaf(-f, A[k * n + j], A[i * n + j]);
     }
   }
+  return 0;
+}
+
+/* x <- A^{-1} x with the factors of lu32 (permute, unit L, then U). */
+static void lu32_solve(const float *A, int n, const int *piv, const float *ud,
+                       float *x) {
+  for (int k = 0; k < n; k++)
+    if (piv[k] != k) {
+      float t = x[k];
+      x[k] = x[piv[k]];
+      x[piv[k]] = t;
+    }
+  for (int k = 0; k < n; k++)
+    for (int i = k + 1; i < n; i++)
+      x[i] = fmaf(-A[i * n + k], x[k], x[i]);
+  for (int i = n - 1; i >= 0; i--) {
+    float sacc = x[i];
+    for (int j = i + 1; j < n; j++)
+      sacc = fmaf(-A[i * n + j], x[j], sacc);
+    x[i] = sacc * ud[i];
+  }
+}
+
+/* One real eigenvalue refined from the FP32 shift lam0 (an eigenvalue of M
+ * rounded to FP32), by the iterative refinement of an eigenpair of
+ * Dongarra, Moler and Wilkinson (SIAM J. Numer. Anal. 20, 1983):
+ *   FP32: x from two inverse-iteration steps with the LU of Mf - lam0 I
+ *         (Mf = M rounded to FP32), scaled so that x_s = 1 at its largest
+ *         entry s; the LU of B = Mf - lam0 I with column s replaced by -x.
+ *   FP64 residual, FP32 correction, three times:
+ *         r = lam x - M x;  z = B^{-1} r;  lam += z_s;  x_j += z_j (j != s)
+ *   (the correction solves (M - lam I) dx - dlam x = r with dx_s = 0).
+ * Converges linearly at a rate of about eps_32 cond(B).  Returns -1 on a
+ * zero FP32 pivot, a vector that vanishes or is not finite, or a last
+ * correction larger than 1e-10 |lam| (not converged: left to the FP64 QR). */
+static int refine_real(const double *M, int n, double lam0d, double *lam) {
+  float A[ORA_MAXV * ORA_MAXV], ud[ORA_MAXV], x[ORA_MAXV], z[ORA_MAXV];
+  int piv[ORA_MAXV];
+  const float lam0 = (float)lam0d;
+  for (int i = 0; i < n * n; i++)
+    A[i] = (float)M[i];
   for (int i = 0; i < n; i++)
-    x[i] = 1.0;
-  for (int it = 0; it < 5; it++) {
-    /* rows were swapped whole (L included): permute first, then solve */
-    for (int k = 0; k < n; k++)
-      if (piv[k] != k) {
-        double t = x[k];
-        x[k] = x[piv[k]];
-        x[piv[k]] = t;
-      }
-    for (int k = 0; k < n; k++)
-      for (int i = k + 1; i < n; i++)
-        x[i] = fma(-A[i * n + k], x[k], x[i]);
-    double mx = 0;
-    for (int i = n - 1; i >= 0; i--) {
-      double s = x[i];
-      for (int j = i + 1; j < n; j++)
-        s = fma(-A[i * n + j], x[j], s);
-      x[i] = s * ud[i];
-      mx = fmax(mx, fabs(x[i]));
-    }
-    if (!(mx > 0.0) || mx != mx)
-      return -1;
-    double inv = 1.0 / mx;
+    A[i * n + i] = A[i * n + i] - lam0;
+  if (lu32(A, n, piv, ud) != 0)
+    return -1;
+  for (int i = 0; i < n; i++)
+    x[i] = 1.0f;
+  int s = 0;
+  for (int it = 0; it < 2; it++) {
+    lu32_solve(A, n, piv, ud, x);
+    float mx = 0.0f;
+    s = 0;
     for (int i = 0; i < n; i++)
-      x[i] *= inv;
+      if (fabsf(x[i]) > mx) {
+        mx = fabsf(x[i]);
+        s = i;
+      }
+    if (!(mx > 0.0f) || !(mx <= 3.0e38f))
+      return -1;
+    const float ix = 1.0f / x[s];
+    for (int i = 0; i < n; i++)
+      x[i] *= ix;
   }
-  double num = 0, den = 0;
+  x[s] = 1.0f;
+  /* the bordered matrix */
+  for (int i = 0; i < n * n; i++)
+    A[i] = (float)M[i];
   for (int i = 0; i < n; i++) {
-    double r = -lam0 * x[i];
-    for (int j = 0; j < n; j++)
-      r = fma(M[i * n + j], x[j], r);
-    num = fma(x[i], r, num);
-    den = fma(x[i], x[i], den);
+    A[i * n + i] = A[i * n + i] - lam0;
+    A[i * n + s] = -x[i];
   }
-  *lam = lam0 + num / den;
+  if (lu32(A, n, piv, ud) != 0)
+    return -1;
+  double xd[ORA_MAXV], l = (double)lam0, dl = 0;
+  for (int i = 0; i < n; i++)
+    xd[i] = (double)x[i];
+  for (int it = 0; it < 3; it++) {
+    for (int i = 0; i < n; i++) {
+      double acc = 0;
+      for (int j = 0; j < n; j++)
+        acc = fma(M[i * n + j], xd[j], acc);
+      z[i] = (float)fma(l, xd[i], -acc);
+    }
+    lu32_solve(A, n, piv, ud, z);
+    dl = (double)z[s];
+    l += dl;
+    for (int i = 0; i < n; i++)
+      if (i != s)
+        xd[i] += (double)z[i];
+  }
+  if (!(fabs(dl) <= 1e-10 * fabs(l)))
+    return -1;
+  *lam = l;
   return 0;
 }
 

@@ -437,82 +437,133 @@ __device__ __noinline__ int eig_vals_f(float *a, float *wr, float *wi) {
 #undef AF
 }
 
-// One real eigenvalue refined in FP64 from the FP32 shift lam0: LU with
-// partial pivoting (whole-row swaps) of M - lam0 I, five inverse-iteration
-// steps from x = 1 with max-normalisation, then lam0 + x.(M - lam0 I)x/x.x.
-// Returns -1 on an exactly singular pivot or a degenerate vector.
+// FP32 LU with partial pivoting (whole-row swaps) of the V x V matrix A in
+// place; ud gets the reciprocals of the pivots.  -1 on a zero pivot.
 template <int V>
-__device__ __forceinline__ int refine_real(const double *M, double lam0,
-                                           double *lam) {
-  double A[V * V], ud[V], x[V];
-  int piv[V];
-#pragma unroll
-  for (int i = 0; i < V * V; i++)
-    A[i] = M[i];
-#pragma unroll
-  for (int i = 0; i < V; i++)
-    A[i * V + i] = M[i * V + i] - lam0;
+__device__ __forceinline__ int lu32(float *A, int *piv, float *ud) {
   for (int k = 0; k < V; k++) {
     int p = k;
     for (int i = k + 1; i < V; i++)
-      if (fabs(A[i * V + k]) > fabs(A[p * V + k]))
+      if (fabsf(A[i * V + k]) > fabsf(A[p * V + k]))
         p = i;
     piv[k] = p;
-    if (A[p * V + k] == 0.0)
+    if (A[p * V + k] == 0.0f)
       return -1;
     if (p != k)
       for (int j = 0; j < V; j++) {
-        double t = A[k * V + j];
+        float t = A[k * V + j];
         A[k * V + j] = A[p * V + j];
         A[p * V + j] = t;
       }
-    ud[k] = 1.0 / A[k * V + k];
+    ud[k] = 1.0f / A[k * V + k];
     for (int i = k + 1; i < V; i++) {
-      double f = A[i * V + k] * ud[k];
+      float f = A[i * V + k] * ud[k];
       A[i * V + k] = f;
       for (int j = k + 1; j < V; j++)
-        A[i * V + j] = fma(-f, A[k * V + j], A[i * V + j]);
+        A[i * V + j] = fmaf(-f, A[k * V + j], A[i * V + j]);
     }
   }
+  return 0;
+}
+
+// x <- A^{-1} x with the factors of lu32 (permute, unit L, then U).
+template <int V>
+__device__ __forceinline__ void lu32_solve(const float *A, const int *piv,
+                                           const float *ud, float *x) {
+  for (int k = 0; k < V; k++)
+    if (piv[k] != k) {
+      float t = x[k];
+      x[k] = x[piv[k]];
+      x[piv[k]] = t;
+    }
+  for (int k = 0; k < V; k++)
+    for (int i = k + 1; i < V; i++)
+      x[i] = fmaf(-A[i * V + k], x[k], x[i]);
+  for (int i = V - 1; i >= 0; i--) {
+    float sacc = x[i];
+    for (int j = i + 1; j < V; j++)
+      sacc = fmaf(-A[i * V + j], x[j], sacc);
+    x[i] = sacc * ud[i];
+  }
+}
+
+// One real eigenvalue refined from the FP32 shift lam0 (an eigenvalue of M
+// rounded to FP32) by the iterative refinement of an eigenpair of Dongarra,
+// Moler and Wilkinson (SIAM J. Numer. Anal. 20, 1983):
+//   FP32: x from two inverse-iteration steps with the LU of Mf - lam0 I
+//         (Mf = M rounded to FP32), scaled so that x_s = 1 at its largest
+//         entry s; the LU of B = Mf - lam0 I with column s replaced by -x.
+//   FP64 residual, FP32 correction, three times:
+//         r = lam x - M x;  z = B^{-1} r;  lam += z_s;  x_j += z_j (j != s)
+// Converges linearly at a rate of about eps_32 cond(B).  Returns -1 on a
+// zero FP32 pivot, a vector that vanishes or is not finite, or a last
+// correction larger than 1e-10 |lam|.  Same operations and order as the
+// host restatement's refine_real.
+template <int V>
+__device__ __forceinline__ int refine_real(const double *M, double lam0d,
+                                           double *lam) {
+  float A[V * V], ud[V], x[V], z[V];
+  int piv[V];
+  const float lam0 = (float)lam0d;
+#pragma unroll
+  for (int i = 0; i < V * V; i++)
+    A[i] = (float)M[i];
 #pragma unroll
   for (int i = 0; i < V; i++)
-    x[i] = 1.0;
-  for (int it = 0; it < 5; it++) {
-    for (int k = 0; k < V; k++)
-      if (piv[k] != k) {
-        double t = x[k];
-        x[k] = x[piv[k]];
-        x[piv[k]] = t;
-      }
-    for (int k = 0; k < V; k++)
-      for (int i = k + 1; i < V; i++)
-        x[i] = fma(-A[i * V + k], x[k], x[i]);
-    double mx = 0;
-    for (int i = V - 1; i >= 0; i--) {
-      double s = x[i];
-      for (int j = i + 1; j < V; j++)
-        s = fma(-A[i * V + j], x[j], s);
-      x[i] = s * ud[i];
-      mx = fmax(mx, fabs(x[i]));
-    }
-    if (!(mx > 0.0) || mx != mx)
-      return -1;
-    double inv = 1.0 / mx;
+    A[i * V + i] = A[i * V + i] - lam0;
+  if (lu32<V>(A, piv, ud) != 0)
+    return -1;
 #pragma unroll
+  for (int i = 0; i < V; i++)
+    x[i] = 1.0f;
+  int s = 0;
+  for (int it = 0; it < 2; it++) {
+    lu32_solve<V>(A, piv, ud, x);
+    float mx = 0.0f;
+    s = 0;
     for (int i = 0; i < V; i++)
-      x[i] *= inv;
+      if (fabsf(x[i]) > mx) {
+        mx = fabsf(x[i]);
+        s = i;
+      }
+    if (!(mx > 0.0f) || !(mx <= 3.0e38f))
+      return -1;
+    const float ix = 1.0f / x[s];
+    for (int i = 0; i < V; i++)
+      x[i] *= ix;
   }
-  double num = 0, den = 0;
+  x[s] = 1.0f;
 #pragma unroll
+  for (int i = 0; i < V * V; i++)
+    A[i] = (float)M[i];
   for (int i = 0; i < V; i++) {
-    double r = -lam0 * x[i];
-#pragma unroll
-    for (int j = 0; j < V; j++)
-      r = fma(M[i * V + j], x[j], r);
-    num = fma(x[i], r, num);
-    den = fma(x[i], x[i], den);
+    A[i * V + i] = A[i * V + i] - lam0;
+    A[i * V + s] = -x[i];
   }
-  *lam = lam0 + num / den;
+  if (lu32<V>(A, piv, ud) != 0)
+    return -1;
+  double xd[V], l = (double)lam0, dl = 0;
+#pragma unroll
+  for (int i = 0; i < V; i++)
+    xd[i] = (double)x[i];
+  for (int it = 0; it < 3; it++) {
+    for (int i = 0; i < V; i++) {
+      double acc = 0;
+#pragma unroll
+      for (int j = 0; j < V; j++)
+        acc = fma(M[i * V + j], xd[j], acc);
+      z[i] = (float)fma(l, xd[i], -acc);
+    }
+    lu32_solve<V>(A, piv, ud, z);
+    dl = (double)z[s];
+    l += dl;
+    for (int i = 0; i < V; i++)
+      if (i != s)
+        xd[i] += (double)z[i];
+  }
+  if (!(fabs(dl) <= 1e-10 * fabs(l)))
+    return -1;
+  *lam = l;
   return 0;
 }
 

@@ -143,32 +143,43 @@ def test_fused_inference_matches_training_forward(gpu_lib):
 
 
 def test_trained_warm_start_end_to_end(gpu_lib):
-    """Train on 20 harvested steps of a 48x48 relaxation problem.  The
-    learned run must give the plain run's answer (Newton to the same 1e-12
-    tolerance: 1e-8 relative L1 per variable after 30 steps) with no Newton
-    failures.  Its iteration count is measured against the plain run's and
-    written to the test output; on this problem the Newton iteration
-    contracts by about 1e-2 per sweep, so a guess must be about 1e-4
-    accurate per cell to save a sweep, and the BF16 network's guess
-    (a few per cent) saves close to none -- the bound checked is that it
-    costs at most 10% more."""
+    """Train on 20 harvested steps of a 48x48 relaxation problem, then run
+    30 steps plain and learned, both with Newton tolerance 1e-12, and
+    compare each with an oracle run at tolerance 1e-15.  Two converged
+    Newton solves started from different guesses differ by the
+    tolerance's effect, which after 30 steps is ~1e-8 relative L1 in the
+    small heat-flux components (the plain form's own error at tolerance
+    1e-12 and 1e-13 measures that floor).  The learned form must stay at
+    the plain form's error level: <= max(1e-8, 3 x the floor).
+    Newton iterations are measured against the plain run and written to
+    the test output: on this problem Newton contracts by about 1e-2 per
+    sweep, so a guess must be ~1e-4 accurate per cell to save a sweep,
+    and the BF16 network's (a few per cent) saves close to none -- the
+    bound checked is that it costs at most 10% more."""
     n, N, K = 48, 2, 30
     u0 = workloads.relaxation(n, 2, seed=11, patches=4)
     s = systems.cattaneo(2)
     ws = warmstart.train_warm_start(u0, 10.0, [1.0, 1.0], F=s.F, S=s.S, cfl=0.8, order=N,
                                     tau_var=6, steps=20, per_step=1024, iters=3000, seed=0)
-    st_p, st_l = {}, {}
-    q_p = u0.copy()
-    pde_solver(q_p, 10.0, [1.0, 1.0], F=s.F, S=s.S, boundaryTypes="periodic", cfl=0.8,
-               order=N, stiff=True, max_steps=K, stats=st_p)
-    q_l = u0.copy()
-    pde_solver(q_l, 10.0, [1.0, 1.0], F=s.F, S=s.S, boundaryTypes="periodic", cfl=0.8,
-               order=N, stiff=True, max_steps=K, stats=st_l, warm_start=ws)
-    assert st_l["steps"] == st_p["steps"] == K and st_l["pred_fail"] == 0
-    err = l1(q_l, q_p)
-    assert np.all(err <= 1e-8), err
+
+    def run(tol, warm=None):
+        q, st = u0.copy(), {}
+        pde_solver(q, 10.0, [1.0, 1.0], F=s.F, S=s.S, boundaryTypes="periodic", cfl=0.8,
+                   order=N, stiff=True, max_steps=K, stats=st, newton_tol=tol,
+                   warm_start=warm)
+        assert st["steps"] == K and st["pred_fail"] == 0
+        return q, st
+
+    q_o, _ = run(1e-15)
+    q_p, st_p = run(1e-12)
+    q_p13, _ = run(1e-13)
+    q_l, st_l = run(1e-12, ws)
+    floor = max(l1(q_p, q_o).max(), l1(q_p13, q_o).max())
+    err = l1(q_l, q_o).max()
     saved = 1 - st_l["pred_iters"] / st_p["pred_iters"]
-    print(f"warm start: train rms {ws.train_rms:.3g}, Newton iterations plain "
-          f"{st_p['pred_iters']} learned {st_l['pred_iters']} (saved {100 * saved:.1f}%), "
-          f"fallbacks {st_l['pred_fallbacks']}, L1 {err.max():.2e}")
+    print(f"warm start: train rms {ws.train_rms:.3g}; L1 vs tol-1e-15 oracle: plain "
+          f"{l1(q_p, q_o).max():.2e}, learned {err:.2e} (floor {floor:.2e}); Newton "
+          f"iterations plain {st_p['pred_iters']} learned {st_l['pred_iters']} "
+          f"(saved {100 * saved:.1f}%), fallbacks {st_l['pred_fallbacks']}")
+    assert err <= max(1e-8, 3 * floor), (err, floor)
     assert st_l["pred_iters"] <= 1.1 * st_p["pred_iters"]
