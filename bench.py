@@ -1,12 +1,23 @@
 """Benchmark: cell-updates/s of the ADER-WENO step on one GB300.
 
-Workload (default): 2-D Euler shear layer, 512x512 periodic cells on [0,1]^2,
-order N=3, Rusanov flux, CFL 0.8, plain FP64 form (the Picard predictor) --
-the configuration the reference's plain GPU-vs-CPU comparison is quoted on.
-Seeded synthetic initial state (pypde_gb300.workloads.shear).  One step is
-one ADER time step over the whole grid.
+Default workload (--workload stiff): 2-D Euler + relaxing heat flux
+(Cattaneo), 7 variables (rho, rho u, rho v, E, q_x, q_y, log10 tau),
+1024x1024 periodic cells on [0,1]^2, order N=2, Rusanov, CFL 0.8, stiff
+Newton predictor to ||obj||_inf <= 1e-12, tau piecewise constant on 16x16
+patches with log10 tau ~ U(-7,-2) (pypde_gb300.workloads.relaxation, seeded
+synthetic data).  Forms measured on the same K steps from the same state:
+  plain    Newton from the plain guess q = w
+  learned  Newton from the learned warm start (network trained here on 20
+           harvested plain steps with the library's own kernels; training
+           time reported, not timed in `value`)
+`value` is the learned form (the metric's "learned" form); `forms` gives
+both, each with its Newton iterations and its relative L1 error per
+variable against an oracle run at Newton tolerance 1e-15 (the GPU plain path
+is bit-identical to the CPU restatement, checked by the GPU tests).
+--workload shear: 2-D Euler shear layer 512x512 N=3, plain FP64 (Picard).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
+                  [--workload stiff|shear]
 
 Our arm prints one JSON line:
   value        cell-updates/s with the state resident in HBM, timed by CUDA
@@ -44,6 +55,12 @@ sys.path.insert(0, HERE)
 METRIC = "cell_updates_per_s"
 UNIT = "cell-updates/s"
 
+WORKLOADS = {
+    # name: (system, n, N, cfl, stiff)
+    "stiff": ("cattaneo", 1024, 2, 0.8, True),
+    "shear": ("euler", 512, 3, 0.8, False),
+}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -51,12 +68,19 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=512, help="cells per side")
-    p.add_argument("--order", type=int, default=3)
+    p.add_argument("--workload", default="stiff", choices=sorted(WORKLOADS))
+    p.add_argument("--n", type=int, default=0, help="cells per side (0: the workload's)")
+    p.add_argument("--order", type=int, default=0, help="N (0: the workload's)")
+    p.add_argument("--train-iters", type=int, default=3000)
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    system, n, N, cfl, stiff = WORKLOADS[a.workload]
+    a.system, a.cfl, a.stiff = system, cfl, stiff
+    a.n = a.n or n
+    a.order = a.order or N
+    return a
 
 
 def dist_init(args):
@@ -132,89 +156,175 @@ class Clocks:
                 else None, "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def cpu_baseline(u0, N, cfl, budget):
+def l1(a, b):
+    """Relative L1 error per variable: sum|a-b| / sum|b| over all cells."""
+    ax = tuple(range(a.ndim - 1))
+    return np.abs(a - b).sum(axis=ax) / np.abs(b).sum(axis=ax)
+
+
+def initial_state(args, seed):
+    from pypde_gb300 import workloads
+    if args.workload == "stiff":
+        return workloads.relaxation(args.n, 2, seed=seed)
+    return workloads.shear(args.n, seed=seed)
+
+
+def workload_name(args):
+    if args.workload == "stiff":
+        return (f"2-D Euler + relaxing heat flux (7 vars), {args.n}x{args.n} periodic, "
+                f"N={args.order}, Rusanov, CFL {args.cfl}, stiff Newton predictor to 1e-12, "
+                "log10 tau ~ U(-7,-2) on 16x16 patches")
+    return (f"2-D Euler shear layer {args.n}x{args.n} periodic, N={args.order}, Rusanov, "
+            f"CFL {args.cfl}, plain FP64 (Picard predictor)")
+
+
+def cpu_run(args, u, steps, cores):
+    from oracle import ora
+    return ora.pde_solver(args.system, u, 10.0, [1.0, 1.0], [1, 1], args.cfl, args.order,
+                          stiff=args.stiff, max_steps=steps, nthreads=cores)
+
+
+def cpu_baseline(args, u0, budget):
     """The CPU restatement on all host cores: whole-grid steps until the
     budget is used (at least one step).  Returns (cell-updates/s, cores,
     sample description)."""
-    from oracle import ora
     cores = os.cpu_count() or 1
     C = int(np.prod(u0.shape[:-1]))
     u = u0
     steps, t0 = 0, time.perf_counter()
     while True:
-        u, _, k, _ = ora.pde_solver("euler", u, 10.0, [1.0, 1.0], [1, 1], cfl, N, max_steps=1,
-                                    nthreads=cores)
+        u, _, k, _ = cpu_run(args, u, 1, cores)
         steps += k
         el = time.perf_counter() - t0
         if el >= budget or steps >= 50:
             break
-    sample = (f"{steps} whole-grid step(s) of the same {u0.shape[0]}x{u0.shape[1]} N={N} "
-              f"workload, {el:.1f} s")
+    sample = (f"{steps} whole-grid step(s) of the same {u0.shape[0]}x{u0.shape[1]} "
+              f"N={args.order} workload from its initial state, {el:.1f} s")
     return C * steps / el, cores, sample
 
 
+class Runner:
+    """Timed runs of the solver through the C ABI (pde_solver_ex)."""
+
+    def __init__(self, args, local):
+        from pypde_gb300 import _lib
+        from pypde_gb300.callbacks import builtin_system
+        self.L = _lib.lib()
+        self._lib = _lib
+        self.args, self.local = args, local
+        self.sys = builtin_system(args.system, 2)
+        self.nX = np.array([args.n, args.n], dtype=np.int32)
+        self.dX = np.array([1.0 / args.n, 1.0 / args.n])
+        self.bt = np.array([1, 1], dtype=np.int32)
+
+    def run(self, u, steps, profile=False, warm=None, tol=0.0):
+        _lib, a = self._lib, self.args
+        opt = _lib.Options()
+        opt.max_steps = steps
+        opt.device = self.local
+        opt.profile_stages = int(profile)
+        opt.newton_tol = tol
+        if warm is not None:
+            opt.warm_start = warm.handle
+        st = _lib.Stats()
+        s = self.sys
+        _lib.check(self.L.pde_solver_ex(s.handle, s.has_F, s.has_B, s.has_S, _lib.c_ptr(u),
+                                        10.0, _lib.c_ptr(self.nX), 2, _lib.c_ptr(self.dX),
+                                        a.cfl, _lib.c_ptr(self.bt), a.stiff, 0, a.order, 1,
+                                        None, opt, st))
+        return st.as_dict()
+
+
+def measure_form(R, args, ws, u0, warm=None):
+    """W warm-up steps, then exactly K timed steps (CUDA events inside the
+    library), then an eagerly launched profile of min(K, 5) steps."""
+    u = u0.copy()
+    R.run(u, args.warmup, warm=warm)
+    barrier(ws)
+    st = R.run(u, args.steps, warm=warm)
+    barrier(ws)
+    sec = allmax(ws, st["device_seconds"])
+    ksteps = max(1, min(args.steps, 5))
+    sp = R.run(u0.copy(), ksteps, profile=True, warm=warm)
+    return st, sec, sp, ksteps
+
+
 def run_ours(args, ws, rank, local):
-    from pypde_gb300 import _lib, systems, work_model, workloads
-    from pypde_gb300.callbacks import builtin_system
+    from pypde_gb300 import _lib, systems, work_model
     from pypde_gb300.solvers import pde_solver
 
     L = _lib.lib()
-    n, N, cfl, V = args.n, args.order, 0.8, 4
+    n, N, V = args.n, args.order, (7 if args.workload == "stiff" else 4)
     C = n * n
-    u0 = workloads.shear(n, seed=rank)
-    sysobj = builtin_system("euler", 2)
-    nX = np.array([n, n], dtype=np.int32)
-    dX = np.array([1.0 / n, 1.0 / n])
-    bt = np.array([1, 1], dtype=np.int32)
-
-    def run(u, steps, profile=False):
-        opt = _lib.Options()
-        opt.max_steps = steps
-        opt.device = local
-        opt.profile_stages = int(profile)
-        st = _lib.Stats()
-        _lib.check(L.pde_solver_ex(sysobj.handle, True, False, False, _lib.c_ptr(u), 10.0,
-                                   _lib.c_ptr(nX), 2, _lib.c_ptr(dX), cfl, _lib.c_ptr(bt),
-                                   False, 0, N, 1, None, opt, st))
-        return st
-
-    # warm-up: W steps (module load, arena allocation, graph capture)
-    u = u0.copy()
-    run(u, args.warmup)
+    u0 = initial_state(args, rank)
+    R = Runner(args, local)
     peak = _lib.ctypes.c_double()
     _lib.check(L.pypde_measure_fp64_peak(local, peak))
+    s = systems.cattaneo(2) if args.workload == "stiff" else systems.euler(2)
 
-    # timed: exactly K steps, state resident in HBM, CUDA events inside
-    barrier(ws)
+    forms = {}
+    warm = None
+    train = None
+    if args.stiff:
+        from pypde_gb300 import warmstart
+        t0 = time.perf_counter()
+        warm = warmstart.train_warm_start(u0, 10.0, [1.0, 1.0], F=s.F, S=s.S, cfl=args.cfl,
+                                          order=N, tau_var=6, steps=20, per_step=16384,
+                                          iters=args.train_iters, seed=rank, device=local)
+        train = {"seconds": time.perf_counter() - t0, "samples": warm.samples,
+                 "iters": args.train_iters, "train_rms_normalised": warm.train_rms,
+                 "harvest": "20 plain steps from the initial state, 16384 cells per step"}
+
+    head = "learned" if args.stiff else "plain"
     with Clocks(local) as clk:
-        st = run(u, args.steps)
-    barrier(ws)
-    sec = allmax(ws, st.device_seconds)
+        st_h, sec, sp, ksteps = measure_form(R, args, ws, u0, warm if args.stiff else None)
+    forms[head] = (st_h, sec, sp, ksteps)
+    if args.stiff:
+        forms["plain"] = measure_form(R, args, ws, u0, None)
     value = ws * C * args.steps / sec
 
-    # stage profile of the same workload (eager launches, events per stage)
-    ksteps = max(1, min(args.steps, 5))
-    sp = run(u0.copy(), ksteps, profile=True).as_dict()
+    # relative L1 per variable after K steps from u0, against a tolerance
+    # 1e-15 oracle run of the same steps
+    errs = {}
+    if args.stiff:
+        q_o = u0.copy()
+        R.run(q_o, args.steps, tol=1e-15)
+        for name, w in (("plain", None), ("learned", warm)):
+            q = u0.copy()
+            R.run(q, args.steps, warm=w)
+            errs[name] = [float(x) for x in l1(q, q_o)]
+
+    def form_summary(name):
+        st, sec_f, sp_f, ks = forms[name]
+        its = st["pred_iters"] / (args.steps * (n + 2) ** 2)
+        d = {"value": ws * C * args.steps / sec_f, "ms_per_step": 1e3 * sec_f / args.steps,
+             "predictor_iters_per_cell": its,
+             "stage_ms_per_step": {k: 1e3 * v / ks for k, v in sp_f["stage_seconds"].items()}}
+        if args.stiff:
+            d["newton_fallbacks"] = st["pred_fallbacks"]
+            d["l1_vs_oracle"] = errs[name]
+        return d
+
     stage_s = sp["stage_seconds"]
     its = sp["pred_iters"] / (ksteps * (n + 2) ** 2)
-    fpf = work_model.face_point_flops("euler", 2, V, N)
+    fpf = work_model.face_point_flops(args.system, 2, V, N)
     fpts = work_model.face_points([n, n], N)
     faces_launch = stage_s["faces"] / ksteps
     achieved = fpts * fpf / faces_launch / 1e12
-    flops = work_model.step_flops("euler", [n, n], V, N, its)
+    flops = work_model.step_flops(args.system, [n, n], V, N, its, stiff=args.stiff)
 
-    # e2e through the public API from pinned host memory
+    # e2e through the public API from pinned host memory (the headline form)
     try:
         import torch
         pinned = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
     except Exception:
         pinned = np.empty(u0.shape)
     pinned[...] = u0
-    s = systems.euler(2)
     barrier(ws)
     t0 = time.perf_counter()
-    pde_solver(pinned, 10.0, [1.0, 1.0], F=s.F, boundaryTypes="periodic", cfl=cfl, order=N,
-               ndt=1, stiff=False, max_steps=args.steps, device=local)
+    pde_solver(pinned, 10.0, [1.0, 1.0], F=s.F, S=s.S if args.stiff else None,
+               boundaryTypes="periodic", cfl=args.cfl, order=N, ndt=1, stiff=args.stiff,
+               max_steps=args.steps, device=local, warm_start=warm if args.stiff else None)
     e2e_s = allmax(ws, time.perf_counter() - t0)
     barrier(ws)
 
@@ -222,12 +332,12 @@ def run_ours(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"2-D Euler shear layer {n}x{n} periodic, N={N}, Rusanov, "
-                               f"CFL {cfl}, plain FP64 (Picard predictor)",
-                   "cells": C, "order": N, "vars": V,
+        "config": {"workload": workload_name(args), "form": head, "cells": C, "order": N,
+                   "vars": V,
                    "l2": "working set > L2 (qh alone is "
                          f"{(n + 2) ** 2 * N ** 3 * V * 8 / 1e6:.0f} MB); no flush",
                    "parallelism": f"replicas x{ws}"},
+        "forms": {k: form_summary(k) for k in forms},
         "e2e": {"value": ws * C * args.steps / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": C * V * 8 / args.steps,
                 "d2h_bytes_per_step": 2 * C * V * 8 / args.steps,
@@ -238,15 +348,20 @@ def run_ours(args, ws, rank, local):
                      "traffic": None,
                      "peak_source": "FP64 FMA loop measured by this run "
                                     "(MEASURED_PEAKS.json has no FP64 figure)",
-                     "flops_per_launch": fpts * fpf, "launch_ms": 1e3 * faces_launch},
+                     "flops_per_launch": fpts * fpf, "launch_ms": 1e3 * faces_launch,
+                     "note": "algorithmic flops count max|eig| as the nominal 10 V^3 of a "
+                             "Hessenberg + Francis QR; the kernel's mixed-precision "
+                             "eigensolver does less FP64 work than that"},
         "stage_ms_per_step": {k: 1e3 * v / ksteps for k, v in stage_s.items()},
         "step_fp64_tflops": sum(flops.values()) / (sec / args.steps) / 1e12,
         "predictor_iters_per_cell": its,
-        "gpu_launches": st.kernel_launches,
+        "gpu_launches": st_h["kernel_launches"],
         "clocks": clk.summary(),
     }
+    if train:
+        out["training"] = train
     if rank == 0 and not args.no_cpu:
-        v, cores, sample = cpu_baseline(u0, N, cfl, args.cpu_seconds)
+        v, cores, sample = cpu_baseline(args, u0, args.cpu_seconds)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                "sample": sample}
     return out
@@ -257,24 +372,19 @@ def run_reference(args, ws, rank):
     reference's own build needs its source tree, absent on the GPU host)."""
     if rank != 0:
         return None
-    from pypde_gb300 import workloads
-    n, N, cfl = args.n, args.order, 0.8
-    u = workloads.shear(n)
+    u = initial_state(args, 0)
     cores = os.cpu_count() or 1
-    from oracle import ora
-    ora.pde_solver("euler", u, 10.0, [1.0, 1.0], [1, 1], cfl, N, max_steps=args.warmup,
-                   nthreads=cores)
+    n = args.n
+    cpu_run(args, u, args.warmup, cores)
     t0 = time.perf_counter()
-    u, _, k, _ = ora.pde_solver("euler", u, 10.0, [1.0, 1.0], [1, 1], cfl, N,
-                                max_steps=args.steps, nthreads=cores)
+    u, _, k, _ = cpu_run(args, u, args.steps, cores)
     el = time.perf_counter() - t0
     v = n * n * k / el
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / k,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": f"2-D Euler shear layer {n}x{n} periodic, N={N}, "
-                                   f"Rusanov, CFL {cfl}, plain FP64", "cells": n * n},
+            "config": {"workload": workload_name(args), "form": "plain", "cells": n * n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{k} whole-grid steps after {args.warmup} warm-up"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,

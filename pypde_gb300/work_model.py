@@ -18,7 +18,7 @@ def f_flops(system, ndim):
     if system == "euler":
         return 3 * ndim + 8
     if system == "cattaneo":
-        return 3 * ndim + 8 + 58 + 4  # + 10^-s (Horner, 18 terms) + T, q, kappa T/tau
+        return 3 * ndim + 8 + 3  # Euler part + T = p/rho, energy += q_d, kappa_h T
     if system == "ncp":
         return 8
     if system == "burgers2":
@@ -31,7 +31,8 @@ def b_flops(system):
 
 
 def s_flops(system, ndim):
-    return {"cattaneo": 58 + ndim, "ncp": 4}.get(system, 0)
+    # cattaneo: 10^-x (Horner, degree 16: 32 + 4) and -q_i / tau
+    return {"cattaneo": 36 + ndim, "ncp": 4}.get(system, 0)
 
 
 def eig_flops(V):
@@ -90,7 +91,20 @@ def predictor_flops_per_iteration(system, ndim, V, N):
     return nodes * per_node
 
 
-def step_flops(system, nX, V, N, pred_iters_per_cell):
+def newton_flops_per_iteration(system, ndim, V, N):
+    """One Newton iteration of one cell (stiff predictor): the residual
+    (as a Picard iteration), the FD Jacobian of S at every space-time node
+    (V+1 S calls, V^2 differences and scalings), and per spatial node a
+    dense LU of the (N V)^2 system (2/3 (NV)^3) and its solve (2 (NV)^2),
+    counted dense and refreshed every iteration (the nominal cost)."""
+    Nd = N ** ndim
+    nl = N * V
+    jac = N * Nd * ((V + 1) * s_flops(system, ndim) + 3 * V * V)
+    lin = Nd * (2 * nl ** 3 // 3 + 2 * nl * nl)
+    return predictor_flops_per_iteration(system, ndim, V, N) + jac + lin
+
+
+def step_flops(system, nX, V, N, pred_iters_per_cell, stiff=False):
     """Whole-step algorithmic flops, per stage."""
     ndim = len(nX)
     C = 1
@@ -112,7 +126,9 @@ def step_flops(system, nX, V, N, pred_iters_per_cell):
         n4 *= N
     out["weno"] = weno
     out["cfl"] = Cw * cfl_flops_per_wcell(system, ndim, V, N)
-    out["predictor"] = Cw * pred_iters_per_cell * predictor_flops_per_iteration(system, ndim, V, N)
+    per_it = (newton_flops_per_iteration if stiff else predictor_flops_per_iteration)(
+        system, ndim, V, N)
+    out["predictor"] = Cw * pred_iters_per_cell * per_it
     out["faces"] = face_points(nX, N) * face_point_flops(system, ndim, V, N)
     return out
 
