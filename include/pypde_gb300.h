@@ -180,6 +180,52 @@ int pypde_tables(int N, double *out);
  * Bench support; no reference counterpart. */
 int pypde_measure_fp64_peak(int device, double *tflops);
 
+/* ---------------- batched problems (no reference counterpart) -----------
+ * Many independent problems of one system (sizes, orders, boundary types
+ * and end times may all differ) stepped together: every stage of a step is
+ * one persistent launch per order whose CTAs drain a queue of cell tiles,
+ * largest problems first, captured in a CUDA graph.  Each problem gives
+ * the same bits as pde_solver_ex on it alone (ndt = 1: only the final
+ * state is returned, written into u). */
+typedef struct {
+  double *u;             /* host, in/out, prod(nX) x V */
+  double tf;
+  int nX[3];             /* first ndim used */
+  double dX[3];
+  int boundaryTypes[3];  /* 0 transmissive, 1 periodic */
+  int N;                 /* order */
+  double cfl;
+} pypde_problem;
+
+typedef struct {
+  long long max_steps;   /* per problem; <= 0: run to tf */
+  double newton_tol;     /* stiff form; 0 -> 1e-12 */
+  int device;
+  int steps_per_graph;   /* 0 -> 8 */
+  int autotune;          /* 1: the first steps try tiles-per-pop 1,2,4,8 per
+                            stage and keep the fastest */
+  int per_pop;           /* tiles per queue pop without autotune (0 -> 1) */
+} pypde_batch_options;
+
+#define PYPDE_BATCH_STAGES 9 /* ghost, WENO x3, CFL, predictor, faces,
+                                centres, gather */
+typedef struct {
+  long long steps;              /* summed over problems */
+  long long max_problem_steps;
+  double device_seconds;        /* the whole stepping loop, tuning included */
+  long long kernel_launches;
+  unsigned long long pred_iters;
+  int nan_found;                /* problems stopped by a NaN */
+  int per_pop[PYPDE_BATCH_STAGES]; /* tile shape chosen (first order group) */
+  double tune_seconds;
+} pypde_batch_stats;
+
+/* steps_out, t_out: per-problem step counts and end times (may be NULL). */
+int pde_solver_batch(const pypde_system *sys, bool STIFF, int FLUX, int nprob,
+                     pypde_problem *problems, const pypde_batch_options *opt,
+                     pypde_batch_stats *stats, long long *steps_out,
+                     double *t_out);
+
 /* ---------------- learned warm start (no reference counterpart) ---------
  * A per-cell MLP maps the WENO coefficients of a cell and log10(dt/tau) to
  * the initial guess of the stiff predictor's Newton iteration, which then

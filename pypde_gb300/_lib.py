@@ -45,6 +45,32 @@ dp = POINTER(c_double)
 ip = POINTER(c_int)
 fp = POINTER(ctypes.c_float)
 
+
+class BatchProblem(Structure):
+    _fields_ = [("u", dp), ("tf", c_double), ("nX", c_int * 3), ("dX", c_double * 3),
+                ("boundaryTypes", c_int * 3), ("N", c_int), ("cfl", c_double)]
+
+
+class BatchOptions(Structure):
+    _fields_ = [("max_steps", c_longlong), ("newton_tol", c_double), ("device", c_int),
+                ("steps_per_graph", c_int), ("autotune", c_int), ("per_pop", c_int)]
+
+
+BATCH_STAGES = ("boundaries", "weno0", "weno1", "weno2", "cfl", "predictor", "faces",
+                "centers", "gather")
+
+
+class BatchStats(Structure):
+    _fields_ = [("steps", c_longlong), ("max_problem_steps", c_longlong),
+                ("device_seconds", c_double), ("kernel_launches", c_longlong),
+                ("pred_iters", c_ulonglong), ("nan_found", c_int), ("per_pop", c_int * 9),
+                ("tune_seconds", c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "per_pop"}
+        d["per_pop"] = dict(zip(BATCH_STAGES, list(self.per_pop)))
+        return d
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "pypde_system_builtin": (c_int, [c_char_p, c_int, POINTER(c_void_p)]),
@@ -68,6 +94,9 @@ SIGNATURES = {
     "pypde_fv": (c_int, [c_void_p, dp, dp, ip, dp, c_int, c_int, c_int, c_double]),
     "pypde_tables": (c_int, [c_int, dp]),
     "pypde_measure_fp64_peak": (c_int, [c_int, dp]),
+    "pde_solver_batch": (c_int, [c_void_p, c_bool, c_int, c_int, POINTER(BatchProblem),
+                                 POINTER(BatchOptions), POINTER(BatchStats),
+                                 POINTER(c_longlong), dp]),
     "pypde_warm_start_shape": (c_int, [c_void_p, c_int, ip, ip, ip]),
     "pypde_warm_start_create": (c_int, [c_void_p, c_int, c_int] + [fp] * 10 +
                                 [c_int, POINTER(c_void_p)]),

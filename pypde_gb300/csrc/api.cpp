@@ -4,6 +4,7 @@
 
 #include <cstring>
 #include <new>
+#include <vector>
 
 struct pypde_system {
   const pypde::SystemDesc *desc;
@@ -239,6 +240,61 @@ int pypde_predictor(const pypde_system *sys, const double *w, long long nrows,
     stats->pred_iters = st.pred_iters;
     stats->pred_max_iters = st.pred_max_iters;
     stats->pred_fail = st.pred_fail;
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------- batch
+
+int pde_solver_batch(const pypde_system *sys, bool STIFF, int FLUX, int nprob,
+                     pypde_problem *problems, const pypde_batch_options *opt,
+                     pypde_batch_stats *stats, long long *steps_out,
+                     double *t_out) {
+  if (!sys || nprob < 1 || !problems || FLUX < 0 || FLUX > 2) {
+    set_error("invalid arguments");
+    return PYPDE_ERR_ARG;
+  }
+  std::vector<ProblemSpec> ps(nprob);
+  for (int p = 0; p < nprob; p++) {
+    ps[p].u = problems[p].u;
+    ps[p].tf = problems[p].tf;
+    ps[p].N = problems[p].N;
+    ps[p].cfl = problems[p].cfl;
+    for (int d = 0; d < 3; d++) {
+      ps[p].nX[d] = d < sys->desc->ndim ? problems[p].nX[d] : 1;
+      ps[p].dX[d] = d < sys->desc->ndim ? problems[p].dX[d] : 1.0;
+      ps[p].bt[d] = d < sys->desc->ndim ? problems[p].boundaryTypes[d] : 0;
+    }
+  }
+  BatchArgs a;
+  a.np = nprob;
+  a.probs = ps.data();
+  a.stiff = STIFF;
+  a.flux = FLUX;
+  if (opt) {
+    a.max_steps = opt->max_steps > 0 ? opt->max_steps : -1;
+    if (opt->newton_tol > 0)
+      a.newton_tol = opt->newton_tol;
+    a.device = opt->device;
+    a.steps_per_graph = opt->steps_per_graph;
+    a.autotune = opt->autotune != 0;
+    a.per_pop = opt->per_pop > 0 ? opt->per_pop : 1;
+  }
+  BatchStats st;
+  st.steps_per_problem = steps_out;
+  st.t_per_problem = t_out;
+  int rc = run_batch(*sys->desc, a, &st);
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->steps = st.steps;
+    stats->max_problem_steps = st.max_problem_steps;
+    stats->device_seconds = st.device_seconds;
+    stats->kernel_launches = st.kernel_launches;
+    stats->pred_iters = st.pred_iters;
+    stats->nan_found = st.nan_found;
+    for (int i = 0; i < PYPDE_BATCH_STAGES && i < BS_COUNT; i++)
+      stats->per_pop[i] = st.per_pop[i];
+    stats->tune_seconds = st.tune_seconds;
   }
   return rc;
 }

@@ -1,0 +1,136 @@
+// batch.cuh -- many independent problems in one launch per stage.
+//
+// Problems of one order N (possibly of different sizes, boundary types and
+// end times) are stepped together: each stage is one persistent launch
+// whose CTAs drain a work queue of tiles, tile = one block of the stage's
+// one-problem launch (a VBlock of that problem), problems listed largest
+// first so that the queue hands out the long work first.  A CTA pops
+// `per_pop` consecutive tiles at a time (the tile shape the autotuner
+// picks).  The per-tile work is the one-problem kernels' bodies, unchanged,
+// so a batched step gives the same bits as the same problem stepped alone.
+// Not in the reference (one grid per pde_solver call).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace pypde {
+
+// One problem of a batched step: its geometry and device buffers.
+struct BatchProblem {
+  Geom g;
+  FaceIndex fi;
+  int N, V;
+  double *u, *ub, *w, *qh, *contrib, *cen, *wprod;
+  // WENO pass d reads win[d] and writes wout[d] (the last writes w)
+  const double *win[3];
+  double *wout[3];
+  long long wn1[3], wn3[3];
+  int wmd[3], wn4[3];
+  DevState *st;
+};
+
+// Tiles of one stage: problem p owns tiles [off[p], off[p+1]); head is a
+// counter zeroed before the launch.
+struct TileQueue {
+  const long long *off;
+  int np;
+  unsigned long long *head;
+};
+
+// Pop per_pop tiles at a time until the queue is empty; body(p, vb) runs
+// one tile of problem p with the whole CTA.
+template <class Body>
+__device__ __forceinline__ void drain(const TileQueue &q, int per_pop,
+                                      Body body) {
+  __shared__ long long s_tile;
+  const long long total = q.off[q.np];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      s_tile = (long long)atomicAdd(q.head, (unsigned long long)per_pop);
+    __syncthreads();
+    const long long t0 = s_tile;
+    if (t0 >= total)
+      break;
+    for (long long t = t0; t < t0 + per_pop && t < total; t++) {
+      int lo = 0, hi = q.np;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (q.off[mid] <= t)
+          lo = mid;
+        else
+          hi = mid;
+      }
+      body(lo, VBlock{t - q.off[lo], q.off[lo + 1] - q.off[lo]});
+      __syncthreads();
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128)
+    kb_weno(const BatchProblem *P, TileQueue q, int per_pop, int d, Tables T) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_weno_pass_body<N>(vb, b.win[d], b.wout[d], b.wn1[d], b.wmd[d], b.wn3[d],
+                        b.wn4[d], b.V, T, b.st);
+  });
+}
+
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    kb_cfl(const BatchProblem *P, TileQueue q, int per_pop, Tables T) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_cfl_body<Sys, N>(vb, b.w, b.g, T, b.wprod, b.st);
+  });
+}
+
+template <class Sys, int N>
+__global__ void kb_predictor(const BatchProblem *P, TileQueue q, int per_pop,
+                             Tables T) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_predictor_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st);
+  });
+}
+
+template <class Sys, int N>
+__global__ void kb_newton(const BatchProblem *P, TileQueue q, int per_pop,
+                          Tables T, double tol) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_newton_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st, tol, 0);
+  });
+}
+
+template <class Sys, int N, int FLUX>
+__global__ void __launch_bounds__(128)
+    kb_faces(const BatchProblem *P, TileQueue q, int per_pop, Tables T) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_faces_body<Sys, N, FLUX>(vb, b.qh, b.contrib, b.g, T, b.fi, b.st);
+  });
+}
+
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    kb_centers(const BatchProblem *P, TileQueue q, int per_pop, Tables T) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_centers_body<Sys, N>(vb, b.qh, b.cen, b.g, T, b.st);
+  });
+}
+
+template <class Sys, int N>
+__global__ void __launch_bounds__(256)
+    kb_gather(const BatchProblem *P, TileQueue q, int per_pop, int use_centers,
+              int use_faces) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_gather_body<Sys, N>(vb, b.u, b.cen, b.contrib, b.g, b.fi, use_centers,
+                          use_faces, b.st);
+  });
+}
+
+} // namespace pypde

@@ -143,9 +143,12 @@ struct JitInfo {
 
 std::mutex g_jit_mu;
 
-const char *KERNELS[] = {"k_cfl",     "k_predictor", "k_newton",
-                         "k_faces0",  "k_faces1",    "k_faces2",
-                         "k_centers", "k_gather",    "k_mlp_guess"};
+const char *KERNELS[] = {"k_cfl",       "k_predictor", "k_newton",
+                         "k_faces0",    "k_faces1",    "k_faces2",
+                         "k_centers",   "k_gather",    "k_mlp_guess",
+                         "kb_cfl",      "kb_predictor", "kb_newton",
+                         "kb_faces0",   "kb_faces1",   "kb_faces2",
+                         "kb_centers",  "kb_gather"};
 
 } // namespace
 
@@ -162,8 +165,8 @@ int jit_ensure(SystemDesc &d, int N) {
   }
   std::string dir = lib_dir() + "/csrc/";
   const char *hdrs[] = {"kernels.cuh", "ader_common.cuh", "eig_full.cuh",
-                        "mlp.cuh"};
-  const int nh = 4;
+                        "mlp.cuh", "batch.cuh"};
+  const int nh = 5;
   std::vector<std::string> hsrc(nh);
   for (int i = 0; i < nh; i++)
     if (!read_file(dir + hdrs[i], &hsrc[i])) {
@@ -172,7 +175,7 @@ int jit_ensure(SystemDesc &d, int N) {
     }
   std::string ns = std::to_string(N);
   std::string sh = "pypde::MlpShape<UserSystem, " + ns + ">";
-  std::string prog = "#include \"mlp.cuh\"\n" + ji->src +
+  std::string prog = "#include \"mlp.cuh\"\n#include \"batch.cuh\"\n" + ji->src +
                      "\n__constant__ int pypde_cfg[11] = {"
                      "pypde::PredCfg<UserSystem, " + ns + ">::THREADS, "
                      "pypde::PredCfg<UserSystem, " + ns + ">::CPB, "
@@ -193,7 +196,15 @@ int jit_ensure(SystemDesc &d, int N) {
       "&pypde::k_faces<UserSystem, " + ns + ", 2>",
       "&pypde::k_centers<UserSystem, " + ns + ">",
       "&pypde::k_gather<UserSystem, " + ns + ">",
-      "&pypde::k_mlp_guess<UserSystem, " + ns + ">"};
+      "&pypde::k_mlp_guess<UserSystem, " + ns + ">",
+      "&pypde::kb_cfl<UserSystem, " + ns + ">",
+      "&pypde::kb_predictor<UserSystem, " + ns + ">",
+      "&pypde::kb_newton<UserSystem, " + ns + ">",
+      "&pypde::kb_faces<UserSystem, " + ns + ", 0>",
+      "&pypde::kb_faces<UserSystem, " + ns + ", 1>",
+      "&pypde::kb_faces<UserSystem, " + ns + ", 2>",
+      "&pypde::kb_centers<UserSystem, " + ns + ">",
+      "&pypde::kb_gather<UserSystem, " + ns + ">"};
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17",
                         "--fmad=false", "-lineinfo", "-DPYPDE_JIT=1"};
   const int nopts = 5;
@@ -226,7 +237,7 @@ int jit_ensure(SystemDesc &d, int N) {
   } else {
     nvrtcProgram p;
     const char *hp[nh] = {hsrc[0].c_str(), hsrc[1].c_str(), hsrc[2].c_str(),
-                          hsrc[3].c_str()};
+                          hsrc[3].c_str(), hsrc[4].c_str()};
     if (nv->create(&p, prog.c_str(), "user_system.cu", nh, hp, hdrs) != 0) {
       set_error("nvrtcCreateProgram failed");
       return PYPDE_ERR_COMPILE;
@@ -287,7 +298,11 @@ int jit_ensure(SystemDesc &d, int N) {
                     &d.sets[N].newton,        &d.sets[N].faces_flux[0],
                     &d.sets[N].faces_flux[1], &d.sets[N].faces_flux[2],
                     &d.sets[N].centers,       &d.sets[N].gather,
-                    &d.sets[N].guess};
+                    &d.sets[N].guess,         &d.sets[N].kb_cfl,
+                    &d.sets[N].kb_predictor,  &d.sets[N].kb_newton,
+                    &d.sets[N].kb_faces[0],   &d.sets[N].kb_faces[1],
+                    &d.sets[N].kb_faces[2],   &d.sets[N].kb_centers,
+                    &d.sets[N].kb_gather};
   for (size_t i = 0; i < exprs.size(); i++) {
     void *f = nullptr;
     if (lowered[i].empty() || getfn(&f, mod, lowered[i].c_str()) != 0) {

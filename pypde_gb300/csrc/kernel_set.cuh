@@ -2,6 +2,7 @@
 // SystemDesc; included by the per-system instantiation units.
 #pragma once
 
+#include "batch.cuh"
 #include "runtime.h"
 #include "systems.cuh"
 
@@ -19,6 +20,14 @@ template <class Sys, int N> KernelSet make_kernel_set() {
   k.centers.aot = (const void *)&k_centers<Sys, N>;
   k.gather.aot = (const void *)&k_gather<Sys, N>;
   k.newton.aot = (const void *)&k_newton<Sys, N>;
+  k.kb_cfl.aot = (const void *)&kb_cfl<Sys, N>;
+  k.kb_predictor.aot = (const void *)&kb_predictor<Sys, N>;
+  k.kb_newton.aot = (const void *)&kb_newton<Sys, N>;
+  k.kb_faces[0].aot = (const void *)&kb_faces<Sys, N, 0>;
+  k.kb_faces[1].aot = (const void *)&kb_faces<Sys, N, 1>;
+  k.kb_faces[2].aot = (const void *)&kb_faces<Sys, N, 2>;
+  k.kb_centers.aot = (const void *)&kb_centers<Sys, N>;
+  k.kb_gather.aot = (const void *)&kb_gather<Sys, N>;
   k.newton_threads = NewtonCfg<Sys, N>::THREADS;
   k.newton_cpb = NewtonCfg<Sys, N>::CPB;
   k.newton_smem = NewtonCfg<Sys, N>::SMEM_BYTES;

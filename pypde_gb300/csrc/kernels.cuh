@@ -28,6 +28,12 @@
 
 namespace pypde {
 
+// The block a kernel body works on: the hardware block of a one-problem
+// launch, or one tile of one problem in a batched launch (b of n).
+struct VBlock {
+  long long b, n;
+};
+
 struct DevState {
   double t, dt, tf, cfl;
   double max_speed;  // CFL reduction target (non-negative doubles)
@@ -80,7 +86,7 @@ __device__ __forceinline__ int renorm_index(int ind, int N, int type,
 // values of its 1-D reconstruction.
 // ---------------------------------------------------------------------
 template <int N>
-__global__ void k_weno_pass(const double *__restrict__ in,
+__device__ __forceinline__ void k_weno_pass_body(VBlock vb_, const double *__restrict__ in,
                             double *__restrict__ out, long long n1, int md,
                             long long n3, int n4, int V, Tables T,
                             const DevState *st) {
@@ -90,8 +96,8 @@ __global__ void k_weno_pass(const double *__restrict__ in,
   constexpr int NST = (N > 2) ? ((N % 2 == 0) ? 4 : 3) : 2;
   const int n2 = md - 2 * (N - 1);
   long long total = n1 * n2 * n3 * (long long)n4 * V;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-       e < total; e += (long long)gridDim.x * blockDim.x) {
+  for (long long e = vb_.b * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)vb_.n * blockDim.x) {
     long long r = e;
     int v = (int)(r % V);
     r /= V;
@@ -151,12 +157,19 @@ __global__ void k_weno_pass(const double *__restrict__ in,
   }
 }
 
+template <int N>
+__global__ void k_weno_pass(const double *__restrict__ in,
+                            double *__restrict__ out, long long n1, int md,
+                            long long n3, int n4, int V, Tables T,
+                            const DevState *st) {
+  k_weno_pass_body<N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, in, out, n1, md, n3, n4, V, T, st);
+}
+
 // ---------------------------------------------------------------------
 // a3/a4: CFL reduction, stepper.cpp:35-76.  One thread per w-cell.
 // ---------------------------------------------------------------------
 template <class Sys, int N>
-__global__ void __launch_bounds__(128)
-    k_cfl(const double *__restrict__ w, Geom g, Tables T,
+__device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict__ w, Geom g, Tables T,
           const double *__restrict__ wprod_g, DevState *st) {
   if (!step_active(st))
     return;
@@ -170,8 +183,8 @@ __global__ void __launch_bounds__(128)
     dervals[i] = T.dervals[i];
   __syncthreads();
   double local_max = 0.0;
-  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-       cell < g.Cw; cell += (long long)gridDim.x * blockDim.x) {
+  for (long long cell = vb_.b * (long long)blockDim.x + threadIdx.x;
+       cell < g.Cw; cell += (long long)vb_.n * blockDim.x) {
     const double *w0 = w + cell * Nd * V;
     double q[V], dq[D * V];
 #pragma unroll
@@ -219,6 +232,13 @@ __global__ void __launch_bounds__(128)
     atomic_max_pos(&st->max_speed, local_max);
 }
 
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    k_cfl(const double *__restrict__ w, Geom g, Tables T,
+          const double *__restrict__ wprod_g, DevState *st) {
+  k_cfl_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, g, T, wprod_g, st);
+}
+
 // ---------------------------------------------------------------------
 // a5/a6: space-time DG predictor, Picard form (dg.cpp:50-126, 156-224).
 // A team of NT = N*Nd threads per cell, one per space-time node (t, idx);
@@ -236,7 +256,7 @@ template <class Sys, int N> struct PredCfg {
 };
 
 template <class Sys, int N>
-__global__ void k_predictor(const double *__restrict__ w,
+__device__ __forceinline__ void k_predictor_body(VBlock vb_, const double *__restrict__ w,
                             double *__restrict__ qh, Geom g, Tables T,
                             const double *__restrict__ wprod_g,
                             DevState *st) {
@@ -267,7 +287,7 @@ __global__ void k_predictor(const double *__restrict__ w,
   const int lc = threadIdx.x / NT;   // local cell
   const int node = threadIdx.x % NT; // t * Nd + idx
   const int t = node / Nd, idx = node % Nd;
-  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const long long cell = (long long)vb_.b * CPB + lc;
   const bool valid = (lc < CPB) && (cell < g.Cw);
   int digs[D > 0 ? D : 1];
   {
@@ -423,6 +443,14 @@ __global__ void k_predictor(const double *__restrict__ w,
   }
 }
 
+template <class Sys, int N>
+__global__ void k_predictor(const double *__restrict__ w,
+                            double *__restrict__ qh, Geom g, Tables T,
+                            const double *__restrict__ wprod_g,
+                            DevState *st) {
+  k_predictor_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st);
+}
+
 // ---------------------------------------------------------------------
 // a7: stiff predictor.  Locally implicit Newton iteration on
 // obj(q) = rhs(q) - DG_U q (dg.cpp:128-154): the source is linearised
@@ -460,7 +488,7 @@ template <class Sys, int N> struct NewtonCfg {
 };
 
 template <class Sys, int N>
-__global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
+__device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restrict__ w, double *__restrict__ qh,
                          Geom g, Tables T, const double *__restrict__ wprod_g,
                          DevState *st, double tol, int guess) {
   using Cfg = NewtonCfg<Sys, N>;
@@ -495,7 +523,7 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
   const int lc = threadIdx.x / NT;
   const int node = threadIdx.x % NT;
   const int t = node / Nd, idx = node % Nd;
-  const long long cell = (long long)blockIdx.x * CPB + lc;
+  const long long cell = (long long)vb_.b * CPB + lc;
   const bool valid = (lc < CPB) && (cell < g.Cw);
   int digs[D > 0 ? D : 1];
   {
@@ -800,6 +828,13 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
   }
 }
 
+template <class Sys, int N>
+__global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
+                         Geom g, Tables T, const double *__restrict__ wprod_g,
+                         DevState *st, double tol, int guess) {
+  k_newton_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st, tol, guess);
+}
+
 // ---------------------------------------------------------------------
 // a9/a10/a12: face fluxes (fv.cpp:124-198, fluxes.cpp:72-117).  One
 // thread per face point (direction d, face, time node t, transverse node
@@ -994,17 +1029,16 @@ struct FaceIndex {
   long long nface[3]; // faces per direction
 };
 
-template <class Sys, int N, int FLUX = 0>
-__global__ void __launch_bounds__(128)
-    k_faces(const double *__restrict__ qh, double *__restrict__ contrib,
+template <class Sys, int N, int FLUX>
+__device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restrict__ qh, double *__restrict__ contrib,
             Geom g, Tables T, FaceIndex fi, DevState *st) {
   constexpr int V = Sys::V, D = Sys::NDIM;
   constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
   if (!step_active(st))
     return;
   const double dt = st->dt;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-       p < fi.off[D]; p += (long long)gridDim.x * blockDim.x) {
+  for (long long p = vb_.b * (long long)blockDim.x + threadIdx.x;
+       p < fi.off[D]; p += (long long)vb_.n * blockDim.x) {
     int d = 0;
     while (d + 1 < D && p >= fi.off[d + 1])
       d++;
@@ -1095,12 +1129,19 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+template <class Sys, int N, int FLUX = 0>
+__global__ void __launch_bounds__(128)
+    k_faces(const double *__restrict__ qh, double *__restrict__ contrib,
+            Geom g, Tables T, FaceIndex fi, DevState *st) {
+  k_faces_body<Sys, N, FLUX>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, qh, contrib, g, T, fi, st);
+}
+
 // ---------------------------------------------------------------------
 // a8: centre (volume) terms, fv.cpp:33-85.  One thread per (u-cell,
 // space-time node): dt W_t prod W (S(qh) - sum_d B_d dqh_d).
 // ---------------------------------------------------------------------
 template <class Sys, int N>
-__global__ void k_centers(const double *__restrict__ qh,
+__device__ __forceinline__ void k_centers_body(VBlock vb_, const double *__restrict__ qh,
                           double *__restrict__ cen, Geom g, Tables T,
                           DevState *st) {
   constexpr int V = Sys::V, D = Sys::NDIM;
@@ -1109,8 +1150,8 @@ __global__ void k_centers(const double *__restrict__ qh,
     return;
   const double dt = st->dt;
   long long total = g.C * NT;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-       e < total; e += (long long)gridDim.x * blockDim.x) {
+  for (long long e = vb_.b * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)vb_.n * blockDim.x) {
     long long uc = e / NT;
     int node = (int)(e % NT);
     int t = node / Nd, idx = node % Nd;
@@ -1174,6 +1215,13 @@ __global__ void k_centers(const double *__restrict__ qh,
   }
 }
 
+template <class Sys, int N>
+__global__ void k_centers(const double *__restrict__ qh,
+                          double *__restrict__ cen, Geom g, Tables T,
+                          DevState *st) {
+  k_centers_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, qh, cen, g, T, st);
+}
+
 // ---------------------------------------------------------------------
 // Apply centre and face contributions to u in the order the reference's
 // loops do (fv.cpp:200-207: centres first, then the face loop over the
@@ -1183,7 +1231,7 @@ __global__ void k_centers(const double *__restrict__ qh,
 // One thread per (u-cell, variable).  Also flags NaN (iterator.cpp:141).
 // ---------------------------------------------------------------------
 template <class Sys, int N>
-__global__ void k_gather(double *__restrict__ u, const double *__restrict__ cen,
+__device__ __forceinline__ void k_gather_body(VBlock vb_, double *__restrict__ u, const double *__restrict__ cen,
                          const double *__restrict__ contrib, Geom g,
                          FaceIndex fi, int use_centers, int use_faces,
                          DevState *st) {
@@ -1193,8 +1241,8 @@ __global__ void k_gather(double *__restrict__ u, const double *__restrict__ cen,
     return;
   long long total = g.C * V;
   bool nan_seen = false;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-       e < total; e += (long long)gridDim.x * blockDim.x) {
+  for (long long e = vb_.b * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)vb_.n * blockDim.x) {
     long long uc = e / V;
     int v = (int)(e % V);
     double val = u[e];
@@ -1248,6 +1296,14 @@ __global__ void k_gather(double *__restrict__ u, const double *__restrict__ cen,
   }
   if (__syncthreads_or(nan_seen) && threadIdx.x == 0)
     atomicOr(&st->nan_now, 1);
+}
+
+template <class Sys, int N>
+__global__ void k_gather(double *__restrict__ u, const double *__restrict__ cen,
+                         const double *__restrict__ contrib, Geom g,
+                         FaceIndex fi, int use_centers, int use_faces,
+                         DevState *st) {
+  k_gather_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, u, cen, contrib, g, fi, use_centers, use_faces, st);
 }
 
 } // namespace pypde

@@ -10,6 +10,7 @@
 #include "step_kernels.cuh"
 #include "../../include/pypde_gb300.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <map>
@@ -798,6 +799,522 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
       out->stage_seconds[i] = stage_s[i];
   }
   return rc;
+}
+
+// ------------------------------------------------------------------
+// batched runs: many problems, one launch per stage and order (batch.cuh)
+// ------------------------------------------------------------------
+static const void *kb_weno_kernel(int N) {
+  switch (N) {
+  case 1: return (const void *)&kb_weno<1>;
+  case 2: return (const void *)&kb_weno<2>;
+  case 3: return (const void *)&kb_weno<3>;
+  case 4: return (const void *)&kb_weno<4>;
+  case 5: return (const void *)&kb_weno<5>;
+  case 6: return (const void *)&kb_weno<6>;
+  default: return nullptr;
+  }
+}
+
+// CTAs of a kernel resident per SM (sizes the persistent grids).
+static int resident_blocks(const KFunc &f, int threads, size_t smem) {
+  int n = 0;
+  if (f.aot) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f.aot, threads,
+                                                      smem) != cudaSuccess)
+      n = 1;
+  } else if (f.jit) {
+    typedef int (*occ_t)(int *, void *, int, size_t);
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(
+            "cuOccupancyMaxActiveBlocksPerMultiprocessor", &p, 12000,
+            cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || ((occ_t)p)(&n, f.jit, threads, smem))
+      n = 1;
+  }
+  return n < 1 ? 1 : n;
+}
+
+namespace {
+// Problems of one order, largest first.
+struct BatchGroup {
+  int N = 0;
+  const KernelSet *ks = nullptr;
+  Tables T;
+  std::vector<int> idx;
+  BatchProblem *dP = nullptr; // device, idx.size() entries
+  long long *dOff[BS_COUNT] = {};
+  long long tiles[BS_COUNT] = {};
+  int per_pop[BS_COUNT] = {};
+  KFunc fn[BS_COUNT];
+  int threads[BS_COUNT] = {};
+  size_t smem[BS_COUNT] = {};
+  int resident[BS_COUNT] = {};
+};
+
+struct BatchCtx {
+  std::vector<BatchGroup> G;
+  BatchProblem *dPall = nullptr;
+  int np = 0, ndim = 1, nsm = 152;
+  unsigned long long *heads = nullptr;
+  bool stiff = false, faces = true, centers = true;
+  int flux = 0;
+  double tol = 1e-12;
+};
+} // namespace
+
+// One batched step.  With ev non-null, an event is recorded before and
+// after every (group, stage) launch: ev[(g * BS_COUNT + stage) * 2 + 0/1].
+static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
+                                      cudaEvent_t *ev = nullptr) {
+  cudaError_t e = cudaMemsetAsync(
+      c.heads, 0, sizeof(unsigned long long) * c.G.size() * BS_COUNT, s);
+  if (e != cudaSuccess)
+    return e;
+  const unsigned pb = (unsigned)((c.np + 127) / 128);
+  kb_step_begin<<<pb, 128, 0, s>>>(c.dPall, c.np);
+  auto stage = [&](size_t gi, int st, int extra, void *x0, void *x1,
+                   void *x2) -> cudaError_t {
+    BatchGroup &g = c.G[gi];
+    if (g.tiles[st] == 0)
+      return cudaSuccess;
+    TileQueue q{g.dOff[st], (int)g.idx.size(), c.heads + gi * BS_COUNT + st};
+    int pp = g.per_pop[st] > 0 ? g.per_pop[st] : 1;
+    long long want = (g.tiles[st] + pp - 1) / pp;
+    long long cap = (long long)g.resident[st] * c.nsm;
+    unsigned grid = (unsigned)(want < cap ? want : cap);
+    void *args[8] = {(void *)&g.dP, (void *)&q, (void *)&pp, x0, x1, x2,
+                     nullptr, nullptr};
+    (void)extra;
+    if (ev)
+      cudaEventRecord(ev[(gi * BS_COUNT + st) * 2], s);
+    cudaError_t r = launch(g.fn[st], dim3(grid), dim3(g.threads[st]),
+                           g.smem[st], s, args);
+    if (ev)
+      cudaEventRecord(ev[(gi * BS_COUNT + st) * 2 + 1], s);
+    return r;
+  };
+  for (size_t gi = 0; gi < c.G.size(); gi++) {
+    BatchGroup &g = c.G[gi];
+    if ((e = stage(gi, BS_BOUNDARIES, 0, nullptr, nullptr, nullptr)))
+      return e;
+    for (int d = 0; d < c.ndim; d++) {
+      int dd = d;
+      if ((e = stage(gi, BS_WENO0 + d, 0, (void *)&dd, (void *)&g.T,
+                     nullptr)))
+        return e;
+    }
+    if ((e = stage(gi, BS_CFL, 0, (void *)&g.T, nullptr, nullptr)))
+      return e;
+  }
+  kb_dt<<<pb, 128, 0, s>>>(c.dPall, c.np);
+  for (size_t gi = 0; gi < c.G.size(); gi++) {
+    BatchGroup &g = c.G[gi];
+    double tol = c.tol;
+    if ((e = stage(gi, BS_PREDICTOR, 0, (void *)&g.T,
+                   c.stiff ? (void *)&tol : nullptr, nullptr)))
+      return e;
+    if (c.faces && (e = stage(gi, BS_FACES, 0, (void *)&g.T, nullptr, nullptr)))
+      return e;
+    if (c.centers &&
+        (e = stage(gi, BS_CENTERS, 0, (void *)&g.T, nullptr, nullptr)))
+      return e;
+    int uc = c.centers ? 1 : 0, uf = c.faces ? 1 : 0;
+    if ((e = stage(gi, BS_GATHER, 0, (void *)&uc, (void *)&uf, nullptr)))
+      return e;
+  }
+  kb_step_end<<<pb, 128, 0, s>>>(c.dPall, c.np);
+  return cudaGetLastError();
+}
+
+static int batch_launches_per_step(const BatchCtx &c) {
+  int n = 3;
+  for (auto &g : c.G)
+    for (int st = 0; st < BS_COUNT; st++)
+      if (g.tiles[st] > 0)
+        n++;
+  return n;
+}
+
+int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
+  if (a.np < 1 || !a.probs) {
+    set_error("empty batch");
+    return PYPDE_ERR_ARG;
+  }
+  const int ndim = sys.ndim, V = sys.V;
+  for (int p = 0; p < a.np; p++) {
+    const ProblemSpec &q = a.probs[p];
+    if (!q.u || !(q.tf >= 0) || q.N < 1 || q.N > MAXN) {
+      set_error("batch problem " + std::to_string(p) + ": invalid arguments");
+      return PYPDE_ERR_ARG;
+    }
+    for (int d = 0; d < ndim; d++)
+      if (q.nX[d] < 1 || !(q.dX[d] > 0) || (q.bt[d] != 0 && q.bt[d] != 1)) {
+        set_error("batch problem " + std::to_string(p) + ": invalid grid");
+        return PYPDE_ERR_ARG;
+      }
+    int rc = check_system(sys, ndim, q.N, a.stiff, a.flux);
+    if (!rc)
+      rc = check_grid(ndim, q.nX, q.bt, q.N);
+    if (rc)
+      return rc;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  int rc = arena_for(a.device, &ar);
+  if (rc)
+    return rc;
+  cudaStream_t s = ar->stream;
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, a.device));
+
+  BatchCtx c;
+  c.np = a.np;
+  c.ndim = ndim;
+  c.nsm = prop.multiProcessorCount;
+  c.stiff = a.stiff;
+  c.flux = a.flux;
+  c.tol = a.newton_tol;
+  c.faces = sys.has_F || sys.has_B;
+  c.centers = sys.has_B || sys.has_S;
+
+  // order groups, problems largest first within each
+  std::vector<Geom> geo(a.np);
+  std::vector<FaceIndex> fis(a.np);
+  for (int p = 0; p < a.np; p++) {
+    fill_geom(geo[p], ndim, a.probs[p].nX, a.probs[p].bt, a.probs[p].dX,
+              a.probs[p].N);
+    fis[p] = face_index(geo[p], a.probs[p].N);
+  }
+  for (int N = 1; N <= MAXN; N++) {
+    BatchGroup g;
+    for (int p = 0; p < a.np; p++)
+      if (a.probs[p].N == N)
+        g.idx.push_back(p);
+    if (g.idx.empty())
+      continue;
+    if ((rc = ensure_kernels(sys, N)))
+      return rc;
+    g.N = N;
+    g.ks = &sys.sets[N];
+    if (!g.ks->kb_cfl.valid() || !kb_weno_kernel(N)) {
+      set_error("no batched kernels for system " + sys.name + " at order " +
+                std::to_string(N));
+      return PYPDE_ERR_UNSUPPORTED;
+    }
+    make_tables(N, &g.T);
+    std::stable_sort(g.idx.begin(), g.idx.end(),
+                     [&](int x, int y) { return geo[x].C > geo[y].C; });
+    c.G.push_back(g);
+  }
+
+  // device memory: one region per buffer kind, carved per problem
+  DeviceBuffers mem;
+  std::vector<BatchProblem> hp(a.np);
+  std::vector<size_t> o_u(a.np), o_ub(a.np), o_ta(a.np), o_tb(a.np),
+      o_w(a.np), o_qh(a.np), o_ct(a.np), o_cen(a.np), o_wp(a.np);
+  size_t t_u = 0, t_ub = 0, t_ta = 0, t_tb = 0, t_w = 0, t_qh = 0, t_ct = 0,
+         t_cen = 0, t_wp = 0;
+  auto carve = [](size_t &tot, size_t doubles) {
+    size_t at = tot;
+    tot += (doubles + 31) / 32 * 32; // 256-byte aligned
+    return at;
+  };
+  for (int p = 0; p < a.np; p++) {
+    const int N = a.probs[p].N, Nd = ipow(N, ndim);
+    const Geom &g = geo[p];
+    long long tmpn = weno_tmp_doubles(g.nXb, ndim, N, V);
+    o_u[p] = carve(t_u, g.C * V);
+    o_ub[p] = carve(t_ub, g.Cb * V);
+    o_ta[p] = carve(t_ta, tmpn);
+    o_tb[p] = carve(t_tb, tmpn);
+    o_w[p] = carve(t_w, g.Cw * Nd * V);
+    o_qh[p] = carve(t_qh, g.Cw * N * Nd * V);
+    o_ct[p] = carve(t_ct, c.faces ? fis[p].off[ndim] * 2 * V : 1);
+    o_cen[p] = carve(t_cen, c.centers ? g.C * N * Nd * V : 1);
+    o_wp[p] = carve(t_wp, Nd);
+  }
+  double *b_u, *b_ub, *b_ta, *b_tb, *b_w, *b_qh, *b_ct, *b_cen, *b_wp;
+  DevState *b_st;
+  CK(mem.alloc((void **)&b_u, t_u * 8));
+  CK(mem.alloc((void **)&b_ub, t_ub * 8));
+  CK(mem.alloc((void **)&b_ta, t_ta * 8));
+  CK(mem.alloc((void **)&b_tb, t_tb * 8));
+  CK(mem.alloc((void **)&b_w, t_w * 8));
+  CK(mem.alloc((void **)&b_qh, t_qh * 8));
+  CK(mem.alloc((void **)&b_ct, t_ct * 8));
+  CK(mem.alloc((void **)&b_cen, t_cen * 8));
+  CK(mem.alloc((void **)&b_wp, t_wp * 8));
+  CK(mem.alloc((void **)&b_st, sizeof(DevState) * a.np));
+  CK(mem.alloc((void **)&c.heads,
+               sizeof(unsigned long long) * c.G.size() * BS_COUNT));
+
+  // problem descriptors and tile tables, in group order
+  std::vector<BatchProblem> order;
+  std::vector<DevState> hs(a.np);
+  for (auto &g : c.G) {
+    const int N = g.N, Nd = ipow(N, ndim), NT = N * Nd;
+    const KernelSet &k = *g.ks;
+    std::vector<long long> off[BS_COUNT];
+    for (int st = 0; st < BS_COUNT; st++)
+      off[st].push_back(0);
+    for (int p : g.idx) {
+      const Geom &ge = geo[p];
+      BatchProblem b;
+      b.g = ge;
+      b.fi = fis[p];
+      b.N = N;
+      b.V = V;
+      b.u = b_u + o_u[p];
+      b.ub = b_ub + o_ub[p];
+      b.w = b_w + o_w[p];
+      b.qh = b_qh + o_qh[p];
+      b.contrib = b_ct + o_ct[p];
+      b.cen = b_cen + o_cen[p];
+      b.wprod = b_wp + o_wp[p];
+      b.st = b_st + p;
+      long long tw[3] = {0, 0, 0};
+      int m[3] = {ge.nXb[0], ge.nXb[1], ge.nXb[2]};
+      const double *src = b.ub;
+      int n4 = 1;
+      for (int d = 0; d < ndim; d++) {
+        long long n1 = 1, n3 = 1;
+        for (int e2 = 0; e2 < d; e2++)
+          n1 *= m[e2];
+        for (int e2 = d + 1; e2 < ndim; e2++)
+          n3 *= m[e2];
+        double *dst = (d == ndim - 1)
+                          ? b.w
+                          : ((d % 2 == 0) ? b_ta + o_ta[p] : b_tb + o_tb[p]);
+        b.win[d] = src;
+        b.wout[d] = dst;
+        b.wn1[d] = n1;
+        b.wn3[d] = n3;
+        b.wmd[d] = m[d];
+        b.wn4[d] = n4;
+        tw[d] = n1 * (m[d] - 2 * (N - 1)) * n3 * (long long)n4 * V;
+        src = dst;
+        m[d] -= 2 * (N - 1);
+        n4 *= N;
+      }
+      for (int d = ndim; d < 3; d++) {
+        b.win[d] = nullptr;
+        b.wout[d] = nullptr;
+        b.wn1[d] = b.wn3[d] = 0;
+        b.wmd[d] = b.wn4[d] = 0;
+      }
+      auto tiles = [](long long work, int per) { return (work + per - 1) / per; };
+      long long tl[BS_COUNT] = {};
+      tl[BS_BOUNDARIES] = tiles(ge.Cb * V, 256);
+      for (int d = 0; d < ndim; d++)
+        tl[BS_WENO0 + d] = tiles(tw[d], 128);
+      tl[BS_CFL] = tiles(ge.Cw, 128);
+      tl[BS_PREDICTOR] = tiles(ge.Cw, a.stiff ? k.newton_cpb : k.pred_cpb);
+      tl[BS_FACES] = c.faces ? tiles(fis[p].off[ndim], 128) : 0;
+      tl[BS_CENTERS] = c.centers ? tiles(ge.C * NT, 128) : 0;
+      tl[BS_GATHER] = tiles(ge.C * V, 256);
+      for (int st = 0; st < BS_COUNT; st++)
+        off[st].push_back(off[st].back() + tl[st]);
+      order.push_back(b);
+      DevState d0;
+      std::memset(&d0, 0, sizeof(d0));
+      d0.tf = a.probs[p].tf;
+      d0.cfl = a.probs[p].cfl;
+      d0.max_steps = a.max_steps > 0 ? a.max_steps : -1;
+      d0.ndt = 1;
+      d0.snap_slot = -1;
+      hs[p] = d0;
+    }
+    for (int st = 0; st < BS_COUNT; st++) {
+      g.tiles[st] = off[st].back();
+      CK(mem.alloc((void **)&g.dOff[st], off[st].size() * 8));
+      CK(cudaMemcpyAsync(g.dOff[st], off[st].data(), off[st].size() * 8,
+                         cudaMemcpyHostToDevice, s));
+      g.per_pop[st] = a.per_pop > 0 ? a.per_pop : 1;
+    }
+    g.fn[BS_BOUNDARIES].aot = (const void *)&kb_boundaries;
+    g.threads[BS_BOUNDARIES] = 256;
+    for (int d = 0; d < 3; d++) {
+      g.fn[BS_WENO0 + d].aot = kb_weno_kernel(N);
+      g.threads[BS_WENO0 + d] = 128;
+    }
+    g.fn[BS_CFL] = k.kb_cfl;
+    g.threads[BS_CFL] = 128;
+    if (a.stiff) {
+      g.fn[BS_PREDICTOR] = k.kb_newton;
+      g.threads[BS_PREDICTOR] = k.newton_threads;
+      g.smem[BS_PREDICTOR] = k.newton_smem;
+    } else {
+      g.fn[BS_PREDICTOR] = k.kb_predictor;
+      g.threads[BS_PREDICTOR] = k.pred_threads;
+      g.smem[BS_PREDICTOR] = k.pred_smem;
+    }
+    g.fn[BS_FACES] = k.kb_faces[a.flux];
+    g.threads[BS_FACES] = 128;
+    g.fn[BS_CENTERS] = k.kb_centers;
+    g.threads[BS_CENTERS] = 128;
+    g.fn[BS_GATHER] = k.kb_gather;
+    g.threads[BS_GATHER] = 256;
+    for (int st = 0; st < BS_COUNT; st++) {
+      if (g.tiles[st] == 0)
+        continue;
+      CK(set_smem(g.fn[st], g.smem[st]));
+      g.resident[st] = resident_blocks(g.fn[st], g.threads[st], g.smem[st]);
+    }
+  }
+  CK(mem.alloc((void **)&c.dPall, sizeof(BatchProblem) * order.size()));
+  CK(cudaMemcpyAsync(c.dPall, order.data(), sizeof(BatchProblem) * order.size(),
+                     cudaMemcpyHostToDevice, s));
+  {
+    size_t at = 0;
+    for (auto &g : c.G) {
+      g.dP = c.dPall + at;
+      at += g.idx.size();
+    }
+  }
+  // the problems' DevStates sit at b_st + p: upload, then states and u
+  CK(cudaMemcpyAsync(b_st, hs.data(), sizeof(DevState) * a.np,
+                     cudaMemcpyHostToDevice, s));
+  for (int p = 0; p < a.np; p++) {
+    const int Nd = ipow(a.probs[p].N, ndim);
+    std::vector<double> wp(Nd);
+    Tables T;
+    make_tables(a.probs[p].N, &T);
+    make_wprod(T, ndim, wp.data());
+    CK(cudaMemcpyAsync(b_wp + o_wp[p], wp.data(), Nd * 8,
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b_u + o_u[p], a.probs[p].u, geo[p].C * V * 8,
+                       cudaMemcpyHostToDevice, s));
+  }
+  std::vector<DevState> host(a.np);
+  auto all_done = [&]() -> cudaError_t {
+    cudaError_t e2 = cudaMemcpyAsync(host.data(), b_st,
+                                     sizeof(DevState) * a.np,
+                                     cudaMemcpyDeviceToHost, s);
+    if (e2 == cudaSuccess)
+      e2 = cudaStreamSynchronize(s);
+    return e2;
+  };
+  auto finished = [&]() {
+    for (int p = 0; p < a.np; p++) {
+      const DevState &h = host[p];
+      if (h.t < h.tf && (h.max_steps < 0 || h.count < h.max_steps) &&
+          !h.nan_found)
+        return false;
+    }
+    return true;
+  };
+
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, s));
+  long long launches = 0;
+  double tune_s = 0;
+  CK(all_done());
+  // autotune: the first steps run eagerly, one tile shape per step, each
+  // (group, stage) launch timed; the fastest shape per launch is kept
+  if (a.autotune && !finished()) {
+    const int cand[4] = {1, 2, 4, 8};
+    const size_t nev = c.G.size() * BS_COUNT * 2;
+    std::vector<cudaEvent_t> ev(nev);
+    for (auto &x : ev)
+      CK(cudaEventCreate(&x));
+    std::vector<float> best(c.G.size() * BS_COUNT, 1e30f);
+    std::vector<int> pick(c.G.size() * BS_COUNT, 1);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int ci = 0; ci < 4 && !finished(); ci++) {
+      for (auto &g : c.G)
+        for (int st = 0; st < BS_COUNT; st++)
+          g.per_pop[st] = cand[ci];
+      CK(enqueue_batch_step(c, s, ev.data()));
+      launches += batch_launches_per_step(c);
+      CK(all_done());
+      for (size_t gi = 0; gi < c.G.size(); gi++)
+        for (int st = 0; st < BS_COUNT; st++) {
+          if (c.G[gi].tiles[st] == 0)
+            continue;
+          float ms = 0;
+          if (cudaEventElapsedTime(&ms, ev[(gi * BS_COUNT + st) * 2],
+                                   ev[(gi * BS_COUNT + st) * 2 + 1]) ==
+                  cudaSuccess &&
+              ms < best[gi * BS_COUNT + st]) {
+            best[gi * BS_COUNT + st] = ms;
+            pick[gi * BS_COUNT + st] = cand[ci];
+          }
+        }
+    }
+    for (size_t gi = 0; gi < c.G.size(); gi++)
+      for (int st = 0; st < BS_COUNT; st++)
+        c.G[gi].per_pop[st] = pick[gi * BS_COUNT + st];
+    for (auto &x : ev)
+      cudaEventDestroy(x);
+    tune_s = std::chrono::duration<double>(std::chrono::steady_clock::now() -
+                                           t0)
+                 .count();
+  }
+  int K = a.steps_per_graph > 0 ? a.steps_per_graph : 8;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (!finished()) {
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaSuccess;
+    for (int k = 0; k < K && ce == cudaSuccess; k++)
+      ce = enqueue_batch_step(c, s);
+    cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) {
+      if (graph)
+        cudaGraphDestroy(graph);
+      set_error(std::string("enqueue batched step: ") + cudaGetErrorString(ce));
+      return PYPDE_ERR_CUDA;
+    }
+    CK(ee);
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+    while (!finished()) {
+      CK(cudaGraphLaunch(exec, s));
+      launches += (long long)K * batch_launches_per_step(c);
+      CK(all_done());
+    }
+  }
+  CK(cudaEventRecord(e1, s));
+  for (int p = 0; p < a.np; p++)
+    CK(cudaMemcpyAsync(a.probs[p].u, b_u + o_u[p], geo[p].C * V * 8,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (exec)
+    cudaGraphExecDestroy(exec);
+  if (graph)
+    cudaGraphDestroy(graph);
+  if (out) {
+    out->steps = 0;
+    out->max_problem_steps = 0;
+    out->pred_iters = 0;
+    out->nan_found = 0;
+    for (int p = 0; p < a.np; p++) {
+      out->steps += host[p].count;
+      out->max_problem_steps = std::max(out->max_problem_steps, host[p].count);
+      out->pred_iters += host[p].pred_iters;
+      out->nan_found += host[p].nan_found ? 1 : 0;
+      if (out->steps_per_problem)
+        out->steps_per_problem[p] = host[p].count;
+      if (out->t_per_problem)
+        out->t_per_problem[p] = host[p].t;
+    }
+    out->device_seconds = ms * 1e-3;
+    out->kernel_launches = launches;
+    out->tune_seconds = tune_s;
+    for (int st = 0; st < BS_COUNT; st++)
+      out->per_pop[st] = c.G.empty() ? 0 : c.G[0].per_pop[st];
+  }
+  int nan_any = 0;
+  for (int p = 0; p < a.np; p++)
+    nan_any |= host[p].nan_found;
+  return nan_any ? PYPDE_NAN_FOUND : PYPDE_OK;
 }
 
 // ------------------------------------------------------------------

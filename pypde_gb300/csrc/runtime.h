@@ -2,6 +2,7 @@
 // (system, order), the step driver and the stage launchers.
 #pragma once
 
+#include "batch.cuh"
 #include "mlp.cuh"
 
 #include <cuda_runtime.h>
@@ -28,6 +29,8 @@ struct KernelSet {
   size_t pred_smem = 0;
   int newton_threads = 0, newton_cpb = 0;
   size_t newton_smem = 0;
+  // batched launches over many problems of this order (batch.cuh)
+  KFunc kb_cfl, kb_predictor, kb_newton, kb_faces[3], kb_centers, kb_gather;
   // learned warm start (k_mlp_guess); guess_k1 == 0: not available
   KFunc guess;
   size_t guess_smem = 0;
@@ -119,6 +122,58 @@ void set_error(const std::string &msg);
 const char *last_error();
 
 int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *st);
+
+// One problem of a batched run.
+struct ProblemSpec {
+  double *u = nullptr; // host, in/out, prod(nX) x V
+  double tf = 0;
+  int nX[3] = {1, 1, 1};
+  double dX[3] = {1, 1, 1};
+  int bt[3] = {0, 0, 0};
+  int N = 2;
+  double cfl = 0.9;
+};
+
+// Stages of a batched step whose tile shape the autotuner picks.
+enum BatchStage {
+  BS_BOUNDARIES = 0,
+  BS_WENO0,
+  BS_WENO1,
+  BS_WENO2,
+  BS_CFL,
+  BS_PREDICTOR,
+  BS_FACES,
+  BS_CENTERS,
+  BS_GATHER,
+  BS_COUNT
+};
+
+struct BatchArgs {
+  int np = 0;
+  ProblemSpec *probs = nullptr;
+  bool stiff = false;
+  int flux = 0;
+  double newton_tol = 1e-12;
+  int device = 0;
+  int steps_per_graph = 0;
+  long long max_steps = -1; // per problem
+  bool autotune = true;
+  int per_pop = 1; // tiles per queue pop when not autotuning
+};
+
+struct BatchStats {
+  long long steps = 0, max_problem_steps = 0;
+  double device_seconds = 0;
+  long long kernel_launches = 0;
+  unsigned long long pred_iters = 0;
+  int nan_found = 0;
+  int per_pop[BS_COUNT] = {};  // chosen tile shape per stage (order group 0)
+  double tune_seconds = 0;
+  long long *steps_per_problem = nullptr; // optional outputs, np each
+  double *t_per_problem = nullptr;
+};
+
+int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *st);
 int stage_boundaries(const double *u, const int *nX, int ndim, const int *bt,
                      int N, int V, double *ub);
 int stage_weno(const double *ub, const int *nXb, int ndim, int N, int V,

@@ -2,18 +2,18 @@
 // ghost fill, dt and the step bookkeeping.  Included by runtime.cu only.
 #pragma once
 
-#include "kernels.cuh"
+#include "batch.cuh"
 
 namespace pypde {
 
-__global__ void k_boundaries(const double *__restrict__ u,
+__device__ __forceinline__ void k_boundaries_body(VBlock vb_, const double *__restrict__ u,
                              double *__restrict__ ub, Geom g, int N, int V,
                              const DevState *st) {
   if (!step_active(st))
     return;
   long long total = g.Cb * V;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-       e < total; e += (long long)gridDim.x * blockDim.x) {
+  for (long long e = vb_.b * (long long)blockDim.x + threadIdx.x;
+       e < total; e += (long long)vb_.n * blockDim.x) {
     long long idx = e / V;
     int v = (int)(e - idx * V);
     long long rem = idx, src = 0, mul = 1;
@@ -27,8 +27,14 @@ __global__ void k_boundaries(const double *__restrict__ u,
   }
 }
 
+__global__ void k_boundaries(const double *__restrict__ u,
+                             double *__restrict__ ub, Geom g, int N, int V,
+                             const DevState *st) {
+  k_boundaries_body(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, u, ub, g, N, V, st);
+}
+
 // dt from the reduced maximum (stepper.cpp:67-75)
-__global__ void k_dt(DevState *st) {
+__device__ __forceinline__ void dt_dev(DevState *st) {
   if (!step_active(st))
     return;
   double dt = st->cfl / st->max_speed;
@@ -38,11 +44,12 @@ __global__ void k_dt(DevState *st) {
     dt = st->tf - st->t;
   st->dt = dt;
 }
+__global__ void k_dt(DevState *st) { dt_dev(st); }
 
 // ---------------------------------------------------------------------
 // Step bookkeeping (iterator.cpp:99-148).
 // ---------------------------------------------------------------------
-__global__ void k_step_begin(DevState *st) {
+__device__ __forceinline__ void step_begin_dev(DevState *st) {
   st->active = (st->t < st->tf) &&
                (st->max_steps < 0 || st->count < st->max_steps) &&
                !st->nan_found;
@@ -50,11 +57,12 @@ __global__ void k_step_begin(DevState *st) {
   st->snap_slot = -1;
   st->nan_now = 0;
 }
+__global__ void k_step_begin(DevState *st) { step_begin_dev(st); }
 
 // t += dt, count += 1, and the snapshot decision of iterator.cpp:136-139.
 // Snapshots go to a ring of device slots the host drains between graph
 // launches: slot = push % ring.
-__global__ void k_step_end(DevState *st, int ring) {
+__device__ __forceinline__ void step_end_dev(DevState *st, int ring) {
   if (!step_active(st))
     return;
   st->t += st->dt;
@@ -66,6 +74,33 @@ __global__ void k_step_end(DevState *st, int ring) {
   }
   if (st->nan_now)
     st->nan_found = 1;
+}
+__global__ void k_step_end(DevState *st, int ring) { step_end_dev(st, ring); }
+
+// Batched bookkeeping: one thread per problem.
+__global__ void kb_step_begin(const BatchProblem *P, int np) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < np)
+    step_begin_dev(P[p].st);
+}
+__global__ void kb_dt(const BatchProblem *P, int np) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < np)
+    dt_dev(P[p].st);
+}
+__global__ void kb_step_end(const BatchProblem *P, int np) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < np)
+    step_end_dev(P[p].st, 1);
+}
+
+// Batched ghost fill (256 threads per tile).
+__global__ void __launch_bounds__(256)
+    kb_boundaries(const BatchProblem *P, TileQueue q, int per_pop) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    k_boundaries_body(vb, b.u, b.ub, b.g, b.N, b.V, b.st);
+  });
 }
 
 // Keep the state of the previous step (the NaN rows of iterator.cpp:141-145).

@@ -14,6 +14,8 @@ Differences from the reference, all at the callback boundary:
     ``warm_start`` (a pypde_gb300.warmstart.WarmStart: learned initial guess
     of the stiff predictor's Newton iteration).
 """
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -76,6 +78,63 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
 
 # The name used by the GB300 build's documentation; same function.
 ader_solver = pde_solver
+
+
+def pde_solver_batch(problems, F=None, B=None, S=None, stiff=True, flux="rusanov", *,
+                     max_steps=None, newton_tol=None, device=0, autotune=True, per_pop=1,
+                     stats=None, jit=False):
+    """Step many independent problems of one system together (one persistent
+    launch per stage and order, see include/pypde_gb300.h).
+
+    problems: a list of dicts with keys Q0 (float64 array (n_1..n_d, V),
+    overwritten with the final state, like pde_solver), tf, L, and optional
+    order (2), boundaryTypes ('transitive'), cfl (0.9).  All problems share
+    F, B, S; sizes, orders, boundary types and end times may differ.
+    Returns the list of final states (the Q0 arrays).  stats (a dict) gets
+    the batch statistics plus per-problem 'steps' and 't_final' lists."""
+    if not problems:
+        raise ValueError("no problems")
+    Q0s = [p["Q0"] for p in problems]
+    ndim = Q0s[0].ndim - 1
+    V = Q0s[0].shape[-1]
+    for q in Q0s:
+        if q.dtype != np.float64 or not q.flags.c_contiguous:
+            raise TypeError("Q0 must be a C-contiguous float64 array")
+        if q.ndim - 1 != ndim or q.shape[-1] != V:
+            raise ValueError("all problems need the same ndim and V")
+    secondOrder = F is not None and nargs(F) == 3
+    system = resolve_system(F, B, S, ndim, V, secondOrder, jit=jit)
+    arr = (_lib.BatchProblem * len(problems))()
+    for i, p in enumerate(problems):
+        q = Q0s[i]
+        nX = q.shape[:-1]
+        L = p["L"]
+        bt = parse_boundary_types(p.get("boundaryTypes", "transitive"), ndim)
+        arr[i].u = _lib.c_ptr(q.reshape(-1))
+        arr[i].tf = float(p["tf"])
+        arr[i].N = int(p.get("order", 2))
+        arr[i].cfl = float(p.get("cfl", 0.9))
+        for d in range(ndim):
+            arr[i].nX[d] = int(nX[d])
+            arr[i].dX[d] = float(L[d]) / nX[d]
+            arr[i].boundaryTypes[d] = int(bt[d])
+    opt = _lib.BatchOptions()
+    opt.max_steps = int(max_steps) if max_steps else -1
+    opt.newton_tol = float(newton_tol) if newton_tol else 0.0
+    opt.device = int(device)
+    opt.autotune = int(bool(autotune))
+    opt.per_pop = int(per_pop)
+    st = _lib.BatchStats()
+    steps = (ctypes.c_longlong * len(problems))()
+    tout = np.zeros(len(problems))
+    code = _lib.lib().pde_solver_batch(system.handle, bool(stiff), FLUXES[flux], len(problems),
+                                       arr, opt, st, steps, _lib.c_ptr(tout))
+    _lib.check(code)
+    if stats is not None:
+        stats.update(st.as_dict())
+        stats["steps_per_problem"] = list(steps)
+        stats["t_final"] = tout.tolist()
+    return Q0s
 
 
 def weno_solver(u, order=2):

@@ -99,3 +99,36 @@ def random_state(system, shape, seed=0):
     if system == "burgers2":
         return 0.5 + 0.3 * rng.standard_normal(tuple(shape) + (1,))
     raise ValueError(system)
+
+
+def batched(nprob=256, seed=0, side=(64, 512), orders=(1, 2, 3), log10_tau=(-6.0, -2.0),
+            tf=0.1, cfl=0.8):
+    """Uneven batch of 2-D Euler + relaxing heat flux problems (7 vars):
+    side floor(64 8^U) (log-uniform in [64, 512]), order N from `orders`,
+    one log10 tau ~ U(-6, -2) per problem, rho = 1 + 0.1 f, p = 1 + 0.1 g
+    with f, g sums of 4 seeded Fourier modes, zero velocity and heat flux,
+    periodic, each to its own tf.  Returns pde_solver_batch problem dicts."""
+    rng = np.random.default_rng(seed)
+    lo, hi = side
+    out = []
+    for _ in range(nprob):
+        n = int(lo * (hi / lo) ** rng.uniform())
+        N = int(rng.choice(orders))
+        x = (np.arange(n) + 0.5) / n
+        X, Y = np.meshgrid(x, x, indexing="ij")
+        f = np.zeros((n, n))
+        g = np.zeros((n, n))
+        for acc in (f, g):
+            for _ in range(4):
+                kx, ky = rng.integers(1, 5, 2)
+                acc += rng.uniform(-0.5, 0.5) * np.sin(2 * np.pi * (kx * X + ky * Y)
+                                                        + rng.uniform(0, 2 * np.pi))
+        rho = 1 + 0.1 * f
+        p = 1 + 0.1 * g
+        u = np.zeros((n, n, 7))
+        u[..., 0] = rho
+        u[..., 3] = _energy(rho, p, 0.0)
+        u[..., 6] = rng.uniform(*log10_tau)
+        out.append({"Q0": u, "tf": tf, "L": [1.0, 1.0], "order": N,
+                    "boundaryTypes": "periodic", "cfl": cfl})
+    return out
