@@ -6,10 +6,12 @@ Default workload (--workload stiff): 2-D Euler + relaxing heat flux
 Newton predictor to ||obj||_inf <= 1e-12, tau piecewise constant on 16x16
 patches with log10 tau ~ U(-7,-2) (pypde_gb300.workloads.relaxation, seeded
 synthetic data).  Forms measured on the same K steps from the same state:
-  plain    Newton from the plain guess q = w
-  learned  Newton from the learned warm start (network trained here on 20
-           harvested plain steps with the library's own kernels; training
-           time reported, not timed in `value`)
+  plain          Newton from the plain guess q = w
+  learned        Newton from the learned warm start (network trained here on
+                 20 harvested plain steps with the library's own kernels;
+                 training time reported, not timed in `value`)
+  mixed          FP32 Newton sweeps, then >= 2 FP64 sweeps to the same 1e-12
+  learned_mixed  both
 `value` is the learned form (the metric's "learned" form); `forms` gives
 both, each with its Newton iterations and its relative L1 error per
 variable against an oracle run at Newton tolerance 1e-15 (the GPU plain path
@@ -75,6 +77,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--batch-problems", type=int, default=256,
+                   help="problems of the batched section (0: skip it)")
+    p.add_argument("--batch-steps", type=int, default=6)
     a = p.parse_args()
     system, n, N, cfl, stiff = WORKLOADS[a.workload]
     a.system, a.cfl, a.stiff = system, cfl, stiff
@@ -217,9 +222,10 @@ class Runner:
         self.dX = np.array([1.0 / args.n, 1.0 / args.n])
         self.bt = np.array([1, 1], dtype=np.int32)
 
-    def run(self, u, steps, profile=False, warm=None, tol=0.0):
+    def run(self, u, steps, profile=False, warm=None, tol=0.0, mixed=False):
         _lib, a = self._lib, self.args
         opt = _lib.Options()
+        opt.mixed_precision = int(mixed)
         opt.max_steps = steps
         opt.device = self.local
         opt.profile_stages = int(profile)
@@ -235,18 +241,60 @@ class Runner:
         return st.as_dict()
 
 
-def measure_form(R, args, ws, u0, warm=None):
+def measure_form(R, args, ws, u0, warm=None, mixed=False):
     """W warm-up steps, then exactly K timed steps (CUDA events inside the
     library), then an eagerly launched profile of min(K, 5) steps."""
     u = u0.copy()
-    R.run(u, args.warmup, warm=warm)
+    R.run(u, args.warmup, warm=warm, mixed=mixed)
     barrier(ws)
-    st = R.run(u, args.steps, warm=warm)
+    st = R.run(u, args.steps, warm=warm, mixed=mixed)
     barrier(ws)
     sec = allmax(ws, st["device_seconds"])
     ksteps = max(1, min(args.steps, 5))
-    sp = R.run(u0.copy(), ksteps, profile=True, warm=warm)
+    sp = R.run(u0.copy(), ksteps, profile=True, warm=warm, mixed=mixed)
     return st, sec, sp, ksteps
+
+
+def run_batched(args, local):
+    """Uneven batch (256 problems, side log-uniform in [64, 512], order in
+    {1, 2, 3}, 2-D Euler + relaxation, stiff Newton): one pde_solver_batch
+    call against the same problems solved one after the other, both for
+    the same number of steps per problem (the autotuner's 4 timed steps
+    included in the batched time)."""
+    from pypde_gb300 import systems, workloads
+    from pypde_gb300.solvers import pde_solver, pde_solver_batch
+    s = systems.cattaneo(2)
+    K = args.batch_steps
+    probs = workloads.batched(args.batch_problems, seed=0)
+    for N in (1, 2, 3):  # load the kernels before timing
+        q = np.ascontiguousarray(workloads.relaxation(16, 2))
+        pde_solver(q, 1.0, [1, 1], F=s.F, S=s.S, boundaryTypes="periodic", order=N,
+                   stiff=True, max_steps=2, device=local)
+    b = [dict(p, Q0=p["Q0"].copy()) for p in probs]
+    st = {}
+    pde_solver_batch(b, F=s.F, S=s.S, stiff=True, max_steps=K, stats=st, device=local)
+    upd = sum(p["Q0"].shape[0] * p["Q0"].shape[1] * k
+              for p, k in zip(probs, st["steps_per_problem"]))
+    seq = 0.0
+    same = True
+    for p, pb in zip(probs, b):
+        q = p["Q0"].copy()
+        s1 = {}
+        pde_solver(q, p["tf"], p["L"], F=s.F, S=s.S, boundaryTypes="periodic", cfl=p["cfl"],
+                   order=p["order"], stiff=True, max_steps=K, stats=s1, device=local)
+        seq += s1["device_seconds"]
+        same &= bool(np.array_equal(q, pb["Q0"]))
+    orders = np.bincount([p["order"] for p in probs], minlength=4)[1:].tolist()
+    return {"problems": len(probs), "orders_1_2_3": orders,
+            "cells": int(sum(p["Q0"].shape[0] * p["Q0"].shape[1] for p in probs)),
+            "steps_per_problem": K, "cell_updates": int(upd),
+            "batched": {"value": upd / st["device_seconds"], "unit": UNIT,
+                        "seconds": st["device_seconds"], "tune_seconds": st["tune_seconds"],
+                        "kernel_launches": st["kernel_launches"],
+                        "tiles_per_pop": st["per_pop"]},
+            "sequential": {"value": upd / seq, "unit": UNIT, "seconds": seq},
+            "batched_over_sequential": seq / st["device_seconds"],
+            "bit_identical_to_sequential": same}
 
 
 def run_ours(args, ws, rank, local):
@@ -281,6 +329,8 @@ def run_ours(args, ws, rank, local):
     forms[head] = (st_h, sec, sp, ksteps)
     if args.stiff:
         forms["plain"] = measure_form(R, args, ws, u0, None)
+        forms["mixed"] = measure_form(R, args, ws, u0, None, mixed=True)
+        forms["learned_mixed"] = measure_form(R, args, ws, u0, warm, mixed=True)
     value = ws * C * args.steps / sec
 
     # relative L1 per variable after K steps from u0, against a tolerance
@@ -289,9 +339,10 @@ def run_ours(args, ws, rank, local):
     if args.stiff:
         q_o = u0.copy()
         R.run(q_o, args.steps, tol=1e-15)
-        for name, w in (("plain", None), ("learned", warm)):
+        for name, w, mx in (("plain", None, False), ("learned", warm, False),
+                            ("mixed", None, True), ("learned_mixed", warm, True)):
             q = u0.copy()
-            R.run(q, args.steps, warm=w)
+            R.run(q, args.steps, warm=w, mixed=mx)
             errs[name] = [float(x) for x in l1(q, q_o)]
 
     def form_summary(name):
@@ -302,6 +353,7 @@ def run_ours(args, ws, rank, local):
              "stage_ms_per_step": {k: 1e3 * v / ks for k, v in sp_f["stage_seconds"].items()}}
         if args.stiff:
             d["newton_fallbacks"] = st["pred_fallbacks"]
+            d["fp32_sweeps_per_cell"] = st["pred_iters32"] / (args.steps * (n + 2) ** 2)
             d["l1_vs_oracle"] = errs[name]
         return d
 
@@ -360,6 +412,8 @@ def run_ours(args, ws, rank, local):
     }
     if train:
         out["training"] = train
+    if args.stiff and args.batch_problems > 0:
+        out["batched_workload"] = run_batched(args, local)
     if rank == 0 and not args.no_cpu:
         v, cores, sample = cpu_baseline(args, u0, args.cpu_seconds)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -51,6 +51,9 @@ typedef struct {
                             events (fills pypde_stats.stage_seconds) */
   const pypde_warm_start *warm_start; /* stiff form: learned initial guess of
                             the Newton predictor (NULL: plain guess) */
+  int mixed_precision;   /* stiff form: Newton sweeps in FP32 first, then at
+                            least two FP64 sweeps to the same tolerance
+                            (systems with FP32 callbacks only) */
 } pypde_options;
 
 /* Stages timed by pypde_options.profile_stages, in this order. */
@@ -76,6 +79,7 @@ typedef struct {
   double stage_seconds[8];         /* per stage, with profile_stages */
   unsigned long long pred_fallbacks; /* warm-started cells that fell back to
                                       the plain guess */
+  unsigned long long pred_iters32;   /* FP32 Newton sweeps, summed over cells */
 } pypde_stats;
 
 /* ---------------- callback systems ---------------- */
@@ -202,9 +206,11 @@ typedef struct {
   double newton_tol;     /* stiff form; 0 -> 1e-12 */
   int device;
   int steps_per_graph;   /* 0 -> 8 */
-  int autotune;          /* 1: the first steps try tiles-per-pop 1,2,4,8 per
-                            stage and keep the fastest */
-  int per_pop;           /* tiles per queue pop without autotune (0 -> 1) */
+  int autotune;          /* 1: the first five steps try, per stage, one block
+                            per tile (0) and tiles-per-pop 1, 2, 4, 8 of the
+                            persistent queue, and keep the fastest */
+  int per_pop;           /* without autotune: tiles per queue pop, 0 = one
+                            block per tile */
 } pypde_batch_options;
 
 #define PYPDE_BATCH_STAGES 9 /* ghost, WENO x3, CFL, predictor, faces,

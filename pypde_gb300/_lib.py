@@ -23,7 +23,7 @@ PYPDE_ERR_COMPILE = 5
 class Options(Structure):
     _fields_ = [("max_steps", c_longlong), ("newton_tol", c_double),
                 ("device", c_int), ("steps_per_graph", c_int), ("profile_stages", c_int),
-                ("warm_start", c_void_p)]
+                ("warm_start", c_void_p), ("mixed_precision", c_int)]
 
 STAGES = ("boundaries", "weno", "cfl", "predictor", "faces", "centers", "gather", "other")
 
@@ -33,7 +33,8 @@ class Stats(Structure):
                 ("pred_iters", c_ulonglong), ("pred_max_iters", c_int),
                 ("pred_fail", c_int), ("nan_found", c_int),
                 ("device_seconds", c_double), ("kernel_launches", c_longlong),
-                ("stage_seconds", c_double * 8), ("pred_fallbacks", c_ulonglong)]
+                ("stage_seconds", c_double * 8), ("pred_fallbacks", c_ulonglong),
+                ("pred_iters32", c_ulonglong)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_seconds"}

@@ -152,6 +152,17 @@ int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
       }
       a.warm = w->ws;
     }
+    a.mixed = opt->mixed_precision != 0;
+  }
+  if (a.mixed) {
+    if (!STIFF) {
+      set_error("mixed_precision applies to the stiff (Newton) predictor");
+      return PYPDE_ERR_ARG;
+    }
+    if (sys->desc->module) {
+      set_error("mixed_precision needs FP32 callbacks: built-in systems only");
+      return PYPDE_ERR_UNSUPPORTED;
+    }
   }
   return run_ex(sys, a, stats);
 }
@@ -172,6 +183,7 @@ static int run_ex(const pypde_system *sys, const RunArgs &a,
     for (int i = 0; i < 8; i++)
       stats->stage_seconds[i] = st.stage_seconds[i];
     stats->pred_fallbacks = st.pred_fallbacks;
+    stats->pred_iters32 = st.pred_iters32;
   }
   return rc;
 }
@@ -278,7 +290,7 @@ int pde_solver_batch(const pypde_system *sys, bool STIFF, int FLUX, int nprob,
     a.device = opt->device;
     a.steps_per_graph = opt->steps_per_graph;
     a.autotune = opt->autotune != 0;
-    a.per_pop = opt->per_pop > 0 ? opt->per_pop : 1;
+    a.per_pop = opt->per_pop >= 0 ? opt->per_pop : 1;
   }
   BatchStats st;
   st.steps_per_problem = steps_out;

@@ -5,8 +5,8 @@
 // whose CTAs drain a work queue of tiles, tile = one block of the stage's
 // one-problem launch (a VBlock of that problem), problems listed largest
 // first so that the queue hands out the long work first.  A CTA pops
-// `per_pop` consecutive tiles at a time (the tile shape the autotuner
-// picks).  The per-tile work is the one-problem kernels' bodies, unchanged,
+// `per_pop` consecutive tiles at a time; per_pop = 0 launches one hardware
+// block per tile instead of the queue (the autotuner picks per stage).  The per-tile work is the one-problem kernels' bodies, unchanged,
 // so a batched step gives the same bits as the same problem stepped alone.
 // Not in the reference (one grid per pde_solver call).
 #pragma once
@@ -37,11 +37,33 @@ struct TileQueue {
   unsigned long long *head;
 };
 
+// The problem owning tile t (binary search over the tile offsets).
+__device__ __forceinline__ int tile_problem(const TileQueue &q, long long t) {
+  int lo = 0, hi = q.np;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (q.off[mid] <= t)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 // Pop per_pop tiles at a time until the queue is empty; body(p, vb) runs
-// one tile of problem p with the whole CTA.
+// one tile of problem p with the whole CTA.  per_pop = 0: no queue, one
+// hardware block per tile (the grid is the tile count).
 template <class Body>
 __device__ __forceinline__ void drain(const TileQueue &q, int per_pop,
                                       Body body) {
+  if (per_pop == 0) {
+    const long long t = blockIdx.x;
+    if (t < q.off[q.np]) {
+      const int p = tile_problem(q, t);
+      body(p, VBlock{t - q.off[p], q.off[p + 1] - q.off[p]});
+    }
+    return;
+  }
   __shared__ long long s_tile;
   const long long total = q.off[q.np];
   for (;;) {
@@ -53,15 +75,8 @@ __device__ __forceinline__ void drain(const TileQueue &q, int per_pop,
     if (t0 >= total)
       break;
     for (long long t = t0; t < t0 + per_pop && t < total; t++) {
-      int lo = 0, hi = q.np;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (q.off[mid] <= t)
-          lo = mid;
-        else
-          hi = mid;
-      }
-      body(lo, VBlock{t - q.off[lo], q.off[lo + 1] - q.off[lo]});
+      const int p = tile_problem(q, t);
+      body(p, VBlock{t - q.off[p], q.off[p + 1] - q.off[p]});
       __syncthreads();
     }
   }
@@ -100,7 +115,7 @@ __global__ void kb_newton(const BatchProblem *P, TileQueue q, int per_pop,
                           Tables T, double tol) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
-    k_newton_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st, tol, 0);
+    k_newton_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st, tol, 0, 0);
   });
 }
 

@@ -49,6 +49,7 @@ struct DevState {
   int pred_max_iters;
   int pred_fail;     // cells whose Newton iteration hit its cap
   unsigned long long pred_fallbacks; // warm-started cells reset to the plain guess
+  unsigned long long pred_iters32;   // FP32 sweeps (mixed-precision form)
 };
 
 // Geometry of one problem, passed by value.
@@ -487,10 +488,294 @@ template <class Sys, int N> struct NewtonCfg {
   static constexpr size_t SMEM_BYTES = (size_t)CPB * CELL_BYTES;
 };
 
+// FP32 sweeps of the mixed-precision stiff predictor: the simplified
+// Newton iteration of k_newton with every quantity in FP32 -- callbacks
+// instantiated with float, the FD step sqrt(eps_32) max(|q|, 1), the LU in
+// FP32 and built once -- started from the cell's q and written back into
+// it.  A cell stops at its FP32 rounding floor (residual <= 64 eps_32
+// scale), at tol, when the residual falls by less than half in a sweep, on
+// a zero pivot, or after NEWTON32_MAXIT sweeps.  Shared scratch: q32 and r32
+// in s_r, fluxes in s_f, the LU in s_A (the FP64 loop rebuilds all three).
+// Returns this thread's cell's sweep count.
+constexpr int NEWTON32_MAXIT = 8;
+
+template <class Sys, int N>
+__device__ __forceinline__ int newton_fp32_sweeps(
+    double *s_q, double *s_r, double *s_f, double *s_A, int *s_piv,
+    const double *Ww, const double *wprod, const double *dervals,
+    const double *dgmat, const double *wg, const Geom &g, double dt,
+    double tol, int lc, int node, int t, int idx, const int *digs,
+    bool valid) {
+  using Cfg = NewtonCfg<Sys, N>;
+  constexpr int V = Cfg::V, D = Cfg::D, Nd = Cfg::Nd, NT = Cfg::NT;
+  constexpr int NL = Cfg::NL, CPB = Cfg::CPB;
+  constexpr float EPS32 = 1.1920928955078125e-07f;
+  constexpr float SQRT_EPS32 = 3.4526698300124393e-04f;
+  __shared__ float wprod32[Nd], dervals32[N * N], dgmat32[N * N], wg32[N];
+  __shared__ unsigned int res32[CPB], scale32[CPB];
+  __shared__ int done32[CPB], lu32[CPB];
+  __shared__ float last32[CPB];
+  for (int i = threadIdx.x; i < Nd; i += blockDim.x)
+    wprod32[i] = (float)wprod[i];
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    dervals32[i] = (float)dervals[i];
+    dgmat32[i] = (float)dgmat[i];
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    wg32[i] = (float)wg[i];
+  float *q32 = (float *)s_r + (lc * NT) * V;
+  float *f32 = (float *)s_f + (lc * NT) * D * V;
+  float *r32 = (float *)s_r + CPB * NT * V + (lc * NT) * V;
+  float *A32 = (float *)s_A + (lc * Nd + idx) * NL * NL;
+  int *piv = s_piv + (lc * Nd + idx) * NL;
+  float Ww32[V];
+  if (threadIdx.x < CPB) {
+    done32[threadIdx.x] = 0;
+    lu32[threadIdx.x] = 0;
+    last32[threadIdx.x] = 3.0e38f;
+  }
+  if (valid) {
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      q32[node * V + v] = (float)s_q[(lc * NT + node) * V + v];
+      Ww32[v] = (float)Ww[v];
+    }
+  } else if (lc < CPB && node == 0) {
+    done32[lc] = 1;
+  }
+  const float dt32 = (float)dt, tol32 = (float)tol;
+  int sweeps = 0;
+  for (int it = 0; it < NEWTON32_MAXIT; it++) {
+    if (lc < CPB && node == 0) {
+      res32[lc] = 0u;
+      scale32[lc] = 0u;
+    }
+    __syncthreads();
+    const bool active = valid && !done32[lc];
+    float dq[D * V];
+    if (active) {
+      if (Sys::SECOND_ORDER || Sys::HAS_B) {
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          const int base = idx - digs[d] * sd;
+          const float rdx = 1.0f / (float)g.dX[d];
+#pragma unroll
+          for (int v = 0; v < V; v++) {
+            float sacc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < N; j++)
+              sacc = fmaf(dervals32[digs[d] * N + j],
+                          q32[(t * Nd + base + j * sd) * V + v], sacc);
+            dq[d * V + v] = sacc * rdx;
+          }
+        }
+      }
+      if (Sys::HAS_F) {
+#pragma unroll
+        for (int d = 0; d < D; d++)
+          Sys::F(f32 + (node * D + d) * V, q32 + node * V, dq, d);
+      }
+    }
+    __syncthreads();
+    if (active) {
+      float r[V];
+      if (Sys::HAS_S)
+        Sys::S(r, q32 + node * V);
+      else
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          r[v] = 0.0f;
+      float cc = wg32[t];
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        if (Sys::HAS_B) {
+          float b[V * V];
+          Sys::B(b, q32 + node * V, d);
+#pragma unroll
+          for (int i = 0; i < V; i++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < V; j++)
+              acc = fmaf(b[i * V + j], dq[d * V + j], acc);
+            r[i] -= acc;
+          }
+        }
+        if (Sys::HAS_F) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          const int base = idx - digs[d] * sd;
+          const float rdx = 1.0f / (float)g.dX[d];
+#pragma unroll
+          for (int v = 0; v < V; v++) {
+            float sacc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < N; j++)
+              sacc = fmaf(dervals32[digs[d] * N + j],
+                          f32[((t * Nd + base + j * sd) * D + d) * V + v], sacc);
+            r[v] -= sacc * rdx;
+          }
+        }
+        cc *= wg32[digs[d]];
+      }
+      unsigned int rm = 0u, sm = 0u;
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        const float rv = fmaf(r[v] * cc, dt32, Ww32[v]);
+        float uq = 0.0f;
+#pragma unroll
+        for (int k = 0; k < N; k++)
+          uq = fmaf(dgmat32[t * N + k], q32[(k * Nd + idx) * V + v], uq);
+        uq *= wprod32[idx];
+        const float ov = rv - uq;
+        r32[node * V + v] = ov;
+        const unsigned int a = __float_as_uint(ov) & 0x7fffffffu;
+        const unsigned int b = __float_as_uint(rv) & 0x7fffffffu;
+        const unsigned int c = __float_as_uint(uq) & 0x7fffffffu;
+        // a NaN or infinity stops the cell's FP32 sweeps (the max is the
+        // largest finite bit pattern then)
+        rm = max(rm, a >= 0x7f800000u ? 0x7f7fffffu : a);
+        sm = max(sm, max(b < 0x7f800000u ? b : 0u, c < 0x7f800000u ? c : 0u));
+      }
+      atomicMax(&res32[lc], rm);
+      atomicMax(&scale32[lc], sm);
+    }
+    __syncthreads();
+    bool stop = false;
+    if (active) {
+      const float res = __uint_as_float(res32[lc]);
+      const float scale = __uint_as_float(scale32[lc]);
+      stop = res <= tol32 || res <= 64.0f * EPS32 * scale ||
+             !(res <= 0.5f * last32[lc]) || res >= 3.0e38f;
+      if (!stop && !lu32[lc]) {
+        // row block t of A: the FD Jacobian of S in FP32
+        float *qn = q32 + node * V;
+        float s0[V], s1[V];
+        if (Sys::HAS_S)
+          Sys::S(s0, qn);
+        for (int wv = 0; wv < V; wv++) {
+          float ih = 0.0f;
+          if (Sys::HAS_S) {
+            const float q0 = qn[wv];
+            const float h = fmaxf(SQRT_EPS32 * fabsf(q0), SQRT_EPS32);
+            qn[wv] = q0 + h;
+            Sys::S(s1, qn);
+            qn[wv] = q0;
+            ih = 1.0f / h;
+          }
+          for (int v = 0; v < V; v++)
+            for (int k = 0; k < N; k++) {
+              float a = 0.0f;
+              if (k == t && Sys::HAS_S)
+                a = dt32 * wg32[t] * ((s1[v] - s0[v]) * ih);
+              A32[(t * V + v) * NL + k * V + wv] = a;
+            }
+        }
+        for (int k = 0; k < N; k++)
+          for (int v = 0; v < V; v++)
+            A32[(t * V + v) * NL + k * V + v] -= dgmat32[t * N + k];
+      }
+    }
+    __syncthreads();
+    bool bad = false;
+    if (active && !stop && t == 0) {
+      bool ok = true;
+      for (int k = 0; k < NL && ok && !lu32[lc]; k++) {
+        int p = k;
+        unsigned int pm = __float_as_uint(A32[k * NL + k]) & 0x7fffffffu;
+        for (int i = k + 1; i < NL; i++) {
+          const unsigned int m = __float_as_uint(A32[i * NL + k]) & 0x7fffffffu;
+          if (m > pm) {
+            p = i;
+            pm = m;
+          }
+        }
+        piv[k] = p;
+        if (pm == 0u) {
+          ok = false;
+          break;
+        }
+        if (p != k)
+          for (int j = 0; j < NL; j++) {
+            const float tmp = A32[k * NL + j];
+            A32[k * NL + j] = A32[p * NL + j];
+            A32[p * NL + j] = tmp;
+          }
+        const float rp = 1.0f / A32[k * NL + k];
+        for (int i = k + 1; i < NL; i++) {
+          const float f = A32[i * NL + k] * rp;
+          A32[i * NL + k] = f;
+          if ((__float_as_uint(f) & 0x7fffffffu) == 0u)
+            continue;
+          for (int j = k + 1; j < NL; j++)
+            A32[i * NL + j] = fmaf(-f, A32[k * NL + j], A32[i * NL + j]);
+        }
+      }
+      if (!ok) {
+        bad = true;
+      } else {
+        float b[NL];
+        const float rwp = 1.0f / wprod32[idx];
+        for (int tt = 0; tt < N; tt++)
+          for (int v = 0; v < V; v++)
+            b[tt * V + v] = r32[(tt * Nd + idx) * V + v] * rwp;
+        for (int k = 0; k < NL; k++)
+          if (piv[k] != k) {
+            const float tmp = b[k];
+            b[k] = b[piv[k]];
+            b[piv[k]] = tmp;
+          }
+        for (int k = 0; k < NL; k++)
+          for (int i = k + 1; i < NL; i++)
+            if ((__float_as_uint(A32[i * NL + k]) & 0x7fffffffu) != 0u)
+              b[i] = fmaf(-A32[i * NL + k], b[k], b[i]);
+        for (int i = NL - 1; i >= 0; i--) {
+          float sacc = b[i];
+          for (int j = i + 1; j < NL; j++)
+            if ((__float_as_uint(A32[i * NL + j]) & 0x7fffffffu) != 0u)
+              sacc = fmaf(-A32[i * NL + j], b[j], sacc);
+          b[i] = sacc / A32[i * NL + i];
+        }
+        for (int tt = 0; tt < N; tt++)
+          for (int v = 0; v < V; v++)
+            q32[(tt * Nd + idx) * V + v] -= b[tt * V + v];
+      }
+    }
+    if (bad)
+      atomicOr(&done32[lc], 2);
+    __syncthreads();
+    if (active && node == 0) {
+      if (stop) {
+        done32[lc] |= 1;
+      } else {
+        last32[lc] = __uint_as_float(res32[lc]);
+        lu32[lc] = 1;
+        sweeps = it + 1;
+      }
+    }
+    bool all_done = true;
+    if (node == 0 && lc < CPB)
+      all_done = done32[lc] != 0;
+    if (__syncthreads_and(all_done))
+      break;
+  }
+  // hand the FP32 iterate to the FP64 sweeps
+  if (valid) {
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      s_q[(lc * NT + node) * V + v] = (double)q32[node * V + v];
+  }
+  __syncthreads();
+  return sweeps;
+}
+
 template <class Sys, int N>
 __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restrict__ w, double *__restrict__ qh,
                          Geom g, Tables T, const double *__restrict__ wprod_g,
-                         DevState *st, double tol, int guess) {
+                         DevState *st, double tol, int guess, int mixed) {
   using Cfg = NewtonCfg<Sys, N>;
   constexpr int V = Cfg::V, D = Cfg::D, Nd = Cfg::Nd, NT = Cfg::NT;
   constexpr int NL = Cfg::NL, CPB = Cfg::CPB;
@@ -560,6 +845,18 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   } else if (lc < CPB && node == 0) {
     cell_done[lc] = 1;
   }
+  if constexpr (Sys::HAS_FP32) {
+    if (mixed) {
+      __syncthreads();
+      const int sw = newton_fp32_sweeps<Sys, N>(
+          s_q, s_r, s_f, s_A, s_piv, Ww, wprod, dervals, dgmat, wg, g, dt,
+          tol, lc, node, t, idx, digs, valid);
+      if (valid && node == 0)
+        atomicAdd(&st->pred_iters32, (unsigned long long)sw);
+    }
+  }
+  // mixed precision: at least two FP64 updates before a cell may stop
+  const int min_updates = mixed ? 2 : 0;
   int iters = 0;
   bool failed = false;
   for (int it = 0; it < NEWTON_MAXIT; it++) {
@@ -675,7 +972,8 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
       res = __longlong_as_double((long long)res_bits[lc]);
       double scale = __longlong_as_double((long long)scale_bits[lc]);
       reset = on_guess[lc] && (bad_res[lc] || !(res < prev_res[lc]));
-      conv = !reset && (res <= tol || res <= 16 * DBL_EPS * scale);
+      conv = !reset && it >= min_updates &&
+             (res <= tol || res <= 16 * DBL_EPS * scale);
       // simplified Newton: factors reused until the residual falls by
       // less than half in an iteration
       refresh = !have_lu[lc] || !(res <= 0.5 * last_res[lc]);
@@ -831,8 +1129,8 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
 template <class Sys, int N>
 __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
                          Geom g, Tables T, const double *__restrict__ wprod_g,
-                         DevState *st, double tol, int guess) {
-  k_newton_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st, tol, guess);
+                         DevState *st, double tol, int guess, int mixed) {
+  k_newton_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st, tol, guess, mixed);
 }
 
 // ---------------------------------------------------------------------

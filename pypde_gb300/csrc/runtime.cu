@@ -293,6 +293,7 @@ struct StepCtx {
       *wprod;
   DevState *st;
   const WarmStart *warm; // learned warm start of the Newton predictor
+  int mixed;             // FP32 Newton sweeps first (mixed precision)
   const double *guess;   // or a given initial guess already in qh
   // harvest of training pairs (device buffers)
   double *hw, *hq, *hdt;
@@ -323,9 +324,10 @@ static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
     } else if (c.guess) {
       guess = 1;
     }
+    int mixed = c.mixed;
     void *na[] = {(void *)&c.w,     (void *)&c.qh, (void *)&g,
                   (void *)&T,       (void *)&c.wprod, (void *)&c.st,
-                  (void *)&tol,     (void *)&guess};
+                  (void *)&tol,     (void *)&guess, (void *)&mixed};
     unsigned blocks = (unsigned)((g.Cw + k.newton_cpb - 1) / k.newton_cpb);
     return launch(k.newton, dim3(blocks), dim3(k.newton_threads),
                   k.newton_smem, s, na);
@@ -607,6 +609,7 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   c.flux = a.flux;
   c.tol = a.newton_tol;
   c.warm = a.warm;
+  c.mixed = a.mixed ? 1 : 0;
   c.guess = nullptr;
   c.hw = c.hq = c.hdt = nullptr;
   c.hstride = 1;
@@ -792,6 +795,7 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
     out->pred_max_iters = h.pred_max_iters;
     out->pred_fail = h.pred_fail;
     out->pred_fallbacks = h.pred_fallbacks;
+    out->pred_iters32 = h.pred_iters32;
     out->nan_found = h.nan_found;
     out->device_seconds = ms * 1e-3;
     out->kernel_launches = launches;
@@ -880,10 +884,15 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
     if (g.tiles[st] == 0)
       return cudaSuccess;
     TileQueue q{g.dOff[st], (int)g.idx.size(), c.heads + gi * BS_COUNT + st};
-    int pp = g.per_pop[st] > 0 ? g.per_pop[st] : 1;
-    long long want = (g.tiles[st] + pp - 1) / pp;
-    long long cap = (long long)g.resident[st] * c.nsm;
-    unsigned grid = (unsigned)(want < cap ? want : cap);
+    int pp = g.per_pop[st] >= 0 ? g.per_pop[st] : 1;
+    unsigned grid;
+    if (pp == 0) { // one block per tile, no queue
+      grid = (unsigned)g.tiles[st];
+    } else {
+      long long want = (g.tiles[st] + pp - 1) / pp;
+      long long cap = (long long)g.resident[st] * c.nsm;
+      grid = (unsigned)(want < cap ? want : cap);
+    }
     void *args[8] = {(void *)&g.dP, (void *)&q, (void *)&pp, x0, x1, x2,
                      nullptr, nullptr};
     (void)extra;
@@ -1131,7 +1140,7 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
       CK(mem.alloc((void **)&g.dOff[st], off[st].size() * 8));
       CK(cudaMemcpyAsync(g.dOff[st], off[st].data(), off[st].size() * 8,
                          cudaMemcpyHostToDevice, s));
-      g.per_pop[st] = a.per_pop > 0 ? a.per_pop : 1;
+      g.per_pop[st] = a.per_pop >= 0 ? a.per_pop : 1;
     }
     g.fn[BS_BOUNDARIES].aot = (const void *)&kb_boundaries;
     g.threads[BS_BOUNDARIES] = 256;
@@ -1213,10 +1222,11 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
   long long launches = 0;
   double tune_s = 0;
   CK(all_done());
-  // autotune: the first steps run eagerly, one tile shape per step, each
+  // autotune: the first steps run eagerly, one tile shape per step (0: a
+  // block per tile; 1-8: tiles per pop of the persistent queue), each
   // (group, stage) launch timed; the fastest shape per launch is kept
   if (a.autotune && !finished()) {
-    const int cand[4] = {1, 2, 4, 8};
+    const int cand[5] = {0, 1, 2, 4, 8};
     const size_t nev = c.G.size() * BS_COUNT * 2;
     std::vector<cudaEvent_t> ev(nev);
     for (auto &x : ev)
@@ -1224,7 +1234,7 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
     std::vector<float> best(c.G.size() * BS_COUNT, 1e30f);
     std::vector<int> pick(c.G.size() * BS_COUNT, 1);
     auto t0 = std::chrono::steady_clock::now();
-    for (int ci = 0; ci < 4 && !finished(); ci++) {
+    for (int ci = 0; ci < 5 && !finished(); ci++) {
       for (auto &g : c.G)
         for (int st = 0; st < BS_COUNT; st++)
           g.per_pop[st] = cand[ci];

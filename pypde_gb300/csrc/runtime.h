@@ -104,6 +104,7 @@ struct RunArgs {
   bool profile = false;
   bool useF = true, useB = true, useS = true;
   const WarmStart *warm = nullptr;    // learned warm start of the Newton predictor
+  bool mixed = false;                 // FP32 Newton sweeps before the FP64 ones
   const HarvestArgs *harvest = nullptr;
 };
 
@@ -113,6 +114,7 @@ struct Stats {
   unsigned long long pred_iters = 0;
   int pred_max_iters = 0, pred_fail = 0, nan_found = 0;
   unsigned long long pred_fallbacks = 0;
+  unsigned long long pred_iters32 = 0;
   double device_seconds = 0;
   long long kernel_launches = 0;
   double stage_seconds[8] = {};

@@ -26,34 +26,37 @@ namespace pypde {
 // 10^x = 2^n e^r with n = round(x log2 10), |r| <= ln2/2, and e^r by its
 // Taylor polynomial of degree 16 in Horner form (truncation below 1e-22),
 // from IEEE +, *, floor and ldexp only, so that host and device agree
-// bitwise.  The coefficients are the doubles nearest to 1/k!.
-__device__ __forceinline__ double pow10_portable(double x) {
+// bitwise.  The coefficients are the doubles nearest to 1/k!.  T = float
+// gives the same recipe in FP32 (for the FP32 Newton sweeps).
+template <class T> __device__ __forceinline__ T pow10_portable(T x) {
   constexpr double c[17] = {
       1.0, 1.0, 0.5, 0.16666666666666666,
       0.041666666666666664, 0.008333333333333333, 0.001388888888888889, 0.0001984126984126984,
       2.48015873015873e-05, 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08,
       2.08767569878681e-09, 1.6059043836821613e-10, 1.1470745597729725e-11, 7.647163731819816e-13,
       4.779477332387385e-14};
-  double y = x * 3.321928094887362;
-  double n = floor(y + 0.5);
-  double r = (y - n) * 0.6931471805599453;
-  double p = c[16];
+  T y = x * T(3.321928094887362);
+  T n = floor(y + T(0.5));
+  T r = (y - n) * T(0.6931471805599453);
+  T p = T(c[16]);
 #pragma unroll
   for (int k = 15; k >= 0; k--)
-    p = p * r + c[k];
+    p = p * r + T(c[k]);
   return ldexp(p, (int)n);
 }
 
+// The callbacks are templates on the scalar type: double for every form,
+// float for the FP32 Newton sweeps of the mixed-precision form (HAS_FP32).
 template <int D> struct EulerCore {
-  static __device__ __forceinline__ double flux(double *out, const double *Q,
-                                                int d) {
-    double r = Q[0];
-    double ke = 0.0;
+  template <class T>
+  static __device__ __forceinline__ T flux(T *out, const T *Q, int d) {
+    T r = Q[0];
+    T ke = T(0.0);
 #pragma unroll
     for (int i = 0; i < D; i++)
       ke += Q[1 + i] * Q[1 + i];
-    double p = (1.4 - 1.0) * (Q[D + 1] - 0.5 * ke / r);
-    double ud = Q[1 + d] / r;
+    T p = (T(1.4) - T(1.0)) * (Q[D + 1] - T(0.5) * ke / r);
+    T ud = Q[1 + d] / r;
     out[0] = Q[1 + d];
 #pragma unroll
     for (int i = 0; i < D; i++)
@@ -67,86 +70,88 @@ template <int D> struct EulerCore {
 template <int D> struct Euler {
   static constexpr int V = D + 2, NDIM = D;
   static constexpr bool HAS_F = true, HAS_B = false, HAS_S = false;
-  static constexpr bool SECOND_ORDER = false;
-  static __device__ __forceinline__ void F(double *out, const double *Q,
-                                           const double *, int d) {
+  static constexpr bool SECOND_ORDER = false, HAS_FP32 = true;
+  template <class T>
+  static __device__ __forceinline__ void F(T *out, const T *Q, const T *, int d) {
     EulerCore<D>::flux(out, Q, d);
   }
-  static __device__ __forceinline__ void B(double *, const double *, int) {}
-  static __device__ __forceinline__ void S(double *, const double *) {}
+  template <class T> static __device__ __forceinline__ void B(T *, const T *, int) {}
+  template <class T> static __device__ __forceinline__ void S(T *, const T *) {}
 };
 
 template <int D> struct Cattaneo {
   static constexpr int V = 2 * D + 3, NDIM = D;
   static constexpr bool HAS_F = true, HAS_B = false, HAS_S = true;
-  static constexpr bool SECOND_ORDER = false;
-  static __device__ __forceinline__ void F(double *out, const double *Q,
-                                           const double *, int d) {
-    double p = EulerCore<D>::flux(out, Q, d);
-    double T = p / Q[0];
+  static constexpr bool SECOND_ORDER = false, HAS_FP32 = true;
+  template <class T>
+  static __device__ __forceinline__ void F(T *out, const T *Q, const T *, int d) {
+    T p = EulerCore<D>::flux(out, Q, d);
+    T Tt = p / Q[0];
     out[D + 1] += Q[D + 2 + d];
 #pragma unroll
     for (int i = 0; i < D; i++)
-      out[D + 2 + i] = 0.0;
-    out[D + 2 + d] = 1.0 * T;
-    out[2 * D + 2] = 0.0;
+      out[D + 2 + i] = T(0.0);
+    out[D + 2 + d] = T(1.0) * Tt;
+    out[2 * D + 2] = T(0.0);
   }
-  static __device__ __forceinline__ void B(double *, const double *, int) {}
-  static __device__ __forceinline__ void S(double *out, const double *Q) {
-    double inv_tau = pow10_portable(-Q[2 * D + 2]);
+  template <class T> static __device__ __forceinline__ void B(T *, const T *, int) {}
+  template <class T>
+  static __device__ __forceinline__ void S(T *out, const T *Q) {
+    T inv_tau = pow10_portable<T>(-Q[2 * D + 2]);
 #pragma unroll
     for (int i = 0; i < D + 2; i++)
-      out[i] = 0.0;
+      out[i] = T(0.0);
 #pragma unroll
     for (int i = 0; i < D; i++)
       out[D + 2 + i] = -Q[D + 2 + i] * inv_tau;
-    out[2 * D + 2] = 0.0;
+    out[2 * D + 2] = T(0.0);
   }
 };
 
-__device__ __forceinline__ double ncp_a(int d) {
-  return d == 0 ? 1.0 : (d == 1 ? 0.5 : 0.25);
+template <class T> __device__ __forceinline__ T ncp_a(int d) {
+  return d == 0 ? T(1.0) : (d == 1 ? T(0.5) : T(0.25));
 }
 
 template <int D> struct Ncp {
   static constexpr int V = 3, NDIM = D;
   static constexpr bool HAS_F = true, HAS_B = true, HAS_S = true;
-  static constexpr bool SECOND_ORDER = false;
-  static __device__ __forceinline__ void F(double *out, const double *Q,
-                                           const double *, int d) {
-    double a = ncp_a(d);
-    out[0] = a * (0.5 * Q[0] * Q[0]);
+  static constexpr bool SECOND_ORDER = false, HAS_FP32 = true;
+  template <class T>
+  static __device__ __forceinline__ void F(T *out, const T *Q, const T *, int d) {
+    T a = ncp_a<T>(d);
+    out[0] = a * (T(0.5) * Q[0] * Q[0]);
     out[1] = a * (Q[0] * Q[1]);
     out[2] = a * (Q[0] * Q[2]);
   }
-  static __device__ __forceinline__ void B(double *out, const double *Q,
-                                           int d) {
-    double a = ncp_a(d);
+  template <class T>
+  static __device__ __forceinline__ void B(T *out, const T *Q, int d) {
+    T a = ncp_a<T>(d);
 #pragma unroll
     for (int i = 0; i < 9; i++)
-      out[i] = 0.0;
+      out[i] = T(0.0);
     out[4] = a * Q[0];
-    out[5] = a * 0.2;
-    out[7] = a * 0.2;
+    out[5] = a * T(0.2);
+    out[7] = a * T(0.2);
     out[8] = a * Q[0];
   }
-  static __device__ __forceinline__ void S(double *out, const double *Q) {
-    out[0] = 0.0;
-    out[1] = 0.1 * (Q[2] - Q[1]);
-    out[2] = -0.1 * (Q[1] + Q[2]);
+  template <class T>
+  static __device__ __forceinline__ void S(T *out, const T *Q) {
+    out[0] = T(0.0);
+    out[1] = T(0.1) * (Q[2] - Q[1]);
+    out[2] = T(-0.1) * (Q[1] + Q[2]);
   }
 };
 
 struct Burgers2 {
   static constexpr int V = 1, NDIM = 1;
   static constexpr bool HAS_F = true, HAS_B = false, HAS_S = false;
-  static constexpr bool SECOND_ORDER = true;
-  static __device__ __forceinline__ void F(double *out, const double *Q,
-                                           const double *dQ, int d) {
-    out[0] = ncp_a(d) * (0.5 * Q[0] * Q[0]) - 0.01 * dQ[d];
+  static constexpr bool SECOND_ORDER = true, HAS_FP32 = true;
+  template <class T>
+  static __device__ __forceinline__ void F(T *out, const T *Q, const T *dQ, int d) {
+    out[0] = ncp_a<T>(d) * (T(0.5) * Q[0] * Q[0]) - T(0.01) * dQ[d];
   }
-  static __device__ __forceinline__ void B(double *, const double *, int) {}
-  static __device__ __forceinline__ void S(double *, const double *) {}
+  template <class T> static __device__ __forceinline__ void B(T *, const T *, int) {}
+  template <class T> static __device__ __forceinline__ void S(T *, const T *) {}
 };
 
 } // namespace pypde

@@ -12,7 +12,9 @@ Differences from the reference, all at the callback boundary:
   * Extensions (keyword-only): ``max_steps``, ``newton_tol``, ``device``,
     ``stats`` (a dict filled with step and iteration counts), ``jit``,
     ``warm_start`` (a pypde_gb300.warmstart.WarmStart: learned initial guess
-    of the stiff predictor's Newton iteration).
+    of the stiff predictor's Newton iteration), ``mixed_precision`` (Newton
+    sweeps in FP32 first, then at least two FP64 sweeps to the same
+    tolerance; built-in systems).
 """
 import ctypes
 
@@ -28,7 +30,7 @@ FLUXES = {"rusanov": 0, "roe": 1, "osher": 2}
 def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cfl=0.9,
                order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *,
                max_steps=None, newton_tol=None, device=0, stats=None, jit=False,
-               warm_start=None):
+               warm_start=None, mixed_precision=False):
     """Solve dQ/dt + div F(Q, grad Q) + B(Q) . grad Q = S(Q) on [0, L] (see
     pypde/solvers.py:28-175 for the full description of the arguments).
 
@@ -62,6 +64,7 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
         if not stiff:
             raise ValueError("warm_start applies to the stiff (Newton) predictor")
         opt.warm_start = warm_start.handle
+    opt.mixed_precision = int(bool(mixed_precision))
     st = _lib.Stats()
     lib = _lib.lib()
     code = lib.pde_solver_ex(system.handle, useF, useB, useS, _lib.c_ptr(ur), float(tf),

@@ -719,7 +719,8 @@ def translate(F, B, S, ndim, V):
              f"  static constexpr int V = {V}, NDIM = {ndim};",
              f"  static constexpr bool HAS_F = {str(F is not None).lower()}, "
              f"HAS_B = {str(B is not None).lower()}, HAS_S = {str(S is not None).lower()};",
-             f"  static constexpr bool SECOND_ORDER = {str(second).lower()};"]
+             f"  static constexpr bool SECOND_ORDER = {str(second).lower()};",
+             "  static constexpr bool HAS_FP32 = false; // double callbacks only"]
     for role, sig in (("F", "static __device__ void F(double *, const double *, const double *, int) {}"),
                       ("B", "static __device__ void B(double *, const double *, int) {}"),
                       ("S", "static __device__ void S(double *, const double *) {}")):

@@ -32,7 +32,7 @@ def _problems(system, seed, stiff):
 
 
 @pytest.mark.parametrize("system,stiff", [("euler", False), ("cattaneo", True)])
-@pytest.mark.parametrize("mode", ["autotune", "per_pop3"])
+@pytest.mark.parametrize("mode", ["autotune", "per_pop3", "direct"])
 def test_batch_matches_single_problems(gpu_lib, system, stiff, mode):
     s = systems.euler(2) if system == "euler" else systems.cattaneo(2)
     probs = _problems(system, 3, stiff)
@@ -46,14 +46,14 @@ def test_batch_matches_single_problems(gpu_lib, system, stiff, mode):
     batch = [dict(p, Q0=p["Q0"].copy()) for p in probs]
     stats = {}
     pde_solver_batch(batch, F=s.F, S=s.S, stiff=stiff, autotune=(mode == "autotune"),
-                     per_pop=3, stats=stats)
+                     per_pop=0 if mode == "direct" else 3, stats=stats)
     for p, (q, st), k, t in zip(batch, singles, stats["steps_per_problem"], stats["t_final"]):
         assert k == st["steps"] and t == st["t_final"]
         assert np.array_equal(p["Q0"], q)
     assert stats["steps"] == sum(st["steps"] for _, st in singles)
     assert stats["nan_found"] == 0
     if mode == "autotune":
-        assert all(v in (1, 2, 4, 8) for v in stats["per_pop"].values() if v)
+        assert all(v in (0, 1, 2, 4, 8) for v in stats["per_pop"].values())
 
 
 def test_batch_max_steps_and_jit(gpu_lib):

@@ -1,0 +1,52 @@
+"""Mixed-precision stiff predictor: FP32 Newton sweeps (FP32 callbacks, FP32
+FD Jacobian and LU), then at least two FP64 sweeps to the same 1e-12
+tolerance.  The answer must stay at the plain FP64 form's error level
+against a tolerance-1e-15 oracle (two converged Newton solves differ by the
+tolerance's own effect, measured by the plain form at tolerances 1e-12 and
+1e-13), and the FP64 sweeps must not increase."""
+import numpy as np
+import pytest
+
+from conftest import l1
+from pypde_gb300 import _lib, systems, workloads
+from pypde_gb300.solvers import pde_solver
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(u0, s, tol, K, **kw):
+    q, st = u0.copy(), {}
+    pde_solver(q, 10.0, [1.0] * (u0.ndim - 1), F=s.F, B=s.B, S=s.S, boundaryTypes="periodic",
+               cfl=0.8, order=2, stiff=True, max_steps=K, stats=st, newton_tol=tol, **kw)
+    assert st["steps"] == K and st["pred_fail"] == 0
+    return q, st
+
+
+@pytest.mark.parametrize("case", ["cattaneo2d", "cattaneo3d", "ncp2d"])
+def test_mixed_precision_matches_plain_error_level(gpu_lib, case):
+    if case == "cattaneo2d":
+        u0, s, K = workloads.relaxation(48, 2, seed=11, patches=4), systems.cattaneo(2), 20
+    elif case == "cattaneo3d":
+        u0, s, K = workloads.relaxation(12, 3, seed=4), systems.cattaneo(3), 6
+    else:
+        u0, s, K = workloads.random_state("ncp", (20, 18), 3), systems.ncp(2), 10
+    q_o, _ = _run(u0, s, 1e-15, K)
+    q_p, st_p = _run(u0, s, 1e-12, K)
+    q_p13, _ = _run(u0, s, 1e-13, K)
+    q_m, st_m = _run(u0, s, 1e-12, K, mixed_precision=True)
+    floor = max(l1(q_p, q_o).max(), l1(q_p13, q_o).max())
+    err = l1(q_m, q_o).max()
+    print(f"{case}: L1 vs oracle plain {l1(q_p, q_o).max():.2e} mixed {err:.2e}; FP64 sweeps "
+          f"plain {st_p['pred_iters']} mixed {st_m['pred_iters']}; FP32 sweeps "
+          f"{st_m['pred_iters32']}")
+    assert err <= max(1e-8, 3 * floor), (err, floor)
+    assert st_m["pred_iters32"] > 0
+    assert st_m["pred_iters"] <= st_p["pred_iters"] * 1.05
+
+
+def test_mixed_precision_refused_where_it_cannot_run(gpu_lib):
+    s = systems.cattaneo(2)
+    u0 = workloads.relaxation(8, 2, seed=1)
+    with pytest.raises(_lib.PyPDEError):
+        pde_solver(u0.copy(), 1.0, [1.0, 1.0], F=s.F, S=s.S, stiff=True, max_steps=1,
+                   mixed_precision=True, jit=True)   # run-time callbacks have no FP32 twin
