@@ -71,7 +71,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="stiff", choices=sorted(WORKLOADS))
-    p.add_argument("--n", type=int, default=0, help="cells per side (0: the workload's)")
+    p.add_argument("--side", type=int, default=0, help="cells per side (0: the workload's)")
     p.add_argument("--order", type=int, default=0, help="N (0: the workload's)")
     p.add_argument("--train-iters", type=int, default=3000)
     p.add_argument("--cpu-seconds", type=float, default=15.0,
@@ -83,7 +83,7 @@ def parse():
     a = p.parse_args()
     system, n, N, cfl, stiff = WORKLOADS[a.workload]
     a.system, a.cfl, a.stiff = system, cfl, stiff
-    a.n = a.n or n
+    a.n = a.side or n
     a.order = a.order or N
     return a
 
