@@ -58,9 +58,10 @@ METRIC = "cell_updates_per_s"
 UNIT = "cell-updates/s"
 
 WORKLOADS = {
-    # name: (system, n, N, cfl, stiff)
-    "stiff": ("cattaneo", 1024, 2, 0.8, True),
-    "shear": ("euler", 512, 3, 0.8, False),
+    # name: (system, ndim, n, N, cfl, stiff)
+    "stiff": ("cattaneo", 2, 1024, 2, 0.8, True),
+    "stiff3d": ("cattaneo", 3, 256, 2, 0.8, True),
+    "shear": ("euler", 2, 512, 3, 0.8, False),
 }
 
 
@@ -81,8 +82,8 @@ def parse():
                    help="problems of the batched section (0: skip it)")
     p.add_argument("--batch-steps", type=int, default=6)
     a = p.parse_args()
-    system, n, N, cfl, stiff = WORKLOADS[a.workload]
-    a.system, a.cfl, a.stiff = system, cfl, stiff
+    system, ndim, n, N, cfl, stiff = WORKLOADS[a.workload]
+    a.system, a.ndim, a.cfl, a.stiff = system, ndim, cfl, stiff
     a.n = a.side or n
     a.order = a.order or N
     return a
@@ -171,10 +172,16 @@ def initial_state(args, seed):
     from pypde_gb300 import workloads
     if args.workload == "stiff":
         return workloads.relaxation(args.n, 2, seed=seed)
+    if args.workload == "stiff3d":
+        return workloads.relaxation(args.n, 3, seed=seed, log10_tau=(-6.0, -3.0), amp=0.05)
     return workloads.shear(args.n, seed=seed)
 
 
 def workload_name(args):
+    if args.workload == "stiff3d":
+        return (f"3-D Euler + relaxing heat flux (9 vars), {args.n}^3 periodic, N={args.order}, "
+                f"Rusanov, CFL {args.cfl}, stiff Newton predictor to 1e-12, log10 tau ~ "
+                "U(-6,-3) per octant")
     if args.workload == "stiff":
         return (f"2-D Euler + relaxing heat flux (7 vars), {args.n}x{args.n} periodic, "
                 f"N={args.order}, Rusanov, CFL {args.cfl}, stiff Newton predictor to 1e-12, "
@@ -185,7 +192,8 @@ def workload_name(args):
 
 def cpu_run(args, u, steps, cores):
     from oracle import ora
-    return ora.pde_solver(args.system, u, 10.0, [1.0, 1.0], [1, 1], args.cfl, args.order,
+    return ora.pde_solver(args.system, u, 10.0, [1.0] * args.ndim, [1] * args.ndim, args.cfl,
+                          args.order,
                           stiff=args.stiff, max_steps=steps, nthreads=cores)
 
 
@@ -194,6 +202,11 @@ def cpu_baseline(args, u0, budget):
     budget is used (at least one step).  Returns (cell-updates/s, cores,
     sample description)."""
     cores = os.cpu_count() or 1
+    if args.ndim == 3 and u0.shape[0] > 48:
+        # one whole 3-D grid step takes minutes on the host: a 48^3 sample of
+        # the same workload (same per-cell work)
+        from pypde_gb300 import workloads
+        u0 = workloads.relaxation(48, 3, seed=0, log10_tau=(-6.0, -3.0), amp=0.05)
     C = int(np.prod(u0.shape[:-1]))
     u = u0
     steps, t0 = 0, time.perf_counter()
@@ -203,8 +216,9 @@ def cpu_baseline(args, u0, budget):
         el = time.perf_counter() - t0
         if el >= budget or steps >= 50:
             break
-    sample = (f"{steps} whole-grid step(s) of the same {u0.shape[0]}x{u0.shape[1]} "
-              f"N={args.order} workload from its initial state, {el:.1f} s")
+    sample = (f"{steps} whole-grid step(s) of the same workload on a "
+              f"{'x'.join(map(str, u0.shape[:-1]))} grid, N={args.order}, from its initial "
+              f"state, {el:.1f} s")
     return C * steps / el, cores, sample
 
 
@@ -217,10 +231,10 @@ class Runner:
         self.L = _lib.lib()
         self._lib = _lib
         self.args, self.local = args, local
-        self.sys = builtin_system(args.system, 2)
-        self.nX = np.array([args.n, args.n], dtype=np.int32)
-        self.dX = np.array([1.0 / args.n, 1.0 / args.n])
-        self.bt = np.array([1, 1], dtype=np.int32)
+        self.sys = builtin_system(args.system, args.ndim)
+        self.nX = np.array([args.n] * args.ndim, dtype=np.int32)
+        self.dX = np.array([1.0 / args.n] * args.ndim)
+        self.bt = np.array([1] * args.ndim, dtype=np.int32)
 
     def run(self, u, steps, profile=False, warm=None, tol=0.0, mixed=False):
         _lib, a = self._lib, self.args
@@ -235,7 +249,8 @@ class Runner:
         st = _lib.Stats()
         s = self.sys
         _lib.check(self.L.pde_solver_ex(s.handle, s.has_F, s.has_B, s.has_S, _lib.c_ptr(u),
-                                        10.0, _lib.c_ptr(self.nX), 2, _lib.c_ptr(self.dX),
+                                        10.0, _lib.c_ptr(self.nX), a.ndim,
+                                        _lib.c_ptr(self.dX),
                                         a.cfl, _lib.c_ptr(self.bt), a.stiff, 0, a.order, 1,
                                         None, opt, st))
         return st.as_dict()
@@ -302,13 +317,16 @@ def run_ours(args, ws, rank, local):
     from pypde_gb300.solvers import pde_solver
 
     L = _lib.lib()
-    n, N, V = args.n, args.order, (7 if args.workload == "stiff" else 4)
-    C = n * n
+    n, N, nd = args.n, args.order, args.ndim
+    V = 2 * nd + 3 if args.system == "cattaneo" else nd + 2
+    C = n ** nd
+    Cw = (n + 2) ** nd
+    L = [1.0] * nd
     u0 = initial_state(args, rank)
     R = Runner(args, local)
     peak = _lib.ctypes.c_double()
     _lib.check(L.pypde_measure_fp64_peak(local, peak))
-    s = systems.cattaneo(2) if args.workload == "stiff" else systems.euler(2)
+    s = systems.cattaneo(nd) if args.system == "cattaneo" else systems.euler(nd)
 
     forms = {}
     warm = None
@@ -316,8 +334,8 @@ def run_ours(args, ws, rank, local):
     if args.stiff:
         from pypde_gb300 import warmstart
         t0 = time.perf_counter()
-        warm = warmstart.train_warm_start(u0, 10.0, [1.0, 1.0], F=s.F, S=s.S, cfl=args.cfl,
-                                          order=N, tau_var=6, steps=20, per_step=16384,
+        warm = warmstart.train_warm_start(u0, 10.0, L, F=s.F, S=s.S, cfl=args.cfl,
+                                          order=N, tau_var=2 * nd + 2, steps=20, per_step=16384,
                                           iters=args.train_iters, seed=rank, device=local)
         train = {"seconds": time.perf_counter() - t0, "samples": warm.samples,
                  "iters": args.train_iters, "train_rms_normalised": warm.train_rms,
@@ -347,23 +365,23 @@ def run_ours(args, ws, rank, local):
 
     def form_summary(name):
         st, sec_f, sp_f, ks = forms[name]
-        its = st["pred_iters"] / (args.steps * (n + 2) ** 2)
+        its = st["pred_iters"] / (args.steps * Cw)
         d = {"value": ws * C * args.steps / sec_f, "ms_per_step": 1e3 * sec_f / args.steps,
              "predictor_iters_per_cell": its,
              "stage_ms_per_step": {k: 1e3 * v / ks for k, v in sp_f["stage_seconds"].items()}}
         if args.stiff:
             d["newton_fallbacks"] = st["pred_fallbacks"]
-            d["fp32_sweeps_per_cell"] = st["pred_iters32"] / (args.steps * (n + 2) ** 2)
+            d["fp32_sweeps_per_cell"] = st["pred_iters32"] / (args.steps * Cw)
             d["l1_vs_oracle"] = errs[name]
         return d
 
     stage_s = sp["stage_seconds"]
-    its = sp["pred_iters"] / (ksteps * (n + 2) ** 2)
-    fpf = work_model.face_point_flops(args.system, 2, V, N)
-    fpts = work_model.face_points([n, n], N)
+    its = sp["pred_iters"] / (ksteps * Cw)
+    fpf = work_model.face_point_flops(args.system, nd, V, N)
+    fpts = work_model.face_points([n] * nd, N)
     faces_launch = stage_s["faces"] / ksteps
     achieved = fpts * fpf / faces_launch / 1e12
-    flops = work_model.step_flops(args.system, [n, n], V, N, its, stiff=args.stiff)
+    flops = work_model.step_flops(args.system, [n] * nd, V, N, its, stiff=args.stiff)
 
     # e2e through the public API from pinned host memory (the headline form)
     try:
@@ -374,7 +392,7 @@ def run_ours(args, ws, rank, local):
     pinned[...] = u0
     barrier(ws)
     t0 = time.perf_counter()
-    pde_solver(pinned, 10.0, [1.0, 1.0], F=s.F, S=s.S if args.stiff else None,
+    pde_solver(pinned, 10.0, L, F=s.F, S=s.S if args.stiff else None,
                boundaryTypes="periodic", cfl=args.cfl, order=N, ndt=1, stiff=args.stiff,
                max_steps=args.steps, device=local, warm_start=warm if args.stiff else None)
     e2e_s = allmax(ws, time.perf_counter() - t0)
@@ -387,7 +405,7 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": workload_name(args), "form": head, "cells": C, "order": N,
                    "vars": V,
                    "l2": "working set > L2 (qh alone is "
-                         f"{(n + 2) ** 2 * N ** 3 * V * 8 / 1e6:.0f} MB); no flush",
+                         f"{Cw * N ** (nd + 1) * V * 8 / 1e6:.0f} MB); no flush",
                    "parallelism": f"replicas x{ws}"},
         "forms": {k: form_summary(k) for k in forms},
         "e2e": {"value": ws * C * args.steps / e2e_s, "unit": UNIT,
@@ -433,12 +451,13 @@ def run_reference(args, ws, rank):
     t0 = time.perf_counter()
     u, _, k, _ = cpu_run(args, u, args.steps, cores)
     el = time.perf_counter() - t0
-    v = n * n * k / el
+    v = n ** args.ndim * k / el
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / k,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": workload_name(args), "form": "plain", "cells": n * n},
+            "config": {"workload": workload_name(args), "form": "plain",
+                       "cells": n ** args.ndim},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{k} whole-grid steps after {args.warmup} warm-up"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,

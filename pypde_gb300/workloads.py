@@ -55,7 +55,7 @@ def shear(n=512, seed=0):
     return u
 
 
-def relaxation(n=1024, ndim=2, seed=0, log10_tau=(-7.0, -2.0), patches=16):
+def relaxation(n=1024, ndim=2, seed=0, log10_tau=(-7.0, -2.0), patches=16, amp=0.1):
     rng = np.random.default_rng(seed)
     x = (np.arange(n) + 0.5) / n
     grids = np.meshgrid(*([x] * ndim), indexing="ij")
@@ -66,7 +66,7 @@ def relaxation(n=1024, ndim=2, seed=0, log10_tau=(-7.0, -2.0), patches=16):
         amp = rng.uniform(-1, 1) / np.sqrt(nmodes)
         ph = rng.uniform(0, 2 * np.pi)
         pert += amp * np.sin(2 * np.pi * sum(k[i] * grids[i] for i in range(ndim)) + ph)
-    rho = 1 + 0.1 * pert
+    rho = 1 + amp * pert
     V = 2 * ndim + 3
     u = np.zeros((n,) * ndim + (V,))
     u[..., 0] = rho
