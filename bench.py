@@ -321,7 +321,7 @@ def run_ours(args, ws, rank, local):
     V = 2 * nd + 3 if args.system == "cattaneo" else nd + 2
     C = n ** nd
     Cw = (n + 2) ** nd
-    L = [1.0] * nd
+    Ls = [1.0] * nd
     u0 = initial_state(args, rank)
     R = Runner(args, local)
     peak = _lib.ctypes.c_double()
@@ -334,7 +334,7 @@ def run_ours(args, ws, rank, local):
     if args.stiff:
         from pypde_gb300 import warmstart
         t0 = time.perf_counter()
-        warm = warmstart.train_warm_start(u0, 10.0, L, F=s.F, S=s.S, cfl=args.cfl,
+        warm = warmstart.train_warm_start(u0, 10.0, Ls, F=s.F, S=s.S, cfl=args.cfl,
                                           order=N, tau_var=2 * nd + 2, steps=20, per_step=16384,
                                           iters=args.train_iters, seed=rank, device=local)
         train = {"seconds": time.perf_counter() - t0, "samples": warm.samples,
@@ -392,7 +392,7 @@ def run_ours(args, ws, rank, local):
     pinned[...] = u0
     barrier(ws)
     t0 = time.perf_counter()
-    pde_solver(pinned, 10.0, L, F=s.F, S=s.S if args.stiff else None,
+    pde_solver(pinned, 10.0, Ls, F=s.F, S=s.S if args.stiff else None,
                boundaryTypes="periodic", cfl=args.cfl, order=N, ndt=1, stiff=args.stiff,
                max_steps=args.steps, device=local, warm_start=warm if args.stiff else None)
     e2e_s = allmax(ws, time.perf_counter() - t0)
