@@ -63,9 +63,9 @@ def relaxation(n=1024, ndim=2, seed=0, log10_tau=(-7.0, -2.0), patches=16, amp=0
     pert = np.zeros((n,) * ndim)
     for _ in range(nmodes):
         k = rng.integers(1, 5, ndim)
-        amp = rng.uniform(-1, 1) / np.sqrt(nmodes)
+        a_k = rng.uniform(-1, 1) / np.sqrt(nmodes)
         ph = rng.uniform(0, 2 * np.pi)
-        pert += amp * np.sin(2 * np.pi * sum(k[i] * grids[i] for i in range(ndim)) + ph)
+        pert += a_k * np.sin(2 * np.pi * sum(k[i] * grids[i] for i in range(ndim)) + ph)
     rho = 1 + amp * pert
     V = 2 * ndim + 3
     u = np.zeros((n,) * ndim + (V,))
