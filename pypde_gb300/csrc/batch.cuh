@@ -84,7 +84,7 @@ __device__ __forceinline__ void drain(const TileQueue &q, int per_pop,
 
 template <int N>
 __global__ void __launch_bounds__(128)
-    kb_weno(const BatchProblem *P, TileQueue q, int per_pop, int d, Tables T) {
+    kb_weno(const BatchProblem *P, TileQueue q, int per_pop, int d, const __grid_constant__ Tables T) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_weno_pass_body<N>(vb, b.win[d], b.wout[d], b.wn1[d], b.wmd[d], b.wn3[d],
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(128)
 
 template <class Sys, int N>
 __global__ void __launch_bounds__(128)
-    kb_cfl(const BatchProblem *P, TileQueue q, int per_pop, Tables T) {
+    kb_cfl(const BatchProblem *P, TileQueue q, int per_pop, const __grid_constant__ Tables T) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_cfl_body<Sys, N>(vb, b.w, b.g, T, b.wprod, b.st);
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(128)
 
 template <class Sys, int N>
 __global__ void kb_predictor(const BatchProblem *P, TileQueue q, int per_pop,
-                             Tables T) {
+                             const __grid_constant__ Tables T) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_predictor_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st);
@@ -112,7 +112,7 @@ __global__ void kb_predictor(const BatchProblem *P, TileQueue q, int per_pop,
 
 template <class Sys, int N>
 __global__ void kb_newton(const BatchProblem *P, TileQueue q, int per_pop,
-                          Tables T, double tol) {
+                          const __grid_constant__ Tables T, double tol) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_newton_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st, tol, 0, 0);
@@ -121,7 +121,7 @@ __global__ void kb_newton(const BatchProblem *P, TileQueue q, int per_pop,
 
 template <class Sys, int N, int FLUX>
 __global__ void __launch_bounds__(128)
-    kb_faces(const BatchProblem *P, TileQueue q, int per_pop, Tables T) {
+    kb_faces(const BatchProblem *P, TileQueue q, int per_pop, const __grid_constant__ Tables T) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_faces_body<Sys, N, FLUX>(vb, b.qh, b.contrib, b.g, T, b.fi, b.st);
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(128)
 
 template <class Sys, int N>
 __global__ void __launch_bounds__(128)
-    kb_centers(const BatchProblem *P, TileQueue q, int per_pop, Tables T) {
+    kb_centers(const BatchProblem *P, TileQueue q, int per_pop, const __grid_constant__ Tables T) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_centers_body<Sys, N>(vb, b.qh, b.cen, b.g, T, b.st);

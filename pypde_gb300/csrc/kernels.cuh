@@ -89,7 +89,7 @@ __device__ __forceinline__ int renorm_index(int ind, int N, int type,
 template <int N>
 __device__ __forceinline__ void k_weno_pass_body(VBlock vb_, const double *__restrict__ in,
                             double *__restrict__ out, long long n1, int md,
-                            long long n3, int n4, int V, Tables T,
+                            long long n3, int n4, int V, const Tables &T,
                             const DevState *st) {
   if (!step_active(st))
     return;
@@ -161,7 +161,7 @@ __device__ __forceinline__ void k_weno_pass_body(VBlock vb_, const double *__res
 template <int N>
 __global__ void k_weno_pass(const double *__restrict__ in,
                             double *__restrict__ out, long long n1, int md,
-                            long long n3, int n4, int V, Tables T,
+                            long long n3, int n4, int V, const __grid_constant__ Tables T,
                             const DevState *st) {
   k_weno_pass_body<N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, in, out, n1, md, n3, n4, V, T, st);
 }
@@ -170,7 +170,7 @@ __global__ void k_weno_pass(const double *__restrict__ in,
 // a3/a4: CFL reduction, stepper.cpp:35-76.  One thread per w-cell.
 // ---------------------------------------------------------------------
 template <class Sys, int N>
-__device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict__ w, Geom g, Tables T,
+__device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict__ w, const Geom &g, const Tables &T,
           const double *__restrict__ wprod_g, DevState *st) {
   if (!step_active(st))
     return;
@@ -235,7 +235,7 @@ __device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict_
 
 template <class Sys, int N>
 __global__ void __launch_bounds__(128)
-    k_cfl(const double *__restrict__ w, Geom g, Tables T,
+    k_cfl(const double *__restrict__ w, const __grid_constant__ Geom g, const __grid_constant__ Tables T,
           const double *__restrict__ wprod_g, DevState *st) {
   k_cfl_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, g, T, wprod_g, st);
 }
@@ -258,7 +258,7 @@ template <class Sys, int N> struct PredCfg {
 
 template <class Sys, int N>
 __device__ __forceinline__ void k_predictor_body(VBlock vb_, const double *__restrict__ w,
-                            double *__restrict__ qh, Geom g, Tables T,
+                            double *__restrict__ qh, const Geom &g, const Tables &T,
                             const double *__restrict__ wprod_g,
                             DevState *st) {
   using Cfg = PredCfg<Sys, N>;
@@ -446,7 +446,7 @@ __device__ __forceinline__ void k_predictor_body(VBlock vb_, const double *__res
 
 template <class Sys, int N>
 __global__ void k_predictor(const double *__restrict__ w,
-                            double *__restrict__ qh, Geom g, Tables T,
+                            double *__restrict__ qh, const __grid_constant__ Geom g, const __grid_constant__ Tables T,
                             const double *__restrict__ wprod_g,
                             DevState *st) {
   k_predictor_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st);
@@ -774,7 +774,7 @@ __device__ __forceinline__ int newton_fp32_sweeps(
 
 template <class Sys, int N>
 __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restrict__ w, double *__restrict__ qh,
-                         Geom g, Tables T, const double *__restrict__ wprod_g,
+                         const Geom &g, const Tables &T, const double *__restrict__ wprod_g,
                          DevState *st, double tol, int guess, int mixed) {
   using Cfg = NewtonCfg<Sys, N>;
   constexpr int V = Cfg::V, D = Cfg::D, Nd = Cfg::Nd, NT = Cfg::NT;
@@ -1128,7 +1128,7 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
 
 template <class Sys, int N>
 __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
-                         Geom g, Tables T, const double *__restrict__ wprod_g,
+                         const __grid_constant__ Geom g, const __grid_constant__ Tables T, const double *__restrict__ wprod_g,
                          DevState *st, double tol, int guess, int mixed) {
   k_newton_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st, tol, guess, mixed);
 }
@@ -1329,7 +1329,7 @@ struct FaceIndex {
 
 template <class Sys, int N, int FLUX>
 __device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restrict__ qh, double *__restrict__ contrib,
-            Geom g, Tables T, FaceIndex fi, DevState *st) {
+            const Geom &g, const Tables &T, const FaceIndex &fi, DevState *st) {
   constexpr int V = Sys::V, D = Sys::NDIM;
   constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
   if (!step_active(st))
@@ -1430,7 +1430,7 @@ __device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restric
 template <class Sys, int N, int FLUX = 0>
 __global__ void __launch_bounds__(128)
     k_faces(const double *__restrict__ qh, double *__restrict__ contrib,
-            Geom g, Tables T, FaceIndex fi, DevState *st) {
+            const __grid_constant__ Geom g, const __grid_constant__ Tables T, const __grid_constant__ FaceIndex fi, DevState *st) {
   k_faces_body<Sys, N, FLUX>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, qh, contrib, g, T, fi, st);
 }
 
@@ -1440,7 +1440,7 @@ __global__ void __launch_bounds__(128)
 // ---------------------------------------------------------------------
 template <class Sys, int N>
 __device__ __forceinline__ void k_centers_body(VBlock vb_, const double *__restrict__ qh,
-                          double *__restrict__ cen, Geom g, Tables T,
+                          double *__restrict__ cen, const Geom &g, const Tables &T,
                           DevState *st) {
   constexpr int V = Sys::V, D = Sys::NDIM;
   constexpr int Nd = IPow<N, D>::value, NT = N * Nd;
@@ -1515,7 +1515,7 @@ __device__ __forceinline__ void k_centers_body(VBlock vb_, const double *__restr
 
 template <class Sys, int N>
 __global__ void k_centers(const double *__restrict__ qh,
-                          double *__restrict__ cen, Geom g, Tables T,
+                          double *__restrict__ cen, const __grid_constant__ Geom g, const __grid_constant__ Tables T,
                           DevState *st) {
   k_centers_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, qh, cen, g, T, st);
 }
@@ -1530,8 +1530,8 @@ __global__ void k_centers(const double *__restrict__ qh,
 // ---------------------------------------------------------------------
 template <class Sys, int N>
 __device__ __forceinline__ void k_gather_body(VBlock vb_, double *__restrict__ u, const double *__restrict__ cen,
-                         const double *__restrict__ contrib, Geom g,
-                         FaceIndex fi, int use_centers, int use_faces,
+                         const double *__restrict__ contrib, const Geom &g,
+                         const FaceIndex &fi, int use_centers, int use_faces,
                          DevState *st) {
   constexpr int V = Sys::V, D = Sys::NDIM;
   constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
@@ -1598,8 +1598,8 @@ __device__ __forceinline__ void k_gather_body(VBlock vb_, double *__restrict__ u
 
 template <class Sys, int N>
 __global__ void k_gather(double *__restrict__ u, const double *__restrict__ cen,
-                         const double *__restrict__ contrib, Geom g,
-                         FaceIndex fi, int use_centers, int use_faces,
+                         const double *__restrict__ contrib, const __grid_constant__ Geom g,
+                         const __grid_constant__ FaceIndex fi, int use_centers, int use_faces,
                          DevState *st) {
   k_gather_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, u, cen, contrib, g, fi, use_centers, use_faces, st);
 }

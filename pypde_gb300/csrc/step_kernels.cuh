@@ -7,7 +7,7 @@
 namespace pypde {
 
 __device__ __forceinline__ void k_boundaries_body(VBlock vb_, const double *__restrict__ u,
-                             double *__restrict__ ub, Geom g, int N, int V,
+                             double *__restrict__ ub, const Geom &g, int N, int V,
                              const DevState *st) {
   if (!step_active(st))
     return;
@@ -28,7 +28,7 @@ __device__ __forceinline__ void k_boundaries_body(VBlock vb_, const double *__re
 }
 
 __global__ void k_boundaries(const double *__restrict__ u,
-                             double *__restrict__ ub, Geom g, int N, int V,
+                             double *__restrict__ ub, const __grid_constant__ Geom g, int N, int V,
                              const DevState *st) {
   k_boundaries_body(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, u, ub, g, N, V, st);
 }
