@@ -652,10 +652,13 @@ __device__ __forceinline__ int newton_fp32_sweeps(
              !(res <= 0.5f * last32[lc]) || res >= 3.0e38f;
       if (!stop && !lu32[lc]) {
         // row block t of A: the FD Jacobian of S in FP32
-        float *qn = q32 + node * V;
-        float s0[V], s1[V];
+        float qn[V], s0[V], s1[V];
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          qn[v] = q32[node * V + v];
         if (Sys::HAS_S)
           Sys::S(s0, qn);
+#pragma unroll
         for (int wv = 0; wv < V; wv++) {
           float ih = 0.0f;
           if (Sys::HAS_S) {
@@ -984,10 +987,16 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
       } else if (!conv && refresh) {
         // row block t of A for spatial node idx: the FD Jacobian of S
         double *A = s_A + ((lc * Nd) + idx) * NL * NL;
-        double *qn = q + node * V;
-        double s0[V], s1[V];
+        // the node's state in registers and the column loop unrolled: each
+        // column's perturbed variable is a constant, so the parts of S that
+        // do not depend on it are computed once
+        double qn[V], s0[V], s1[V];
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          qn[v] = q[node * V + v];
         if (Sys::HAS_S)
           Sys::S(s0, qn);
+#pragma unroll
         for (int wv = 0; wv < V; wv++) {
           double ih = 0.0;
           if (Sys::HAS_S) {
