@@ -345,9 +345,15 @@ __device__ __forceinline__ void k_predictor_body(VBlock vb_, const double *__res
         }
       }
       if (Sys::HAS_F) {
+        // the node's state in registers: the parts of F shared by the D
+        // directions (pressure, temperature, ...) are computed once
+        double qr[V];
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          qr[v] = q0[node * V + v];
 #pragma unroll
         for (int d = 0; d < D; d++)
-          Sys::F(ff + (node * D + d) * V, q0 + node * V, dq, d);
+          Sys::F(ff + (node * D + d) * V, qr, dq, d);
       }
     }
     __syncthreads();
@@ -574,9 +580,13 @@ __device__ __forceinline__ int newton_fp32_sweeps(
         }
       }
       if (Sys::HAS_F) {
+        float qr[V];
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          qr[v] = q32[node * V + v];
 #pragma unroll
         for (int d = 0; d < D; d++)
-          Sys::F(f32 + (node * D + d) * V, q32 + node * V, dq, d);
+          Sys::F(f32 + (node * D + d) * V, qr, dq, d);
       }
     }
     __syncthreads();
@@ -892,9 +902,15 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
         }
       }
       if (Sys::HAS_F) {
+        // the node's state in registers: the parts of F shared by the D
+        // directions (pressure, temperature, ...) are computed once
+        double qr[V];
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          qr[v] = q[node * V + v];
 #pragma unroll
         for (int d = 0; d < D; d++)
-          Sys::F(ff + (node * D + d) * V, q + node * V, dq, d);
+          Sys::F(ff + (node * D + d) * V, qr, dq, d);
       }
     }
     __syncthreads();
