@@ -82,3 +82,33 @@ def test_untranslatable_callback_is_rejected():
     from pypde_gb300.translate import TranslateError
     with pytest.raises(TranslateError, match="untranslatable_flux"):
         pde_solver(np.ones((8, 3)), 0.1, [1.0], F=untranslatable_flux, stiff=False)
+
+
+def test_batch_arguments_checked_before_device_work():
+    """pde_solver_batch validates every problem on the host: a bad order, a
+    periodic axis shorter than the order, or mismatched shapes fail with
+    PYPDE_ERR_ARG (or a Python error) before any device call."""
+    from pypde_gb300 import _lib, systems
+    from pypde_gb300.solvers import pde_solver_batch
+    s = systems.cattaneo(2)
+    good = {"Q0": np.ones((8, 8, 7)), "tf": 0.1, "L": [1.0, 1.0], "order": 2}
+    with pytest.raises(_lib.PyPDEError) as e:
+        pde_solver_batch([good, dict(good, Q0=np.ones((8, 8, 7)), order=0)], F=s.F, S=s.S)
+    assert e.value.code == _lib.PYPDE_ERR_ARG
+    with pytest.raises(_lib.PyPDEError) as e:
+        pde_solver_batch([dict(good, Q0=np.ones((1, 8, 7)), boundaryTypes="periodic")],
+                         F=s.F, S=s.S)
+    assert e.value.code == _lib.PYPDE_ERR_ARG
+    with pytest.raises(ValueError):
+        pde_solver_batch([good, dict(good, Q0=np.ones((8, 8, 4)))], F=s.F, S=s.S)
+    with pytest.raises(ValueError):
+        pde_solver_batch([], F=s.F, S=s.S)
+
+
+def test_empty_grid_rejected_before_device_work():
+    from pypde_gb300 import _lib, systems
+    from pypde_gb300.solvers import pde_solver
+    s = systems.euler(1)
+    with pytest.raises(_lib.PyPDEError) as e:
+        pde_solver(np.ones((0, 3)), 0.1, [1.0], F=s.F, stiff=False)
+    assert e.value.code == _lib.PYPDE_ERR_ARG
