@@ -878,7 +878,7 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
     return e;
   const unsigned pb = (unsigned)((c.np + 127) / 128);
   kb_step_begin<<<pb, 128, 0, s>>>(c.dPall, c.np);
-  auto stage = [&](size_t gi, int st, int extra, void *x0, void *x1,
+  auto stage = [&](size_t gi, int st, void *x0, void *x1,
                    void *x2) -> cudaError_t {
     BatchGroup &g = c.G[gi];
     if (g.tiles[st] == 0)
@@ -895,7 +895,6 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
     }
     void *args[8] = {(void *)&g.dP, (void *)&q, (void *)&pp, x0, x1, x2,
                      nullptr, nullptr};
-    (void)extra;
     if (ev)
       cudaEventRecord(ev[(gi * BS_COUNT + st) * 2], s);
     cudaError_t r = launch(g.fn[st], dim3(grid), dim3(g.threads[st]),
@@ -906,31 +905,31 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
   };
   for (size_t gi = 0; gi < c.G.size(); gi++) {
     BatchGroup &g = c.G[gi];
-    if ((e = stage(gi, BS_BOUNDARIES, 0, nullptr, nullptr, nullptr)))
+    if ((e = stage(gi, BS_BOUNDARIES, nullptr, nullptr, nullptr)))
       return e;
     for (int d = 0; d < c.ndim; d++) {
       int dd = d;
-      if ((e = stage(gi, BS_WENO0 + d, 0, (void *)&dd, (void *)&g.T,
+      if ((e = stage(gi, BS_WENO0 + d, (void *)&dd, (void *)&g.T,
                      nullptr)))
         return e;
     }
-    if ((e = stage(gi, BS_CFL, 0, (void *)&g.T, nullptr, nullptr)))
+    if ((e = stage(gi, BS_CFL, (void *)&g.T, nullptr, nullptr)))
       return e;
   }
   kb_dt<<<pb, 128, 0, s>>>(c.dPall, c.np);
   for (size_t gi = 0; gi < c.G.size(); gi++) {
     BatchGroup &g = c.G[gi];
     double tol = c.tol;
-    if ((e = stage(gi, BS_PREDICTOR, 0, (void *)&g.T,
+    if ((e = stage(gi, BS_PREDICTOR, (void *)&g.T,
                    c.stiff ? (void *)&tol : nullptr, nullptr)))
       return e;
-    if (c.faces && (e = stage(gi, BS_FACES, 0, (void *)&g.T, nullptr, nullptr)))
+    if (c.faces && (e = stage(gi, BS_FACES, (void *)&g.T, nullptr, nullptr)))
       return e;
     if (c.centers &&
-        (e = stage(gi, BS_CENTERS, 0, (void *)&g.T, nullptr, nullptr)))
+        (e = stage(gi, BS_CENTERS, (void *)&g.T, nullptr, nullptr)))
       return e;
     int uc = c.centers ? 1 : 0, uf = c.faces ? 1 : 0;
-    if ((e = stage(gi, BS_GATHER, 0, (void *)&uc, (void *)&uf, nullptr)))
+    if ((e = stage(gi, BS_GATHER, (void *)&uc, (void *)&uf, nullptr)))
       return e;
   }
   kb_step_end<<<pb, 128, 0, s>>>(c.dPall, c.np);
