@@ -5,7 +5,7 @@ linked into one shared library with the CUDA runtime linked statically, so
 that the library loads (and reports errors) on a machine without a GPU
 driver.  Kernels are compiled with --fmad=false: the plain FP64 form is
 bit-faithful to the host restatement of the reference algorithm, which
-never contracts a multiply and an add.
+fuses a multiply and an add only where both sides call fma() explicitly.
 """
 import os
 import shutil

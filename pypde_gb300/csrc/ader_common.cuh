@@ -6,7 +6,9 @@
 // reference's Eigen expressions as the reference build evaluates them
 // (cited per function; paths relative to haranjackson/PyPDE), and the
 // translation units are compiled with --fmad=false so that no multiply-add
-// is contracted.  This matters more than usual here: the Rusanov and CFL
+// is contracted implicitly; the fused multiply-adds that are used are
+// explicit fma() calls, the same ones in the host restatement.  This
+// matters more than usual here: the Rusanov and CFL
 // eigenvalues come from a forward-difference Jacobian with step
 // h = 2^-26 max(|q|, 1) (src/eigs/NumericalDiff.h:6-44), which turns any
 // last-bit change of its input state into a ~1e-8 relative change of the

@@ -10,8 +10,8 @@
 // systems compiled at run time (NVRTC) provide the same struct.
 //
 // Formulas and operation order match the host test callbacks, so host and
-// device produce the same bits (the kernels are compiled without FMA
-// contraction):
+// device produce the same bits (the kernels are compiled without implicit
+// FMA contraction, and the callbacks use no fma()):
 //   Euler<D>     V = D+2   (rho, m_0..m_{D-1}, E), gamma = 1.4
 //   Cattaneo<D>  V = 2D+3  Euler + relaxing heat flux q + passive
 //                s = log10(tau); T = p/rho; F_d adds q_d to the energy flux

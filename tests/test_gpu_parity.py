@@ -2,7 +2,8 @@
 golden vectors, through the C ABI.
 
 The plain FP64 form is built to be bit-identical to the restatement: same
-algorithms, same summation orders, no contracted multiply-adds.  So every
+algorithms, same summation orders, the same explicit fma() calls and no
+implicit contraction on either side.  So every
 stage is compared for exact equality, and full runs must agree to well
 inside the 1e-10 relative L1 bar (they are expected to agree exactly).
 """
