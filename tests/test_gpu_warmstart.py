@@ -154,7 +154,8 @@ def test_trained_warm_start_end_to_end(gpu_lib):
     Newton iterations are measured against the plain run and written to
     the test output: on this problem Newton contracts by about 1e-2 per
     sweep, so a guess must be ~1e-4 accurate per cell to save a sweep,
-    and the BF16 network's (a few per cent) saves close to none -- the
+    and the BF16 network's (median 6-25% per cell, heavy tail) saves close
+    to none -- the
     bound checked is that it costs at most 10% more."""
     n, N, K = 48, 2, 30
     u0 = workloads.relaxation(n, 2, seed=11, patches=4)
