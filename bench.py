@@ -434,9 +434,9 @@ def run_ours(args, ws, rank, local):
     }
     if train:
         out["training"] = train
-    if args.stiff and args.batch_problems > 0:
+    if args.stiff and args.batch_problems > 0 and ws == 1:
         out["batched_workload"] = run_batched(args, local)
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu:
         v, cores, sample = cpu_baseline(args, u0, args.cpu_seconds)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                "sample": sample}
