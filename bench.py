@@ -258,7 +258,8 @@ class Runner:
 
 def measure_form(R, args, ws, u0, warm=None, mixed=False):
     """W warm-up steps, then exactly K timed steps (CUDA events inside the
-    library), then an eagerly launched profile of min(K, 5) steps."""
+    library), then an eagerly launched profile of min(K, 5) steps from the
+    same state as the timed steps."""
     u = u0.copy()
     R.run(u, args.warmup, warm=warm, mixed=mixed)
     u_warm = u.copy()
@@ -267,7 +268,7 @@ def measure_form(R, args, ws, u0, warm=None, mixed=False):
     barrier(ws)
     sec = allmax(ws, st["device_seconds"])
     ksteps = max(1, min(args.steps, 5))
-    sp = R.run(u0.copy(), ksteps, profile=True, warm=warm, mixed=mixed)
+    sp = R.run(u_warm.copy(), ksteps, profile=True, warm=warm, mixed=mixed)
     return st, sec, sp, ksteps, u_warm
 
 
@@ -423,9 +424,11 @@ def run_ours(args, ws, rank, local):
                      "peak_source": "FP64 FMA loop measured by this run "
                                     "(MEASURED_PEAKS.json has no FP64 figure)",
                      "flops_per_launch": fpts * fpf, "launch_ms": 1e3 * faces_launch,
-                     "note": "algorithmic flops count max|eig| as the nominal 10 V^3 of a "
-                             "Hessenberg + Francis QR; the kernel's mixed-precision "
-                             "eigensolver does less FP64 work than that"},
+                     "note": "algorithmic flops count max|eig| as the nominal 10 m^3 of a "
+                             "Hessenberg + Francis QR of the m x m active block of the flux "
+                             "Jacobian (m = V, or V minus the system's passive variables); "
+                             "the kernel's mixed-precision eigensolver does less FP64 work "
+                             "than that"},
         "stage_ms_per_step": {k: 1e3 * v / ksteps for k, v in stage_s.items()},
         "step_fp64_tflops": sum(flops.values()) / (sec / args.steps) / 1e12,
         "predictor_iters_per_cell": its,

@@ -13,10 +13,12 @@
  * behaviour the reference leaves undefined:
  *  - WENO and DG linear systems use precomputed inverses instead of a
  *    ColPivHouseholderQR solve per call (weno.cpp:28, dg.cpp:192).
- *  - max|eig| uses a Hessenberg + Francis double-shift QR for every V, where
- *    the reference uses Eigen::EigenSolver for V<6 and Spectra Arnoldi with
- *    ncv=V for V>=6 (eigs/system.cpp:28-43); both return the exact spectrum
- *    of the same FD Jacobian up to rounding.
+ *  - max|eig| uses FP32 Hessenberg + Francis double-shift QR candidates
+ *    refined in FP64 for every V (on the active block where a system
+ *    declares passive variables), where the reference uses
+ *    Eigen::EigenSolver for V<6 and Spectra Arnoldi with ncv=V for V>=6
+ *    (eigs/system.cpp:28-43); all return the spectrum of the same FD
+ *    Jacobian up to rounding.
  *  - stiff=True: the reference's Newton-Krylov (scipy/algos, tolerance 6e-6
  *    absolute) is replaced by the per-cell locally implicit Newton iteration
  *    of the GPU form (Newton on the source terms, fixed point on the fluxes)
@@ -1338,11 +1340,54 @@ static void system_matrix(const ctx_t *c, double *M, double *q, double *dq,
   }
 }
 
+/* max |eigenvalue| of the system matrix M in direction d (destroyed).
+ * Where the system declares its passive variables (ora_system_eig_active)
+ * and their rows and columns of M are zero off the diagonal (checked),
+ * each carries the eigenvalue M_ii and the rest of the spectrum is that of
+ * the active block: the permutation step of Parlett and Reinsch's
+ * balancing (Numer. Math. 13, 1969) with the permutation known in advance.
+ * Otherwise, or if a passive diagonal entry is not finite, the full
+ * matrix.  Exact up to the rounding of the eigenvalue solver, which then
+ * runs on the smaller block. */
+static double max_abs_eig_sys(const ctx_t *c, double *M, int d) {
+  const int V = c->V;
+  int act[ORA_MAXV];
+  const int m = c->F ? ora_system_eig_active(c->F, c->ndim, d, act) : 0;
+  if (m > 0 && m < V) {
+    int is_act[ORA_MAXV] = {0};
+    for (int k = 0; k < m; k++)
+      is_act[act[k]] = 1;
+    int ok = 1;
+    double iso = 0.0;
+    for (int i = 0; i < V; i++) {
+      if (is_act[i])
+        continue;
+      for (int j = 0; j < V; j++)
+        if (j != i && (M[i * V + j] != 0.0 || M[j * V + i] != 0.0))
+          ok = 0;
+      const double di = fabs(M[i * V + i]);
+      if (!(di <= DBL_MAX))
+        ok = 0;
+      else if (di > iso)
+        iso = di;
+    }
+    if (ok) {
+      double S[ORA_MAXV * ORA_MAXV];
+      for (int r = 0; r < m; r++)
+        for (int k = 0; k < m; k++)
+          S[r * m + k] = M[act[r] * V + act[k]];
+      const double r = ora_max_abs_eig(S, m);
+      return (r < iso) ? iso : r;
+    }
+  }
+  return ora_max_abs_eig(M, V);
+}
+
 static double max_abs_eigs(const ctx_t *c, double *q, double *dq, int d,
                            double *f0) {
   double M[ORA_MAXV * ORA_MAXV];
   system_matrix(c, M, q, dq, d, f0);
-  return ora_max_abs_eig(M, c->V);
+  return max_abs_eig_sys(c, M, d);
 }
 
 static double max_abs_eigs_2nd(const ctx_t *c, double *q, double *dq, int d) {
@@ -2256,7 +2301,7 @@ double ora_system_max_abs_eigs(ora_flux_fn F, ora_ncp_fn B, int ndim, int V,
   system_matrix(c, M, q, dq, d, NULL);
   double Mc[ORA_MAXV * ORA_MAXV];
   memcpy(Mc, M, sizeof(double) * V * V);
-  double r = ora_max_abs_eig(Mc, V);
+  double r = max_abs_eig_sys(c, Mc, d);
   free(c);
   return r;
 }

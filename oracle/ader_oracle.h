@@ -28,6 +28,9 @@ typedef void (*ora_src_fn)(double *out, double *Q);
 #define ORA_MAXV 24
 
 /* Built-in test systems (oracle_systems.c).  Returns 0 on success. */
+/* Active (transported) variables of a test system's flux in direction d:
+ * their count (0 if the system declares none) and indices in idx. */
+int ora_system_eig_active(ora_flux_fn F, int ndim, int d, int *idx);
 int ora_system_lookup(const char *name, int ndim, int *V, ora_flux_fn *F,
                       ora_ncp_fn *B, ora_src_fn *S, int *secondOrder);
 

@@ -131,6 +131,21 @@ static void burgers2_F(double *out, double *Q, double *dQ, int d) {
   out[0] = NCP_A[d] * (0.5 * Q[0] * Q[0]) - 0.01 * dQ[d];
 }
 
+/* The variables that the flux in direction d transports, for a system
+ * that declares them (the device systems' EIG_ACTIVE / eig_active): fills
+ * idx (ascending) and returns their count, or 0.  cattaneo: rho, the
+ * momenta, E and q_d; the other heat-flux components and log tau are
+ * passive. */
+int ora_system_eig_active(ora_flux_fn F, int ndim, int d, int *idx) {
+  if (F == cattaneo_F) {
+    for (int k = 0; k < ndim + 2; k++)
+      idx[k] = k;
+    idx[ndim + 2] = ndim + 2 + d;
+    return ndim + 3;
+  }
+  return 0;
+}
+
 int ora_system_lookup(const char *name, int ndim, int *V, ora_flux_fn *F,
                       ora_ncp_fn *B, ora_src_fn *S, int *secondOrder) {
   if (ndim < 1 || ndim > 3)

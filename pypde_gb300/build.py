@@ -18,6 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpypde_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+ORDERS = (1, 2, 3)  # orders of the ahead-of-time kernels (MAXN in runtime.h)
 
 
 def nvcc():
@@ -50,17 +51,24 @@ def build(verbose=False, jobs=None):
     objs = []
     for f in sources():
         src = os.path.join(CSRC, f)
-        obj = os.path.join(OBJ, f + ".o")
-        objs.append(obj)
-        if _needs(obj, [src] + headers + [__file__]):
-            cmds.append([nv, *flags, "-x", "cu", "-c", src, "-o", obj])
+        # an instantiation unit is compiled once per order, so that the
+        # (system, order) pairs compile in parallel
+        variants = ([(f"{f}.n{n}.o", [f"-DPYPDE_ORDER={n}"]) for n in ORDERS]
+                    if f.startswith("inst_") else [(f + ".o", [])])
+        for oname, extra in variants:
+            obj = os.path.join(OBJ, oname)
+            objs.append(obj)
+            if _needs(obj, [src] + headers + [__file__]):
+                cmds.append([nv, *flags, *extra, "-x", "cu", "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
 
     failed = []
-    with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
+    # the longest units first, so that they do not finish last
+    cmds.sort(key=lambda c: ("inst_cattaneo" not in c[-3], "-DPYPDE_ORDER=3" not in c))
+    with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         for cmd, r in ex.map(run, cmds):
             if verbose or r.returncode:
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

@@ -650,6 +650,69 @@ __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
   }
 }
 
+// A system that declares EIG_ACTIVE and eig_active(d, k) names, for each
+// direction d, the EIG_ACTIVE variables that its flux in direction d
+// transports (k = 0 .. EIG_ACTIVE-1, ascending); the others are passive:
+// no flux component depends on them and their own flux is constant.
+template <class...> using void_t_ = void;
+template <class S, class = void> struct HasEigActive {
+  static constexpr bool value = false;
+};
+template <class S>
+struct HasEigActive<S, void_t_<decltype(S::EIG_ACTIVE)>> {
+  static constexpr bool value = true;
+};
+
+// max |eigenvalue| of the system matrix M in direction d (destroyed).
+// Where the system declares its passive variables and their rows and
+// columns of M are zero off the diagonal (checked), each carries the
+// eigenvalue M_ii, and the rest of the spectrum is that of the active
+// block (the permutation step of Parlett and Reinsch's balancing, Numer.
+// Math. 13, 1969, with the permutation known in advance): max|eig| is
+// taken over the active block and the passive diagonal.  The block has the
+// same size for every matrix of the system, so all threads run the same
+// solver.  Otherwise, or if a passive diagonal entry is not finite, the
+// full matrix.  Same steps as the host restatement.
+template <class Sys>
+__device__ __forceinline__ double max_abs_eig_sys(double *M, int d) {
+  constexpr int V = Sys::V;
+  if constexpr (HasEigActive<Sys>::value) {
+    constexpr int MA = Sys::EIG_ACTIVE;
+    static_assert(MA >= 1 && MA < V, "EIG_ACTIVE out of range");
+    unsigned active = 0;
+#pragma unroll
+    for (int k = 0; k < MA; k++)
+      active |= 1u << Sys::eig_active(d, k);
+    bool ok = true;
+    double iso = 0.0;
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+      if (active >> i & 1u)
+        continue;
+#pragma unroll
+      for (int j = 0; j < V; j++)
+        if (j != i && (M[i * V + j] != 0.0 || M[j * V + i] != 0.0))
+          ok = false;
+      const double di = fabs(M[i * V + i]);
+      if (!(di <= DBL_MAX_VAL))
+        ok = false;
+      else if (di > iso)
+        iso = di;
+    }
+    if (ok) {
+      double S[MA * MA];
+#pragma unroll
+      for (int r = 0; r < MA; r++)
+#pragma unroll
+        for (int c = 0; c < MA; c++)
+          S[r * MA + c] = M[Sys::eig_active(d, r) * V + Sys::eig_active(d, c)];
+      const double r = max_abs_eig<MA>(S);
+      return (r < iso) ? iso : r;
+    }
+  }
+  return max_abs_eig<V>(M);
+}
+
 // system_matrix + max|eig| (src/eigs/system.cpp:6-51)
 template <class Sys>
 __device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d,
@@ -667,7 +730,7 @@ __device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d,
     for (int i = 0; i < V * V; i++)
       M[i] += b[i];
   }
-  return max_abs_eig<V>(M);
+  return max_abs_eig_sys<Sys>(M, d);
 }
 
 // The FD Jacobian + B itself (src/eigs/system.cpp:6-26).

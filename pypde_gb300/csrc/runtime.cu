@@ -39,7 +39,20 @@ static std::vector<SystemDesc> &builtins() {
   static std::vector<SystemDesc> v;
   return v;
 }
-void register_builtin(const SystemDesc &d) { builtins().push_back(d); }
+// Each instantiation unit registers one (system, order); the orders of a
+// system are merged into one description.
+void register_builtin(const SystemDesc &d) {
+  for (auto &e : builtins())
+    if (e.name == d.name && e.ndim == d.ndim) {
+      for (int n = 0; n <= MAXN; n++)
+        if (d.have[n]) {
+          e.sets[n] = d.sets[n];
+          e.have[n] = true;
+        }
+      return;
+    }
+  builtins().push_back(d);
+}
 const SystemDesc *find_builtin(const std::string &name, int ndim) {
   for (auto &d : builtins())
     if (d.name == name && d.ndim == ndim)
@@ -79,8 +92,11 @@ static cudaError_t launch(const KFunc &f, dim3 grid, dim3 block, size_t smem,
   return r == 0 ? cudaSuccess : cudaErrorLaunchFailure;
 }
 
+// Opts the kernel in to `bytes` of dynamic shared memory.  Set whenever the
+// kernel uses any: the 48 KB default covers static plus dynamic shared
+// memory, and the static part is only known after the device link.
 static cudaError_t set_smem(const KFunc &f, size_t bytes) {
-  if (bytes <= 48 * 1024)
+  if (bytes == 0)
     return cudaSuccess;
   if (f.aot)
     return cudaFuncSetAttribute(f.aot,

@@ -46,7 +46,8 @@ struct SystemDesc {
   void *module = nullptr; // CUmodule of a run-time compiled system
 };
 
-// Built-in systems, registered by the instantiation units.
+// Built-in systems, registered by the instantiation units (one order per
+// unit, merged by name and dimension).
 void register_builtin(const SystemDesc &d);
 const SystemDesc *find_builtin(const std::string &name, int ndim);
 

@@ -81,6 +81,12 @@ template <int D> struct Euler {
 
 template <int D> struct Cattaneo {
   static constexpr int V = 2 * D + 3, NDIM = D;
+  // the flux in direction d transports rho, the momenta, E and q_d; the
+  // other heat-flux components and log tau are passive
+  static constexpr int EIG_ACTIVE = D + 3;
+  static __host__ __device__ constexpr int eig_active(int d, int k) {
+    return k < D + 2 ? k : D + 2 + d;
+  }
   static constexpr bool HAS_F = true, HAS_B = false, HAS_S = true;
   static constexpr bool SECOND_ORDER = false, HAS_FP32 = true;
   template <class T>

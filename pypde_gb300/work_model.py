@@ -3,8 +3,11 @@
 The counts follow the reference algorithm (haranjackson/PyPDE src/), not
 this implementation: they are what `roofline.achieved` divides by kernel
 time.  Flops count +, -, *, / and sqrt as one each; a callback counts the
-operations of its formula (F_FLOPS); max|eig| of a V x V matrix counts the
-nominal 10 V^3 of a Hessenberg reduction plus Francis QR.
+operations of its formula (F_FLOPS); max|eig| counts the nominal 10 m^3 of
+a Hessenberg reduction plus Francis QR of the m x m block that carries the
+spectrum: m = V, or the active block of a system whose passive variables
+have zero rows and columns (their eigenvalues are isolated by a
+permutation, exactly, as in LAPACK's balancing).
 
 Units:
   face point   one (face, time node, transverse node) of fv.cpp:144-196
@@ -39,11 +42,19 @@ def eig_flops(V):
     return 10 * V ** 3
 
 
+def eig_active(system, ndim, V):
+    """Size of the block of the flux Jacobian that carries its spectrum:
+    cattaneo transports rho, the momenta, E and q_d in direction d; the
+    other heat-flux components and log tau are passive."""
+    return ndim + 3 if system == "cattaneo" else V
+
+
 def max_abs_eigs_flops(system, ndim, V):
     """FD Jacobian (V+1 callbacks, V columns of V differences and V
-    divisions, step h) + B + max|eig| (src/eigs/system.cpp:6-51)."""
+    divisions, step h) + B + max|eig| of the active block
+    (src/eigs/system.cpp:6-51)."""
     jac = (V + 1) * f_flops(system, ndim) + V * (2 + 2 * V)
-    return jac + (V * V if b_flops(system) else 0) + eig_flops(V)
+    return jac + (V * V if b_flops(system) else 0) + eig_flops(eig_active(system, ndim, V))
 
 
 def face_point_flops(system, ndim, V, N):

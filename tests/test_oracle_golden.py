@@ -113,6 +113,42 @@ def test_eigen_solver_against_numpy():
             assert abs(got - want) <= 1e-12 * max(1.0, want)
 
 
+def test_eigen_passive_block():
+    """The relaxation system's passive variables (the heat-flux components
+    other than q_d, and log tau) have zero rows and columns in the flux
+    Jacobian of direction d; max|eig| over the active block equals numpy's
+    over the full matrix, in 2-D and 3-D, including states with zero
+    velocity (more exact zeros in the active block)."""
+    import ctypes
+    lib = ora.port()
+    lib.ora_system_max_abs_eigs.restype = ctypes.c_double
+    lib.ora_system_max_abs_eigs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_int, ora.dp, ora.dp, ctypes.c_int, ora.dp]
+    rng = np.random.default_rng(11)
+    for ndim in (2, 3):
+        s = ora.PortSystem("cattaneo", ndim)
+        V = s.V
+        for trial in range(40):
+            q = np.zeros(V)
+            q[0] = 1.0 + 0.5 * rng.random()
+            if trial % 4:
+                q[1:ndim + 1] = 0.3 * rng.standard_normal(ndim)
+            q[ndim + 1] = 2.5 + rng.random() + 0.5 * q[0] * np.sum((q[1:ndim + 1] / q[0]) ** 2)
+            q[ndim + 2:2 * ndim + 2] = 0.1 * rng.standard_normal(ndim)
+            q[2 * ndim + 2] = -rng.uniform(2, 7)
+            dq = np.zeros(ndim * V)
+            for d in range(ndim):
+                M = np.zeros(V * V)
+                got = lib.ora_system_max_abs_eigs(s.F, s.B, ndim, V, ora.ptr(q.copy()),
+                                                  ora.ptr(dq), d, ora.ptr(M))
+                M = M.reshape(V, V)
+                passive = [i for i in range(ndim + 2, 2 * ndim + 3) if i != ndim + 2 + d]
+                for i in passive:
+                    assert not np.any(np.delete(M[i], i)) and not np.any(np.delete(M[:, i], i))
+                want = np.abs(np.linalg.eigvals(M)).max()
+                assert abs(got - want) <= 1e-12 * max(1.0, want), (ndim, trial, d)
+
+
 def test_slab_count_invariance():
     """The reference's x-slab threading is bit-invariant (iterator.cpp:68-84);
     so is the port's."""
