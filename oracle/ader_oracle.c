@@ -1383,8 +1383,60 @@ static double max_abs_eig_sys(const ctx_t *c, double *M, int d) {
   return ora_max_abs_eig(M, V);
 }
 
+/* The FD Jacobian of F restricted to the active block of a system with
+ * passive variables and no B: only the m active columns are evaluated (no
+ * flux component depends on a passive variable), each entry exactly as
+ * fd_jacobian computes it, into the m x m block S.  The passive rows of
+ * those columns must come out zero (constant flux); returns 0 if one does
+ * not. */
+static int fd_jacobian_active(const ctx_t *c, double *S, const int *act, int m,
+                              double *q, double *dq, int d, double *f0) {
+  const int V = c->V;
+  int pos[ORA_MAXV];
+  for (int r = 0; r < V; r++)
+    pos[r] = -1;
+  for (int k = 0; k < m; k++)
+    pos[act[k]] = k;
+  double v1[ORA_MAXV], v2[ORA_MAXV];
+  c->F(v1, q, dq, d);
+  if (f0)
+    for (int r = 0; r < V; r++)
+      f0[r] = v1[r];
+  int ok = 1;
+  for (int k = 0; k < m; k++) {
+    const int i = act[k];
+    const double qi0 = q[i];
+    const double h = fmax(SQRT_EPS * fabs(qi0), SQRT_EPS);
+    q[i] += h;
+    c->F(v2, q, dq, d);
+    q[i] = qi0;
+    const double ih = 1.0 / h;
+    for (int r = 0; r < V; r++) {
+      const double jr = (v2[r] - v1[r]) * ih;
+      if (pos[r] >= 0)
+        S[pos[r] * m + k] = jr;
+      else if (jr != 0.0)
+        ok = 0;
+    }
+  }
+  return ok;
+}
+
+/* system_matrix + max|eig| (system.cpp:6-51).  For a system with passive
+ * variables and no B the Jacobian is built on the active block directly;
+ * its passive eigenvalues are zero (constant flux).  If a passive row is
+ * not zero, the full matrix path decides. */
 static double max_abs_eigs(const ctx_t *c, double *q, double *dq, int d,
                            double *f0) {
+  if (c->F && !c->B) {
+    int act[ORA_MAXV];
+    const int m = ora_system_eig_active(c->F, c->ndim, d, act);
+    if (m > 0 && m < c->V) {
+      double S[ORA_MAXV * ORA_MAXV];
+      if (fd_jacobian_active(c, S, act, m, q, dq, d, f0))
+        return ora_max_abs_eig(S, m);
+    }
+  }
   double M[ORA_MAXV * ORA_MAXV];
   system_matrix(c, M, q, dq, d, f0);
   return max_abs_eig_sys(c, M, d);

@@ -713,11 +713,63 @@ __device__ __forceinline__ double max_abs_eig_sys(double *M, int d) {
   return max_abs_eig<V>(M);
 }
 
-// system_matrix + max|eig| (src/eigs/system.cpp:6-51)
+// The FD Jacobian of F restricted to the active block, for a system that
+// declares its passive variables (no B): only the active columns are
+// evaluated (no flux component depends on a passive variable), each entry
+// exactly as fd_jacobian computes it, into the EIG_ACTIVE x EIG_ACTIVE
+// block S.  The passive rows of those columns must come out zero (their
+// flux is constant); returns false if one does not.
+template <class Sys>
+__device__ __forceinline__ bool fd_jacobian_active(double *S, double *q,
+                                                   double *dq, int d,
+                                                   double *f0) {
+  constexpr int V = Sys::V, MA = Sys::EIG_ACTIVE;
+  unsigned active = 0;
+#pragma unroll
+  for (int k = 0; k < MA; k++)
+    active |= 1u << Sys::eig_active(d, k);
+  double v1[V], v2[V];
+  Sys::F(v1, q, dq, d);
+  if (f0)
+#pragma unroll
+    for (int r = 0; r < V; r++)
+      f0[r] = v1[r];
+  bool ok = true;
+  for (int k = 0; k < MA; k++) {
+    const int i = Sys::eig_active(d, k);
+    const double qi0 = q[i];
+    const double h = fmax(SQRT_EPS * fabs(qi0), SQRT_EPS);
+    q[i] += h;
+    Sys::F(v2, q, dq, d);
+    q[i] = qi0;
+    const double ih = 1.0 / h;
+    int rk = 0;
+#pragma unroll
+    for (int r = 0; r < V; r++) {
+      const double jr = (v2[r] - v1[r]) * ih;
+      if (active >> r & 1u)
+        S[(rk++) * MA + k] = jr;
+      else if (jr != 0.0)
+        ok = false;
+    }
+  }
+  return ok;
+}
+
+// system_matrix + max|eig| (src/eigs/system.cpp:6-51).  For a system with
+// passive variables and no B, the Jacobian is built on the active block
+// directly; its passive eigenvalues are zero (constant flux).  If a
+// passive row is not zero, the full matrix path below decides.
 template <class Sys>
 __device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d,
                                                double *f0 = nullptr) {
   constexpr int V = Sys::V;
+  if constexpr (HasEigActive<Sys>::value && Sys::HAS_F && !Sys::HAS_B) {
+    constexpr int MA = Sys::EIG_ACTIVE;
+    double S[MA * MA];
+    if (fd_jacobian_active<Sys>(S, q, dq, d, f0))
+      return max_abs_eig<MA>(S);
+  }
   double M[V * V];
   if (Sys::HAS_F)
     fd_jacobian<Sys>(M, q, dq, d, false, f0);
