@@ -64,6 +64,14 @@ WORKLOADS = {
     "shear": ("euler", 2, 512, 3, 0.8, False),
 }
 
+# DRAM bytes (read + write) of one k_faces launch per face point, from ncu
+# captures of smaller grids of the same workload (a full-size launch is
+# scaled by its face points): the relaxation system at 512^2, N=2 (238 MB
+# read + 393 MB written over 2,101,248 face points); the Euler shear layer
+# at 256^2, N=3 (108 + 67 MB over 1,184,256).  The command lines are in
+# the k_faces summaries under profiles/.
+FACES_DRAM_BYTES_PER_POINT = {("cattaneo", 2, 2): 300.0, ("euler", 2, 3): 147.8}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -384,6 +392,13 @@ def run_ours(args, ws, rank, local):
     fpts = work_model.face_points([n] * nd, N)
     faces_launch = stage_s["faces"] / ksteps
     achieved = fpts * fpf / faces_launch / 1e12
+    per_point = FACES_DRAM_BYTES_PER_POINT.get((args.system, nd, N))
+    traffic = None if per_point is None else per_point * fpts
+    traffic_src = ("none: no ncu capture of this workload" if per_point is None else
+                   f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_faces launch "
+                   f"on a smaller grid of this workload, {per_point:.0f} B per face point, "
+                   f"times {fpts} face points; the algorithmic bytes are "
+                   f"{work_model.faces_bytes_per_launch([n] * nd, V, N):.3e}")
     flops = work_model.step_flops(args.system, [n] * nd, V, N, its, stiff=args.stiff)
 
     # e2e through the public API from pinned host memory (the headline form),
@@ -420,7 +435,8 @@ def run_ours(args, ws, rank, local):
                         "once, the final state plus the snapshot row come out once"},
         "roofline": {"bound": "fp64", "kernel": "k_faces", "achieved": achieved,
                      "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
-                     "traffic": None,
+                     "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_source": "FP64 FMA loop measured by this run "
                                     "(MEASURED_PEAKS.json has no FP64 figure)",
                      "flops_per_launch": fpts * fpf, "launch_ms": 1e3 * faces_launch,

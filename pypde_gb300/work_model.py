@@ -160,3 +160,13 @@ def bytes_per_cell_update(nX, V, N):
         "predictor": 8 * V * Nd * (1 + N) * Cw / C,
         "fv": 8 * V * N * Nd * Cw / C + 16 * V,
     }
+
+
+def faces_bytes_per_launch(nX, V, N):
+    """Algorithmic HBM bytes of one k_faces launch: the predictor qh read
+    once (N time nodes x N^d spatial nodes x V per w-cell) and the two
+    contributions of every face point written (2 V each)."""
+    Cw = 1
+    for n in nX:
+        Cw *= n + 2
+    return 8.0 * (Cw * N * N ** len(nX) * V + face_points(nX, N) * 2 * V)
