@@ -396,7 +396,8 @@ def run_ours(args, ws, rank, local):
     traffic = None if per_point is None else per_point * fpts
     traffic_src = ("none: no ncu capture of this workload" if per_point is None else
                    f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_faces launch "
-                   f"on a smaller grid of this workload, {per_point:.0f} B per face point, "
+                   f"of this workload captured on another grid size, {per_point:.0f} B per "
+                   f"face point, "
                    f"times {fpts} face points; the algorithmic bytes are "
                    f"{work_model.faces_bytes_per_launch([n] * nd, V, N):.3e}")
     flops = work_model.step_flops(args.system, [n] * nd, V, N, its, stiff=args.stiff)
