@@ -39,6 +39,29 @@ def test_library_loads_without_gpu_and_fails_loudly(gpu_lib):
     assert e.value.code == _lib.PYPDE_ERR_CUDA
 
 
+BUILTINS = [("euler", 1, 3), ("euler", 2, 4), ("euler", 3, 5), ("cattaneo", 2, 7),
+            ("cattaneo", 3, 9), ("ncp", 1, 3), ("ncp", 2, 3), ("burgers2", 1, 1)]
+
+
+@pytest.mark.parametrize("case", BUILTINS, ids=lambda c: f"{c[0]}{c[1]}")
+def test_builtin_orders_registered(gpu_lib, case):
+    """Each (system, order) pair is compiled in its own unit and the units
+    register into one description per system: orders 1-3 pass the host's
+    order check and only then meet the missing GPU (a CUDA error); order 4
+    is refused as unsupported before any CUDA call."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from pypde_gb300 import _lib, stages
+    name, ndim, V = case
+    for N in (1, 2, 3, 4):
+        w = np.zeros((N ** ndim, V))
+        with pytest.raises(_lib.PyPDEError) as e:
+            stages.timestep(name, w, [1.0] * ndim, N, 0.9, 1.0, 0.0, 7)
+        want = _lib.PYPDE_ERR_CUDA if N <= 3 else _lib.PYPDE_ERR_UNSUPPORTED
+        assert e.value.code == want, (N, e.value)
+
+
 @pytest.mark.parametrize("N", range(1, 7))
 def test_tables_bitwise_equal_to_port(gpu_lib, N):
     from pypde_gb300 import stages
