@@ -159,7 +159,8 @@ def ref_flux_points():
     R.ref_flux.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int] + [ora.dp] * 4 + \
         [ctypes.c_int, ctypes.c_int, ora.dp, ora.dp]
     out = {}
-    for name, ndim, N in (("euler", 1, 2), ("euler", 2, 3), ("ncp", 2, 2), ("cattaneo", 2, 2)):
+    for name, ndim, N in (("euler", 1, 2), ("euler", 2, 3), ("ncp", 2, 2), ("cattaneo", 2, 2),
+                          ("cattaneo", 3, 2)):
         u = workloads.random_state(name, (6,) * ndim, 11).reshape(-1, workloads.random_state(
             name, (1,) * ndim, 0).shape[-1])
         if name == "cattaneo":
