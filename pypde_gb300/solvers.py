@@ -28,7 +28,7 @@ FLUXES = {"rusanov": 0, "roe": 1, "osher": 2}
 
 
 def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cfl=0.9,
-               order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *,
+               order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *, M=None,
                max_steps=None, newton_tol=None, device=0, stats=None, jit=False,
                warm_start=None, mixed_precision=False):
     """Solve dQ/dt + div F(Q, grad Q) + B(Q) . grad Q = S(Q) on [0, L] (see
@@ -39,6 +39,10 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
     reference, the final state is also written into Q0 when Q0 is a
     contiguous float64 array.
     """
+    if M is not None:
+        # the reference's pde_solver (pypde/solvers.py:13-25) has no M
+        raise NotImplementedError("M has no counterpart in the reference's pde_solver; "
+                                  "only M=None is accepted")
     nX = np.array(Q0.shape[:-1], dtype="int32")
     ndim = len(nX)
     V = Q0.shape[-1]
@@ -79,7 +83,7 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
     return ret.reshape((ndt,) + Q0.shape)
 
 
-# The name used by the GB300 build's documentation; same function.
+# Another name for pde_solver (same function, same arguments, M=None).
 ader_solver = pde_solver
 
 

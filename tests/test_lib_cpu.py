@@ -135,3 +135,14 @@ def test_empty_grid_rejected_before_device_work():
     with pytest.raises(_lib.PyPDEError) as e:
         pde_solver(np.ones((0, 3)), 0.1, [1.0], F=s.F, stiff=False)
     assert e.value.code == _lib.PYPDE_ERR_ARG
+
+
+def test_ader_solver_alias_takes_only_m_none():
+    """ader_solver is pde_solver; M is accepted only as None (the
+    reference's pde_solver has no M), and refused before any GPU work."""
+    from pypde_gb300 import ader_solver, pde_solver, systems
+    assert ader_solver is pde_solver
+    s = systems.euler(1)
+    with pytest.raises(NotImplementedError):
+        ader_solver(np.ones((8, 3)), 0.1, [1.0], F=s.F, M=lambda Q: Q, stiff=False)
+
