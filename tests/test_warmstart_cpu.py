@@ -92,6 +92,38 @@ def test_port_newton_from_guess():
     assert np.abs(q1 - qh).max() <= 1e-10 * np.abs(qh).max()
 
 
+def test_guess_accuracy_needed_to_save_iterations():
+    """How accurate a warm start must be before Newton saves sweeps, on the
+    restatement (24^2 relaxation state after 10 steps, the step-9 dt): a
+    guess that carries the converged correction with a relative error eps
+    per entry.  The plain guess (w at every time node) needs ~5.8 sweeps per
+    cell; eps = 1e-4 saves more than one, eps = 1e-2 less than half a sweep,
+    and eps = 0.1, the accuracy class of a BF16 network, costs sweeps."""
+    n, N = 24, 2
+    u0 = workloads.relaxation(n, 2, seed=0)
+    u = ora.pde_solver("cattaneo", u0, 1.0, [1.0, 1.0], [1, 1], 0.8, N, stiff=True,
+                       max_steps=10, nthreads=2)[0]
+    dX = [1.0 / n] * 2
+    w = ora.weno(ora.boundaries(u, N, [1, 1]), N)
+    dt = ora.timestep("cattaneo", w, dX, N, 0.8, 1.0, 0.0, 9)
+    qh, its, _ = ora.predictor("cattaneo", w, dX, N, True, dt)
+    cells = w.shape[0] // N ** 2
+    wq = np.repeat(w.reshape(cells, 1, N * N, 7), N, axis=1).reshape(qh.shape)
+    corr = qh - wq
+    rng = np.random.default_rng(0)
+    plain = its / cells
+    sweeps = {}
+    for eps in (1e-8, 1e-4, 1e-2, 0.1):
+        g = wq + corr * (1 + eps * rng.standard_normal(corr.shape))
+        _, it, _, fb = ora.predictor_guess("cattaneo", w, dX, N, dt, g)
+        assert fb == 0
+        sweeps[eps] = it / cells
+    assert sweeps[1e-8] < sweeps[1e-4] < sweeps[1e-2] < sweeps[0.1]
+    assert sweeps[1e-4] < plain - 1.0
+    assert sweeps[1e-2] > plain - 0.5
+    assert sweeps[0.1] > plain
+
+
 def test_port_fallback_to_plain_guess():
     """A non-finite guess falls back at iteration 0; the cell then runs the
     plain iteration and gives the plain result bit for bit."""
