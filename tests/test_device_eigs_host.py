@@ -1,13 +1,16 @@
-"""The device max|eig| path, compiled as host C++ (tests/device_eigs_host.cpp
-includes pypde_gb300/csrc/ader_common.cuh and systems.cuh), against the C
-restatement, bit for bit, on the CPU.
+"""Device code compiled as host C++, against the C restatement, bit for bit,
+on the CPU: the max|eig| path (tests/device_eigs_host.cpp, with
+pypde_gb300/csrc/ader_common.cuh and systems.cuh) and the face fluxes
+(tests/device_flux_host.cpp, with kernels.cuh).
 
 The GPU parity tests compare the kernels with the restatement on the GPU;
 this test checks the same source's operation order without one.  It covers:
 - the FD Jacobian, including the active-column form of systems with passive
   variables;
 - the FP32 Hessenberg/QR candidates, the DMW refinement and its fallbacks;
-- systems with a B matrix."""
+- systems with a B matrix;
+- the Rusanov, Roe and Osher fluxes (full complex eigendecompositions) and
+  the B path integral, orders 1-3, and the second-order flux form."""
 import ctypes
 import os
 import shutil
@@ -21,18 +24,30 @@ from oracle import ora
 from pypde_gb300 import workloads
 
 
-@pytest.fixture(scope="module")
-def host_lib(tmp_path_factory):
+def _host_build(tmp_path_factory, name):
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("no g++")
-    out = str(tmp_path_factory.mktemp("devhost") / "libdevice_eigs_host.so")
-    src = os.path.join(ROOT, "tests", "device_eigs_host.cpp")
+    out = str(tmp_path_factory.mktemp("devhost") / f"lib{name}.so")
+    src = os.path.join(ROOT, "tests", name + ".cpp")
     subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
                     "-Wno-unknown-pragmas", "-o", out, src], check=True)
-    L = ctypes.CDLL(out)
+    return ctypes.CDLL(out)
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    L = _host_build(tmp_path_factory, "device_eigs_host")
     L.host_max_abs_eigs.restype = ctypes.c_double
     L.host_max_abs_eigs.argtypes = [ctypes.c_char_p, ctypes.c_int, ora.dp, ora.dp, ctypes.c_int]
+    return L
+
+
+@pytest.fixture(scope="module")
+def flux_lib(tmp_path_factory):
+    L = _host_build(tmp_path_factory, "device_flux_host")
+    L.host_face_flux.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int] + [ora.dp] * 4 + \
+        [ctypes.c_int, ctypes.c_int] + [ora.dp] * 4
     return L
 
 
@@ -61,3 +76,43 @@ def test_device_eigs_equal_port(host_lib, case):
             got = host_lib.host_max_abs_eigs(name.encode(), ndim, ora.ptr(q.copy()),
                                              ora.ptr(dq.copy()), d)
             assert got == want or (np.isnan(got) and np.isnan(want)), (q, d, got, want)
+
+
+FLUX_CASES = CASES + [("burgers2", 1)]
+
+
+@pytest.mark.parametrize("case", FLUX_CASES, ids=lambda c: f"{c[0]}{c[1]}")
+def test_device_face_fluxes_equal_port(flux_lib, case):
+    name, ndim = case
+    s = ora.PortSystem(name, ndim)
+    P = ora.port()
+    P.ora_face_flux.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_int] * 4 + [ora.dp] * 4 + \
+        [ctypes.c_int, ctypes.c_int, ora.dp, ora.dp]
+    rng = np.random.default_rng(7)
+    states = workloads.random_state(name, (13,) + (1,) * (ndim - 1), 5).reshape(-1, s.V)
+    if name == "cattaneo":
+        states[::2, -1] = -6.0
+    for N in (1, 2, 3):
+        tab = ora.tables(N)
+        nodes, wghts = tab[:N].copy(), tab[N:2 * N].copy()
+        for flux in (0, 1, 2):
+            for i in range(len(states) - 1):
+                qL, qR = states[i].copy(), states[i + 1].copy()
+                d = i % ndim
+                if s.second_order:
+                    dqL, dqR = 0.1 * rng.standard_normal((2, ndim * s.V))
+                else:
+                    dqL, dqR = np.zeros((2, ndim * s.V))
+                f0, b0 = np.zeros(s.V), np.zeros(s.V)
+                P.ora_face_flux(s.F, s.B, ndim, N, s.V, s.second_order, ora.ptr(qL.copy()),
+                                ora.ptr(qR.copy()), ora.ptr(dqL.copy()), ora.ptr(dqR.copy()), d,
+                                flux, ora.ptr(f0), ora.ptr(b0))
+                f1, b1 = np.zeros(s.V), np.zeros(s.V)
+                rc = flux_lib.host_face_flux(name.encode(), ndim, N, ora.ptr(qL.copy()),
+                                             ora.ptr(qR.copy()), ora.ptr(dqL.copy()),
+                                             ora.ptr(dqR.copy()), d, flux, ora.ptr(nodes),
+                                             ora.ptr(wghts), ora.ptr(f1), ora.ptr(b1))
+                assert rc == 0
+                assert np.array_equal(f1, f0), (N, flux, i, f1 - f0)
+                assert np.array_equal(b1, b0), (N, flux, i, b1 - b0)
+
