@@ -118,7 +118,8 @@ def test_eigen_passive_block():
     other than q_d, and log tau) have zero rows and columns in the flux
     Jacobian of direction d; max|eig| over the active block equals numpy's
     over the full matrix, in 2-D and 3-D, including states with zero
-    velocity (more exact zeros in the active block)."""
+    velocity (more exact zeros in the active block), and equals the same
+    solver run on the full matrix bit for bit."""
     import ctypes
     lib = ora.port()
     lib.ora_system_max_abs_eigs.restype = ctypes.c_double
@@ -147,6 +148,11 @@ def test_eigen_passive_block():
                     assert not np.any(np.delete(M[i], i)) and not np.any(np.delete(M[:, i], i))
                 want = np.abs(np.linalg.eigvals(M)).max()
                 assert abs(got - want) <= 1e-12 * max(1.0, want), (ndim, trial, d)
+                # the solver on the full matrix gives the same bits: the FP64
+                # refinement reaches the same fixed point, and the zero
+                # entries add nothing to its residual
+                full = lib.ora_max_abs_eig(ora.ptr(M.ravel().copy()), V)
+                assert got == full, (ndim, trial, d, got, full)
 
 
 def test_slab_count_invariance():
