@@ -199,6 +199,8 @@ def main():
     ref_run("run_shear32_N3_K10", "euler", workloads.shear(32), 3, [1, 1], 0.8, 10)
     ref_run("run_shear16_N2_K10", "euler", workloads.shear(16), 2, [1, 0], 0.8, 10)
     print(ref_stiff_predictor((6, 5), 2, 7, 2e-3))
+    print(ref_stiff_predictor((6, 5), 1, 7, 2e-3))
+    print(ref_stiff_predictor((5, 4), 3, 8, 2e-3))
 
 
 if __name__ == "__main__":

@@ -91,10 +91,14 @@ def test_runs_within_reference_band(fixture):
     assert np.all(err <= np.maximum(20 * band, 1e-13)), (err, band)
 
 
-def test_stiff_predictor_matches_tight_reference():
+STIFF = sorted(os.path.basename(f) for f in glob.glob(os.path.join(GOLDEN, "stiff_*.npz")))
+
+
+@pytest.mark.parametrize("fixture", STIFF)
+def test_stiff_predictor_matches_tight_reference(fixture):
     """Newton to ||obj||_inf <= 1e-12 against the reference's Newton-Krylov
-    predictor built with DG_TOL = 1e-12 (same fixed point)."""
-    z = load("stiff_cattaneo_6x5_N2.npz")
+    predictor built with DG_TOL = 1e-12 (same fixed point), orders 1-3."""
+    z = load(fixture)
     qh, its, mx = ora.predictor("cattaneo", z["w"], z["dX"], int(z["N"]), True, float(z["dt"]),
                                 1e-12)
     assert rel(qh, z["qh"]) < 1e-10
