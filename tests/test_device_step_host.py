@@ -1,0 +1,176 @@
+"""The whole device step on the CPU: the kernels of pypde_gb300/csrc compiled
+as host C++ (tests/device_step_host.cpp) and run with every CUDA thread of a
+block as a fiber, against the C restatement, bit for bit.
+
+The GPU parity tests compare the kernels with the restatement on the GPU.
+This test checks the same source, with the runtime's launch shapes and stage
+order, without one:
+- ghost fill, the WENO passes, the CFL reduction (warp shuffles and
+  atomics), the Picard and Newton predictors (shared memory, block barriers
+  with AND reductions), face fluxes, centres and the gather;
+- full runs of every built-in system, orders 1-3, 1-D to 3-D, periodic and
+  transmissive axes, Rusanov/Roe/Osher fluxes, B terms, the second-order
+  form and the stiff Newton predictor: final state, t and step count equal;
+- the predictor stage alone with its iteration counts;
+- the fibers of a block run in thread order and in reverse order, and the
+  results must agree: a read of shared memory that no barrier orders after
+  its write would change with the order.
+
+The only edit to the device headers is the one the host compiler needs:
+`extern __shared__ double smem[];` becomes a pointer to a host buffer."""
+import ctypes
+import glob
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, l1
+from oracle import ora
+from pypde_gb300 import stages, workloads
+
+CSRC = os.path.join(ROOT, "pypde_gb300", "csrc")
+DYN_SMEM = "extern __shared__ double smem[];"
+
+
+@pytest.fixture(scope="module")
+def step_lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    inc = tmp_path_factory.mktemp("devstep")
+    for f in glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")):
+        shutil.copy(f, inc)
+    k = os.path.join(inc, "kernels.cuh")
+    text = open(k).read()
+    assert text.count(DYN_SMEM) == 2
+    open(k, "w").write(text.replace(DYN_SMEM, "double *smem = host_dynamic_smem();"))
+    out = str(inc / "libdevice_step_host.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                    "-Wno-unknown-pragmas", "-I", str(inc), "-o", out,
+                    os.path.join(ROOT, "tests", "device_step_host.cpp")], check=True)
+    L = ctypes.CDLL(out)
+    c_int, c_ll, c_d = ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+    L.host_run.restype = c_ll
+    L.host_run.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, ora.dp, ora.ip, ora.ip, ora.dp,
+                           ora.dp, c_d, c_d, c_int, c_d, c_int, c_ll, ctypes.POINTER(c_d),
+                           ctypes.POINTER(ctypes.c_ulonglong)]
+    L.host_predictor.restype = c_int
+    L.host_predictor.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, ora.dp, c_ll, ora.dp,
+                                 c_d, c_d, ora.dp, ora.dp, ctypes.POINTER(ctypes.c_ulonglong),
+                                 ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    L.host_set_order.argtypes = [c_int]
+    return L
+
+
+def _run(L, name, u0, N, bt, cfl, K, stiff=False, flux=0, tol=1e-12, mixed=0, reverse=False):
+    nX = np.array(u0.shape[:-1], dtype=np.int32)
+    dX = np.array([1.0 / n for n in nX])
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    t, its = ctypes.c_double(), ctypes.c_ulonglong()
+    L.host_set_order(int(reverse))
+    steps = L.host_run(name.encode(), len(nX), N, flux, ora.ptr(u), ora.ptr(nX),
+                       ora.ptr(np.array(bt, dtype=np.int32)), ora.ptr(dX),
+                       ora.ptr(stages.tables(N)), 10.0, cfl, int(stiff), tol, mixed, K,
+                       ctypes.byref(t), ctypes.byref(its))
+    assert steps >= 0, "combination not instantiated" if steps == -1 else "barrier deadlock"
+    return u, steps, t.value, its.value
+
+
+def _state(system, shape, seed, log10_tau=(-4.0, -2.0)):
+    u = workloads.random_state(system, shape, seed)
+    if system == "cattaneo":
+        u[..., -1] = np.random.default_rng(seed).uniform(*log10_tau, shape)
+    return u
+
+
+RUNS = [
+    ("euler", workloads.sod(40), 2, [0], 0.9, 10, False, 0, "sod40-N2"),
+    ("euler", _state("euler", (17,), 1), 1, [1], 0.9, 6, False, 0, "euler17-N1"),
+    ("euler", _state("euler", (24,), 2), 3, [1], 0.9, 6, False, 0, "euler24-N3"),
+    ("euler", workloads.shear(16), 2, [1, 0], 0.8, 10, False, 0, "shear16-N2"),
+    ("euler", _state("euler", (12, 10), 3), 3, [1, 1], 0.5, 4, False, 0, "euler12x10-N3"),
+    ("euler", _state("euler", (6, 5, 7), 6), 2, [1, 1, 0], 0.5, 4, False, 0, "euler3d-N2"),
+    ("euler", workloads.sod(16), 2, [0], 0.9, 6, False, 1, "sod16-roe"),
+    ("euler", workloads.sod(16), 2, [0], 0.9, 6, False, 2, "sod16-osher"),
+    ("ncp", _state("ncp", (16,), 4), 2, [0], 0.5, 6, False, 0, "ncp16-N2"),
+    ("ncp", _state("ncp", (12, 10), 4), 2, [1, 1], 0.5, 6, False, 0, "ncp12x10-N2"),
+    ("burgers2", _state("burgers2", (32,), 5), 3, [1], 0.5, 6, False, 0, "burgers32-N3"),
+    ("cattaneo", workloads.relaxation(24, 2, seed=3), 2, [1, 1], 0.8, 4, True, 0,
+     "relax24-stiff-N2"),
+    ("cattaneo", workloads.relaxation(12, 2, seed=5), 1, [1, 1], 0.8, 4, True, 0,
+     "relax12-stiff-N1"),
+    ("cattaneo", workloads.relaxation(12, 2, seed=6), 3, [1, 1], 0.8, 3, True, 0,
+     "relax12-stiff-N3"),
+    ("cattaneo", _state("cattaneo", (6, 5, 4), 7), 2, [1, 1, 1], 0.8, 2, True, 0,
+     "cattaneo3d-stiff-N2"),
+    ("cattaneo", _state("cattaneo", (10, 8), 8, (-1.0, 0.0)), 2, [1, 0], 0.8, 4, False, 0,
+     "cattaneo10x8-picard"),
+]
+
+
+@pytest.mark.parametrize("run", RUNS, ids=[r[-1] for r in RUNS])
+def test_device_step_equals_port(step_lib, run):
+    name, u0, N, bt, cfl, K, stiff, flux, _ = run
+    u_o, _, steps_o, t_o = ora.pde_solver(name, u0, 10.0, [1.0] * (u0.ndim - 1), bt, cfl, N,
+                                          stiff=stiff, flux=flux, max_steps=K)
+    u_f, steps_f, t_f, its_f = _run(step_lib, name, u0, N, bt, cfl, K, stiff, flux)
+    u_r, steps_r, t_r, its_r = _run(step_lib, name, u0, N, bt, cfl, K, stiff, flux,
+                                    reverse=True)
+    assert steps_f == steps_o == K
+    assert t_f == t_o
+    assert np.array_equal(u_f, u_o), np.abs(u_f - u_o).max()
+    assert (steps_r, t_r, its_r) == (steps_f, t_f, its_f)
+    assert np.array_equal(u_r, u_f)
+
+
+PRED_CASES = [("cattaneo", (10, 8), 2, True), ("cattaneo", (6, 5, 4), 2, True),
+              ("cattaneo", (9, 7), 3, True), ("cattaneo", (8, 7), 1, True),
+              ("ncp", (12,), 2, True), ("euler", (8, 6), 2, True), ("euler", (8, 6), 2, False),
+              ("euler", (9,), 3, False), ("ncp", (7, 6), 2, False)]
+
+
+@pytest.mark.parametrize("case", PRED_CASES,
+                         ids=[f"{c[0]}-{len(c[1])}d-N{c[2]}-{'newton' if c[3] else 'picard'}"
+                              for c in PRED_CASES])
+def test_device_predictor_equals_port(step_lib, case):
+    """The predictor stage on the same w and dt: qh and the iteration counts
+    (sum over cells and maximum) equal the restatement's."""
+    system, shape, N, stiff = case
+    u = workloads.random_state(system, shape, 2)
+    dX = np.array([1.0 / n for n in shape])
+    bt = [1] * len(shape)
+    w = ora.weno(ora.boundaries(u, N, bt), N)
+    dt = ora.timestep(system, w, dX, N, 0.9, 1.0, 0.0, 9)
+    qh_o, its_o, mx_o = ora.predictor(system, w, dX, N, stiff, dt, 1e-12)
+    for reverse in (False, True):
+        step_lib.host_set_order(int(reverse))
+        qh = np.zeros_like(qh_o)
+        its, mx, fail = ctypes.c_ulonglong(), ctypes.c_int(), ctypes.c_int()
+        rc = step_lib.host_predictor(system.encode(), len(shape), N, int(stiff), ora.ptr(w),
+                                     w.shape[0], ora.ptr(dX), dt, 1e-12,
+                                     ora.ptr(stages.tables(N)), ora.ptr(qh), ctypes.byref(its),
+                                     ctypes.byref(mx), ctypes.byref(fail))
+        assert rc == 0
+        assert np.array_equal(qh, qh_o), np.abs(qh - qh_o).max()
+        assert its.value == its_o and mx.value == mx_o and fail.value == 0
+
+
+def test_device_mixed_precision_step(step_lib):
+    """The mixed-precision Newton predictor (FP32 sweeps, then FP64 to the
+    same 1e-12): independent of the fibers' order, and at the plain form's
+    error level against a tolerance-1e-15 run of the restatement."""
+    u0 = workloads.relaxation(16, 2, seed=11, patches=4)
+    K = 6
+    u_ref, _, _, t_ref = ora.pde_solver("cattaneo", u0, 10.0, [1.0, 1.0], [1, 1], 0.8, 2,
+                                        stiff=True, max_steps=K, newton_tol=1e-15)
+    u_p, _, _, _ = ora.pde_solver("cattaneo", u0, 10.0, [1.0, 1.0], [1, 1], 0.8, 2, stiff=True,
+                                  max_steps=K)
+    u_m, steps, t, its = _run(step_lib, "cattaneo", u0, 2, [1, 1], 0.8, K, stiff=True, mixed=1)
+    u_mr, _, _, its_r = _run(step_lib, "cattaneo", u0, 2, [1, 1], 0.8, K, stiff=True, mixed=1,
+                             reverse=True)
+    assert steps == K and its == its_r and np.array_equal(u_m, u_mr)
+    floor = l1(u_p, u_ref).max()
+    assert l1(u_m, u_ref).max() <= max(1e-8, 3 * floor), (l1(u_m, u_ref).max(), floor)
