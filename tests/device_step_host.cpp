@@ -31,7 +31,8 @@
 //
 // The launch shapes (grid and block sizes) and the stage order follow the
 // one-problem step of pypde_gb300/csrc/runtime.cu (enqueue_step,
-// enqueue_weno, enqueue_predictor).
+// enqueue_weno, enqueue_predictor) and its batched step (run_batch,
+// enqueue_batch_step: the kb_* kernels of batch.cuh over a tile queue).
 #include <ucontext.h>
 
 #include <cmath>
@@ -557,5 +558,181 @@ extern "C" int host_predictor(const char *name, int ndim, int N, int stiff,
   }
   HOST_CASES(PRED_CASE)
 #undef PRED_CASE
+  return -1;
+}
+
+namespace {
+// Batched steps of problems of one system and order, as run_batch enqueues
+// them (enqueue_batch_step): every stage is one launch over all problems
+// whose blocks drain a queue of tiles, tile = one block of the stage's
+// one-problem launch.  per_pop = 0 launches one block per tile; otherwise
+// `ctas` persistent blocks pop per_pop tiles at a time.
+enum { B_BND, B_W0, B_W1, B_W2, B_CFL, B_PRED, B_FACES, B_CEN, B_GATHER, B_N };
+
+template <class Sys, int N, int FLUX>
+void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
+                     const int *bt_all, const double *dX_all,
+                     const double *tf_all, const double *cfl_all,
+                     const double *tabs, int stiff, double tol, int per_pop,
+                     int ctas, long long max_steps, long long *steps_out,
+                     double *t_out) {
+  constexpr int V = Sys::V;
+  const Tables T = unpack_tables(N, tabs);
+  const int Nd = ipow(N, ndim), NT = N * Nd;
+  const bool faces = Sys::HAS_F || Sys::HAS_B;
+  const bool centers = Sys::HAS_B || Sys::HAS_S;
+  const std::vector<double> wprod = make_wprod(T, ndim);
+  std::vector<BatchProblem> P(np);
+  std::vector<DevState> S(np);
+  std::vector<std::vector<double>> bufs;
+  auto buf = [&](long long n) {
+    bufs.emplace_back(n > 0 ? n : 1);
+    return bufs.back().data();
+  };
+  std::vector<long long> off[B_N];
+  for (int st = 0; st < B_N; st++)
+    off[st].push_back(0);
+  long long uoff = 0;
+  for (int p = 0; p < np; p++) {
+    BatchProblem &b = P[p];
+    std::memset(&b, 0, sizeof(b));
+    b.g = make_geom(ndim, nX_all + p * ndim, bt_all + p * ndim,
+                    dX_all + p * ndim, N);
+    b.fi = make_face_index(b.g, N);
+    b.N = N;
+    b.V = V;
+    b.u = u_all + uoff;
+    uoff += b.g.C * V;
+    b.ub = buf(b.g.Cb * V);
+    b.w = buf(b.g.Cw * Nd * V);
+    b.qh = buf(b.g.Cw * N * Nd * V);
+    b.contrib = buf((faces ? b.fi.off[ndim] : 1) * 2 * V);
+    b.cen = buf((centers ? b.g.C * NT : 1) * V);
+    b.wprod = const_cast<double *>(wprod.data());
+    long long tw[3] = {0, 0, 0};
+    int m[3] = {b.g.nXb[0], b.g.nXb[1], b.g.nXb[2]};
+    const double *src = b.ub;
+    int n4 = 1;
+    for (int d = 0; d < ndim; d++) {
+      long long n1 = 1, n3 = 1;
+      for (int e = 0; e < d; e++)
+        n1 *= m[e];
+      for (int e = d + 1; e < ndim; e++)
+        n3 *= m[e];
+      tw[d] = n1 * (m[d] - 2 * (N - 1)) * n3 * (long long)n4 * V;
+      // each work item writes the N nodal values of one 1-D reconstruction
+      double *dst = (d == ndim - 1) ? b.w : buf(tw[d] * N);
+      b.win[d] = src;
+      b.wout[d] = dst;
+      b.wn1[d] = n1;
+      b.wn3[d] = n3;
+      b.wmd[d] = m[d];
+      b.wn4[d] = n4;
+      src = dst;
+      m[d] -= 2 * (N - 1);
+      n4 *= N;
+    }
+    auto tiles = [](long long work, int per) { return (work + per - 1) / per; };
+    long long tl[B_N] = {};
+    tl[B_BND] = tiles(b.g.Cb * V, 256);
+    for (int d = 0; d < ndim; d++)
+      tl[B_W0 + d] = tiles(tw[d], 128);
+    tl[B_CFL] = tiles(b.g.Cw, 128);
+    tl[B_PRED] = tiles(b.g.Cw, stiff ? NewtonCfg<Sys, N>::CPB
+                                     : PredCfg<Sys, N>::CPB);
+    tl[B_FACES] = faces ? tiles(b.fi.off[ndim], 128) : 0;
+    tl[B_CEN] = centers ? tiles(b.g.C * NT, 128) : 0;
+    tl[B_GATHER] = tiles(b.g.C * V, 256);
+    for (int st = 0; st < B_N; st++)
+      off[st].push_back(off[st].back() + tl[st]);
+    DevState &d0 = S[p];
+    std::memset(&d0, 0, sizeof(d0));
+    d0.tf = tf_all[p];
+    d0.cfl = cfl_all[p];
+    d0.max_steps = max_steps > 0 ? max_steps : -1;
+    d0.ndt = 1;
+    d0.snap_slot = -1;
+    b.st = &d0;
+  }
+  unsigned long long heads[B_N];
+  auto stage = [&](int st, unsigned threads, size_t smem,
+                   const std::function<void(TileQueue, int)> &k) {
+    const long long total = off[st].back();
+    if (total == 0)
+      return;
+    heads[st] = 0;
+    TileQueue q{off[st].data(), np, &heads[st]};
+    unsigned grid;
+    if (per_pop == 0) {
+      grid = (unsigned)total;
+    } else {
+      const long long want = (total + per_pop - 1) / per_pop;
+      grid = (unsigned)(want < ctas ? want : ctas);
+    }
+    emu::launch(grid, threads, smem, [&] { k(q, per_pop); });
+  };
+  const BatchProblem *dP = P.data();
+  for (;;) {
+    int any = 0;
+    for (int p = 0; p < np; p++) {
+      step_begin_dev(P[p].st);
+      any |= P[p].st->active;
+    }
+    if (!any || emu::g_deadlock)
+      break;
+    stage(B_BND, 256, 0, [&](TileQueue q, int pp) { kb_boundaries(dP, q, pp); });
+    for (int d = 0; d < ndim; d++)
+      stage(B_W0 + d, 128, 0,
+            [&](TileQueue q, int pp) { kb_weno<N>(dP, q, pp, d, T); });
+    stage(B_CFL, 128, 0,
+          [&](TileQueue q, int pp) { kb_cfl<Sys, N>(dP, q, pp, T); });
+    for (int p = 0; p < np; p++)
+      dt_dev(P[p].st);
+    if (stiff)
+      stage(B_PRED, NewtonCfg<Sys, N>::THREADS, NewtonCfg<Sys, N>::SMEM_BYTES,
+            [&](TileQueue q, int pp) { kb_newton<Sys, N>(dP, q, pp, T, tol); });
+    else
+      stage(B_PRED, PredCfg<Sys, N>::THREADS,
+            (size_t)PredCfg<Sys, N>::SMEM_DOUBLES * 8,
+            [&](TileQueue q, int pp) { kb_predictor<Sys, N>(dP, q, pp, T); });
+    if (faces)
+      stage(B_FACES, 128, 0,
+            [&](TileQueue q, int pp) { kb_faces<Sys, N, FLUX>(dP, q, pp, T); });
+    if (centers)
+      stage(B_CEN, 128, 0,
+            [&](TileQueue q, int pp) { kb_centers<Sys, N>(dP, q, pp, T); });
+    stage(B_GATHER, 256, 0, [&](TileQueue q, int pp) {
+      kb_gather<Sys, N>(dP, q, pp, centers ? 1 : 0, faces ? 1 : 0);
+    });
+    for (int p = 0; p < np; p++)
+      step_end_dev(P[p].st, 1);
+  }
+  for (int p = 0; p < np; p++) {
+    steps_out[p] = S[p].count;
+    t_out[p] = S[p].t;
+  }
+}
+} // namespace
+
+// np problems of one built-in system and order stepped as one batch; u_all
+// holds their states one after the other, nX/bt/dX are np x ndim.  0, -1
+// for an unknown combination, or -2 when a block deadlocked.
+extern "C" int host_run_batch(const char *name, int ndim, int N, int flux,
+                              int np, double *u_all, const int *nX,
+                              const int *bt, const double *dX,
+                              const double *tf, const double *cfl,
+                              const double *tabs, int stiff, double tol,
+                              int per_pop, int ctas, long long max_steps,
+                              long long *steps_out, double *t_out) {
+  emu::g_deadlock = false;
+#define BATCH_CASE(NAME, NDIM, SYS, ORD, FL)                                   \
+  if (!std::strcmp(name, NAME) && ndim == NDIM && N == ORD && flux == FL) {    \
+    run_batch_steps<SYS, ORD, FL>(np, u_all, ndim, nX, bt, dX, tf, cfl, tabs,  \
+                                  stiff, tol, per_pop, ctas, max_steps,        \
+                                  steps_out, t_out);                           \
+    return emu::g_deadlock ? -2 : 0;                                           \
+  }
+  HOST_CASES(BATCH_CASE)
+#undef BATCH_CASE
   return -1;
 }

@@ -12,6 +12,8 @@ order, without one:
   transmissive axes, Rusanov/Roe/Osher fluxes, B terms, the second-order
   form and the stiff Newton predictor: final state, t and step count equal;
 - the predictor stage alone with its iteration counts;
+- batched steps (batch.cuh) of problems of mixed sizes, boundary types and
+  end times: each problem equals the restatement run on it alone;
 - the fibers of a block run in thread order and in reverse order, and the
   results must agree: a read of shared memory that no barrier orders after
   its write would change with the order.
@@ -62,6 +64,10 @@ def step_lib(tmp_path_factory):
                                  c_d, c_d, ora.dp, ora.dp, ctypes.POINTER(ctypes.c_ulonglong),
                                  ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.host_set_order.argtypes = [c_int]
+    L.host_run_batch.restype = c_int
+    L.host_run_batch.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, c_int, ora.dp, ora.ip,
+                                 ora.ip, ora.dp, ora.dp, ora.dp, ora.dp, c_int, c_d, c_int, c_int,
+                                 c_ll, ctypes.POINTER(c_ll), ora.dp]
     return L
 
 
@@ -174,3 +180,48 @@ def test_device_mixed_precision_step(step_lib):
     assert steps == K and its == its_r and np.array_equal(u_m, u_mr)
     floor = l1(u_p, u_ref).max()
     assert l1(u_m, u_ref).max() <= max(1e-8, 3 * floor), (l1(u_m, u_ref).max(), floor)
+
+
+BATCHES = [
+    ("cattaneo", [workloads.relaxation(n, 2, seed=n) for n in (20, 12, 7)], 2,
+     [[1, 1], [0, 1], [1, 0]], [0.8, 0.7, 0.9], [10.0, 10.0, 0.004], 4, True, "relax-stiff-N2"),
+    ("euler", [workloads.shear(16), _state("euler", (12, 10), 3), _state("euler", (5, 7), 4)], 3,
+     [[1, 0], [1, 1], [0, 0]], [0.8, 0.5, 0.5], [10.0, 10.0, 10.0], 3, False, "euler2d-N3"),
+    ("ncp", [_state("ncp", (9, 8), 1), _state("ncp", (6, 11), 2)], 2, [[1, 0], [1, 1]],
+     [0.5, 0.5], [10.0, 10.0], 4, False, "ncp2d-N2"),
+]
+
+
+@pytest.mark.parametrize("per_pop", [0, 1, 3])
+@pytest.mark.parametrize("batch", BATCHES, ids=[b[-1] for b in BATCHES])
+def test_device_batch_equals_port(step_lib, batch, per_pop):
+    """Problems of mixed sizes, boundary types and end times stepped as one
+    batch (batch.cuh: one launch per stage, tiles drained from a queue by
+    persistent blocks, or one block per tile for per_pop = 0): each equals
+    the restatement run on it alone, bit for bit, in both fiber orders."""
+    name, us, N, bts, cfls, tfs, K, stiff, _ = batch
+    nX = np.array([u.shape[:-1] for u in us], dtype=np.int32).ravel()
+    dX = np.array([[1.0 / n for n in u.shape[:-1]] for u in us]).ravel()
+    results = []
+    for reverse in (False, True):
+        step_lib.host_set_order(int(reverse))
+        u_all = np.concatenate([u.ravel() for u in us])
+        steps = (ctypes.c_longlong * len(us))()
+        t = np.zeros(len(us))
+        rc = step_lib.host_run_batch(name.encode(), us[0].ndim - 1, N, 0, len(us),
+                                     ora.ptr(u_all), ora.ptr(nX),
+                                     ora.ptr(np.array(bts, dtype=np.int32).ravel()),
+                                     ora.ptr(dX), ora.ptr(np.array(tfs)), ora.ptr(np.array(cfls)),
+                                     ora.ptr(stages.tables(N)), int(stiff), 1e-12, per_pop, 3, K,
+                                     steps, ora.ptr(t))
+        assert rc == 0
+        results.append((u_all, list(steps), t))
+    (u_f, steps_f, t_f), (u_r, steps_r, t_r) = results
+    assert np.array_equal(u_f, u_r) and steps_f == steps_r and np.array_equal(t_f, t_r)
+    o = 0
+    for p, u0 in enumerate(us):
+        u_o, _, steps_o, t_o = ora.pde_solver(name, u0, tfs[p], [1.0] * (u0.ndim - 1), bts[p],
+                                              cfls[p], N, stiff=stiff, max_steps=K)
+        assert steps_f[p] == steps_o and t_f[p] == t_o
+        assert np.array_equal(u_f[o:o + u0.size].reshape(u0.shape), u_o)
+        o += u0.size
