@@ -71,6 +71,11 @@ int pypde_system_compile(const char *src, const char *name, int ndim, int V,
   if (rc)
     return rc;
   *out = new (std::nothrow) pypde_system{d, d};
+  if (!*out) {
+    release_system(d);
+    set_error("out of host memory");
+    return PYPDE_ERR_ARG;
+  }
   return PYPDE_OK;
 }
 

@@ -518,6 +518,11 @@ static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
     set_error("system was built for another number of dimensions");
     return PYPDE_ERR_ARG;
   }
+  // checked for every system: faces_flux[flux] is indexed at launch
+  if (flux < 0 || flux > 2) {
+    set_error("FLUX must be 0 (Rusanov), 1 (Roe) or 2 (Osher)");
+    return PYPDE_ERR_ARG;
+  }
   if (sys.module && N >= 1 && N <= 3)
     return PYPDE_OK; // compiled on first use (ensure_kernels)
   if (N < 1 || N > MAXN || !sys.have[N]) {
@@ -529,9 +534,10 @@ static int check_system(const SystemDesc &sys, int ndim, int N, bool stiff,
     set_error("stiff predictor not built for system " + sys.name);
     return PYPDE_ERR_UNSUPPORTED;
   }
-  if (flux < 0 || flux > 2 || !sys.sets[N].faces_flux[flux].valid()) {
-    set_error("FLUX must be 0 (Rusanov), 1 (Roe) or 2 (Osher)");
-    return PYPDE_ERR_ARG;
+  if (!sys.sets[N].faces_flux[flux].valid()) {
+    set_error("flux " + std::to_string(flux) + " is not built for system " +
+              sys.name);
+    return PYPDE_ERR_UNSUPPORTED;
   }
   return PYPDE_OK;
 }

@@ -146,3 +146,37 @@ def test_ader_solver_alias_takes_only_m_none():
     with pytest.raises(NotImplementedError):
         ader_solver(np.ones((8, 3)), 0.1, [1.0], F=s.F, M=lambda Q: Q, stiff=False)
 
+
+
+def test_flux_code_checked_before_device_work(gpu_lib):
+    """FLUX outside 0-2 is refused with PYPDE_ERR_ARG on the host for
+    built-in and run-time compiled systems alike (a run-time system's
+    kernels are compiled on first use, after this check)."""
+    import ctypes
+
+    from pypde_gb300 import _lib
+    u = np.ones((8, 3))
+    nX = np.array([8], dtype=np.int32)
+    dX = np.array([1.0 / 8])
+    bt = np.array([0], dtype=np.int32)
+    ret = np.zeros((1, 8, 3))
+    handles = []
+    h = ctypes.c_void_p()
+    _lib.check(gpu_lib.pypde_system_builtin(b"euler", 1, ctypes.byref(h)))
+    handles.append(h)
+    h = ctypes.c_void_p()
+    src = b"struct UserSystem {};"  # recorded only: compiled on first use
+    _lib.check(gpu_lib.pypde_system_compile(src, b"user", 1, 3, 1, 0, 0, 0, ctypes.byref(h)))
+    handles.append(h)
+    try:
+        for h in handles:
+            for flux in (-1, 3):
+                rc = gpu_lib.pde_solver_ex(h, True, False, False, _lib.c_ptr(u), 0.1,
+                                           _lib.c_ptr(nX), 1, _lib.c_ptr(dX), 0.9,
+                                           _lib.c_ptr(bt), False, flux, 2, 1, _lib.c_ptr(ret),
+                                           None, None)
+                assert rc == _lib.PYPDE_ERR_ARG
+                assert b"FLUX" in gpu_lib.pypde_last_error()
+    finally:
+        for h in handles:
+            gpu_lib.pypde_system_free(h)
