@@ -493,6 +493,11 @@ static int check_grid(int ndim, const int *nX, const int *bt, int N) {
       set_error("grid sizes must be positive");
       return PYPDE_ERR_ARG;
     }
+    // the ghost fill treats every non-zero type as periodic
+    if (bt && bt[d] != 0 && bt[d] != 1) {
+      set_error("boundaryTypes must be 0 (transmissive) or 1 (periodic)");
+      return PYPDE_ERR_ARG;
+    }
     if (bt && bt[d] == 1 && nX[d] < N) {
       set_error("a periodic axis needs at least N cells (axis " +
                 std::to_string(d) + " has " + std::to_string(nX[d]) + ")");

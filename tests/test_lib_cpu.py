@@ -180,3 +180,19 @@ def test_flux_code_checked_before_device_work(gpu_lib):
     finally:
         for h in handles:
             gpu_lib.pypde_system_free(h)
+
+
+def test_boundary_codes_checked_before_device_work(gpu_lib):
+    """The ghost-fill entry point refuses boundary codes other than 0 and 1
+    on the host (the kernel would treat them as periodic without the
+    periodic axis-length check)."""
+    from pypde_gb300 import _lib
+    u = np.ones((3, 4, 2))
+    nX = np.array([3, 4], dtype=np.int32)
+    ub = np.zeros((3 + 4, 4 + 4, 2))
+    for bt in ([2, 0], [0, -1]):
+        rc = gpu_lib.pypde_boundaries(_lib.c_ptr(u), _lib.c_ptr(nX), 2,
+                                      _lib.c_ptr(np.array(bt, dtype=np.int32)), 2, 2,
+                                      _lib.c_ptr(ub))
+        assert rc == _lib.PYPDE_ERR_ARG
+        assert b"boundaryTypes" in gpu_lib.pypde_last_error()
