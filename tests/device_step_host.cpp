@@ -351,15 +351,16 @@ std::vector<double> make_wprod(const Tables &T, int ndim) {
 
 // The predictor stage of one step: Picard (k_predictor) or Newton
 // (k_newton), launched as enqueue_predictor does.
+// With guess = 1 the Newton iteration starts from the qh already given.
 template <class Sys, int N>
 void predictor_stage(bool stiff, const double *w, double *qh, const Geom &g,
                      const Tables &T, const double *wprod, DevState *st,
-                     double tol, int mixed) {
+                     double tol, int mixed, int guess = 0) {
   if (stiff) {
     using NC = NewtonCfg<Sys, N>;
     const unsigned blocks = (unsigned)((g.Cw + NC::CPB - 1) / NC::CPB);
     emu::launch(blocks, NC::THREADS, NC::SMEM_BYTES, [&] {
-      k_newton<Sys, N>(w, qh, g, T, wprod, st, tol, 0, mixed);
+      k_newton<Sys, N>(w, qh, g, T, wprod, st, tol, guess, mixed);
     });
   } else {
     using PC = PredCfg<Sys, N>;
@@ -472,12 +473,15 @@ long long run_steps(double *u, int ndim, const int *nX, const int *bt,
 }
 
 // The predictor stage alone on given reconstruction data w (nrows = cells
-// x N^ndim rows), as stage_predictor sets it up.
+// x N^ndim rows), as stage_predictor sets it up; with guess non-null the
+// stiff predictor starts from it (the given initial guess of
+// stage_predictor).
 template <class Sys, int N>
 void predictor_only(int ndim, int stiff, const double *w, long long nrows,
                     const double *dX, double dt, double tol, const double *tabs,
                     double *qh, unsigned long long *iters, int *max_iters,
-                    int *fail) {
+                    int *fail, const double *guess = nullptr,
+                    unsigned long long *fallbacks = nullptr) {
   const Tables T = unpack_tables(N, tabs);
   const int ones[3] = {1, 1, 1};
   Geom g = make_geom(ndim, ones, nullptr, dX, N);
@@ -491,10 +495,15 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
   st.dt = dt;
   st.max_steps = -1;
   st.snap_slot = -1;
-  predictor_stage<Sys, N>(stiff != 0, w, qh, g, T, wprod.data(), &st, tol, 0);
+  if (guess)
+    std::memcpy(qh, guess, sizeof(double) * nrows * N * Sys::V);
+  predictor_stage<Sys, N>(stiff != 0, w, qh, g, T, wprod.data(), &st, tol, 0,
+                          guess ? 1 : 0);
   *iters = st.pred_iters;
   *max_iters = st.pred_max_iters;
   *fail = st.pred_fail;
+  if (fallbacks)
+    *fallbacks = st.pred_fallbacks;
 }
 } // namespace
 
@@ -713,6 +722,30 @@ void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
   }
 }
 } // namespace
+
+// The stiff predictor started from a given guess (nrows x N rows of V):
+// qh, iteration counts and the cells that fell back to the plain guess;
+// 0, -1 for an unknown combination, or -2 when a block deadlocked.
+extern "C" int host_predictor_guess(const char *name, int ndim, int N,
+                                    const double *w, long long nrows,
+                                    const double *dX, double dt, double tol,
+                                    const double *tabs, const double *guess,
+                                    double *qh, unsigned long long *iters,
+                                    int *max_iters,
+                                    unsigned long long *fallbacks) {
+  emu::g_deadlock = false;
+  int fail = 0;
+#define GUESS_CASE(NAME, NDIM, SYS, ORD, FL)                                   \
+  if (FL == 0 && SYS::HAS_S && !std::strcmp(name, NAME) && ndim == NDIM &&     \
+      N == ORD) {                                                              \
+    predictor_only<SYS, ORD>(ndim, 1, w, nrows, dX, dt, tol, tabs, qh, iters,  \
+                             max_iters, &fail, guess, fallbacks);              \
+    return emu::g_deadlock ? -2 : 0;                                           \
+  }
+  HOST_CASES(GUESS_CASE)
+#undef GUESS_CASE
+  return -1;
+}
 
 // np problems of one built-in system and order stepped as one batch; u_all
 // holds their states one after the other, nX/bt/dX are np x ndim.  0, -1

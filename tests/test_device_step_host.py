@@ -11,7 +11,8 @@ order, without one:
 - full runs of every built-in system, orders 1-3, 1-D to 3-D, periodic and
   transmissive axes, Rusanov/Roe/Osher fluxes, B terms, the second-order
   form and the stiff Newton predictor: final state, t and step count equal;
-- the predictor stage alone with its iteration counts;
+- the predictor stage alone with its iteration counts, and the Newton
+  predictor started from a given guess with its fallbacks;
 - batched steps (batch.cuh) of problems of mixed sizes, boundary types and
   end times: each problem equals the restatement run on it alone;
 - the fibers of a block run in thread order and in reverse order, and the
@@ -64,6 +65,11 @@ def step_lib(tmp_path_factory):
                                  c_d, c_d, ora.dp, ora.dp, ctypes.POINTER(ctypes.c_ulonglong),
                                  ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     L.host_set_order.argtypes = [c_int]
+    L.host_predictor_guess.restype = c_int
+    L.host_predictor_guess.argtypes = [ctypes.c_char_p, c_int, c_int, ora.dp, c_ll, ora.dp, c_d,
+                                       c_d, ora.dp, ora.dp, ora.dp,
+                                       ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(c_int),
+                                       ctypes.POINTER(ctypes.c_ulonglong)]
     L.host_run_batch.restype = c_int
     L.host_run_batch.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, c_int, ora.dp, ora.ip,
                                  ora.ip, ora.dp, ora.dp, ora.dp, ora.dp, c_int, c_d, c_int, c_int,
@@ -162,6 +168,39 @@ def test_device_predictor_equals_port(step_lib, case):
         assert rc == 0
         assert np.array_equal(qh, qh_o), np.abs(qh - qh_o).max()
         assert its.value == its_o and mx.value == mx_o and fail.value == 0
+
+
+@pytest.mark.parametrize("kind", ["exact", "close", "rough", "nan", "huge"])
+def test_device_newton_from_guess_equals_port(step_lib, kind):
+    """The Newton predictor started from a given guess (the warm start's
+    entry): qh, iteration counts and the cells reset to the plain guess
+    (non-finite or non-decreasing residual) equal the restatement's."""
+    n, N = 12, 2
+    u = workloads.relaxation(n, 2, seed=5)
+    dX = np.array([1 / n, 1 / n])
+    w = ora.weno(ora.boundaries(u, N, [1, 1]), N)
+    dt = ora.timestep("cattaneo", w, dX, N, 0.8, 10.0, 0.0, 0)
+    qh, _, _ = ora.predictor("cattaneo", w, dX, N, True, dt)
+    wb = np.repeat(w.reshape(-1, 1, 4, 7), N, axis=1).reshape(qh.shape)
+    rng = np.random.default_rng(1)
+    g = {"exact": qh, "close": qh + 1e-7 * (qh - wb) * rng.standard_normal(qh.shape),
+         "rough": qh + 0.3 * (qh - wb) * rng.standard_normal(qh.shape),
+         "nan": np.where(rng.random(qh.shape) < 0.01, np.nan, qh),
+         "huge": qh * 1e30}[kind]
+    q_o, it_o, mx_o, fb_o = ora.predictor_guess("cattaneo", w, dX, N, dt, g)
+    for reverse in (False, True):
+        step_lib.host_set_order(int(reverse))
+        q = np.zeros_like(qh)
+        its, mx, fb = ctypes.c_ulonglong(), ctypes.c_int(), ctypes.c_ulonglong()
+        rc = step_lib.host_predictor_guess(b"cattaneo", 2, N, ora.ptr(w), w.shape[0],
+                                           ora.ptr(dX), dt, 1e-12, ora.ptr(stages.tables(N)),
+                                           ora.ptr(np.ascontiguousarray(g)), ora.ptr(q),
+                                           ctypes.byref(its), ctypes.byref(mx), ctypes.byref(fb))
+        assert rc == 0
+        assert np.array_equal(q, q_o)
+        assert (its.value, mx.value, fb.value) == (it_o, mx_o, fb_o)
+    if kind == "nan":
+        assert fb_o > 0
 
 
 def test_device_mixed_precision_step(step_lib):
