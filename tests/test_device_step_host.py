@@ -264,3 +264,43 @@ def test_device_batch_equals_port(step_lib, batch, per_pop):
         assert steps_f[p] == steps_o and t_f[p] == t_o
         assert np.array_equal(u_f[o:o + u0.size].reshape(u0.shape), u_o)
         o += u0.size
+
+
+# (system, ndim, order, flux, stiff) combinations the host unit instantiates
+FUZZ_COMBOS = [("euler", 1, 1, 0, False), ("euler", 1, 2, 0, False), ("euler", 1, 3, 0, False),
+               ("euler", 1, 2, 1, False), ("euler", 1, 2, 2, False), ("euler", 2, 2, 0, False),
+               ("euler", 2, 3, 0, False), ("euler", 3, 2, 0, False),
+               ("cattaneo", 2, 1, 0, True), ("cattaneo", 2, 2, 0, True),
+               ("cattaneo", 2, 3, 0, True), ("cattaneo", 3, 2, 0, True),
+               ("ncp", 1, 2, 0, False), ("ncp", 2, 2, 0, False), ("burgers2", 1, 3, 0, False)]
+
+
+def test_device_step_fuzzed_small_grids(step_lib):
+    """Hypothesis-drawn small grids (1-7 cells per axis), boundary types,
+    states and step counts for every instantiated (system, ndim, order,
+    flux): the device step equals the restatement bit for bit."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @st.composite
+    def problems(draw):
+        name, ndim, N, flux, stiff = draw(st.sampled_from(FUZZ_COMBOS))
+        shape = tuple(draw(st.integers(1, 7)) for _ in range(ndim))
+        # a periodic axis needs at least N cells (the reference's wrap rule)
+        bt = [draw(st.integers(0, 1)) if n >= N else 0 for n in shape]
+        return name, shape, N, flux, stiff, bt, draw(st.integers(0, 2 ** 16)), \
+            draw(st.integers(1, 3)), draw(st.sampled_from([0.5, 0.8, 0.9]))
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True,
+                  suppress_health_check=list(hyp.HealthCheck))
+    @hyp.given(problems())
+    def check(prob):
+        name, shape, N, flux, stiff, bt, seed, K, cfl = prob
+        u0 = _state(name, shape, seed)
+        u_o, _, steps_o, t_o = ora.pde_solver(name, u0, 10.0, [1.0] * len(shape), bt, cfl, N,
+                                              stiff=stiff, flux=flux, max_steps=K)
+        u, steps, t, _ = _run(step_lib, name, u0, N, bt, cfl, K, stiff, flux)
+        assert steps == steps_o == K and t == t_o
+        assert np.array_equal(u, u_o, equal_nan=True), (prob, np.abs(u - u_o).max())
+
+    check()
