@@ -239,9 +239,13 @@ static inline double __longlong_as_double(long long x) {
 template <class T> static inline T max(T a, T b) { return a > b ? a : b; }
 template <class T> static inline T min(T a, T b) { return a < b ? a : b; }
 
+using std::exp;
 using std::fabs;
 using std::fma;
 using std::fmax;
+using std::fmin;
+using std::log;
+using std::pow;
 using std::sqrt;
 
 #include "step_kernels.cuh"
@@ -507,7 +511,18 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
 }
 } // namespace
 
-// The (system, ndim, order, flux) combinations this unit instantiates.
+// The (system, ndim, order, flux) combinations this unit instantiates:
+// with HOST_USER_SYSTEM (a file holding the `struct UserSystem` that
+// pypde_gb300.translate makes from Python callbacks, as the run-time
+// compiled kernels include it) and HOST_USER_N, that system under the name
+// "user" at order HOST_USER_N with each flux; otherwise the built-ins.
+#ifdef HOST_USER_SYSTEM
+#include HOST_USER_SYSTEM
+#define HOST_CASES(X)                                                          \
+  X("user", UserSystem::NDIM, UserSystem, HOST_USER_N, 0)                      \
+  X("user", UserSystem::NDIM, UserSystem, HOST_USER_N, 1)                      \
+  X("user", UserSystem::NDIM, UserSystem, HOST_USER_N, 2)
+#else
 #define HOST_CASES(X)                                                          \
   X("euler", 1, Euler<1>, 1, 0)                                                \
   X("euler", 1, Euler<1>, 2, 0)                                                \
@@ -524,6 +539,7 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
   X("ncp", 1, Ncp<1>, 2, 0)                                                    \
   X("ncp", 2, Ncp<2>, 2, 0)                                                    \
   X("burgers2", 1, Burgers2, 3, 0)
+#endif
 
 // Fibers run in reverse thread order when reverse is non-zero.
 extern "C" void host_set_order(int reverse) { emu::g_reverse = reverse != 0; }

@@ -22,59 +22,18 @@ order, without one:
 The only edit to the device headers is the one the host compiler needs:
 `extern __shared__ double smem[];` becomes a pointer to a host buffer."""
 import ctypes
-import glob
-import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
-from conftest import ROOT, l1
+from conftest import build_device_host, l1, load_device_host
 from oracle import ora
 from pypde_gb300 import stages, workloads
-
-CSRC = os.path.join(ROOT, "pypde_gb300", "csrc")
-DYN_SMEM = "extern __shared__ double smem[];"
 
 
 @pytest.fixture(scope="module")
 def step_lib(tmp_path_factory):
-    cxx = shutil.which("g++")
-    if cxx is None:
-        pytest.skip("no g++")
-    inc = tmp_path_factory.mktemp("devstep")
-    for f in glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")):
-        shutil.copy(f, inc)
-    k = os.path.join(inc, "kernels.cuh")
-    text = open(k).read()
-    assert text.count(DYN_SMEM) == 2
-    open(k, "w").write(text.replace(DYN_SMEM, "double *smem = host_dynamic_smem();"))
-    out = str(inc / "libdevice_step_host.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
-                    "-Wno-unknown-pragmas", "-I", str(inc), "-o", out,
-                    os.path.join(ROOT, "tests", "device_step_host.cpp")], check=True)
-    L = ctypes.CDLL(out)
-    c_int, c_ll, c_d = ctypes.c_int, ctypes.c_longlong, ctypes.c_double
-    L.host_run.restype = c_ll
-    L.host_run.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, ora.dp, ora.ip, ora.ip, ora.dp,
-                           ora.dp, c_d, c_d, c_int, c_d, c_int, c_ll, ctypes.POINTER(c_d),
-                           ctypes.POINTER(ctypes.c_ulonglong)]
-    L.host_predictor.restype = c_int
-    L.host_predictor.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, ora.dp, c_ll, ora.dp,
-                                 c_d, c_d, ora.dp, ora.dp, ctypes.POINTER(ctypes.c_ulonglong),
-                                 ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
-    L.host_set_order.argtypes = [c_int]
-    L.host_predictor_guess.restype = c_int
-    L.host_predictor_guess.argtypes = [ctypes.c_char_p, c_int, c_int, ora.dp, c_ll, ora.dp, c_d,
-                                       c_d, ora.dp, ora.dp, ora.dp,
-                                       ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(c_int),
-                                       ctypes.POINTER(ctypes.c_ulonglong)]
-    L.host_run_batch.restype = c_int
-    L.host_run_batch.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, c_int, ora.dp, ora.ip,
-                                 ora.ip, ora.dp, ora.dp, ora.dp, ora.dp, c_int, c_d, c_int, c_int,
-                                 c_ll, ctypes.POINTER(c_ll), ora.dp]
-    return L
+    return load_device_host(build_device_host(tmp_path_factory.mktemp("devstep")))
 
 
 def _run(L, name, u0, N, bt, cfl, K, stiff=False, flux=0, tol=1e-12, mixed=0, reverse=False):
