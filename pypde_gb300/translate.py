@@ -15,12 +15,23 @@ Supported subset (what the reference's example systems use):
     at translation time, return;
   * + - * / ** (x**2 -> x*x, x**0.5 -> sqrt), unary -, comparisons, and/or/
     not, `a if c else b`; arrays combine elementwise and broadcast scalars;
-  * Q[i], Q[a:b], DQ[d][i], DQ[d, i], DQ[d]; zeros(n), zeros((n, m)),
-    array([...]), array([[...], ...]), len(), abs/min/max, sqrt, exp, log,
-    sin, cos, tan, tanh, pow, floor, sum, dot (with or without a numpy /
-    math prefix);
-  * calls to other plain Python functions (translated as device functions)
-    and numeric constants from the callback's globals or closure.
+  * Q[i], Q[a:b], DQ[d][i], DQ[d, i], DQ[d]; slices are views, as numpy's,
+    so `ret[a:b] = x` and `ret[i, a:b] -= x` write into ret; slice bounds
+    are constants or x + a : x + b around one expression (`5 + d:8 + d`);
+  * zeros(n), zeros((n, m)), eye(n), array([...]), array([[...], ...]),
+    len(), abs/min/max, sqrt, exp, log, sin, cos, tan, tanh, pow, floor,
+    sum, trace, det (up to 3x3), dot / @ for vectors and matrices, and the
+    array methods and attributes copy, reshape, ravel, flatten, sum, dot,
+    transpose and .T (with or without a numpy / numpy.linalg / math prefix);
+  * calls to other plain Python functions, also through a module attribute
+    (translated as device functions; a numba-jitted helper contributes its
+    Python function), including helpers that return a tuple, which unpacks
+    at the call site: `rho, v, A = get_variables(Q)`;
+  * numeric constants from the callback's globals, closure or an imported
+    module; comparisons of constants fold, so a branch on a module flag
+    (`if EOS == STIFFENED_GAS:`, `if tau == inf:`) keeps only its taken side
+    and code after a return that always runs is not translated;
+  * any Python identifier (Greek letters included): C names are ASCII.
 Every expression is emitted in Python's evaluation order with no algebraic
 rewriting, so a callback that a C restatement writes the same way gives the
 same bits (the kernels are compiled without FMA contraction).
@@ -40,12 +51,21 @@ class TranslateError(ValueError):
     pass
 
 
-class T:
-    """Type of a translated expression: int, float, or an array shape."""
-    INT, FLT, ARR = "int", "float", "arr"
+def _cid(name):
+    """An ASCII C identifier for a Python identifier (Python allows letters
+    such as the Greek ones the reference's examples use; C++ compilers need
+    not): other characters become _u<hex>_."""
+    return "".join(c if (c.isascii() and (c.isalnum() or c == "_")) else f"_u{ord(c):x}_"
+                   for c in name)
 
-    def __init__(self, kind, shape=()):
-        self.kind, self.shape = kind, tuple(shape)
+
+class T:
+    """Type of a translated expression: int, float, an array shape, or the
+    tuple a helper function returns (elems: the types of its items)."""
+    INT, FLT, ARR, TUP = "int", "float", "arr", "tuple"
+
+    def __init__(self, kind, shape=(), elems=()):
+        self.kind, self.shape, self.elems = kind, tuple(shape), tuple(elems)
 
     @property
     def n(self):
@@ -131,6 +151,11 @@ class Fn:
             self.emit(f"double {name}{' = ' + init if init else ''};")
         return name
 
+    def copy(self, v, t):
+        out = self.new(t)
+        self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {v}[i_];")
+        return out
+
     def emit(self, s):
         self.lines.append("  " * self.depth + s)
 
@@ -150,12 +175,39 @@ class Fn:
             if node.id in ("V",) and "V" not in self.globals:
                 return self.tr.V
             v = self.globals.get(node.id)
-            if isinstance(v, (int, float)) and not isinstance(v, bool):
+            if isinstance(v, (int, float)):
                 return v
             return None
         if isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name):
-            if node.value.id in ("math", "np", "numpy") and node.attr in ("pi", "e"):
+            if node.value.id in ("math", "np", "numpy") and node.attr in ("pi", "e", "inf"):
                 return getattr(math, node.attr)
+            mod = self.globals.get(node.value.id)
+            if node.value.id not in self.env and inspect.ismodule(mod):
+                v = getattr(mod, node.attr, None)
+                if isinstance(v, (int, float)) and not isinstance(v, bool):
+                    return v
+            return None
+        if isinstance(node, ast.Compare):
+            # comparisons of translation-time constants fold, so branches on
+            # module flags (an equation-of-state switch, an infinite
+            # relaxation time) drop out with the code they guard
+            vals = [self.const(node.left)] + [self.const(c) for c in node.comparators]
+            if any(v is None for v in vals):
+                return None
+            cmp = {ast.Lt: lambda x, y: x < y, ast.LtE: lambda x, y: x <= y,
+                   ast.Gt: lambda x, y: x > y, ast.GtE: lambda x, y: x >= y,
+                   ast.Eq: lambda x, y: x == y, ast.NotEq: lambda x, y: x != y}
+            if any(type(op) not in cmp for op in node.ops):
+                return None
+            return all(cmp[type(op)](a, b) for op, a, b in zip(node.ops, vals, vals[1:]))
+        if isinstance(node, ast.BoolOp):
+            vals = [self.const(v) for v in node.values]
+            if any(v is None for v in vals):
+                return None
+            return all(vals) if isinstance(node.op, ast.And) else any(vals)
+        if isinstance(node, ast.UnaryOp) and isinstance(node.op, ast.Not):
+            v = self.const(node.operand)
+            return None if v is None else (not v)
         if isinstance(node, ast.UnaryOp) and isinstance(node.op, ast.USub):
             v = self.const(node.operand)
             return None if v is None else -v
@@ -205,7 +257,7 @@ class Fn:
             except (TypeError, ValueError):
                 vals = None
             if vals is not None:
-                cn = f"g_{node.id}"
+                cn = f"g_{_cid(node.id)}"
                 pad = "  " * self.base_depth
                 self.lines.insert(0, f"{pad}const double {cn}[{len(vals)}] = "
                                      f"{{{', '.join(self.lit(v) for v in vals)}}};")
@@ -255,6 +307,9 @@ class Fn:
             return self.subscript(node)
         if isinstance(node, ast.Call):
             return self.call(node)
+        if isinstance(node, ast.Attribute) and node.attr == "T":
+            v, t = self.expr(node.value)
+            return self.transpose(v, t, node)
         if isinstance(node, (ast.List, ast.Tuple)):
             return self.array_literal(node.elts, node)
         self.err(node, f"unsupported expression {type(node).__name__}")
@@ -270,42 +325,89 @@ class Fn:
             self.err(node, "index must be an integer expression")
         return v, None
 
-    def subscript(self, node):
+    def _offset(self, node):
+        """Split node into (x, a) with node == x + a for a constant integer
+        a (a = 0 when there is none)."""
+        if isinstance(node, ast.BinOp) and isinstance(node.op, (ast.Add, ast.Sub)):
+            c = self.const(node.right)
+            if isinstance(c, int) and not isinstance(c, bool):
+                return node.left, (c if isinstance(node.op, ast.Add) else -c)
+            c = self.const(node.left)
+            if isinstance(c, int) and not isinstance(c, bool) and isinstance(node.op, ast.Add):
+                return node.right, c
+        return node, 0
+
+    def _slice(self, s, size, node):
+        """(C expression of the start, length) of a step-1 slice whose length
+        is known at translation time: constant bounds (numpy's negative and
+        clipped bounds included), or bounds x + a : x + b around one
+        expression x."""
+        if s.step is not None and self.const(s.step) != 1:
+            self.err(node, "slices need step 1")
+        lo = 0 if s.lower is None else self.const(s.lower)
+        hi = size if s.upper is None else self.const(s.upper)
+        if lo is not None and hi is not None:
+            lo = max(lo + size, 0) if lo < 0 else min(lo, size)
+            hi = max(hi + size, 0) if hi < 0 else min(hi, size)
+            if hi <= lo:
+                self.err(node, "empty slice")
+            return str(lo), hi - lo
+        if s.lower is None or s.upper is None:
+            self.err(node, "slices need constant bounds or bounds x + a : x + b")
+        xl, al = self._offset(s.lower)
+        xu, au = self._offset(s.upper)
+        if ast.dump(xl) != ast.dump(xu) or au <= al:
+            self.err(node, "slices need constant bounds or bounds x + a : x + b")
+        lo_c, _ = self.index_expr(s.lower)
+        return lo_c, au - al
+
+    def subscript(self, node, target=False):
+        """Elements, rows and slices.  Slices and rows of contiguous memory
+        are views (a pointer into the array), as numpy's are, so they can be
+        assigned to; a column slice of a 2-D array is a copy and cannot."""
         base, bt = self.expr(node.value)
         if bt.kind != T.ARR:
             self.err(node, "subscript of a scalar")
         sl = node.slice
-        if isinstance(sl, ast.Tuple):
-            idx = sl.elts
-        else:
-            idx = [sl]
+        idx = sl.elts if isinstance(sl, ast.Tuple) else [sl]
         if len(idx) == 1 and isinstance(idx[0], ast.Slice):
-            s = idx[0]
-            lo = 0 if s.lower is None else self.const(s.lower)
-            hi = bt.shape[0] if s.upper is None else self.const(s.upper)
-            if lo is None or hi is None or s.step is not None:
-                self.err(node, "slices need constant bounds")
-            if lo < 0:
-                lo += bt.shape[0]
-            if hi < 0:
-                hi += bt.shape[0]
-            if len(bt.shape) != 1:
-                self.err(node, "slices of 2-D arrays are not supported")
-            t = _arr(hi - lo)
-            out = self.new(t)
-            self.emit(f"for (int i_ = 0; i_ < {hi - lo}; i_++) {out}[i_] = {base}[{lo} + i_];")
-            return out, t
+            lo, n = self._slice(idx[0], bt.shape[0], node)
+            if len(bt.shape) == 1:
+                return f"({base} + {lo})", _arr(n)
+            return f"({base} + ({lo}) * {bt.shape[1]})", _arr(n, bt.shape[1])
         if len(idx) == 1 and len(bt.shape) == 2:
             r, _ = self.index_expr(idx[0])
-            t = _arr(bt.shape[1])
-            return f"({base} + ({r}) * {bt.shape[1]})", t  # row view
+            return f"({base} + ({r}) * {bt.shape[1]})", _arr(bt.shape[1])  # row view
         if len(idx) == 1:
             i, _ = self.index_expr(idx[0])
             return f"{base}[{i}]", FLT
         if len(idx) == 2 and len(bt.shape) == 2:
-            i, _ = self.index_expr(idx[0])
-            j, _ = self.index_expr(idx[1])
-            return f"{base}[({i}) * {bt.shape[1]} + ({j})]", FLT
+            ncol = bt.shape[1]
+            rs, cs = isinstance(idx[0], ast.Slice), isinstance(idx[1], ast.Slice)
+            if not rs and not cs:
+                i, _ = self.index_expr(idx[0])
+                j, _ = self.index_expr(idx[1])
+                return f"{base}[({i}) * {ncol} + ({j})]", FLT
+            if not rs:  # part of one row: contiguous
+                i, _ = self.index_expr(idx[0])
+                lo, n = self._slice(idx[1], ncol, node)
+                return f"({base} + ({i}) * {ncol} + ({lo}))", _arr(n)
+            if target:
+                self.err(node, "assignment to a column slice of a 2-D array")
+            rlo, nr = self._slice(idx[0], bt.shape[0], node)
+            if not cs:
+                j, _ = self.index_expr(idx[1])
+                t = _arr(nr)
+                out = self.new(t)
+                self.emit(f"for (int i_ = 0; i_ < {nr}; i_++) "
+                          f"{out}[i_] = {base}[(({rlo}) + i_) * {ncol} + ({j})];")
+                return out, t
+            clo, nc = self._slice(idx[1], ncol, node)
+            t = _arr(nr, nc)
+            out = self.new(t)
+            self.emit(f"for (int i_ = 0; i_ < {nr * nc}; i_++) {out}[i_] = "
+                      f"{base}[(({rlo}) + i_ / {nc}) * {ncol} + ({clo}) + i_ % {nc}];")
+            return out, t
         self.err(node, "unsupported subscript")
 
     def array_literal(self, elts, node):
@@ -333,6 +435,8 @@ class Fn:
 
     def binop(self, node):
         op = node.op
+        if isinstance(op, ast.MatMult):
+            return self.dot(*self.expr(node.left), *self.expr(node.right), node)
         if isinstance(op, ast.Pow):
             b, tb = self.expr(node.left)
             e = self.const(node.right)
@@ -374,16 +478,148 @@ class Fn:
         self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {ai} {sym} {bi};")
         return out, t
 
+    def transpose(self, v, t, node):
+        if t.kind != T.ARR or len(t.shape) > 2:
+            self.err(node, "transpose of a scalar")
+        if len(t.shape) == 1:
+            return v, t
+        m, n = t.shape
+        rt = _arr(n, m)
+        out = self.new(rt)
+        self.emit(f"for (int i_ = 0; i_ < {m * n}; i_++) "
+                  f"{out}[i_] = {v}[(i_ % {m}) * {n} + i_ / {m}];")
+        return out, rt
+
+    def dot(self, a, ta, b, tb, node):
+        """numpy's dot / @ for 1-D and 2-D operands; each sum runs over the
+        shared index in increasing order."""
+        if ta.kind != T.ARR or tb.kind != T.ARR:
+            self.err(node, "dot of a scalar")
+        sa, sb = ta.shape, tb.shape
+        if sa[-1] != sb[0]:
+            self.err(node, f"dot of shapes {sa} and {sb}")
+        k = sa[-1]
+        if len(sa) == 1 and len(sb) == 1:
+            acc = self.new(FLT, "0.0")
+            self.emit(f"for (int i_ = 0; i_ < {k}; i_++) {acc} += {a}[i_] * {b}[i_];")
+            return acc, FLT
+        m = sa[0] if len(sa) == 2 else 1
+        n = sb[1] if len(sb) == 2 else 1
+        shape = tuple(x for x, keep in ((m, len(sa) == 2), (n, len(sb) == 2)) if keep)
+        rt = _arr(*shape)
+        out = self.new(rt)
+        self.emit(f"for (int i_ = 0; i_ < {m}; i_++) for (int j_ = 0; j_ < {n}; j_++) {{")
+        self.emit(f"  double s_ = 0.0;")
+        self.emit(f"  for (int k_ = 0; k_ < {k}; k_++) "
+                  f"s_ += {a}[i_ * {k} + k_] * {b}[k_ * {n} + j_];")
+        self.emit(f"  {out}[i_ * {n} + j_] = s_;")
+        self.emit("}")
+        return out, rt
+
+    def det(self, v, t, node):
+        """Determinant of a 1x1, 2x2 or 3x3 matrix by cofactor expansion
+        along the first row."""
+        if t.kind != T.ARR or len(t.shape) != 2 or t.shape[0] != t.shape[1] or t.shape[0] > 3:
+            self.err(node, "det() of a 1x1, 2x2 or 3x3 matrix only")
+        n = t.shape[0]
+        a = [[f"{v}[{i * n + j}]" for j in range(n)] for i in range(n)]
+        if n == 1:
+            return a[0][0], FLT
+        if n == 2:
+            return f"({a[0][0]} * {a[1][1]} - {a[0][1]} * {a[1][0]})", FLT
+        m = [f"({a[1][1]} * {a[2][2]} - {a[1][2]} * {a[2][1]})",
+             f"({a[1][0]} * {a[2][2]} - {a[1][2]} * {a[2][0]})",
+             f"({a[1][0]} * {a[2][1]} - {a[1][1]} * {a[2][0]})"]
+        return f"({a[0][0]} * {m[0]} - {a[0][1]} * {m[1]} + {a[0][2]} * {m[2]})", FLT
+
+    def method(self, node, obj, attr, args):
+        """Array methods: copy, reshape, ravel/flatten, transpose, sum, dot."""
+        v, t = self.expr(obj)
+        if t.kind != T.ARR:
+            self.err(node, f".{attr}() of a scalar")
+        if attr == "copy":
+            return self.copy(v, t), t
+        if attr == "reshape":
+            dims = args[0].elts if len(args) == 1 and isinstance(args[0], (ast.Tuple, ast.List)) \
+                else args
+            shape = [self.const(x) for x in dims]
+            if any(not isinstance(x, int) for x in shape):
+                self.err(node, "reshape() needs a constant shape")
+            if -1 in shape:
+                rest = 1
+                for x in shape:
+                    rest *= x if x != -1 else 1
+                shape[shape.index(-1)] = t.n // rest
+            nt = _arr(*shape)
+            if nt.n != t.n:
+                self.err(node, f"cannot reshape {t.shape} to {tuple(shape)}")
+            return v, nt
+        if attr in ("ravel", "flatten"):
+            return (self.copy(v, t) if attr == "flatten" else v), _arr(t.n)
+        if attr == "transpose":
+            return self.transpose(v, t, node)
+        if attr == "sum" and not args:
+            acc = self.new(FLT, "0.0")
+            self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {acc} += {v}[i_];")
+            return acc, FLT
+        if attr == "dot" and len(args) == 1:
+            return self.dot(v, t, *self.expr(args[0]), node)
+        self.err(node, f"unsupported array method .{attr}()")
+
     def call(self, node):
         f = node.func
-        if isinstance(f, ast.Attribute) and isinstance(f.value, ast.Name) and \
-                f.value.id in ("np", "numpy", "math"):
-            name = f.attr
+        args = node.args
+        name = None
+        if isinstance(f, ast.Attribute):
+            # np.f, numpy.linalg.f, math.f, a module's function, or a method
+            chain, base = [f.attr], f.value
+            while isinstance(base, ast.Attribute):
+                chain.append(base.attr)
+                base = base.value
+            root = base.id if isinstance(base, ast.Name) else None
+            mod = None if root is None or root in self.env else self.globals.get(root)
+            if root in ("np", "numpy", "math") or (inspect.ismodule(mod) and
+                                                   mod.__name__.split(".")[0] in
+                                                   ("numpy", "math")):
+                name = f.attr
+            elif inspect.ismodule(mod):
+                target = mod
+                for a in reversed(chain):
+                    target = getattr(target, a, None)
+                if target is not None and hasattr(target, "py_func"):
+                    target = target.py_func
+                if callable(target) and hasattr(target, "__code__"):
+                    return self.tr.call_helper(self, target, args, node)
+                self.err(node, f"unsupported function {'.'.join([root] + chain[::-1])}")
+            else:
+                return self.method(node, f.value, f.attr, args)
         elif isinstance(f, ast.Name):
             name = f.id
         else:
             self.err(node, "unsupported call")
-        args = node.args
+        if name in ("eye", "identity"):
+            n = self.const(args[0])
+            if not isinstance(n, int):
+                self.err(node, f"{name}() needs a constant size")
+            t = _arr(n, n)
+            out = self.new(t)
+            self.emit(f"for (int i_ = 0; i_ < {n * n}; i_++) "
+                      f"{out}[i_] = (i_ % {n + 1} == 0) ? 1.0 : 0.0;")
+            return out, t
+        if name == "transpose" and len(args) == 1:
+            return self.transpose(*self.expr(args[0]), node)
+        if name == "trace" and len(args) == 1:
+            v, t = self.expr(args[0])
+            if t.kind != T.ARR or len(t.shape) != 2:
+                self.err(node, "trace() of a matrix only")
+            acc = self.new(FLT, "0.0")
+            self.emit(f"for (int i_ = 0; i_ < {min(t.shape)}; i_++) "
+                      f"{acc} += {v}[i_ * {t.shape[1] + 1}];")
+            return acc, FLT
+        if name == "det" and len(args) == 1:
+            return self.det(*self.expr(args[0]), node)
+        if name in ("matmul",) and len(args) == 2:
+            return self.dot(*self.expr(args[0]), *self.expr(args[1]), node)
         if name in ("zeros", "empty", "zeros_like"):
             if name == "zeros_like":
                 _, t = self.expr(args[0])
@@ -435,11 +671,7 @@ class Fn:
             self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {acc} += {v}[i_];")
             return acc, FLT
         if name in ("dot", "inner") and len(args) == 2:
-            a, ta = self.expr(args[0])
-            b, tb = self.expr(args[1])
-            acc = self.new(FLT, "0.0")
-            self.emit(f"for (int i_ = 0; i_ < {ta.n}; i_++) {acc} += {a}[i_] * {b}[i_];")
-            return acc, FLT
+            return self.dot(*self.expr(args[0]), *self.expr(args[1]), node)
         if name in ("float",):
             v, _ = self.expr(args[0])
             return f"(double)({v})", FLT
@@ -471,7 +703,7 @@ class Fn:
             return
         # Python names live for the whole function: declare at the top so a
         # name first bound inside an if/for block is visible after it
-        cn = f"v_{name}"
+        cn = f"v_{_cid(name)}"
         pad = "  " * self.base_depth
         if t.kind == T.ARR:
             self.lines.insert(0, f"{pad}double {cn}[{t.n}];")
@@ -489,14 +721,25 @@ class Fn:
                 self.err(node, "chained assignment")
             tgt = node.targets[0]
             if isinstance(tgt, ast.Tuple):
-                if not isinstance(node.value, ast.Tuple) or len(node.value.elts) != len(tgt.elts):
-                    self.err(node, "tuple assignment needs a tuple of the same length")
-                vals = [self.expr(e) for e in node.value.elts]
-                tmps = []
-                for v, t in vals:
-                    if t.kind == T.ARR:
-                        self.err(node, "tuple assignment of arrays")
-                    tmps.append((self.new(t, v), t))
+                if not all(isinstance(e, ast.Name) for e in tgt.elts):
+                    self.err(node, "tuple assignment to names only")
+                nt = len(tgt.elts)
+                if isinstance(node.value, ast.Tuple):
+                    if len(node.value.elts) != nt:
+                        self.err(node, "tuple assignment needs a tuple of the same length")
+                    vals = [self.expr(e) for e in node.value.elts]
+                else:
+                    # a helper's tuple, or the items of a 1-D array
+                    v, t = self.expr(node.value)
+                    if t.kind == T.TUP and len(t.elems) == nt:
+                        vals = list(zip(v, t.elems))
+                    elif t.kind == T.ARR and len(t.shape) == 1 and t.shape[0] == nt:
+                        vals = [(f"{v}[{k}]", FLT) for k in range(nt)]
+                    else:
+                        self.err(node, "tuple assignment needs a tuple of the same length")
+                # evaluate every item before binding any name (a, b = b, a)
+                tmps = [(self.copy(v, t) if t.kind == T.ARR else self.new(t, v), t)
+                        for v, t in vals]
                 for tg, (v, t) in zip(tgt.elts, tmps):
                     self.assign_name(tg.id, v, t, node)
                 return
@@ -505,6 +748,8 @@ class Fn:
                 self.assign_name(tgt.id, v, t, node)
                 return
             if isinstance(tgt, ast.Subscript):
+                if t.kind == T.ARR and v.startswith("("):  # a view: may overlap
+                    v = self.copy(v, t)
                 lhs, lt = self.subscript_target(tgt)
                 if lt.kind == T.ARR:
                     if t.kind == T.ARR:
@@ -520,6 +765,8 @@ class Fn:
             if sym is None:
                 self.err(node, "unsupported augmented assignment")
             v, t = self.expr(node.value)
+            if t.kind == T.ARR and v.startswith("("):  # a view: may overlap
+                v = self.copy(v, t)
             if isinstance(node.target, ast.Name):
                 cn, ct = self.env[node.target.id]
                 if ct.kind == T.ARR:
@@ -536,14 +783,19 @@ class Fn:
                 self.emit(f"{lhs} = {lhs} {sym} {v};")
             return
         if isinstance(node, ast.If):
+            k = self.const(node.test)
+            if k is not None:  # known at translation time: only the taken side
+                return self.run(node.body if k else node.orelse)
             c, _ = self.expr(node.test)
             self.emit(f"if ({c}) {{")
-            self.block(node.body)
+            ends = self.block(node.body)
             if node.orelse:
                 self.emit("} else {")
-                self.block(node.orelse)
+                ends = self.block(node.orelse) and ends
+            else:
+                ends = False
             self.emit("}")
-            return
+            return ends
         if isinstance(node, ast.For):
             if not (isinstance(node.iter, ast.Call) and isinstance(node.iter.func, ast.Name) and
                     node.iter.func.id == "range" and isinstance(node.target, ast.Name)):
@@ -556,7 +808,7 @@ class Fn:
             if step == 0:
                 self.err(node, "range() step of 0")
             var = node.target.id
-            cn = f"v_{var}"
+            cn = f"v_{_cid(var)}"
             cmp = "<" if step > 0 else ">"
             self.emit(f"for (int {cn} = {lo}; {cn} {cmp} {hi}; {cn} += {step}) {{")
             old = self.env.get(var)
@@ -569,23 +821,37 @@ class Fn:
             self.emit("}")
             return
         if isinstance(node, ast.Return):
+            if getattr(self, "is_helper", False) and isinstance(node.value, ast.Tuple):
+                vals = [self.expr(e) for e in node.value.elts]
+                self.tr.on_return(self, [v for v, _ in vals],
+                                  T(T.TUP, elems=[t for _, t in vals]), node)
+                return True
             v, t = self.expr(node.value)
             self.tr.on_return(self, v, t, node)
-            return
+            return True
         if isinstance(node, ast.Pass):
             return
         self.err(node, f"unsupported statement {type(node).__name__}")
 
     def subscript_target(self, node):
-        v, t = self.subscript(node)
+        v, t = self.subscript(node, target=True)
         return v, t
+
+    def run(self, body):
+        """Translate statements until one that always returns (the rest is
+        dead code, which may name things that exist only on other paths);
+        True when the body always returns."""
+        for s in body:
+            if self.stmt(s):
+                return True
+        return False
 
     def block(self, body):
         # names first bound inside a block are hoisted so they outlive it
         self.depth += 1
-        for s in body:
-            self.stmt(s)
+        ends = self.run(body)
         self.depth -= 1
+        return ends
 
     def hoist(self):
         """Declare, before the body, every name assigned in a nested block."""
@@ -618,6 +884,14 @@ class Translator:
                 target, [None if v is None else v[1] for v in vals], consts)
         cname, rt = self.helpers[key]
         argv = ", ".join(v[0] for v in vals if v is not None)
+        if rt.kind == T.TUP:
+            outs, refs = [], []
+            for et in rt.elems:
+                o = fn.new(et)
+                outs.append(o)
+                refs.append(o if et.kind == T.ARR else f"&{o}")
+            fn.emit(f"{cname}({argv}{', ' if argv else ''}{', '.join(refs)});")
+            return outs, rt
         if rt.kind == T.ARR:
             out = fn.new(rt)
             fn.emit(f"{cname}({argv}{', ' if argv else ''}{out});")
@@ -626,6 +900,7 @@ class Translator:
 
     def translate_helper(self, func, arg_types, consts):
         h = Fn(self, func, None)
+        h.is_helper = True
         names = [a.arg for a in h.node.args.args]
         if len(names) != len(arg_types):
             raise TranslateError(f"{func.__name__}: wrong number of arguments")
@@ -635,32 +910,58 @@ class Translator:
                 h.globals[nm] = c
                 continue
             if t.kind == T.ARR:
-                params.append(f"const double *p_{nm}")
+                params.append(f"const double *p_{_cid(nm)}")
             elif t.kind == T.INT:
-                params.append(f"int p_{nm}")
+                params.append(f"int p_{_cid(nm)}")
             else:
-                params.append(f"double p_{nm}")
-            h.env[nm] = (f"p_{nm}", t)
+                params.append(f"double p_{_cid(nm)}")
+            h.env[nm] = (f"p_{_cid(nm)}", t)
         rtype = {}
 
+        def same(a, b):
+            return a.kind == b.kind and a.shape == b.shape or \
+                (a.kind != T.ARR and b.kind != T.ARR and T.TUP not in (a.kind, b.kind))
+
         def on_ret(fn, v, t, node):
-            if "t" not in rtype:
-                rtype["t"] = t
+            # every return of a helper gives the same kind of value; a scalar
+            # helper returns double when any of its returns is a float
+            first = rtype.setdefault("t", t)
+            if t.kind == T.TUP:
+                if first.kind != T.TUP or len(first.elems) != len(t.elems) or \
+                        not all(same(a, b) for a, b in zip(first.elems, t.elems)):
+                    fn.err(node, "returns of different shapes")
+                rtype["t"] = first = T(T.TUP, elems=[
+                    FLT if FLT in (a, b) or T.FLT in (a.kind, b.kind) and a.kind != T.ARR
+                    else a for a, b in zip(first.elems, t.elems)])
+                for k, (vk, tk) in enumerate(zip(v, first.elems)):
+                    if tk.kind == T.ARR:
+                        fn.emit(f"for (int i_ = 0; i_ < {tk.n}; i_++) ret{k}_[i_] = {vk}[i_];")
+                    else:
+                        fn.emit(f"*ret{k}_ = {vk};")
+                fn.emit("return;")
+                return
+            if not same(first, t):
+                fn.err(node, "returns of different shapes")
             if t.kind == T.ARR:
                 fn.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) ret_[i_] = {v}[i_];")
                 fn.emit("return;")
             else:
+                if t.kind == T.FLT:
+                    rtype["t"] = FLT
                 fn.emit(f"return {v};")
         saved = self.on_return
         self.on_return = on_ret
         try:
-            for s in h.node.body:
-                h.stmt(s)
+            h.run(h.node.body)
         finally:
             self.on_return = saved
         rt = rtype.get("t", FLT)
-        cname = f"h_{func.__name__.strip('<>')}_{len(self.helpers)}"
-        if rt.kind == T.ARR:
+        cname = f"h_{_cid(func.__name__.strip('<>'))}_{len(self.helpers)}"
+        if rt.kind == T.TUP:
+            outs = [f"{'int' if et.kind == T.INT else 'double'} *ret{k}_"
+                    for k, et in enumerate(rt.elems)]
+            sig = f"__device__ __forceinline__ void {cname}({', '.join(params + outs)})"
+        elif rt.kind == T.ARR:
             sig = f"__device__ __forceinline__ void {cname}({', '.join(params + ['double *ret_'])})"
         else:
             ctype = "int" if rt.kind == T.INT else "double"
@@ -701,8 +1002,7 @@ class Translator:
                 raise TranslateError("S takes (Q)")
             fn.env[names[0]] = ("Q", _arr(V))
         fn.depth = fn.base_depth = 2
-        for s in fn.node.body:
-            fn.stmt(s)
+        fn.run(fn.node.body)
         body = "\n".join(fn.lines)
         return f"  {sig} {{\n{body}\n  }}\n"
 

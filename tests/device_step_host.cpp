@@ -41,6 +41,12 @@
 #include <functional>
 #include <vector>
 
+// Entry points are the only exported symbols: the unit is built with hidden
+// visibility and without GNU unique symbols, so that the block-shared
+// statics of two of these libraries loaded into one process (two run-time
+// systems, each a `UserSystem`) stay apart.
+#define HOST_API extern "C" __attribute__((visibility("default")))
+
 #define __device__
 #define __host__
 #define __global__
@@ -542,12 +548,12 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
 #endif
 
 // Fibers run in reverse thread order when reverse is non-zero.
-extern "C" void host_set_order(int reverse) { emu::g_reverse = reverse != 0; }
+HOST_API void host_set_order(int reverse) { emu::g_reverse = reverse != 0; }
 
 // K steps of a built-in system through the device kernels; returns the
 // steps taken, -1 for a combination this unit does not instantiate, or -2
 // when a block deadlocked at its barriers.
-extern "C" long long host_run(const char *name, int ndim, int N, int flux,
+HOST_API long long host_run(const char *name, int ndim, int N, int flux,
                               double *u, const int *nX, const int *bt,
                               const double *dX, const double *tabs, double tf,
                               double cfl, int stiff, double tol, int mixed,
@@ -568,7 +574,7 @@ extern "C" long long host_run(const char *name, int ndim, int N, int flux,
 
 // The predictor stage alone; 0, -1 for an unknown combination, or -2 when
 // a block deadlocked at its barriers.
-extern "C" int host_predictor(const char *name, int ndim, int N, int stiff,
+HOST_API int host_predictor(const char *name, int ndim, int N, int stiff,
                               const double *w, long long nrows,
                               const double *dX, double dt, double tol,
                               const double *tabs, double *qh,
@@ -742,7 +748,7 @@ void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
 // The stiff predictor started from a given guess (nrows x N rows of V):
 // qh, iteration counts and the cells that fell back to the plain guess;
 // 0, -1 for an unknown combination, or -2 when a block deadlocked.
-extern "C" int host_predictor_guess(const char *name, int ndim, int N,
+HOST_API int host_predictor_guess(const char *name, int ndim, int N,
                                     const double *w, long long nrows,
                                     const double *dX, double dt, double tol,
                                     const double *tabs, const double *guess,
@@ -766,7 +772,7 @@ extern "C" int host_predictor_guess(const char *name, int ndim, int N,
 // np problems of one built-in system and order stepped as one batch; u_all
 // holds their states one after the other, nX/bt/dX are np x ndim.  0, -1
 // for an unknown combination, or -2 when a block deadlocked.
-extern "C" int host_run_batch(const char *name, int ndim, int N, int flux,
+HOST_API int host_run_batch(const char *name, int ndim, int N, int flux,
                               int np, double *u_all, const int *nX,
                               const int *bt, const double *dX,
                               const double *tf, const double *cfl,

@@ -189,13 +189,16 @@ def _port_callbacks(F, B, S, ndim, V):
         q = np.ctypeslib.as_array(Q, (V,)).copy()
         if nargs(F) == 3:
             r = F(q, np.ctypeslib.as_array(dQ, (ndim * V,)).reshape(ndim, V).copy(), d)
-        else:
+        elif nargs(F) == 2:
             r = F(q, d)
+        else:
+            r = F(q)
         np.ctypeslib.as_array(out, (V,))[:] = r
 
     def wrap_b(out, Q, d):
+        q = np.ctypeslib.as_array(Q, (V,)).copy()
         np.ctypeslib.as_array(out, (V * V,))[:] = \
-            np.asarray(B(np.ctypeslib.as_array(Q, (V,)).copy(), d)).reshape(-1)
+            np.asarray(B(q, d) if nargs(B) == 2 else B(q)).reshape(-1)
 
     def wrap_s(out, Q):
         np.ctypeslib.as_array(out, (V,))[:] = S(np.ctypeslib.as_array(Q, (V,)).copy())
