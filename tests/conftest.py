@@ -58,10 +58,16 @@ def build_device_host(out_dir, defines=()):
     assert text.count(DYN_SMEM) == 2
     open(k, "w").write(text.replace(DYN_SMEM, "double *smem = host_dynamic_smem();"))
     out = os.path.join(out_dir, "libdevice_step_host.so")
+    # PYPDE_HOST_ASAN=1 builds with AddressSanitizer, a bounds check of the
+    # kernel source on the CPU (run with LD_PRELOAD=$(g++
+    # -print-file-name=libasan.so) and ASAN_OPTIONS=detect_leaks=0:
+    # detect_stack_use_after_return=0, the fibers switch stacks)
+    opt = ["-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer"] \
+        if os.environ.get("PYPDE_HOST_ASAN") == "1" else ["-O2"]
     # hidden visibility and no GNU unique symbols: the shared-memory statics
     # of kernel templates over different UserSystem structs in two of these
     # libraries would otherwise be merged by the dynamic linker
-    subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+    subprocess.run([cxx] + opt + ["-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
                     "-fvisibility=hidden", "-fvisibility-inlines-hidden", "-fno-gnu-unique",
                     "-Wno-unknown-pragmas", "-I", str(out_dir)] + [f"-D{d}" for d in defines] +
                    ["-o", out, os.path.join(ROOT, "tests", "device_step_host.cpp")], check=True)
