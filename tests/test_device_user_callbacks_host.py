@@ -15,6 +15,7 @@ topography, a non-conservative B(Q) with a stiff friction source.  The
 callbacks use IEEE arithmetic and sqrt only, so both sides give the same
 bits: the final states must be identical."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -214,21 +215,53 @@ def _port_callbacks(F, B, S, ndim, V):
     return ptrs, keep
 
 
-def _port_run(F, B, S, u0, N, bt, cfl, stiff, flux, K):
+def _port_run_ptrs(ptrs, second_order, u0, N, bt, cfl, stiff, flux, K):
+    """K steps of the restatement with the callbacks behind ptrs (F, B, S
+    function pointers or None); dX = 1/n.  Returns (u, steps, t)."""
     nX = np.array(u0.shape[:-1], dtype=np.int32)
     ndim, V = len(nX), u0.shape[-1]
-    (pF, pB, pS), keep = _port_callbacks(F, B, S, ndim, V)
     dX = np.array([1.0 / n for n in nX])
     u = u0.copy()
     ret = np.zeros((1,) + u.shape)
     tout = ctypes.c_double()
-    steps = ora.port().ora_pde_solver(pF, pB, pS, ora.ptr(u), 10.0, ora.ptr(nX), ndim,
-                                      ora.ptr(dX), cfl, ora.ptr(np.array(bt, dtype=np.int32)),
-                                      int(stiff), flux, N, V, 1,
-                                      int(F is not None and nargs(F) == 3), ora.ptr(ret), 1, K,
+    steps = ora.port().ora_pde_solver(*ptrs, ora.ptr(u), 10.0, ora.ptr(nX), ndim, ora.ptr(dX),
+                                      cfl, ora.ptr(np.array(bt, dtype=np.int32)), int(stiff),
+                                      flux, N, V, 1, int(second_order), ora.ptr(ret), 1, K,
                                       1e-12, ctypes.byref(tout))
-    del keep
     return u, steps, tout.value
+
+
+def _port_run(F, B, S, u0, N, bt, cfl, stiff, flux, K):
+    """The restatement running the Python callbacks themselves."""
+    ptrs, keep = _port_callbacks(F, B, S, u0.ndim - 1, u0.shape[-1])
+    out = _port_run_ptrs(ptrs, F is not None and nargs(F) == 3, u0, N, bt, cfl, stiff, flux, K)
+    del keep
+    return out
+
+
+def callback_lib(dirpath, src):
+    """The translated callbacks compiled as host C++ into C functions with
+    the reference's callback signatures (cbF, cbB, cbS), for the
+    restatement; the same source the device kernels include."""
+    import subprocess
+    cpp = os.path.join(str(dirpath), "callbacks.cpp")
+    with open(cpp, "w") as f:
+        f.write("#include <cmath>\nusing namespace std;\n#define __device__\n"
+                "#define __forceinline__ inline\n" + src +
+                "\n#define API extern \"C\" __attribute__((visibility(\"default\")))"
+                "\nAPI void cbF(double *o, double *Q, double *dQ, int d) "
+                "{ UserSystem::F(o, Q, dQ, d); }"
+                "\nAPI void cbB(double *o, double *Q, int d) { UserSystem::B(o, Q, d); }"
+                "\nAPI void cbS(double *o, double *Q) { UserSystem::S(o, Q); }\n")
+    so = os.path.join(str(dirpath), "libcallbacks.so")
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fvisibility=hidden",
+                    "-fvisibility-inlines-hidden", "-fno-gnu-unique", cpp, "-o", so], check=True)
+    return ctypes.CDLL(so)
+
+
+def callback_ptrs(lib, F, B, S):
+    return [ctypes.cast(getattr(lib, f"cb{r}"), ctypes.c_void_p) if fn is not None else None
+            for r, fn in (("F", F), ("B", B), ("S", S))]
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
@@ -248,6 +281,105 @@ def test_translated_callbacks_device_step_equals_port(tmp_path, case):
         u = u0.copy()
         t, its = ctypes.c_double(), ctypes.c_ulonglong()
         steps = L.host_run(b"user", ndim, N, flux, ora.ptr(u), ora.ptr(nX),
+                           ora.ptr(np.array(bt, dtype=np.int32)), ora.ptr(dX),
+                           ora.ptr(stages.tables(N)), 10.0, cfl, int(stiff), 1e-12, 0, K,
+                           ctypes.byref(t), ctypes.byref(its))
+        assert steps == K and t.value == t_o
+        assert np.array_equal(u, u_o), np.abs(u - u_o).max()
+
+
+# A 13-variable system in the style of the reference's GPR example: density,
+# momentum and a distortion matrix A, written with tuple-returning helpers,
+# matrix products, transposes, reshape / ravel, trace / eye / det and slice
+# updates around d; arithmetic only, so device and host evaluate it to the
+# same bits.
+CS2 = 1.0
+P0 = 1.0
+TAU_A = 1e-2
+
+
+def mat_unpack(Q):
+    rho = Q[0]
+    v = Q[1:4] / rho
+    A = Q[4:13].copy().reshape((3, 3))
+    return rho, v, A
+
+
+def mat_dev(A):
+    G = A.T @ A
+    return G - np.trace(G) / 3.0 * np.eye(3)
+
+
+def mat_flux(Q, d):
+    ret = np.zeros(13)
+    rho, v, A = mat_unpack(Q)
+    sig = -rho * CS2 * np.dot(A.T, mat_dev(A))
+    ret[0] = rho * v[d]
+    ret[1:4] = rho * v[d] * v
+    ret[1 + d] += P0 * rho
+    ret[1:4] -= sig[d]
+    Av = np.dot(A, v)
+    ret[4 + d] = Av[0]
+    ret[7 + d] = Av[1]
+    ret[10 + d] = Av[2]
+    return ret
+
+
+def mat_ncp(Q, d):
+    ret = np.zeros((13, 13))
+    v = Q[1:4] / Q[0]
+    for i in range(4, 13):
+        ret[i, i] = v[d]
+    ret[4 + d, 4 + d:7 + d] -= v
+    ret[7 + d, 7 + d:10 + d] -= v
+    ret[10 + d, 10:13] -= v
+    return ret
+
+
+def mat_src(Q):
+    ret = np.zeros(13)
+    rho, v, A = mat_unpack(Q)
+    ret[4:13] = -mat_dev(A).ravel() * (np.linalg.det(A) / (TAU_A * rho))
+    return ret
+
+
+def _mat_state(n, seed):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n
+    u = np.zeros((n, 13))
+    for i in range(n):
+        s = 0.5 * (1 + np.tanh((x[i] - 0.5) / 0.1))
+        rho = 1.0 + 0.5 * s
+        A = rho ** (1 / 3) * np.eye(3) + 0.01 * rng.standard_normal((3, 3))
+        u[i] = np.concatenate([[rho], rho * np.array([0.4 - 0.3 * s, 0.1, 0.0]), A.ravel()])
+    return u
+
+
+# name, F, B, S, state, order, boundary types, cfl, stiff, flux, steps
+MATRIX_CASE = ("matrix-13var-stiff", mat_flux, mat_ncp, mat_src, _mat_state(20, 9), 2, [0],
+               0.6, True, 0, 3)
+
+
+def test_matrix_system_device_step_equals_port(tmp_path):
+    """The matrix-style system: the device step with its translated source
+    equals the restatement running the same translated callbacks, bit for
+    bit, in both fiber orders."""
+    name, F, B, S, u0, N, bt, cfl, stiff, flux, K = MATRIX_CASE
+    src = translate(F, B, S, 1, 13)
+    (tmp_path / "user_system.h").write_text(src)
+    cb = callback_lib(tmp_path, src)
+    u_o, steps_o, t_o = _port_run_ptrs(callback_ptrs(cb, F, B, S), False, u0, N, bt, cfl, stiff,
+                                       flux, K)
+    assert steps_o == K and np.all(np.isfinite(u_o)) and np.abs(u_o - u0).max() > 0
+    L = load_device_host(build_device_host(
+        tmp_path, [f'HOST_USER_SYSTEM="{tmp_path / "user_system.h"}"', f"HOST_USER_N={N}"]))
+    nX = np.array(u0.shape[:-1], dtype=np.int32)
+    dX = np.array([1.0 / n for n in nX])
+    for reverse in (False, True):
+        L.host_set_order(int(reverse))
+        u = u0.copy()
+        t, its = ctypes.c_double(), ctypes.c_ulonglong()
+        steps = L.host_run(b"user", 1, N, flux, ora.ptr(u), ora.ptr(nX),
                            ora.ptr(np.array(bt, dtype=np.int32)), ora.ptr(dX),
                            ora.ptr(stages.tables(N)), 10.0, cfl, int(stiff), 1e-12, 0, K,
                            ctypes.byref(t), ctypes.byref(its))

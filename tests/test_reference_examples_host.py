@@ -23,7 +23,6 @@ import contextlib
 import ctypes
 import importlib
 import os
-import subprocess
 import sys
 import types
 
@@ -35,7 +34,7 @@ from oracle import ora
 from pypde_gb300 import stages
 from pypde_gb300.translate import translate
 from pypde_gb300.utils import nargs
-from test_device_user_callbacks_host import _port_run
+from test_device_user_callbacks_host import _port_run, _port_run_ptrs, callback_lib, callback_ptrs
 
 EXAMPLES = os.path.join(ora.REF_SRC, "pypde", "tests")
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(EXAMPLES, "gpr")),
@@ -145,30 +144,12 @@ def _examples():
 EX = _examples() if os.path.isdir(os.path.join(EXAMPLES, "gpr")) else {}
 
 
-def _callback_lib(tmp_path, src):
-    """The translated callbacks as C functions with the reference's callback
-    signatures, for the restatement."""
-    cpp = tmp_path / "callbacks.cpp"
-    cpp.write_text("#include <cmath>\nusing namespace std;\n#define __device__\n"
-                   "#define __forceinline__ inline\n" + src +
-                   "\n#define API extern \"C\" __attribute__((visibility(\"default\")))"
-                   "\nAPI void cbF(double *o, double *Q, double *dQ, int d) "
-                   "{ UserSystem::F(o, Q, dQ, d); }"
-                   "\nAPI void cbB(double *o, double *Q, int d) { UserSystem::B(o, Q, d); }"
-                   "\nAPI void cbS(double *o, double *Q) { UserSystem::S(o, Q); }\n")
-    so = str(tmp_path / "libcallbacks.so")
-    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fvisibility=hidden",
-                    "-fvisibility-inlines-hidden", "-fno-gnu-unique", str(cpp), "-o", so],
-                   check=True)
-    return ctypes.CDLL(so)
-
-
 @pytest.mark.parametrize("name", sorted(EX))
 def test_reference_example_through_translation(tmp_path, name):
     F, B, S, u0, N, bt, cfl, stiff, flux, K = EX[name]
     ndim, V = u0.ndim - 1, u0.shape[-1]
     src = translate(F, B, S, ndim, V)
-    cb = _callback_lib(tmp_path, src)
+    cb = callback_lib(tmp_path, src)
     dp = ctypes.POINTER(ctypes.c_double)
 
     # 1. translated callbacks against the Python functions
@@ -202,22 +183,15 @@ def test_reference_example_through_translation(tmp_path, name):
         tmp_path, [f'HOST_USER_SYSTEM="{tmp_path / "user_system.h"}"', f"HOST_USER_N={N}"]))
     nX = np.array(u0.shape[:-1], dtype=np.int32)
     dX = np.array([1.0 / n for n in nX])
-    ptrs = [ctypes.cast(getattr(cb, f"cb{r}"), ctypes.c_void_p) if fn is not None else None
-            for r, fn in (("F", F), ("B", B), ("S", S))]
-    u_c = u0.copy()
-    ret = np.zeros((1,) + u0.shape)
-    t_c = ctypes.c_double()
-    steps_c = ora.port().ora_pde_solver(*ptrs, ora.ptr(u_c), 10.0, ora.ptr(nX), ndim,
-                                        ora.ptr(dX), cfl, ora.ptr(np.array(bt, dtype=np.int32)),
-                                        int(stiff), flux, N, V, 1, int(nargs(F) == 3),
-                                        ora.ptr(ret), 1, K, 1e-12, ctypes.byref(t_c))
+    u_c, steps_c, t_c = _port_run_ptrs(callback_ptrs(cb, F, B, S), nargs(F) == 3, u0, N, bt,
+                                       cfl, stiff, flux, K)
     u = u0.copy()
     t, its = ctypes.c_double(), ctypes.c_ulonglong()
     steps = L.host_run(b"user", ndim, N, flux, ora.ptr(u), ora.ptr(nX),
                        ora.ptr(np.array(bt, dtype=np.int32)), ora.ptr(dX),
                        ora.ptr(stages.tables(N)), 10.0, cfl, int(stiff), 1e-12, 0, K,
                        ctypes.byref(t), ctypes.byref(its))
-    assert steps == steps_c == K and t.value == t_c.value
+    assert steps == steps_c == K and t.value == t_c
     assert np.all(np.isfinite(u)) and np.abs(u - u0).max() > 0
     assert np.array_equal(u, u_c), np.abs(u - u_c).max()
 
