@@ -10,6 +10,8 @@
 #include "step_kernels.cuh"
 #include "../../include/pypde_gb300.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -18,6 +20,28 @@
 #include <vector>
 
 namespace pypde {
+
+// NVTX ranges name a run and, when the stages are launched one by one
+// (profile mode), each stage, so a profiler can select a stage's kernels
+// (ncu --nvtx --nvtx-include).  Without a profiler attached they cost a
+// branch.  Stages: pop the previous range and push the next.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+struct NvtxStages {
+  bool open = false;
+  void next(const char *name) {
+    if (open)
+      nvtxRangePop();
+    nvtxRangePushA(name);
+    open = true;
+  }
+  ~NvtxStages() {
+    if (open)
+      nvtxRangePop();
+  }
+};
 
 static thread_local std::string g_err;
 void set_error(const std::string &m) { g_err = m; }
@@ -396,9 +420,15 @@ static int kernels_per_step(const StepCtx &c) {
 static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
                                 cudaEvent_t *ev = nullptr) {
   cudaError_t e;
+  static const char *const kStage[8] = {"ghost fill", "weno",  "cfl+dt",
+                                        "predictor",  "faces", "centres",
+                                        "gather",     "step end"};
+  NvtxStages nv;
   auto mark = [&](int i) {
     if (ev)
       cudaEventRecord(ev[i], s);
+    if (i < 8)
+      nv.next(kStage[i]);
   };
   k_step_begin<<<1, 1, 0, s>>>(c.st);
   long long n = c.g.C * c.V;
@@ -591,6 +621,7 @@ static int check_warm(const SystemDesc &sys, int N, bool stiff, int device,
 }
 
 int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
+  NvtxRange nvtx_run("pde_solver");
   if (a.ndim < 1 || a.ndim > 3 || !a.u || a.tf < 0 || a.ndt < 1) {
     set_error("invalid arguments");
     return PYPDE_ERR_ARG;
@@ -973,6 +1004,7 @@ static int batch_launches_per_step(const BatchCtx &c) {
 }
 
 int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
+  NvtxRange nvtx_run("pde_solver_batch");
   if (a.np < 1 || !a.probs) {
     set_error("empty batch");
     return PYPDE_ERR_ARG;
