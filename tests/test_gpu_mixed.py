@@ -4,7 +4,6 @@ tolerance.  The answer must stay at the plain FP64 form's error level
 against a tolerance-1e-15 oracle (two converged Newton solves differ by the
 tolerance's own effect, measured by the plain form at tolerances 1e-12 and
 1e-13), and the FP64 sweeps must not increase."""
-import numpy as np
 import pytest
 
 from conftest import l1
