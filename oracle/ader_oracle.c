@@ -1270,6 +1270,11 @@ typedef struct {
   ora_tables T;
   double wprod[ORA_MAXN * ORA_MAXN * ORA_MAXN]; /* prod_d W[i_d] per node */
   double rwprod[ORA_MAXN * ORA_MAXN * ORA_MAXN]; /* 1 / wprod */
+  /* mixed-precision stiff predictor: FP32 sweeps with these callbacks */
+  int mixed;
+  ora_flux32_fn F32;
+  ora_ncp32_fn B32;
+  ora_src32_fn S32;
 } ctx_t;
 
 static void ctx_init(ctx_t *c, ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
@@ -1283,6 +1288,10 @@ static void ctx_init(ctx_t *c, ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
   c->Nd = ipow(N, ndim);
   c->dX = dX;
   c->secondOrder = so;
+  c->mixed = 0;
+  c->F32 = 0;
+  c->B32 = 0;
+  c->S32 = 0;
   ora_make_tables(N, &c->T);
   for (int idx = 0; idx < c->Nd; idx++) { /* stepper.cpp:24-32 */
     double p = 1.0;
@@ -1728,10 +1737,13 @@ static void lu_solve(const double *a, int n, const int *piv, double *b) {
  * q_plain the plain guess: the first iteration whose residual does not
  * fall below the previous one, or has an entry that is not finite, spends
  * itself resetting q to q_plain, after which the iteration is the plain
- * one (factors discarded); *fell_back is set. */
+ * one (factors discarded); *fell_back is set.
+ *
+ * A cell stops only after at least min_updates updates (2 after the FP32
+ * sweeps of the mixed-precision form, else 0). */
 static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
                      double tol, dg_scratch *s, const double *q_plain,
-                     int *fell_back) {
+                     int *fell_back, int min_updates) {
   int N = c->N, V = c->V, Nd = c->Nd;
   int n = N * Nd * V, nl = N * V;
   double r[ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXV];
@@ -1771,7 +1783,7 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
       }
       prev = res;
     }
-    if (res <= tol || res <= 16 * DBL_EPSILON * scale)
+    if (it >= min_updates && (res <= tol || res <= 16 * DBL_EPSILON * scale))
       return it;
     int refresh = !have_lu || !(res <= 0.5 * last);
     last = res;
@@ -1823,9 +1835,277 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
   return NEWTON_MAXIT;
 }
 
+/* FP32 sweeps of the mixed-precision stiff predictor (not in the
+ * reference): the simplified Newton iteration of dg_newton with every
+ * quantity in FP32 -- the FP32 callbacks, the FD step sqrt(eps_32)
+ * max(|q|, 1), the tables rounded to float, the Newton matrix built and
+ * factored once -- started from q and written back into it.  The cell
+ * stops at its FP32 rounding floor (residual <= 64 eps_32 scale), at tol,
+ * when the residual falls by less than half in a sweep, on a zero pivot, or
+ * after NEWTON32_MAXIT sweeps.  Residual and scale are maxima of magnitude
+ * bits, a non-finite residual entry counting as the largest finite float.
+ * Returns the sweeps that updated q.  This restates the device routine
+ * newton_fp32_sweeps operation for operation, its per-node phases in turn. */
+#define NEWTON32_MAXIT 8
+static unsigned f32_bits(float x) {
+  unsigned u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+}
+static float f32_from_bits(unsigned u) {
+  float x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+}
+
+static int dg_newton32(const ctx_t *c, double *q, const double *Ww, double dt,
+                       double tol) {
+  enum { MNT = ORA_MAXN * ORA_MAXN * ORA_MAXN * ORA_MAXN };
+  const int N = c->N, V = c->V, Nd = c->Nd, D = c->ndim;
+  const int NT = N * Nd, NL = N * V;
+  const float EPS32 = 1.1920928955078125e-07f;
+  const float SQRT_EPS32 = 3.4526698300124393e-04f;
+  float wprod32[ORA_MAXN * ORA_MAXN * ORA_MAXN], dervals32[ORA_MAXN * ORA_MAXN];
+  float dgmat32[ORA_MAXN * ORA_MAXN], wg32[ORA_MAXN];
+  for (int i = 0; i < Nd; i++)
+    wprod32[i] = (float)c->wprod[i];
+  for (int i = 0; i < N * N; i++) {
+    dervals32[i] = (float)c->T.dervals[i];
+    dgmat32[i] = (float)c->T.dgmat[i];
+  }
+  for (int i = 0; i < N; i++)
+    wg32[i] = (float)c->T.wghts[i];
+  float *q32 = malloc(sizeof(float) * NT * V * (4 + D + D));
+  float *Ww32 = q32 + NT * V, *r32 = Ww32 + NT * V, *f32 = r32 + NT * V;
+  float *dqn = f32 + NT * D * V; /* per node: dq[D][V] */
+  float *A32 = malloc(sizeof(float) * Nd * NL * NL);
+  int *piv = malloc(sizeof(int) * Nd * NL);
+  (void)MNT;
+  for (int i = 0; i < NT * V; i++) {
+    q32[i] = (float)q[i];
+    Ww32[i] = (float)Ww[i];
+  }
+  const float dt32 = (float)dt, tol32 = (float)tol;
+  int lu = 0, done = 0, sweeps = 0;
+  float last = 3.0e38f;
+  for (int it = 0; it < NEWTON32_MAXIT && !done; it++) {
+    /* phase 1: state derivatives and fluxes at every node */
+    for (int node = 0; node < NT; node++) {
+      const int t = node / Nd, idx = node % Nd;
+      int digs[3] = {0, 0, 0}, rem = idx;
+      for (int d = D - 1; d >= 0; d--) {
+        digs[d] = rem % N;
+        rem /= N;
+      }
+      float *dq = dqn + node * D * V;
+      if (c->secondOrder || c->B32)
+        for (int d = 0; d < D; d++) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          const int base = idx - digs[d] * sd;
+          const float rdx = 1.0f / (float)c->dX[d];
+          for (int v = 0; v < V; v++) {
+            float sacc = 0.0f;
+            for (int j = 0; j < N; j++)
+              sacc = fmaf(dervals32[digs[d] * N + j], q32[(t * Nd + base + j * sd) * V + v],
+                          sacc);
+            dq[d * V + v] = sacc * rdx;
+          }
+        }
+      if (c->F32) {
+        float qr[ORA_MAXV];
+        for (int v = 0; v < V; v++)
+          qr[v] = q32[node * V + v];
+        for (int d = 0; d < D; d++)
+          c->F32(f32 + (node * D + d) * V, qr, dq, d);
+      }
+    }
+    /* phase 2: residual at every node, cell maxima of its magnitude */
+    unsigned rm = 0u, sm = 0u;
+    for (int node = 0; node < NT; node++) {
+      const int t = node / Nd, idx = node % Nd;
+      int digs[3] = {0, 0, 0}, rem = idx;
+      for (int d = D - 1; d >= 0; d--) {
+        digs[d] = rem % N;
+        rem /= N;
+      }
+      const float *dq = dqn + node * D * V;
+      float r[ORA_MAXV];
+      if (c->S32)
+        c->S32(r, q32 + node * V);
+      else
+        for (int v = 0; v < V; v++)
+          r[v] = 0.0f;
+      float cc = wg32[t];
+      for (int d = 0; d < D; d++) {
+        if (c->B32) {
+          float b[ORA_MAXV * ORA_MAXV];
+          c->B32(b, q32 + node * V, d);
+          for (int i = 0; i < V; i++) {
+            float acc = 0.0f;
+            for (int j = 0; j < V; j++)
+              acc = fmaf(b[i * V + j], dq[d * V + j], acc);
+            r[i] -= acc;
+          }
+        }
+        if (c->F32) {
+          int sd = 1;
+          for (int e = d + 1; e < D; e++)
+            sd *= N;
+          const int base = idx - digs[d] * sd;
+          const float rdx = 1.0f / (float)c->dX[d];
+          for (int v = 0; v < V; v++) {
+            float sacc = 0.0f;
+            for (int j = 0; j < N; j++)
+              sacc = fmaf(dervals32[digs[d] * N + j],
+                          f32[((t * Nd + base + j * sd) * D + d) * V + v], sacc);
+            r[v] -= sacc * rdx;
+          }
+        }
+        cc *= wg32[digs[d]];
+      }
+      for (int v = 0; v < V; v++) {
+        const float rv = fmaf(r[v] * cc, dt32, Ww32[node * V + v]);
+        float uq = 0.0f;
+        for (int k = 0; k < N; k++)
+          uq = fmaf(dgmat32[t * N + k], q32[(k * Nd + idx) * V + v], uq);
+        uq *= wprod32[idx];
+        const float ov = rv - uq;
+        r32[node * V + v] = ov;
+        const unsigned a = f32_bits(ov) & 0x7fffffffu;
+        const unsigned bb = f32_bits(rv) & 0x7fffffffu;
+        const unsigned cb = f32_bits(uq) & 0x7fffffffu;
+        const unsigned am = a >= 0x7f800000u ? 0x7f7fffffu : a;
+        const unsigned b0 = bb < 0x7f800000u ? bb : 0u, c0 = cb < 0x7f800000u ? cb : 0u;
+        if (am > rm)
+          rm = am;
+        if ((b0 > c0 ? b0 : c0) > sm)
+          sm = b0 > c0 ? b0 : c0;
+      }
+    }
+    const float res = f32_from_bits(rm), scale = f32_from_bits(sm);
+    const int stop = res <= tol32 || res <= 64.0f * EPS32 * scale || !(res <= 0.5f * last) ||
+                     res >= 3.0e38f;
+    if (stop)
+      break;
+    /* phase 3: the Newton matrix, row block t at every node (first sweep) */
+    if (!lu)
+      for (int node = 0; node < NT; node++) {
+        const int t = node / Nd, idx = node % Nd;
+        float *A = A32 + (size_t)idx * NL * NL;
+        float qn[ORA_MAXV], s0[ORA_MAXV], s1[ORA_MAXV];
+        for (int v = 0; v < V; v++)
+          qn[v] = q32[node * V + v];
+        if (c->S32)
+          c->S32(s0, qn);
+        for (int wv = 0; wv < V; wv++) {
+          float ih = 0.0f;
+          if (c->S32) {
+            const float q0 = qn[wv];
+            const float h = fmaxf(SQRT_EPS32 * fabsf(q0), SQRT_EPS32);
+            qn[wv] = q0 + h;
+            c->S32(s1, qn);
+            qn[wv] = q0;
+            ih = 1.0f / h;
+          }
+          for (int v = 0; v < V; v++)
+            for (int k = 0; k < N; k++) {
+              float a = 0.0f;
+              if (k == t && c->S32)
+                a = dt32 * wg32[t] * ((s1[v] - s0[v]) * ih);
+              A[(t * V + v) * NL + k * V + wv] = a;
+            }
+        }
+        for (int k = 0; k < N; k++)
+          for (int v = 0; v < V; v++)
+            A[(t * V + v) * NL + k * V + v] -= dgmat32[t * N + k];
+      }
+    /* phase 4: per spatial node, factor (first sweep) and solve */
+    int bad = 0;
+    for (int idx = 0; idx < Nd; idx++) {
+      float *A = A32 + (size_t)idx * NL * NL;
+      int *pv = piv + idx * NL;
+      int ok = 1;
+      for (int k = 0; k < NL && ok && !lu; k++) {
+        int p = k;
+        unsigned pm = f32_bits(A[k * NL + k]) & 0x7fffffffu;
+        for (int i = k + 1; i < NL; i++) {
+          const unsigned m = f32_bits(A[i * NL + k]) & 0x7fffffffu;
+          if (m > pm) {
+            p = i;
+            pm = m;
+          }
+        }
+        pv[k] = p;
+        if (pm == 0u) {
+          ok = 0;
+          break;
+        }
+        if (p != k)
+          for (int j = 0; j < NL; j++) {
+            const float tmp = A[k * NL + j];
+            A[k * NL + j] = A[p * NL + j];
+            A[p * NL + j] = tmp;
+          }
+        const float rp = 1.0f / A[k * NL + k];
+        for (int i = k + 1; i < NL; i++) {
+          const float f = A[i * NL + k] * rp;
+          A[i * NL + k] = f;
+          if ((f32_bits(f) & 0x7fffffffu) == 0u)
+            continue;
+          for (int j = k + 1; j < NL; j++)
+            A[i * NL + j] = fmaf(-f, A[k * NL + j], A[i * NL + j]);
+        }
+      }
+      if (!ok) {
+        bad = 1;
+        continue;
+      }
+      float b[ORA_MAXN * ORA_MAXV];
+      const float rwp = 1.0f / wprod32[idx];
+      for (int tt = 0; tt < N; tt++)
+        for (int v = 0; v < V; v++)
+          b[tt * V + v] = r32[(tt * Nd + idx) * V + v] * rwp;
+      for (int k = 0; k < NL; k++)
+        if (pv[k] != k) {
+          const float tmp = b[k];
+          b[k] = b[pv[k]];
+          b[pv[k]] = tmp;
+        }
+      for (int k = 0; k < NL; k++)
+        for (int i = k + 1; i < NL; i++)
+          if ((f32_bits(A[i * NL + k]) & 0x7fffffffu) != 0u)
+            b[i] = fmaf(-A[i * NL + k], b[k], b[i]);
+      for (int i = NL - 1; i >= 0; i--) {
+        float sacc = b[i];
+        for (int j = i + 1; j < NL; j++)
+          if ((f32_bits(A[i * NL + j]) & 0x7fffffffu) != 0u)
+            sacc = fmaf(-A[i * NL + j], b[j], sacc);
+        b[i] = sacc / A[i * NL + i];
+      }
+      for (int tt = 0; tt < N; tt++)
+        for (int v = 0; v < V; v++)
+          q32[(tt * Nd + idx) * V + v] -= b[tt * V + v];
+    }
+    last = res;
+    lu = 1;
+    sweeps = it + 1;
+    done = bad; /* a zero pivot ends the FP32 sweeps after this one */
+  }
+  /* hand the FP32 iterate to the FP64 sweeps */
+  for (int i = 0; i < NT * V; i++)
+    q[i] = (double)q32[i];
+  free(q32);
+  free(A32);
+  free(piv);
+  return sweeps;
+}
+
 static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
                             int stiff, double dt, double tol, double *qh,
-                            int *maxit, const double *guess, long *fallbacks) {
+                            int *maxit, const double *guess, long *fallbacks,
+                            long *sweeps32) {
   int N = c->N, V = c->V, Nd = c->Nd;
   int n = N * Nd * V;
   dg_scratch *s = malloc(sizeof(dg_scratch));
@@ -1842,12 +2122,17 @@ static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
       int fb = 0;
       memcpy(q1, q0, sizeof(double) * n);
       memcpy(q0, guess + cell * n, sizeof(double) * n);
-      it = dg_newton(c, q0, Ww, dt, tol, s, q1, &fb);
+      it = dg_newton(c, q0, Ww, dt, tol, s, q1, &fb, 0);
       memcpy(qh + cell * n, q0, sizeof(double) * n);
       if (fallbacks)
         *fallbacks += fb;
     } else if (stiff) {
-      it = dg_newton(c, q0, Ww, dt, tol, s, NULL, NULL);
+      if (c->mixed) {
+        const int sw = dg_newton32(c, q0, Ww, dt, tol);
+        if (sweeps32)
+          *sweeps32 += sw;
+      }
+      it = dg_newton(c, q0, Ww, dt, tol, s, NULL, NULL, c->mixed ? 2 : 0);
       memcpy(qh + cell * n, q0, sizeof(double) * n);
     } else {
       it = dg_picard(c, q0, Ww, dt, q1, s);
@@ -1875,7 +2160,7 @@ long ora_predictor(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, const double *w,
   if (maxit)
     *maxit = 0;
   long r = predictor_range(c, w, 0, nrows / c->Nd, stiff, dt, newton_tol, qh,
-                           maxit, NULL, NULL);
+                           maxit, NULL, NULL, NULL);
   free(c);
   return r;
 }
@@ -1892,7 +2177,29 @@ long ora_predictor_guess(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
   if (fallbacks)
     *fallbacks = 0;
   long r = predictor_range(c, w, 0, nrows / c->Nd, 1, dt, newton_tol, qh,
-                           maxit, guess, fallbacks);
+                           maxit, guess, fallbacks, NULL);
+  free(c);
+  return r;
+}
+
+long ora_predictor_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                         ora_flux32_fn F32, ora_ncp32_fn B32, ora_src32_fn S32,
+                         const double *w, long nrows, const double *dX,
+                         int ndim, int N, int V, double dt, double newton_tol,
+                         double *qh, int *maxit, long *sweeps32,
+                         int secondOrder) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  c->mixed = 1;
+  c->F32 = F32;
+  c->B32 = B32;
+  c->S32 = S32;
+  if (maxit)
+    *maxit = 0;
+  if (sweeps32)
+    *sweeps32 = 0;
+  long r = predictor_range(c, w, 0, nrows / c->Nd, 1, dt, newton_tol, qh,
+                           maxit, NULL, NULL, sweeps32);
   free(c);
   return r;
 }
@@ -2230,7 +2537,7 @@ static void *job_run(void *arg) {
     j->out_max = cfl_max(j->c, j->w, c0, c1);
   } else {
     j->iters = predictor_range(j->c, j->w, c0, c1, j->stiff, j->dt, j->tol,
-                               j->qh, &j->maxit, NULL, NULL);
+                               j->qh, &j->maxit, NULL, NULL, NULL);
     fv_range(j->c, j->u, j->qh, j->nX, j->dt, j->flux, j->a0, j->b0);
   }
   return NULL;
@@ -2243,6 +2550,12 @@ static int any_nan(const double *u, long n) {
   return 0;
 }
 
+static long pde_solver_run(ctx_t *c, double *u, double tf, const int *nX,
+                           int ndim, const double *dX, double CFL,
+                           const int *bt, int stiff, int flux, int N, int V,
+                           int ndt, double *ret, int nThreads, long maxsteps,
+                           double newton_tol, double *t_out);
+
 long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
                     double tf, const int *nX, int ndim, const double *dX,
                     double CFL, const int *bt, int stiff, int flux, int N,
@@ -2250,6 +2563,34 @@ long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
                     long maxsteps, double newton_tol, double *t_out) {
   ctx_t *c = malloc(sizeof(ctx_t));
   ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  return pde_solver_run(c, u, tf, nX, ndim, dX, CFL, bt, stiff, flux, N, V,
+                        ndt, ret, nThreads, maxsteps, newton_tol, t_out);
+}
+
+long ora_pde_solver_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                          ora_flux32_fn F32, ora_ncp32_fn B32, ora_src32_fn S32,
+                          double *u, double tf, const int *nX, int ndim,
+                          const double *dX, double CFL, const int *bt,
+                          int flux, int N, int V, int ndt, int secondOrder,
+                          double *ret, int nThreads, long maxsteps,
+                          double newton_tol, double *t_out) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  c->mixed = 1;
+  c->F32 = F32;
+  c->B32 = B32;
+  c->S32 = S32;
+  return pde_solver_run(c, u, tf, nX, ndim, dX, CFL, bt, 1, flux, N, V, ndt,
+                        ret, nThreads, maxsteps, newton_tol, t_out);
+}
+
+/* The time loop of ora_pde_solver on a prepared context; frees c. */
+static long pde_solver_run(ctx_t *c, double *u, double tf, const int *nX,
+                           int ndim, const double *dX, double CFL,
+                           const int *bt, int stiff, int flux, int N, int V,
+                           int ndt, double *ret, int nThreads, long maxsteps,
+                           double newton_tol, double *t_out) {
+  (void)dX;
   if (nThreads < 1)
     nThreads = (int)sysconf(_SC_NPROCESSORS_ONLN);
   if (nThreads > nX[0])

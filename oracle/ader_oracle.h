@@ -23,6 +23,11 @@ extern "C" {
 typedef void (*ora_flux_fn)(double *out, double *Q, double *dQ, int d);
 typedef void (*ora_ncp_fn)(double *out, double *Q, int d);
 typedef void (*ora_src_fn)(double *out, double *Q);
+/* FP32 twins of the callbacks, for the FP32 Newton sweeps of the
+ * mixed-precision stiff predictor (not in the reference). */
+typedef void (*ora_flux32_fn)(float *out, const float *Q, const float *dQ, int d);
+typedef void (*ora_ncp32_fn)(float *out, const float *Q, int d);
+typedef void (*ora_src32_fn)(float *out, const float *Q);
 
 #define ORA_MAXN 8
 #define ORA_MAXV 24
@@ -33,6 +38,9 @@ typedef void (*ora_src_fn)(double *out, double *Q);
 int ora_system_eig_active(ora_flux_fn F, int ndim, int d, int *idx);
 int ora_system_lookup(const char *name, int ndim, int *V, ora_flux_fn *F,
                       ora_ncp_fn *B, ora_src_fn *S, int *secondOrder);
+/* The FP32 callbacks of the same test system (null where it has none). */
+int ora_system_lookup32(const char *name, int ndim, ora_flux32_fn *F,
+                        ora_ncp32_fn *B, ora_src32_fn *S);
 
 /* Constant tables of one (ndim, N) solver (src/poly/basis.cpp,
  * src/solvers/weno/weno_matrices.cpp, src/solvers/dg/dg_matrices.cpp). */
@@ -76,6 +84,19 @@ long ora_predictor_guess(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
                          int ndim, int N, int V, double dt, double newton_tol,
                          const double *guess, double *qh, int *maxit,
                          long *fallbacks, int secondOrder);
+/* The mixed-precision stiff predictor (not in the reference): per cell,
+ * FP32 sweeps of the simplified Newton iteration with the FP32 callbacks
+ * (at most 8; stopping at the FP32 rounding floor, at tol, when the
+ * residual falls by less than half, or on a zero pivot), then the FP64
+ * iteration from that iterate, which makes at least two updates before it
+ * may stop at tol.  Returns the FP64 iterations; *sweeps32 (may be null)
+ * gets the FP32 sweeps. */
+long ora_predictor_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                         ora_flux32_fn F32, ora_ncp32_fn B32, ora_src32_fn S32,
+                         const double *w, long nrows, const double *dX,
+                         int ndim, int N, int V, double dt, double newton_tol,
+                         double *qh, int *maxit, long *sweeps32,
+                         int secondOrder);
 /* FV corrector (FVSolver::apply) on u (prod(nX) rows) using qh over the
  * w-grid nX+2. */
 void ora_fv(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
@@ -91,6 +112,15 @@ long ora_pde_solver(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,
                     double CFL, const int *bt, int stiff, int flux, int N,
                     int V, int ndt, int secondOrder, double *ret, int nThreads,
                     long maxsteps, double newton_tol, double *t_out);
+
+/* ora_pde_solver with the mixed-precision stiff predictor (stiff implied). */
+long ora_pde_solver_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                          ora_flux32_fn F32, ora_ncp32_fn B32, ora_src32_fn S32,
+                          double *u, double tf, const int *nX, int ndim,
+                          const double *dX, double CFL, const int *bt,
+                          int flux, int N, int V, int ndt, int secondOrder,
+                          double *ret, int nThreads, long maxsteps,
+                          double newton_tol, double *t_out);
 
 /* max |eigenvalue| of a general real n x n row-major matrix: FP32
  * eigenvalues refined in FP64 (ora_max_abs_eig), or the FP64 Francis QR

@@ -77,6 +77,15 @@ def port():
         L.ora_weno.argtypes = [dp, ip, c_int, c_int, c_int, dp]
         L.ora_system_lookup.argtypes = [c_char_p, c_int, ip, POINTER(c_void_p),
                                         POINTER(c_void_p), POINTER(c_void_p), ip]
+        L.ora_system_lookup32.argtypes = [c_char_p, c_int, POINTER(c_void_p),
+                                          POINTER(c_void_p), POINTER(c_void_p)]
+        L.ora_predictor_mixed.restype = c_long
+        L.ora_predictor_mixed.argtypes = [c_void_p] * 6 + [dp, c_long, dp, c_int, c_int, c_int,
+                                                           D, D, dp, ip, POINTER(c_long), c_int]
+        L.ora_pde_solver_mixed.restype = c_long
+        L.ora_pde_solver_mixed.argtypes = [c_void_p] * 6 + [dp, D, ip, c_int, dp, D, ip, c_int,
+                                                            c_int, c_int, c_int, c_int, dp,
+                                                            c_int, c_long, D, dp]
         L.ora_max_abs_eig.restype = D
         L.ora_max_abs_eig.argtypes = [dp, c_int]
         L.ora_eig.argtypes = [dp, c_int, dp, dp, dp, dp]
@@ -118,6 +127,9 @@ class PortSystem:
         if rc:
             raise ValueError(f"unknown system {name}/{ndim}")
         self.name, self.ndim, self.V, self.second_order = name, ndim, V.value, so.value
+        self.F32, self.B32, self.S32 = c_void_p(), c_void_p(), c_void_p()
+        port().ora_system_lookup32(name.encode(), ndim, ctypes.byref(self.F32),
+                                   ctypes.byref(self.B32), ctypes.byref(self.S32))
 
 
 # ---------------------------------------------------------------- stages
@@ -175,6 +187,21 @@ def predictor_guess(sysname, w, dX, N, dt, guess, tol=1e-12):
     return qh, its, mi.value, fb.value
 
 
+def predictor_mixed(sysname, w, dX, N, dt, tol=1e-12):
+    """The mixed-precision stiff predictor: FP32 sweeps, then FP64 Newton
+    with at least two updates; returns (qh, FP64 iterations, their per-cell
+    maximum, FP32 sweeps)."""
+    dX = np.asarray(dX, dtype=np.float64)
+    s = PortSystem(sysname, len(dX))
+    qh = np.zeros((w.shape[0] * N, s.V))
+    mi = c_int()
+    sw = ctypes.c_long()
+    its = port().ora_predictor_mixed(s.F, s.B, s.S, s.F32, s.B32, s.S32, ptr(w), w.shape[0],
+                                     ptr(dX), len(dX), N, s.V, dt, tol, ptr(qh),
+                                     ctypes.byref(mi), ctypes.byref(sw), s.second_order)
+    return qh, its, mi.value, sw.value
+
+
 def fv(sysname, u, qh, dX, N, dt, flux=0):
     dX = np.asarray(dX, dtype=np.float64)
     s = PortSystem(sysname, len(dX))
@@ -186,8 +213,9 @@ def fv(sysname, u, qh, dX, N, dt, flux=0):
 
 
 def pde_solver(sysname, u0, tf, L, bt, cfl, N, stiff=False, flux=0, ndt=1, nthreads=1,
-               max_steps=-1, newton_tol=1e-12):
-    """Run the port; returns (u_final, ret, steps, t_final)."""
+               max_steps=-1, newton_tol=1e-12, mixed=False):
+    """Run the port; returns (u_final, ret, steps, t_final).  mixed=True: the
+    mixed-precision stiff predictor (stiff implied)."""
     nX = np.array(u0.shape[:-1], dtype=np.int32)
     ndim = len(nX)
     s = PortSystem(sysname, ndim)
@@ -195,6 +223,13 @@ def pde_solver(sysname, u0, tf, L, bt, cfl, N, stiff=False, flux=0, ndt=1, nthre
     u = np.ascontiguousarray(u0, dtype=np.float64).copy()
     ret = np.zeros((ndt,) + u.shape)
     tout = D()
+    if mixed:
+        steps = port().ora_pde_solver_mixed(s.F, s.B, s.S, s.F32, s.B32, s.S32, ptr(u), tf,
+                                            ptr(nX), ndim, ptr(dX), cfl,
+                                            ptr(np.array(bt, dtype=np.int32)), flux, N, s.V, ndt,
+                                            s.second_order, ptr(ret), nthreads, max_steps,
+                                            newton_tol, ctypes.byref(tout))
+        return u, ret, steps, tout.value
     steps = port().ora_pde_solver(s.F, s.B, s.S, ptr(u), tf, ptr(nX), ndim, ptr(dX), cfl,
                                   ptr(np.array(bt, dtype=np.int32)), int(stiff), flux, N, s.V,
                                   ndt, s.second_order, ptr(ret), nthreads, max_steps, newton_tol,

@@ -176,3 +176,114 @@ int ora_system_lookup(const char *name, int ndim, int *V, ora_flux_fn *F,
   }
   return 0;
 }
+
+/* ---- FP32 twins, for the FP32 Newton sweeps of the mixed-precision
+ * stiff predictor: the device systems instantiated with float
+ * (pypde_gb300/csrc/systems.cuh, templates on the scalar type), in the same
+ * operation order, every constant rounded to float before it is used. */
+static float pow10_portable32(float x) {
+  float y = x * (float)3.321928094887362;
+  float n = floorf(y + 0.5f);
+  float r = (y - n) * (float)0.6931471805599453;
+  float p = (float)INV_FACT[16];
+  for (int k = 15; k >= 0; k--)
+    p = p * r + (float)INV_FACT[k];
+  return ldexpf(p, (int)n);
+}
+
+static float euler_core32(float *out, const float *Q, int ndim, int d) {
+  float r = Q[0];
+  float ke = 0.0f;
+  for (int i = 0; i < ndim; i++)
+    ke += Q[1 + i] * Q[1 + i];
+  float p = ((float)1.4 - 1.0f) * (Q[ndim + 1] - 0.5f * ke / r);
+  float ud = Q[1 + d] / r;
+  out[0] = Q[1 + d];
+  for (int i = 0; i < ndim; i++)
+    out[1 + i] = Q[1 + i] * ud;
+  out[1 + d] += p;
+  out[ndim + 1] = (Q[ndim + 1] + p) * ud;
+  return p;
+}
+
+static void euler_F32(float *out, const float *Q, const float *dQ, int d) {
+  (void)dQ;
+  euler_core32(out, Q, g_ndim, d);
+}
+
+static void cattaneo_F32(float *out, const float *Q, const float *dQ, int d) {
+  (void)dQ;
+  int nd = g_ndim;
+  float p = euler_core32(out, Q, nd, d);
+  float T = p / Q[0];
+  out[nd + 1] += Q[nd + 2 + d];
+  for (int i = 0; i < nd; i++)
+    out[nd + 2 + i] = 0.0f;
+  out[nd + 2 + d] = 1.0f * T;
+  out[2 * nd + 2] = 0.0f;
+}
+
+static void cattaneo_S32(float *out, const float *Q) {
+  int nd = g_ndim;
+  float inv_tau = pow10_portable32(-Q[2 * nd + 2]);
+  for (int i = 0; i < nd + 2; i++)
+    out[i] = 0.0f;
+  for (int i = 0; i < nd; i++)
+    out[nd + 2 + i] = -Q[nd + 2 + i] * inv_tau;
+  out[2 * nd + 2] = 0.0f;
+}
+
+static float ncp_a32(int d) { return d == 0 ? 1.0f : (d == 1 ? 0.5f : 0.25f); }
+
+static void ncp_F32(float *out, const float *Q, const float *dQ, int d) {
+  (void)dQ;
+  float a = ncp_a32(d);
+  out[0] = a * (0.5f * Q[0] * Q[0]);
+  out[1] = a * (Q[0] * Q[1]);
+  out[2] = a * (Q[0] * Q[2]);
+}
+
+static void ncp_B32(float *out, const float *Q, int d) {
+  float a = ncp_a32(d);
+  for (int i = 0; i < 9; i++)
+    out[i] = 0.0f;
+  out[4] = a * Q[0];
+  out[5] = a * (float)0.2;
+  out[7] = a * (float)0.2;
+  out[8] = a * Q[0];
+}
+
+static void ncp_S32(float *out, const float *Q) {
+  out[0] = 0.0f;
+  out[1] = (float)0.1 * (Q[2] - Q[1]);
+  out[2] = (float)-0.1 * (Q[1] + Q[2]);
+}
+
+static void burgers2_F32(float *out, const float *Q, const float *dQ, int d) {
+  out[0] = ncp_a32(d) * (0.5f * Q[0] * Q[0]) - (float)0.01 * dQ[d];
+}
+
+int ora_system_lookup32(const char *name, int ndim, ora_flux32_fn *F,
+                        ora_ncp32_fn *B, ora_src32_fn *S) {
+  if (ndim < 1 || ndim > 3)
+    return -1;
+  g_ndim = ndim;
+  *F = 0;
+  *B = 0;
+  *S = 0;
+  if (!strcmp(name, "euler")) {
+    *F = euler_F32;
+  } else if (!strcmp(name, "cattaneo")) {
+    *F = cattaneo_F32;
+    *S = cattaneo_S32;
+  } else if (!strcmp(name, "ncp")) {
+    *F = ncp_F32;
+    *B = ncp_B32;
+    *S = ncp_S32;
+  } else if (!strcmp(name, "burgers2")) {
+    *F = burgers2_F32;
+  } else {
+    return -2;
+  }
+  return 0;
+}

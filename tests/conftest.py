@@ -94,6 +94,9 @@ def load_device_host(path):
     L.host_predictor_guess.argtypes = [ctypes.c_char_p, c_int, c_int, ora.dp, c_ll, ora.dp, c_d,
                                        c_d, ora.dp, ora.dp, ora.dp, u64p, ctypes.POINTER(c_int),
                                        u64p]
+    L.host_predictor_mixed.restype = c_int
+    L.host_predictor_mixed.argtypes = [ctypes.c_char_p, c_int, c_int, ora.dp, c_ll, ora.dp, c_d,
+                                       c_d, ora.dp, ora.dp, u64p, ctypes.POINTER(c_int), u64p]
     L.host_run_batch.restype = c_int
     L.host_run_batch.argtypes = [ctypes.c_char_p, c_int, c_int, c_int, c_int, ora.dp, ora.ip,
                                  ora.ip, ora.dp, ora.dp, ora.dp, ora.dp, c_int, c_d, c_int, c_int,

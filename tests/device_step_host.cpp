@@ -491,7 +491,8 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
                     const double *dX, double dt, double tol, const double *tabs,
                     double *qh, unsigned long long *iters, int *max_iters,
                     int *fail, const double *guess = nullptr,
-                    unsigned long long *fallbacks = nullptr) {
+                    unsigned long long *fallbacks = nullptr, int mixed = 0,
+                    unsigned long long *iters32 = nullptr) {
   const Tables T = unpack_tables(N, tabs);
   const int ones[3] = {1, 1, 1};
   Geom g = make_geom(ndim, ones, nullptr, dX, N);
@@ -507,13 +508,15 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
   st.snap_slot = -1;
   if (guess)
     std::memcpy(qh, guess, sizeof(double) * nrows * N * Sys::V);
-  predictor_stage<Sys, N>(stiff != 0, w, qh, g, T, wprod.data(), &st, tol, 0,
+  predictor_stage<Sys, N>(stiff != 0, w, qh, g, T, wprod.data(), &st, tol, mixed,
                           guess ? 1 : 0);
   *iters = st.pred_iters;
   *max_iters = st.pred_max_iters;
   *fail = st.pred_fail;
   if (fallbacks)
     *fallbacks = st.pred_fallbacks;
+  if (iters32)
+    *iters32 = st.pred_iters32;
 }
 } // namespace
 
@@ -766,6 +769,29 @@ HOST_API int host_predictor_guess(const char *name, int ndim, int N,
   }
   HOST_CASES(GUESS_CASE)
 #undef GUESS_CASE
+  return -1;
+}
+
+// The mixed-precision stiff predictor alone (FP32 sweeps, then FP64): qh,
+// FP64 iterations, their per-cell maximum and the FP32 sweeps; 0, -1 for an
+// unknown combination, or -2 when a block deadlocked.
+HOST_API int host_predictor_mixed(const char *name, int ndim, int N,
+                                  const double *w, long long nrows,
+                                  const double *dX, double dt, double tol,
+                                  const double *tabs, double *qh,
+                                  unsigned long long *iters, int *max_iters,
+                                  unsigned long long *iters32) {
+  emu::g_deadlock = false;
+  int fail = 0;
+#define MIXED_CASE(NAME, NDIM, SYS, ORD, FL)                                   \
+  if (FL == 0 && SYS::HAS_FP32 && !std::strcmp(name, NAME) && ndim == NDIM &&  \
+      N == ORD) {                                                              \
+    predictor_only<SYS, ORD>(ndim, 1, w, nrows, dX, dt, tol, tabs, qh, iters,  \
+                             max_iters, &fail, nullptr, nullptr, 1, iters32);  \
+    return emu::g_deadlock ? -2 : 0;                                           \
+  }
+  HOST_CASES(MIXED_CASE)
+#undef MIXED_CASE
   return -1;
 }
 

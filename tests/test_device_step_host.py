@@ -15,6 +15,8 @@ order, without one:
   predictor started from a given guess with its fallbacks;
 - batched steps (batch.cuh) of problems of mixed sizes, boundary types and
   end times: each problem equals the restatement run on it alone;
+- the mixed-precision stiff predictor (FP32 sweeps, then FP64) against the
+  restatement's mixed form, FP32 sweep counts included;
 - the fibers of a block run in thread order and in reverse order, and the
   results must agree: a read of shared memory that no barrier orders after
   its write would change with the order.
@@ -162,22 +164,62 @@ def test_device_newton_from_guess_equals_port(step_lib, kind):
         assert fb_o > 0
 
 
-def test_device_mixed_precision_step(step_lib):
-    """The mixed-precision Newton predictor (FP32 sweeps, then FP64 to the
-    same 1e-12): independent of the fibers' order, and at the plain form's
-    error level against a tolerance-1e-15 run of the restatement."""
-    u0 = workloads.relaxation(16, 2, seed=11, patches=4)
-    K = 6
-    u_ref, _, _, t_ref = ora.pde_solver("cattaneo", u0, 10.0, [1.0, 1.0], [1, 1], 0.8, 2,
-                                        stiff=True, max_steps=K, newton_tol=1e-15)
-    u_p, _, _, _ = ora.pde_solver("cattaneo", u0, 10.0, [1.0, 1.0], [1, 1], 0.8, 2, stiff=True,
-                                  max_steps=K)
-    u_m, steps, t, its = _run(step_lib, "cattaneo", u0, 2, [1, 1], 0.8, K, stiff=True, mixed=1)
-    u_mr, _, _, its_r = _run(step_lib, "cattaneo", u0, 2, [1, 1], 0.8, K, stiff=True, mixed=1,
-                             reverse=True)
-    assert steps == K and its == its_r and np.array_equal(u_m, u_mr)
+MIXED_RUNS = [("cattaneo", workloads.relaxation(16, 2, seed=11, patches=4), 2, [1, 1], 6),
+              ("ncp", workloads.random_state("ncp", (12, 10), 3), 2, [1, 0], 4),
+              ("cattaneo", workloads.relaxation(6, 3, seed=4), 2, [1, 1, 1], 2),
+              ("cattaneo", workloads.relaxation(10, 2, seed=2), 3, [1, 1], 3)]
+
+
+@pytest.mark.parametrize("run", MIXED_RUNS,
+                         ids=[f"{r[0]}-{r[1].ndim - 1}d-N{r[2]}" for r in MIXED_RUNS])
+def test_device_mixed_precision_step_equals_port(step_lib, run):
+    """The mixed-precision stiff predictor (FP32 sweeps with the FP32
+    callbacks, then at least two FP64 updates to the same 1e-12): equal to
+    the restatement's mixed form bit for bit, in both fiber orders, and at
+    the plain form's error level against a tolerance-1e-15 run."""
+    name, u0, N, bt, K = run
+    L = [1.0] * (u0.ndim - 1)
+    u_o, _, steps_o, t_o = ora.pde_solver(name, u0, 10.0, L, bt, 0.8, N, stiff=True,
+                                          max_steps=K, mixed=True)
+    for reverse in (False, True):
+        u_m, steps, t, _ = _run(step_lib, name, u0, N, bt, 0.8, K, stiff=True, mixed=1,
+                                reverse=reverse)
+        assert steps == steps_o == K and t == t_o
+        assert np.array_equal(u_m, u_o), np.abs(u_m - u_o).max()
+    u_ref, _, _, _ = ora.pde_solver(name, u0, 10.0, L, bt, 0.8, N, stiff=True, max_steps=K,
+                                    newton_tol=1e-15)
+    u_p, _, _, _ = ora.pde_solver(name, u0, 10.0, L, bt, 0.8, N, stiff=True, max_steps=K)
     floor = l1(u_p, u_ref).max()
-    assert l1(u_m, u_ref).max() <= max(1e-8, 3 * floor), (l1(u_m, u_ref).max(), floor)
+    assert not np.array_equal(u_o, u_p)          # the FP32 sweeps change the iterate
+    assert l1(u_o, u_ref).max() <= max(1e-8, 3 * floor), (l1(u_o, u_ref).max(), floor)
+
+
+@pytest.mark.parametrize("case", [("cattaneo", (10, 8), 2), ("cattaneo", (9, 7), 3),
+                                  ("cattaneo", (6, 5, 4), 2), ("ncp", (12,), 2),
+                                  ("ncp", (7, 6), 2)],
+                         ids=lambda c: f"{c[0]}-{len(c[1])}d-N{c[2]}")
+def test_device_mixed_predictor_equals_port(step_lib, case):
+    """The mixed predictor stage on the same w and dt: qh, the FP64
+    iterations (sum and per-cell maximum) and the FP32 sweeps equal the
+    restatement's."""
+    system, shape, N = case
+    u = workloads.random_state(system, shape, 2)
+    dX = np.array([1.0 / n for n in shape])
+    w = ora.weno(ora.boundaries(u, N, [1] * len(shape)), N)
+    dt = ora.timestep(system, w, dX, N, 0.9, 1.0, 0.0, 9)
+    qh_o, its_o, mx_o, sw_o = ora.predictor_mixed(system, w, dX, N, dt, 1e-12)
+    assert sw_o > 0
+    for reverse in (False, True):
+        step_lib.host_set_order(int(reverse))
+        qh = np.zeros_like(qh_o)
+        its, mx, sw = ctypes.c_ulonglong(), ctypes.c_int(), ctypes.c_ulonglong()
+        rc = step_lib.host_predictor_mixed(system.encode(), len(shape), N, ora.ptr(w),
+                                           w.shape[0], ora.ptr(dX), dt, 1e-12,
+                                           ora.ptr(stages.tables(N)), ora.ptr(qh),
+                                           ctypes.byref(its), ctypes.byref(mx), ctypes.byref(sw))
+        assert rc == 0
+        assert np.array_equal(qh, qh_o), np.abs(qh - qh_o).max()
+        assert (its.value, mx.value, sw.value) == (its_o, mx_o, sw_o)
 
 
 BATCHES = [

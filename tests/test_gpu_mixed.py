@@ -49,3 +49,30 @@ def test_mixed_precision_refused_where_it_cannot_run(gpu_lib):
     with pytest.raises(_lib.PyPDEError):
         pde_solver(u0.copy(), 1.0, [1.0, 1.0], F=s.F, S=s.S, stiff=True, max_steps=1,
                    mixed_precision=True, jit=True)   # run-time callbacks have no FP32 twin
+
+
+@pytest.mark.parametrize("case", ["cattaneo2d", "cattaneo3d", "ncp2d", "cattaneo2d-N3"])
+def test_mixed_precision_run_matches_port(gpu_lib, case):
+    """The mixed form against the restatement's mixed form (the same FP32
+    sweeps with FP32 twins of the callbacks, then the FP64 iteration with at
+    least two updates): bit for bit after K steps."""
+    import numpy as np
+
+    from oracle import ora
+    N = 3 if case.endswith("N3") else 2
+    if case.startswith("cattaneo2d"):
+        u0, s, name, K = workloads.relaxation(16, 2, seed=11, patches=4), systems.cattaneo(2), \
+            "cattaneo", 6
+    elif case == "cattaneo3d":
+        u0, s, name, K = workloads.relaxation(6, 3, seed=4), systems.cattaneo(3), "cattaneo", 2
+    else:
+        u0, s, name, K = workloads.random_state("ncp", (12, 10), 3), systems.ncp(2), "ncp", 4
+    ndim = u0.ndim - 1
+    u_o, _, steps_o, t_o = ora.pde_solver(name, u0, 10.0, [1.0] * ndim, [1] * ndim, 0.8, N,
+                                          stiff=True, max_steps=K, mixed=True)
+    q, st = u0.copy(), {}
+    pde_solver(q, 10.0, [1.0] * ndim, F=s.F, B=s.B, S=s.S, boundaryTypes="periodic", cfl=0.8,
+               order=N, stiff=True, max_steps=K, stats=st, mixed_precision=True)
+    assert st["steps"] == steps_o == K and st["t_final"] == t_o
+    assert st["pred_iters32"] > 0
+    assert np.array_equal(q, u_o), np.abs(q - u_o).max()
