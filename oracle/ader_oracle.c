@@ -2122,7 +2122,12 @@ static long predictor_range(const ctx_t *c, const double *w, long c0, long c1,
       int fb = 0;
       memcpy(q1, q0, sizeof(double) * n);
       memcpy(q0, guess + cell * n, sizeof(double) * n);
-      it = dg_newton(c, q0, Ww, dt, tol, s, q1, &fb, 0);
+      if (c->mixed) { /* FP32 sweeps from the guess */
+        const int sw = dg_newton32(c, q0, Ww, dt, tol);
+        if (sweeps32)
+          *sweeps32 += sw;
+      }
+      it = dg_newton(c, q0, Ww, dt, tol, s, q1, &fb, c->mixed ? 2 : 0);
       memcpy(qh + cell * n, q0, sizeof(double) * n);
       if (fallbacks)
         *fallbacks += fb;
@@ -2178,6 +2183,32 @@ long ora_predictor_guess(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
     *fallbacks = 0;
   long r = predictor_range(c, w, 0, nrows / c->Nd, 1, dt, newton_tol, qh,
                            maxit, guess, fallbacks, NULL);
+  free(c);
+  return r;
+}
+
+long ora_predictor_guess_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                               ora_flux32_fn F32, ora_ncp32_fn B32,
+                               ora_src32_fn S32, const double *w, long nrows,
+                               const double *dX, int ndim, int N, int V,
+                               double dt, double newton_tol,
+                               const double *guess, double *qh, int *maxit,
+                               long *fallbacks, long *sweeps32,
+                               int secondOrder) {
+  ctx_t *c = malloc(sizeof(ctx_t));
+  ctx_init(c, F, B, S, ndim, N, V, dX, secondOrder);
+  c->mixed = 1;
+  c->F32 = F32;
+  c->B32 = B32;
+  c->S32 = S32;
+  if (maxit)
+    *maxit = 0;
+  if (fallbacks)
+    *fallbacks = 0;
+  if (sweeps32)
+    *sweeps32 = 0;
+  long r = predictor_range(c, w, 0, nrows / c->Nd, 1, dt, newton_tol, qh,
+                           maxit, guess, fallbacks, sweeps32);
   free(c);
   return r;
 }

@@ -97,6 +97,17 @@ long ora_predictor_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
                          int ndim, int N, int V, double dt, double newton_tol,
                          double *qh, int *maxit, long *sweeps32,
                          int secondOrder);
+/* The mixed form started from a given guess (the learned warm start with
+ * FP32 sweeps): the FP32 sweeps start from the guess; the FP64 iteration
+ * falls back to the plain guess as ora_predictor_guess does. */
+long ora_predictor_guess_mixed(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S,
+                               ora_flux32_fn F32, ora_ncp32_fn B32,
+                               ora_src32_fn S32, const double *w, long nrows,
+                               const double *dX, int ndim, int N, int V,
+                               double dt, double newton_tol,
+                               const double *guess, double *qh, int *maxit,
+                               long *fallbacks, long *sweeps32,
+                               int secondOrder);
 /* FV corrector (FVSolver::apply) on u (prod(nX) rows) using qh over the
  * w-grid nX+2. */
 void ora_fv(ora_flux_fn F, ora_ncp_fn B, ora_src_fn S, double *u,

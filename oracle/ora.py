@@ -82,6 +82,10 @@ def port():
         L.ora_predictor_mixed.restype = c_long
         L.ora_predictor_mixed.argtypes = [c_void_p] * 6 + [dp, c_long, dp, c_int, c_int, c_int,
                                                            D, D, dp, ip, POINTER(c_long), c_int]
+        L.ora_predictor_guess_mixed.restype = c_long
+        L.ora_predictor_guess_mixed.argtypes = [c_void_p] * 6 + [
+            dp, c_long, dp, c_int, c_int, c_int, D, D, dp, dp, ip, POINTER(ctypes.c_long),
+            POINTER(c_long), c_int]
         L.ora_pde_solver_mixed.restype = c_long
         L.ora_pde_solver_mixed.argtypes = [c_void_p] * 6 + [dp, D, ip, c_int, dp, D, ip, c_int,
                                                             c_int, c_int, c_int, c_int, dp,
@@ -172,15 +176,24 @@ def predictor(sysname, w, dX, N, stiff, dt, tol=1e-12):
     return qh, its, mi.value
 
 
-def predictor_guess(sysname, w, dX, N, dt, guess, tol=1e-12):
+def predictor_guess(sysname, w, dX, N, dt, guess, tol=1e-12, mixed=False):
     """Stiff predictor from a warm start; returns (qh, iters, max_iters,
-    cells that fell back to the plain guess)."""
+    cells that fell back to the plain guess).  mixed=True: FP32 sweeps from
+    the guess first, and a fifth item, the FP32 sweeps."""
     dX = np.asarray(dX, dtype=np.float64)
     s = PortSystem(sysname, len(dX))
     qh = np.zeros((w.shape[0] * N, s.V))
     g = np.ascontiguousarray(guess, dtype=np.float64).reshape(qh.shape)
     mi = c_int()
     fb = ctypes.c_long()
+    if mixed:
+        sw = ctypes.c_long()
+        its = port().ora_predictor_guess_mixed(s.F, s.B, s.S, s.F32, s.B32, s.S32, ptr(w),
+                                               w.shape[0], ptr(dX), len(dX), N, s.V, dt, tol,
+                                               ptr(g), ptr(qh), ctypes.byref(mi),
+                                               ctypes.byref(fb), ctypes.byref(sw),
+                                               s.second_order)
+        return qh, its, mi.value, fb.value, sw.value
     its = port().ora_predictor_guess(s.F, s.B, s.S, ptr(w), w.shape[0], ptr(dX), len(dX), N,
                                      s.V, dt, tol, ptr(g), ptr(qh), ctypes.byref(mi),
                                      ctypes.byref(fb), s.second_order)

@@ -93,7 +93,7 @@ def load_device_host(path):
     L.host_predictor_guess.restype = c_int
     L.host_predictor_guess.argtypes = [ctypes.c_char_p, c_int, c_int, ora.dp, c_ll, ora.dp, c_d,
                                        c_d, ora.dp, ora.dp, ora.dp, u64p, ctypes.POINTER(c_int),
-                                       u64p]
+                                       u64p, c_int, u64p]
     L.host_predictor_mixed.restype = c_int
     L.host_predictor_mixed.argtypes = [ctypes.c_char_p, c_int, c_int, ora.dp, c_ll, ora.dp, c_d,
                                        c_d, ora.dp, ora.dp, u64p, ctypes.POINTER(c_int), u64p]

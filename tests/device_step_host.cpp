@@ -748,8 +748,9 @@ void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
 }
 } // namespace
 
-// The stiff predictor started from a given guess (nrows x N rows of V):
-// qh, iteration counts and the cells that fell back to the plain guess;
+// The stiff predictor started from a given guess (nrows x N rows of V),
+// with FP32 sweeps first when mixed is non-zero: qh, iteration counts, the
+// cells that fell back to the plain guess and the FP32 sweeps;
 // 0, -1 for an unknown combination, or -2 when a block deadlocked.
 HOST_API int host_predictor_guess(const char *name, int ndim, int N,
                                     const double *w, long long nrows,
@@ -757,14 +758,16 @@ HOST_API int host_predictor_guess(const char *name, int ndim, int N,
                                     const double *tabs, const double *guess,
                                     double *qh, unsigned long long *iters,
                                     int *max_iters,
-                                    unsigned long long *fallbacks) {
+                                    unsigned long long *fallbacks, int mixed,
+                                    unsigned long long *iters32) {
   emu::g_deadlock = false;
   int fail = 0;
 #define GUESS_CASE(NAME, NDIM, SYS, ORD, FL)                                   \
   if (FL == 0 && SYS::HAS_S && !std::strcmp(name, NAME) && ndim == NDIM &&     \
       N == ORD) {                                                              \
     predictor_only<SYS, ORD>(ndim, 1, w, nrows, dX, dt, tol, tabs, qh, iters,  \
-                             max_iters, &fail, guess, fallbacks);              \
+                             max_iters, &fail, guess, fallbacks,               \
+                             SYS::HAS_FP32 ? mixed : 0, iters32);              \
     return emu::g_deadlock ? -2 : 0;                                           \
   }
   HOST_CASES(GUESS_CASE)

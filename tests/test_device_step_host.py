@@ -131,11 +131,14 @@ def test_device_predictor_equals_port(step_lib, case):
         assert its.value == its_o and mx.value == mx_o and fail.value == 0
 
 
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("kind", ["exact", "close", "rough", "nan", "huge"])
-def test_device_newton_from_guess_equals_port(step_lib, kind):
+def test_device_newton_from_guess_equals_port(step_lib, kind, mixed):
     """The Newton predictor started from a given guess (the warm start's
-    entry): qh, iteration counts and the cells reset to the plain guess
-    (non-finite or non-decreasing residual) equal the restatement's."""
+    entry), in FP64 or with FP32 sweeps from the guess first (the learned
+    and mixed form): qh, iteration counts, FP32 sweeps and the cells reset
+    to the plain guess (non-finite or non-decreasing residual) equal the
+    restatement's."""
     n, N = 12, 2
     u = workloads.relaxation(n, 2, seed=5)
     dX = np.array([1 / n, 1 / n])
@@ -148,18 +151,22 @@ def test_device_newton_from_guess_equals_port(step_lib, kind):
          "rough": qh + 0.3 * (qh - wb) * rng.standard_normal(qh.shape),
          "nan": np.where(rng.random(qh.shape) < 0.01, np.nan, qh),
          "huge": qh * 1e30}[kind]
-    q_o, it_o, mx_o, fb_o = ora.predictor_guess("cattaneo", w, dX, N, dt, g)
+    out = ora.predictor_guess("cattaneo", w, dX, N, dt, g, mixed=mixed)
+    q_o, it_o, mx_o, fb_o = out[:4]
+    sw_o = out[4] if mixed else 0
     for reverse in (False, True):
         step_lib.host_set_order(int(reverse))
         q = np.zeros_like(qh)
         its, mx, fb = ctypes.c_ulonglong(), ctypes.c_int(), ctypes.c_ulonglong()
+        sw = ctypes.c_ulonglong()
         rc = step_lib.host_predictor_guess(b"cattaneo", 2, N, ora.ptr(w), w.shape[0],
                                            ora.ptr(dX), dt, 1e-12, ora.ptr(stages.tables(N)),
                                            ora.ptr(np.ascontiguousarray(g)), ora.ptr(q),
-                                           ctypes.byref(its), ctypes.byref(mx), ctypes.byref(fb))
+                                           ctypes.byref(its), ctypes.byref(mx), ctypes.byref(fb),
+                                           int(mixed), ctypes.byref(sw))
         assert rc == 0
         assert np.array_equal(q, q_o)
-        assert (its.value, mx.value, fb.value) == (it_o, mx_o, fb_o)
+        assert (its.value, mx.value, fb.value, sw.value) == (it_o, mx_o, fb_o, sw_o)
     if kind == "nan":
         assert fb_o > 0
 
