@@ -18,9 +18,12 @@ Supported subset (what the reference's example systems use):
   * Q[i], Q[a:b], DQ[d][i], DQ[d, i], DQ[d]; slices are views, as numpy's,
     so `ret[a:b] = x` and `ret[i, a:b] -= x` write into ret; slice bounds
     are constants or x + a : x + b around one expression (`5 + d:8 + d`);
-  * zeros(n), zeros((n, m)), eye(n), array([...]), array([[...], ...]),
-    len(), abs/min/max, sqrt, exp, log, sin, cos, tan, tanh, pow, floor,
-    sum, trace, det (up to 3x3), dot / @ for vectors and matrices, and the
+  * zeros(n), zeros((n, m)), ones, full, eye(n), array([...]),
+    array([[...], ...]), concatenate / hstack of vectors and scalars, len(),
+    abs, min/max of two values (elementwise for arrays) or of one array,
+    maximum/minimum, sign, square, clip, sqrt, exp, log, sin, cos, tan,
+    tanh, pow, floor, sum, prod, norm, outer, cross (3-vectors), trace,
+    det (up to 3x3), dot / @ for vectors and matrices, and the
     array methods and attributes copy, reshape, ravel, flatten, sum, dot,
     transpose and .T (with or without a numpy / numpy.linalg / math prefix);
   * calls to other plain Python functions, also through a module attribute
@@ -636,6 +639,97 @@ class Fn:
             out = self.new(t)
             self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = 0.0;")
             return out, t
+        if name in ("ones", "full", "ones_like", "full_like"):
+            if name.endswith("_like"):
+                shape = self.expr(args[0])[1].shape
+            else:
+                a0 = args[0]
+                shape = tuple(self.const(e) for e in a0.elts) \
+                    if isinstance(a0, (ast.Tuple, ast.List)) else (self.const(a0),)
+                if any(not isinstance(x, int) for x in shape):
+                    self.err(node, f"{name}() needs a constant shape")
+            fill = "1.0"
+            if name.startswith("full"):
+                fv, ft = self.expr(args[1])
+                if ft.kind == T.ARR:
+                    self.err(node, f"{name}() needs a scalar fill value")
+                fill = f"(double)({fv})"
+            t = _arr(*shape)
+            out = self.new(t)
+            self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {fill};")
+            return out, t
+        if name in ("max", "min", "amax", "amin") and len(args) == 1:
+            # the largest / smallest element, found in index order
+            v, t = self.expr(args[0])
+            if t.kind != T.ARR:
+                self.err(node, f"{name}() of one scalar")
+            acc = self.new(FLT, f"{v}[0]")
+            cmp = ">" if name in ("max", "amax") else "<"
+            self.emit(f"for (int i_ = 1; i_ < {t.n}; i_++) "
+                      f"if ({v}[i_] {cmp} {acc}) {acc} = {v}[i_];")
+            return acc, FLT
+        if name in ("sign", "square", "clip"):
+            v, t = self.expr(args[0])
+            if name == "clip":
+                lo, _ = self.expr(args[1])
+                hi, _ = self.expr(args[2])
+
+            def one(x):
+                if name == "sign":
+                    return f"(({x}) > 0.0 ? 1.0 : (({x}) < 0.0 ? -1.0 : 0.0))"
+                if name == "square":
+                    return f"(({x}) * ({x}))"
+                return f"fmin(fmax((double)({x}), (double)({lo})), (double)({hi}))"
+            if t.kind == T.ARR:
+                out = self.new(t)
+                self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {one(f'{v}[i_]')};")
+                return out, t
+            return one(v), (FLT if name != "square" or t.kind != T.INT else INT)
+        if name == "prod" and len(args) == 1:
+            v, t = self.expr(args[0])
+            acc = self.new(FLT, "1.0")
+            self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {acc} *= {v}[i_];")
+            return acc, FLT
+        if name == "norm" and len(args) == 1:
+            # 2-norm of a vector, Frobenius norm of a matrix
+            v, t = self.expr(args[0])
+            acc = self.new(FLT, "0.0")
+            self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {acc} += {v}[i_] * {v}[i_];")
+            return f"sqrt({acc})", FLT
+        if name == "outer" and len(args) == 2:
+            a, ta = self.expr(args[0])
+            b, tb = self.expr(args[1])
+            t = _arr(ta.n, tb.n)
+            out = self.new(t)
+            self.emit(f"for (int i_ = 0; i_ < {ta.n * tb.n}; i_++) "
+                      f"{out}[i_] = {a}[i_ / {tb.n}] * {b}[i_ % {tb.n}];")
+            return out, t
+        if name == "cross" and len(args) == 2:
+            a, ta = self.expr(args[0])
+            b, tb = self.expr(args[1])
+            if ta.shape != (3,) or tb.shape != (3,):
+                self.err(node, "cross() of two 3-vectors only")
+            t = _arr(3)
+            out = self.new(t)
+            for i in range(3):
+                j, k = (i + 1) % 3, (i + 2) % 3
+                self.emit(f"{out}[{i}] = {a}[{j}] * {b}[{k}] - {a}[{k}] * {b}[{j}];")
+            return out, t
+        if name in ("concatenate", "hstack") and len(args) == 1 and \
+                isinstance(args[0], (ast.Tuple, ast.List)):
+            parts = [self.expr(e) for e in args[0].elts]
+            n = sum(pt.n if pt.kind == T.ARR else 1 for _, pt in parts)
+            t = _arr(n)
+            out = self.new(t)
+            off = 0
+            for pv, pt in parts:
+                if pt.kind == T.ARR:
+                    self.emit(f"for (int i_ = 0; i_ < {pt.n}; i_++) {out}[{off} + i_] = {pv}[i_];")
+                    off += pt.n
+                else:
+                    self.emit(f"{out}[{off}] = (double)({pv});")
+                    off += 1
+            return out, t
         if name in ("array", "asarray"):
             a0 = args[0]
             if isinstance(a0, (ast.List, ast.Tuple)):
@@ -654,6 +748,15 @@ class Fn:
             a, ta = self.expr(args[0])
             b, tb = self.expr(args[1])
             fn = "fmin" if name in ("min", "fmin", "minimum") else "fmax"
+            if T.ARR in (ta.kind, tb.kind):  # elementwise, scalars broadcast
+                t = ta if ta.kind == T.ARR else tb
+                if ta.kind == tb.kind == T.ARR and ta.n != tb.n:
+                    self.err(node, "arrays of different lengths")
+                out = self.new(t)
+                ai = f"{a}[i_]" if ta.kind == T.ARR else f"(double)({a})"
+                bi = f"{b}[i_]" if tb.kind == T.ARR else f"(double)({b})"
+                self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {fn}({ai}, {bi});")
+                return out, t
             if ta.kind == tb.kind == T.INT:
                 return f"(({a}) {'<' if fn == 'fmin' else '>'} ({b}) ? ({a}) : ({b}))", INT
             return f"{fn}((double)({a}), (double)({b}))", FLT

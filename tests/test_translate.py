@@ -275,3 +275,32 @@ def test_slice_assignment_writes_the_array():
             out = np.zeros(36 if role == "B" else 6)
             lib.call(_p(out), _p(Q), _p(np.zeros(6)), d)
             assert np.array_equal(out, np.asarray(fn(Q, d)).reshape(-1)), (role, d, out)
+
+
+def numpy_helpers_flux(Q, d):
+    """ones / full, one-argument max / min, elementwise maximum / minimum,
+    sign, square, clip, prod, norm, outer, cross, concatenate / hstack."""
+    v = Q[0:3]
+    w = Q[3:6]
+    ret = np.full(6, 0.25) + np.ones(6)
+    ret[0] = max(v) - np.min(w) + np.amax(Q)
+    ret[1:4] = np.maximum(v, 0.5) + np.minimum(w, v) + np.sign(v - 0.6)
+    ret[4] = np.square(Q[0]) + np.prod(v) + np.linalg.norm(w) + np.clip(Q[1], 0.2, 0.7)
+    ret[5] = np.trace(np.outer(v, w)) + np.cross(v, w)[d]
+    ret += np.concatenate((v, w)) * 0.5 + np.hstack([w, v]) * np.square(w[0])
+    return ret
+
+
+def test_numpy_helpers_translate():
+    """The added numpy functions, translated, against the Python function on
+    random states (norm sums in index order, numpy through BLAS: a few ulp)."""
+    src = translate(numpy_helpers_flux, None, None, 1, 6)
+    lib = _host_lib(src, "F")
+    rng = np.random.default_rng(9)
+    for k in range(60):
+        Q = rng.random(6)
+        for d in range(3):
+            out = np.zeros(6)
+            lib.call(_p(out), _p(Q), _p(np.zeros(6)), d)
+            want = numpy_helpers_flux(Q, d)
+            assert np.abs(out - want).max() <= 1e-14 * np.abs(want).max(), (k, d, out, want)
