@@ -20,7 +20,8 @@ Supported subset (what the reference's example systems use):
     are constants or x + a : x + b around one expression (`5 + d:8 + d`);
   * zeros(n), zeros((n, m)), ones, full, eye(n), array([...]),
     array([[...], ...]), concatenate / hstack of vectors and scalars, len(),
-    abs, min/max of two values (elementwise for arrays) or of one array,
+    list comprehensions `[expr for i in range(...)]`, abs, min/max of two
+    values (elementwise for arrays) or of one array,
     maximum/minimum, sign, square, clip, sqrt, exp, log, sin, cos, tan,
     tanh, pow, floor, sum, prod, norm, outer, cross (3-vectors), trace,
     det (up to 3x3), dot / @ for vectors and matrices, and the
@@ -315,7 +316,50 @@ class Fn:
             return self.transpose(v, t, node)
         if isinstance(node, (ast.List, ast.Tuple)):
             return self.array_literal(node.elts, node)
+        if isinstance(node, ast.ListComp):
+            return self.list_comp(node)
         self.err(node, f"unsupported expression {type(node).__name__}")
+
+    def list_comp(self, node):
+        """[expr for i in range(...)] with bounds known at translation time
+        and a scalar expr: a loop that fills an array."""
+        if len(node.generators) != 1 or node.generators[0].ifs or \
+                node.generators[0].is_async:
+            self.err(node, "list comprehensions need one `for i in range(...)` and no if")
+        gen = node.generators[0]
+        if not (isinstance(gen.iter, ast.Call) and isinstance(gen.iter.func, ast.Name) and
+                gen.iter.func.id == "range" and isinstance(gen.target, ast.Name)):
+            self.err(node, "list comprehensions need `for i in range(...)`")
+        a = [self.const(x) for x in gen.iter.args]
+        if any(not isinstance(x, int) for x in a):
+            self.err(node, "range() bounds must be known at translation time")
+        lo, hi = (0, a[0]) if len(a) == 1 else (a[0], a[1])
+        step = a[2] if len(a) == 3 else 1
+        if step == 0:
+            self.err(node, "range() step of 0")
+        count = len(range(lo, hi, step))
+        if count < 1:
+            self.err(node, "empty list comprehension")
+        t = _arr(count)
+        out = self.new(t)
+        var = gen.target.id
+        cn = f"v_{_cid(var)}"
+        cmp = "<" if step > 0 else ">"
+        self.emit(f"for (int {cn} = {lo}, k_ = 0; {cn} {cmp} {hi}; {cn} += {step}, k_++) {{")
+        old = self.env.get(var)
+        self.env[var] = (cn, INT)
+        self.depth += 1
+        v, vt = self.expr(node.elt)
+        if vt.kind == T.ARR:
+            self.err(node, "list comprehension items must be scalars")
+        self.emit(f"{out}[k_] = {v};")
+        self.depth -= 1
+        if old is None:
+            del self.env[var]
+        else:
+            self.env[var] = old
+        self.emit("}")
+        return out, t
 
     def index_expr(self, node):
         c = self.const(node)

@@ -304,3 +304,20 @@ def test_numpy_helpers_translate():
             lib.call(_p(out), _p(Q), _p(np.zeros(6)), d)
             want = numpy_helpers_flux(Q, d)
             assert np.abs(out - want).max() <= 1e-14 * np.abs(want).max(), (k, d, out, want)
+
+
+def comprehension_flux(Q, d):
+    scale = np.array([1.0 + 0.5 * i for i in range(4)])
+    return np.array([Q[i] * scale[i] + Q[(i + d) % 4] for i in range(4)])
+
+
+def test_list_comprehension_translates():
+    """[expr for i in range(n)] becomes a loop filling an array; the loop
+    variable may index and take part in integer arithmetic."""
+    src = translate(comprehension_flux, None, None, 1, 4)
+    lib = _host_lib(src, "F")
+    Q = np.array([0.3, 1.7, -2.2, 4.1])
+    for d in range(3):
+        out = np.zeros(4)
+        lib.call(_p(out), _p(Q), _p(np.zeros(4)), d)
+        assert np.array_equal(out, comprehension_flux(Q, d)), (d, out)
