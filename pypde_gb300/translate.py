@@ -22,7 +22,8 @@ Supported subset (what the reference's example systems use):
     array([[...], ...]), concatenate / hstack of vectors and scalars, len(),
     list comprehensions `[expr for i in range(...)]`, abs, min/max of two
     values (elementwise for arrays) or of one array,
-    maximum/minimum, sign, square, clip, sqrt, exp, log, sin, cos, tan,
+    maximum/minimum, where, sign, square, clip, arctan2, hypot, copysign,
+    fmod, sqrt, exp, log, sin, cos, tan,
     tanh, pow, floor, sum, prod, norm, outer, cross (3-vectors), trace,
     det (up to 3x3), dot / @ for vectors and matrices, and the
     array methods and attributes copy, reshape, ravel, flatten, sum, dot,
@@ -290,7 +291,20 @@ class Fn:
         if isinstance(node, ast.Compare):
             ops = {ast.Lt: "<", ast.LtE: "<=", ast.Gt: ">", ast.GtE: ">=", ast.Eq: "==",
                    ast.NotEq: "!="}
-            left, _ = self.expr(node.left)
+            left, tl = self.expr(node.left)
+            if len(node.ops) == 1 and type(node.ops[0]) in ops:
+                r, tr = self.expr(node.comparators[0])
+                if T.ARR in (tl.kind, tr.kind):  # elementwise: 1.0 / 0.0 per item
+                    t = tl if tl.kind == T.ARR else tr
+                    if tl.kind == tr.kind == T.ARR and tl.n != tr.n:
+                        self.err(node, "arrays of different lengths")
+                    out = self.new(t)
+                    li = f"{left}[i_]" if tl.kind == T.ARR else left
+                    ri = f"{r}[i_]" if tr.kind == T.ARR else r
+                    self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) "
+                              f"{out}[i_] = ({li} {ops[type(node.ops[0])]} {ri}) ? 1.0 : 0.0;")
+                    return out, t
+                return f"(({left}) {ops[type(node.ops[0])]} ({r}))", INT
             parts = []
             for op, right in zip(node.ops, node.comparators):
                 r, _ = self.expr(right)
@@ -729,6 +743,31 @@ class Fn:
                 self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {one(f'{v}[i_]')};")
                 return out, t
             return one(v), (FLT if name != "square" or t.kind != T.INT else INT)
+        if name in ("arctan2", "atan2", "hypot", "copysign", "fmod") and len(args) == 2:
+            fn = {"arctan2": "atan2"}.get(name, name)
+            a, ta = self.expr(args[0])
+            b, tb = self.expr(args[1])
+            if T.ARR in (ta.kind, tb.kind):
+                t = ta if ta.kind == T.ARR else tb
+                out = self.new(t)
+                ai = f"{a}[i_]" if ta.kind == T.ARR else f"(double)({a})"
+                bi = f"{b}[i_]" if tb.kind == T.ARR else f"(double)({b})"
+                self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {fn}({ai}, {bi});")
+                return out, t
+            return f"{fn}((double)({a}), (double)({b}))", FLT
+        if name == "where" and len(args) == 3:
+            c, tc = self.expr(args[0])
+            a, ta = self.expr(args[1])
+            b, tb = self.expr(args[2])
+            if T.ARR in (tc.kind, ta.kind, tb.kind):  # elementwise, scalars broadcast
+                t = next(x for x in (tc, ta, tb) if x.kind == T.ARR)
+                out = self.new(t)
+                ci, ai, bi = ((f"{v}[i_]" if tv.kind == T.ARR else f"({v})")
+                              for v, tv in ((c, tc), (a, ta), (b, tb)))
+                self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) "
+                          f"{out}[i_] = ({ci}) ? (double){ai} : (double){bi};")
+                return out, t
+            return f"(({c}) ? (double)({a}) : (double)({b}))", FLT
         if name == "prod" and len(args) == 1:
             v, t = self.expr(args[0])
             acc = self.new(FLT, "1.0")

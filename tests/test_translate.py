@@ -321,3 +321,25 @@ def test_list_comprehension_translates():
         out = np.zeros(4)
         lib.call(_p(out), _p(Q), _p(np.zeros(4)), d)
         assert np.array_equal(out, comprehension_flux(Q, d)), (d, out)
+
+
+def where_atan2_flux(Q, d):
+    v = Q[0:3]
+    ret = np.zeros(5)
+    ret[0:3] = np.where(v > 0.5, v * 2.0, -v) + np.arctan2(v, 0.3)
+    ret[3] = np.where(Q[3] > Q[4], Q[3], 0.0) + math.hypot(Q[3], Q[4]) + math.atan2(Q[d], 1.5)
+    ret[4] = math.copysign(Q[4], -1.0) + math.fmod(Q[3] * 7.0, 1.3)
+    return ret
+
+
+def test_where_and_two_argument_functions_translate():
+    src = translate(where_atan2_flux, None, None, 1, 5)
+    lib = _host_lib(src, "F")
+    rng = np.random.default_rng(11)
+    for k in range(40):
+        Q = rng.random(5)
+        for d in range(3):
+            out = np.zeros(5)
+            lib.call(_p(out), _p(Q), _p(np.zeros(5)), d)
+            want = where_atan2_flux(Q, d)
+            assert np.abs(out - want).max() <= 4e-16 * np.abs(want).max(), (k, d, out, want)
