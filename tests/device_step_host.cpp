@@ -540,13 +540,17 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
   X("euler", 1, Euler<1>, 2, 2)                                                \
   X("euler", 2, Euler<2>, 2, 0)                                                \
   X("euler", 2, Euler<2>, 3, 0)                                                \
+  X("euler", 2, Euler<2>, 2, 1)                                                \
+  X("euler", 2, Euler<2>, 2, 2)                                                \
   X("euler", 3, Euler<3>, 2, 0)                                                \
   X("cattaneo", 2, Cattaneo<2>, 1, 0)                                          \
   X("cattaneo", 2, Cattaneo<2>, 2, 0)                                          \
+  X("cattaneo", 2, Cattaneo<2>, 2, 1)                                          \
   X("cattaneo", 2, Cattaneo<2>, 3, 0)                                          \
   X("cattaneo", 3, Cattaneo<3>, 2, 0)                                          \
   X("ncp", 1, Ncp<1>, 2, 0)                                                    \
   X("ncp", 2, Ncp<2>, 2, 0)                                                    \
+  X("ncp", 2, Ncp<2>, 2, 2)                                                    \
   X("burgers2", 1, Burgers2, 3, 0)
 #endif
 

@@ -68,6 +68,11 @@ RUNS = [
     ("euler", _state("euler", (6, 5, 7), 6), 2, [1, 1, 0], 0.5, 4, False, 0, "euler3d-N2"),
     ("euler", workloads.sod(16), 2, [0], 0.9, 6, False, 1, "sod16-roe"),
     ("euler", workloads.sod(16), 2, [0], 0.9, 6, False, 2, "sod16-osher"),
+    ("euler", _state("euler", (7, 6), 5), 2, [1, 0], 0.6, 3, False, 1, "euler2d-roe"),
+    ("euler", _state("euler", (6, 7), 6), 2, [0, 1], 0.6, 3, False, 2, "euler2d-osher"),
+    ("ncp", _state("ncp", (7, 6), 7), 2, [1, 1], 0.5, 3, False, 2, "ncp2d-osher"),
+    ("cattaneo", workloads.relaxation(8, 2, seed=9), 2, [1, 1], 0.8, 2, True, 1,
+     "relax8-stiff-roe"),
     ("ncp", _state("ncp", (16,), 4), 2, [0], 0.5, 6, False, 0, "ncp16-N2"),
     ("ncp", _state("ncp", (12, 10), 4), 2, [1, 1], 0.5, 6, False, 0, "ncp12x10-N2"),
     ("burgers2", _state("burgers2", (32,), 5), 3, [1], 0.5, 6, False, 0, "burgers32-N3"),
@@ -277,7 +282,8 @@ def test_device_batch_equals_port(step_lib, batch, per_pop):
 # (system, ndim, order, flux, stiff) combinations the host unit instantiates
 FUZZ_COMBOS = [("euler", 1, 1, 0, False), ("euler", 1, 2, 0, False), ("euler", 1, 3, 0, False),
                ("euler", 1, 2, 1, False), ("euler", 1, 2, 2, False), ("euler", 2, 2, 0, False),
-               ("euler", 2, 3, 0, False), ("euler", 3, 2, 0, False),
+               ("euler", 2, 3, 0, False), ("euler", 2, 2, 1, False), ("euler", 2, 2, 2, False),
+               ("euler", 3, 2, 0, False), ("cattaneo", 2, 2, 1, True), ("ncp", 2, 2, 2, False),
                ("cattaneo", 2, 1, 0, True), ("cattaneo", 2, 2, 0, True),
                ("cattaneo", 2, 3, 0, True), ("cattaneo", 3, 2, 0, True),
                ("ncp", 1, 2, 0, False), ("ncp", 2, 2, 0, False), ("burgers2", 1, 3, 0, False)]
