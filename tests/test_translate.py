@@ -135,7 +135,9 @@ def test_unsupported_constructs_are_reported():
         translate(bad, None, None, 1, 3)
 
 
-def test_nvrtc_compiles_the_kernels_for_a_translated_system():
+def _nvrtc_compile(src, kernels):
+    """Compile the translated source with the kernel templates for sm_103a
+    by NVRTC (no GPU needed); asserts success with the log."""
     try:
         nv = ctypes.CDLL("libnvrtc.so")
     except OSError:
@@ -146,14 +148,13 @@ def test_nvrtc_compiles_the_kernels_for_a_translated_system():
     here = os.path.join(os.path.dirname(__file__), "..", "pypde_gb300", "csrc")
     names = ["kernels.cuh", "ader_common.cuh", "eig_full.cuh", "mlp.cuh"]
     hdrs = [open(os.path.join(here, n)).read().encode() for n in names]
-    src = ('#include "mlp.cuh"\n' + translate(user_euler2, user_ncp, user_src, 2, 4)).encode()
+    src = ('#include "mlp.cuh"\n' + src).encode()
     prog = ctypes.c_void_p()
     arr = ctypes.c_char_p * len(names)
     assert nv.nvrtcCreateProgram(ctypes.byref(prog), src, b"u.cu", len(names), arr(*hdrs),
                                  arr(*[n.encode() for n in names])) == 0
-    for e in (b"&pypde::k_faces<UserSystem, 2, 0>", b"&pypde::k_newton<UserSystem, 2>",
-              b"&pypde::k_mlp_guess<UserSystem, 2>"):
-        nv.nvrtcAddNameExpression(prog, e)
+    for e in kernels:
+        nv.nvrtcAddNameExpression(prog, f"&pypde::{e}".encode())
     opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", b"--fmad=false"]
     rc = nv.nvrtcCompileProgram(prog, len(opts), (ctypes.c_char_p * len(opts))(*opts))
     n = ctypes.c_size_t()
@@ -161,6 +162,12 @@ def test_nvrtc_compiles_the_kernels_for_a_translated_system():
     log = ctypes.create_string_buffer(n.value)
     nv.nvrtcGetProgramLog(prog, log)
     assert rc == 0, log.value.decode()[:4000]
+
+
+def test_nvrtc_compiles_the_kernels_for_a_translated_system():
+    _nvrtc_compile(translate(user_euler2, user_ncp, user_src, 2, 4),
+                   ["k_faces<UserSystem, 2, 0>", "k_newton<UserSystem, 2>",
+                    "k_mlp_guess<UserSystem, 2>"])
 
 
 def test_lambda_callback_translates():
@@ -343,3 +350,20 @@ def test_where_and_two_argument_functions_translate():
             lib.call(_p(out), _p(Q), _p(np.zeros(5)), d)
             want = where_atan2_flux(Q, d)
             assert np.abs(out - want).max() <= 4e-16 * np.abs(want).max(), (k, d, out, want)
+
+
+
+@pytest.mark.parametrize("case", ["matrix", "numpy_helpers", "comprehension", "where"])
+def test_nvrtc_compiles_the_newer_constructs(case):
+    """The translations that use tuple-returning helpers, matrix products,
+    det, slices around d, list comprehensions, where and the added numpy
+    functions compile with the kernel templates for sm_103a."""
+    if case == "matrix":
+        src, ks = translate(flux_matrix_style, ncp_matrix_style, src_matrix_style, 1, 13), \
+            ["k_faces<UserSystem, 2, 1>", "k_newton<UserSystem, 2>"]
+    else:
+        fn = {"numpy_helpers": numpy_helpers_flux, "comprehension": comprehension_flux,
+              "where": where_atan2_flux}[case]
+        V = {"numpy_helpers": 6, "comprehension": 4, "where": 5}[case]
+        src, ks = translate(fn, None, None, 1, V), ["k_faces<UserSystem, 2, 0>"]
+    _nvrtc_compile(src, ks)
