@@ -201,3 +201,16 @@ def test_reference_example_through_translation(tmp_path, name):
     scale = np.abs(u_p).reshape(-1, V).sum(axis=0)
     err = np.abs(u - u_p).reshape(-1, V).sum(axis=0) / np.where(scale > 0, scale, 1.0)
     assert err.max() <= 1e-7, err
+
+
+@pytest.mark.parametrize("name", [n for n in ("gpr-viscous-shock-1d", "detonation-roe-N3")
+                                  if n in EX])
+def test_reference_example_compiles_with_nvrtc(name):
+    """The translated GPR (17 variables, F, B and stiff S) and detonation
+    (Roe flux at order 3) systems compile with the kernel templates for
+    sm_103a, as the run-time path compiles them."""
+    from test_translate import _nvrtc_compile
+    F, B, S, u0, N, bt, cfl, stiff, flux, K = EX[name]
+    kernels = [f"k_faces<UserSystem, {N}, {flux}>"] + \
+        ([f"k_newton<UserSystem, {N}>"] if stiff else [])
+    _nvrtc_compile(translate(F, B, S, u0.ndim - 1, u0.shape[-1]), kernels)
