@@ -13,7 +13,8 @@ Supported subset (what the reference's example systems use):
   * assignment, augmented assignment, subscript assignment a[i] = ...,
     a[i, j] = ..., if / elif / else, `for i in range(...)` with bounds known
     at translation time, return;
-  * + - * / ** (x**2 -> x*x, x**0.5 -> sqrt), unary -, comparisons, and/or/
+  * + - * / ** (x**2 -> x*x, x**0.5 -> sqrt; elementwise for an array with
+    a constant exponent), unary -, comparisons, and/or/
     not, `a if c else b`; arrays combine elementwise and broadcast scalars;
   * Q[i], Q[a:b], DQ[d][i], DQ[d, i], DQ[d]; slices are views, as numpy's,
     so `ret[a:b] = x` and `ret[i, a:b] -= x` write into ret; slice bounds
@@ -501,8 +502,16 @@ class Fn:
         if isinstance(op, ast.Pow):
             b, tb = self.expr(node.left)
             e = self.const(node.right)
-            if tb.kind == T.ARR:
-                self.err(node, "array ** is not supported")
+            if tb.kind == T.ARR:  # elementwise, with the scalar rules below
+                if e is None:
+                    self.err(node, "array ** needs a constant exponent")
+                out = self.new(tb)
+                x = f"{b}[i_]"
+                item = f"{x} * {x}" if e == 2 else (f"sqrt({x})" if e == 0.5 else
+                                                    (x if e == 1 else
+                                                     f"pow({x}, (double)({self.lit(e)}))"))
+                self.emit(f"for (int i_ = 0; i_ < {tb.n}; i_++) {out}[i_] = {item};")
+                return out, tb
             if e == 2:
                 tmp = self.new(FLT, b if tb.kind != T.INT else f"(double)({b})")
                 return f"({tmp} * {tmp})", FLT

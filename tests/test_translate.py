@@ -367,3 +367,20 @@ def test_nvrtc_compiles_the_newer_constructs(case):
         V = {"numpy_helpers": 6, "comprehension": 4, "where": 5}[case]
         src, ks = translate(fn, None, None, 1, V), ["k_faces<UserSystem, 2, 0>"]
     _nvrtc_compile(src, ks)
+
+
+def array_power_flux(Q, d):
+    v = Q[0:3]
+    return np.array([np.sum(v ** 2), np.sum(v ** 0.5), np.sum(v ** 3) + Q[3] ** 2, Q[3]])
+
+
+def test_array_power_translates():
+    """x**2 of an array squares each item, x**0.5 takes square roots and
+    other constant exponents call pow, as numpy does item by item."""
+    src = translate(array_power_flux, None, None, 1, 4)
+    lib = _host_lib(src, "F")
+    Q = np.array([0.3, 1.7, 2.2, 4.1])
+    out = np.zeros(4)
+    lib.call(_p(out), _p(Q), _p(np.zeros(4)), 0)
+    want = array_power_flux(Q, 0)
+    assert np.abs(out - want).max() <= 4e-16 * np.abs(want).max(), (out, want)
