@@ -37,7 +37,8 @@ Supported subset (what the reference's example systems use):
     module; comparisons of constants fold, so a branch on a module flag
     (`if EOS == STIFFENED_GAS:`, `if tau == inf:`) keeps only its taken side
     and code after a return that always runs is not translated;
-  * any Python identifier (Greek letters included): C names are ASCII.
+  * any Python identifier (Greek letters included): C names are ASCII;
+  * integer // and % floor as Python's do, negative operands included.
 Every expression is emitted in Python's evaluation order with no algebraic
 rewriting, so a callback that a C restatement writes the same way gives the
 same bits (the kernels are compiled without FMA contraction).
@@ -534,7 +535,13 @@ class Fn:
                     else f"({a} / {b})", FLT
             if isinstance(op, (ast.FloorDiv, ast.Mod)):
                 if ta.kind == T.INT and tb.kind == T.INT:
-                    return f"({a} {sym} {b})", INT
+                    # Python floors: when the remainder is non-zero and the
+                    # operands' signs differ, C's truncated quotient is one
+                    # too large and its remainder lacks one divisor
+                    adj = f"((({a}) % ({b})) != 0 && ((({a}) < 0) != (({b}) < 0)))"
+                    if isinstance(op, ast.FloorDiv):
+                        return f"((({a}) / ({b})) - {adj})", INT
+                    return f"((({a}) % ({b})) + ({adj} ? ({b}) : 0))", INT
                 self.err(node, "// and % need integers")
             t = INT if ta.kind == tb.kind == T.INT else FLT
             return f"({a} {sym} {b})", t

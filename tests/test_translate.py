@@ -384,3 +384,22 @@ def test_array_power_translates():
     lib.call(_p(out), _p(Q), _p(np.zeros(4)), 0)
     want = array_power_flux(Q, 0)
     assert np.abs(out - want).max() <= 4e-16 * np.abs(want).max(), (out, want)
+
+
+def floor_mod_flux(Q, d):
+    ret = np.zeros(6)
+    for i in range(-3, 3):
+        ret[i + 3] = Q[(i - d) % 6] * 10.0 + float((i - 2 * d) // 4) + float(i % -4)
+    return ret
+
+
+def test_integer_floor_division_and_modulo_follow_python():
+    """// and % of integers floor as Python does (a periodic index (i - d) % n
+    stays in range), also for negative operands."""
+    src = translate(floor_mod_flux, None, None, 1, 6)
+    lib = _host_lib(src, "F")
+    Q = np.arange(1.0, 7.0)
+    for d in range(3):
+        out = np.zeros(6)
+        lib.call(_p(out), _p(Q), _p(np.zeros(6)), d)
+        assert np.array_equal(out, floor_mod_flux(Q, d)), (d, out, floor_mod_flux(Q, d))
