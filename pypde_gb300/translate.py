@@ -38,7 +38,9 @@ Supported subset (what the reference's example systems use):
     (`if EOS == STIFFENED_GAS:`, `if tau == inf:`) keeps only its taken side
     and code after a return that always runs is not translated;
   * any Python identifier (Greek letters included): C names are ASCII;
-  * integer // and % floor as Python's do, negative operands included.
+  * integer // and % floor as Python's do, negative operands included;
+    a constant negative index counts from the end, and a constant index
+    outside its dimension is refused.
 Every expression is emitted in Python's evaluation order with no algebraic
 rewriting, so a callback that a C restatement writes the same way gives the
 same bits (the kernels are compiled without FMA contraction).
@@ -377,11 +379,19 @@ class Fn:
         self.emit("}")
         return out, t
 
-    def index_expr(self, node):
+    def index_expr(self, node, size=None):
+        """C expression of an integer index.  A constant index into a
+        dimension of the given size wraps from the end when negative, as in
+        Python, and must lie inside it."""
         c = self.const(node)
         if c is not None:
-            if not isinstance(c, int):
+            if not isinstance(c, int) or isinstance(c, bool):
                 self.err(node, "index must be an integer")
+            if size is not None:
+                if c < 0:
+                    c += size
+                if not 0 <= c < size:
+                    self.err(node, f"index out of range for a dimension of {size}")
             return str(c), c
         v, t = self.expr(node)
         if t.kind != T.INT:
@@ -439,27 +449,27 @@ class Fn:
                 return f"({base} + {lo})", _arr(n)
             return f"({base} + ({lo}) * {bt.shape[1]})", _arr(n, bt.shape[1])
         if len(idx) == 1 and len(bt.shape) == 2:
-            r, _ = self.index_expr(idx[0])
+            r, _ = self.index_expr(idx[0], bt.shape[0])
             return f"({base} + ({r}) * {bt.shape[1]})", _arr(bt.shape[1])  # row view
         if len(idx) == 1:
-            i, _ = self.index_expr(idx[0])
+            i, _ = self.index_expr(idx[0], bt.shape[0])
             return f"{base}[{i}]", FLT
         if len(idx) == 2 and len(bt.shape) == 2:
             ncol = bt.shape[1]
             rs, cs = isinstance(idx[0], ast.Slice), isinstance(idx[1], ast.Slice)
             if not rs and not cs:
-                i, _ = self.index_expr(idx[0])
-                j, _ = self.index_expr(idx[1])
+                i, _ = self.index_expr(idx[0], bt.shape[0])
+                j, _ = self.index_expr(idx[1], ncol)
                 return f"{base}[({i}) * {ncol} + ({j})]", FLT
             if not rs:  # part of one row: contiguous
-                i, _ = self.index_expr(idx[0])
+                i, _ = self.index_expr(idx[0], bt.shape[0])
                 lo, n = self._slice(idx[1], ncol, node)
                 return f"({base} + ({i}) * {ncol} + ({lo}))", _arr(n)
             if target:
                 self.err(node, "assignment to a column slice of a 2-D array")
             rlo, nr = self._slice(idx[0], bt.shape[0], node)
             if not cs:
-                j, _ = self.index_expr(idx[1])
+                j, _ = self.index_expr(idx[1], ncol)
                 t = _arr(nr)
                 out = self.new(t)
                 self.emit(f"for (int i_ = 0; i_ < {nr}; i_++) "

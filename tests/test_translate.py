@@ -403,3 +403,31 @@ def test_integer_floor_division_and_modulo_follow_python():
         out = np.zeros(6)
         lib.call(_p(out), _p(Q), _p(np.zeros(6)), d)
         assert np.array_equal(out, floor_mod_flux(Q, d)), (d, out, floor_mod_flux(Q, d))
+
+
+def negative_index_flux(Q, d):
+    ret = np.zeros(4)
+    ret[-1] = Q[-1] * 2.0
+    ret[0] = Q[-2] + Q[-4]
+    m = np.zeros((2, 2))
+    m[-1, -2] = Q[1]
+    m[-2] = Q[2:4]
+    ret[1] = m[1, 0] + m[-2, -1]
+    return ret
+
+
+def out_of_range_flux(Q, d):
+    return np.array([Q[4], Q[0], Q[1], Q[2]])
+
+
+def test_constant_indices_follow_python():
+    """A constant negative index counts from the end, as in Python; a
+    constant index outside the dimension is refused at translation time."""
+    src = translate(negative_index_flux, None, None, 1, 4)
+    lib = _host_lib(src, "F")
+    Q = np.array([0.3, 1.7, -2.2, 4.1])
+    out = np.zeros(4)
+    lib.call(_p(out), _p(Q), _p(np.zeros(4)), 0)
+    assert np.array_equal(out, negative_index_flux(Q, 0)), out
+    with pytest.raises(TranslateError, match="out of range"):
+        translate(out_of_range_flux, None, None, 1, 4)
