@@ -39,7 +39,8 @@ Supported subset (what the reference's example systems use):
     and code after a return that always runs is not translated;
   * any Python identifier (Greek letters included): C names are ASCII;
   * integer // and % floor as Python's do, negative operands included;
-    a constant negative index counts from the end, and a constant index
+    a negative index counts from the end (a computed index is checked for
+    this when its expression contains a minus sign), and a constant index
     outside its dimension is refused.
 Every expression is emitted in Python's evaluation order with no algebraic
 rewriting, so a callback that a C restatement writes the same way gives the
@@ -396,6 +397,12 @@ class Fn:
         v, t = self.expr(node)
         if t.kind != T.INT:
             self.err(node, "index must be an integer expression")
+        if size is not None and any(isinstance(n, ast.Sub) or
+                                    (isinstance(n, ast.UnaryOp) and isinstance(n.op, ast.USub))
+                                    for n in ast.walk(node)):
+            # an index that can go negative (i - 1) counts from the end, as
+            # in Python; indices without a minus sign are used as they are
+            v = f"(({v}) < 0 ? ({v}) + {size} : ({v}))"
         return v, None
 
     def _offset(self, node):

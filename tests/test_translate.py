@@ -431,3 +431,21 @@ def test_constant_indices_follow_python():
     assert np.array_equal(out, negative_index_flux(Q, 0)), out
     with pytest.raises(TranslateError, match="out of range"):
         translate(out_of_range_flux, None, None, 1, 4)
+
+
+def computed_negative_index_flux(Q, d):
+    ret = np.zeros(4)
+    for i in range(4):
+        ret[i] = Q[i - 1] * 10.0 + Q[-1 - i] + Q[1 + d]
+    return ret
+
+
+def test_computed_negative_indices_follow_python():
+    """Q[i - 1] at i = 0 is the last element, as in Python."""
+    src = translate(computed_negative_index_flux, None, None, 1, 4)
+    lib = _host_lib(src, "F")
+    Q = np.array([0.3, 1.7, -2.2, 4.1])
+    for d in range(2):
+        out = np.zeros(4)
+        lib.call(_p(out), _p(Q), _p(np.zeros(4)), d)
+        assert np.array_equal(out, computed_negative_index_flux(Q, d)), (d, out)
