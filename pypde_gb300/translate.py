@@ -285,13 +285,20 @@ class Fn:
             if isinstance(node.op, ast.UAdd):
                 return v, t
             if isinstance(node.op, ast.Not):
+                if t.kind == T.ARR:
+                    self.err(node, "`not` of an array (its truth value is ambiguous)")
                 return f"(!({v}))", INT
             self.err(node, "unsupported unary operator")
         if isinstance(node, ast.BinOp):
             return self.binop(node)
         if isinstance(node, ast.BoolOp):
             op = " && " if isinstance(node.op, ast.And) else " || "
-            parts = [self.expr(v)[0] for v in node.values]
+            parts = []
+            for v in node.values:
+                pv, pt = self.expr(v)
+                if pt.kind == T.ARR:
+                    self.err(node, "and/or of an array (its truth value is ambiguous)")
+                parts.append(pv)
             return "(" + op.join(f"({p})" for p in parts) + ")", INT
         if isinstance(node, ast.Compare):
             ops = {ast.Lt: "<", ast.LtE: "<=", ast.Gt: ">", ast.GtE: ">=", ast.Eq: "==",
@@ -319,7 +326,9 @@ class Fn:
                 left = r
             return "(" + " && ".join(parts) + ")", INT
         if isinstance(node, ast.IfExp):
-            c, _ = self.expr(node.test)
+            c, tc = self.expr(node.test)
+            if tc.kind == T.ARR:
+                self.err(node, "the condition is an array (its truth value is ambiguous)")
             a, ta = self.expr(node.body)
             b, tb = self.expr(node.orelse)
             if ta.kind == T.ARR or tb.kind == T.ARR:
@@ -1005,7 +1014,9 @@ class Fn:
             k = self.const(node.test)
             if k is not None:  # known at translation time: only the taken side
                 return self.run(node.body if k else node.orelse)
-            c, _ = self.expr(node.test)
+            c, tc = self.expr(node.test)
+            if tc.kind == T.ARR:
+                self.err(node, "the condition is an array (its truth value is ambiguous)")
             self.emit(f"if ({c}) {{")
             ends = self.block(node.body)
             if node.orelse:

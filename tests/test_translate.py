@@ -449,3 +449,23 @@ def test_computed_negative_indices_follow_python():
         out = np.zeros(4)
         lib.call(_p(out), _p(Q), _p(np.zeros(4)), d)
         assert np.array_equal(out, computed_negative_index_flux(Q, d)), (d, out)
+
+
+def array_truth_if(Q, d):
+    ret = np.zeros(3)
+    if Q[0:2] > 0.5:
+        ret[0] = 1.0
+    return ret
+
+
+def array_truth_and(Q, d):
+    return Q * (1.0 if (Q > 0.0) and Q[0] > 1.0 else 2.0)
+
+
+def test_array_truth_values_are_refused():
+    """An array where Python needs one truth value (if, and/or, not, a
+    conditional expression) raises in Python; the translation refuses it
+    instead of testing a pointer."""
+    for fn in (array_truth_if, array_truth_and):
+        with pytest.raises(TranslateError, match="ambiguous"):
+            translate(fn, None, None, 1, 3)
