@@ -1064,6 +1064,12 @@ class Fn:
         self.err(node, f"unsupported statement {type(node).__name__}")
 
     def subscript_target(self, node):
+        base = node.value
+        while isinstance(base, ast.Subscript):
+            base = base.value
+        if isinstance(base, ast.Name) and self.env.get(base.id, ("",))[0] in ("Q", "dQ"):
+            self.err(node, f"assignment into the callback's input {base.id}; "
+                           f"copy it first ({base.id}.copy())")
         v, t = self.subscript(node, target=True)
         return v, t
 

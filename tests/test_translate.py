@@ -469,3 +469,26 @@ def test_array_truth_values_are_refused():
     for fn in (array_truth_if, array_truth_and):
         with pytest.raises(TranslateError, match="ambiguous"):
             translate(fn, None, None, 1, 3)
+
+
+def writes_input_flux(Q, d):
+    Q[0] = 2.0
+    return Q
+
+
+def writes_copy_flux(Q, d):
+    q = Q.copy()
+    q[0] = 2.0
+    return q
+
+
+def test_assignment_into_the_input_is_refused():
+    """The callback's Q is the solver's state: writing into it is refused
+    with a message naming the fix, and writing into a copy translates."""
+    with pytest.raises(TranslateError, match="copy it first"):
+        translate(writes_input_flux, None, None, 1, 3)
+    lib = _host_lib(translate(writes_copy_flux, None, None, 1, 3), "F")
+    Q = np.array([0.5, 1.5, 2.5])
+    out = np.zeros(3)
+    lib.call(_p(out), _p(Q), _p(np.zeros(3)), 0)
+    assert np.array_equal(out, [2.0, 1.5, 2.5]) and Q[0] == 0.5
