@@ -26,6 +26,17 @@
  *    dg.cpp:128-154; the tolerance-tightened reference build checks it.
  *  - NaN rows (iterator.cpp:141-145) are written only while in range; the
  *    reference writes past ret's last row.
+ *  - Inside the predictor (derivs, its solve) multiply-adds are fused.
+ *    The reference's predictor output is not reproducible to the last bit
+ *    (its QR solve), so this costs no agreement.
+ * Everything that becomes the input of a callback whose Jacobian is taken
+ * by forward differences -- the face states (endpts), the time step's
+ * quadrature averages and gradients, the B path points -- and the FD
+ * quotients themselves are rounded as the reference's x86-64 build rounds
+ * them: each product and sum on its own, in the summation order of the
+ * Eigen kernel that evaluates them (gemv_lane), divisions as divisions.
+ * With that, one FV update from the reference's own predictor output agrees
+ * with the reference's to ~1e-15 relative; with fused face sums it was 5e-9.
  */
 #define _GNU_SOURCE
 #include "ader_oracle.h"
@@ -431,10 +442,52 @@ void ora_weno(const double *ub, const int *nXb, int ndim, int N, int V,
 /* ------------------------------------------------------------------ */
 /* Node-block helpers, poly/evaluations.cpp:23-70                      */
 /* ------------------------------------------------------------------ */
+/* One output lane of the column-major matrix-vector product that the
+ * reference's Eigen 3.3 build evaluates for `row * matrix` and
+ * `vector^T * matrix` (include/eigen3/src/Core/products/
+ * GeneralMatrixVector.h:88-315, SSE2 packets of two doubles, result
+ * buffer 16-byte aligned): sum_k a[k] x[k xstride], k over n columns.
+ * Columns go in blocks of four from column `rot` on; a packet lane
+ * (packet != 0) adds each block as ((c0 + c1) + (c2 + c3)), the odd last
+ * lane adds it left to right; leftover columns follow left to right, and
+ * with rot = 1 column 0 comes last.  Eigen skips one column (rot = 1) when
+ * the matrix's column stride is odd and its first element is not 16-byte
+ * aligned, so that later columns load aligned (gemv_rot).  Every product
+ * and sum is rounded on its own, as the reference's x86-64 build (no FMA)
+ * rounds them. */
+static double gemv_lane(const double *a, const double *x, long xstride, int n,
+                        int packet, int rot) {
+  double s = 0;
+  const int k0 = rot ? 1 : 0;
+  const int bound = ((n - k0) / 4) * 4 + k0;
+  for (int k = k0; k < bound; k += 4) {
+    double a0 = a[k] * x[k * xstride], a1 = a[k + 1] * x[(k + 1) * xstride];
+    double a2 = a[k + 2] * x[(k + 2) * xstride];
+    double a3 = a[k + 3] * x[(k + 3) * xstride];
+    if (packet)
+      s = s + ((a0 + a1) + (a2 + a3));
+    else
+      s = (((s + a0) + a1) + a2) + a3;
+  }
+  for (int k = bound; k < n; k++)
+    s = s + a[k] * x[k * xstride];
+  if (rot)
+    s = s + a[0] * x[0];
+  return s;
+}
+
+/* Whether that product skips its first column: V > 1 result lanes, an odd
+ * column stride (in doubles) and a first element at an odd double offset
+ * from a 16-byte boundary (the reference's matrices start on one). */
+static int gemv_rot(int V, long stride, long offset) {
+  return V > 1 && (stride & 1) && (offset & 1);
+}
+
 /* ret[idx] = (sum_j DERVALS[i_d][j] q[idx with i_d=j]) / dX  over an Nd x V
- * block (rows strided by rstride doubles).  Fused multiply-adds and one
- * reciprocal of dX: the reference sums with Eigen products and divides
- * (evaluations.cpp:23-47); the difference is at rounding level. */
+ * block (rows strided by rstride doubles).  Predictor form: fused
+ * multiply-adds and one reciprocal of dX.  The reference's predictor
+ * solves its space-time system by Householder QR (dg.cpp:197), so its
+ * last bits are not reproducible here and this sum is free to be fused. */
 static void derivs(const ora_tables *T, const double *q, long rstride,
                    double *ret, long ostride, int d, int ndim, int V,
                    double dXd) {
@@ -453,21 +506,49 @@ static void derivs(const ora_tables *T, const double *q, long rstride,
   }
 }
 
+/* derivs rounded as the reference rounds it (evaluations.cpp:23-47):
+ * Eigen's coefficient-based product sums left to right, each product and
+ * sum rounded on its own, then `ret /= dX(d)` divides.  Used where the
+ * result reaches a callback whose output is differentiated numerically
+ * (the second-order face and time-step gradients), since there a last-bit
+ * difference of the input is amplified ~1e8 by the FD step. */
+static void derivs_ref(const ora_tables *T, const double *q, long rstride,
+                       double *ret, long ostride, int d, int ndim, int V,
+                       double dXd) {
+  int N = T->N, Nd = ipow(N, ndim);
+  int sd = ipow(N, ndim - d - 1);
+  for (int idx = 0; idx < Nd; idx++) {
+    int id = (idx / sd) % N;
+    int base = idx - id * sd;
+    for (int v = 0; v < V; v++) {
+      double s = 0;
+      for (int j = 0; j < N; j++)
+        s = s + T->dervals[id * N + j] * q[(base + j * sd) * rstride + v];
+      ret[idx * ostride + v] = s / dXd;
+    }
+  }
+}
+
 /* ret[i] = sum_j ENDVALS[e][j] q[line i, node j] along axis d; i runs over
- * the N^(ndim-1) transverse nodes in row-major order */
+ * the N^(ndim-1) transverse nodes in row-major order.  The face states
+ * are callback inputs whose flux Jacobian is taken by forward differences,
+ * so they follow the reference's rounding exactly: `ENDVALS.row(e) * qh_`
+ * (evaluations.cpp:49-70) is Eigen's column-major GEMV over the N node
+ * rows of the line (gemv_lane), whose first row lies `off + base V`
+ * doubles from the start of the reference's qh buffer. */
 static void endpts(const ora_tables *T, const double *q, long rstride,
-                   double *ret, long ostride, int d, int e, int ndim, int V) {
+                   double *ret, long ostride, int d, int e, int ndim, int V,
+                   long off) {
   int N = T->N, Nd_ = ipow(N, ndim - 1);
   int sd = ipow(N, ndim - d - 1);
   for (int ind = 0; ind < Nd_; ind++) {
     int hi = ind / sd, lo = ind % sd; /* zero_index, evaluations.cpp:4-21 */
     int base = hi * sd * N + lo;
-    for (int v = 0; v < V; v++) {
-      double s = 0;
-      for (int j = 0; j < N; j++)
-        s = fma(T->endvals[e * N + j], q[(base + j * sd) * rstride + v], s);
-      ret[ind * ostride + v] = s;
-    }
+    const int rot = gemv_rot(V, (long)sd * V, off + (long)base * V);
+    for (int v = 0; v < V; v++)
+      ret[ind * ostride + v] =
+          gemv_lane(T->endvals + e * N, q + base * rstride + v, sd * rstride, N,
+                    v < (V & ~1), rot);
   }
 }
 
@@ -1327,9 +1408,8 @@ static void fd_jacobian(const ctx_t *c, double *jac, double *q, double *dq,
     *qi += h;
     c->F(v2, q, dq, d);
     *qi = qi0;
-    double ih = 1.0 / h; /* one division per column */
-    for (int r = 0; r < V; r++)
-      jac[r * V + i] = (v2[r] - v1[r]) * ih;
+    for (int r = 0; r < V; r++) /* NumericalDiff.h:31 */
+      jac[r * V + i] = (v2[r] - v1[r]) / h;
   }
 }
 
@@ -1419,12 +1499,11 @@ static int fd_jacobian_active(const ctx_t *c, double *S, const int *act, int m,
     q[i] += h;
     c->F(v2, q, dq, d);
     q[i] = qi0;
-    const double ih = 1.0 / h;
     for (int r = 0; r < V; r++) {
-      const double jr = (v2[r] - v1[r]) * ih;
+      /* a passive entry (v2 - v1) / h is zero exactly when v2 - v1 is */
       if (pos[r] >= 0)
-        S[pos[r] * m + k] = jr;
-      else if (jr != 0.0)
+        S[pos[r] * m + k] = (v2[r] - v1[r]) / h;
+      else if (v2[r] - v1[r] != 0.0)
         ok = 0;
     }
   }
@@ -1460,32 +1539,6 @@ static double max_abs_eigs_2nd(const ctx_t *c, double *q, double *dq, int d) {
 /* ------------------------------------------------------------------ */
 /* a3: CFL timestep, solvers/stepper.cpp:35-76                         */
 /* ------------------------------------------------------------------ */
-/* The quadrature averages of stepper.cpp:49,53 are Eigen row-vector x
- * matrix products; the reference build evaluates them with Eigen's
- * column-major GEMV kernel, whose summation order is: blocks of four nodes,
- * summed pairwise ((a0+a1)+(a2+a3)) into the running total for result
- * lanes that fall in a 2-double packet (v < V & ~1) and left to right for
- * the odd last lane, then the leftover nodes left to right.  The order is
- * restated here because the FD Jacobian that follows amplifies a one-ulp
- * change of its input state ~1e8-fold. */
-static double wavg(const double *wp, const double *x, long stride, int n,
-                   int packet) {
-  double s = 0;
-  int k = 0;
-  for (; k + 3 < n; k += 4) {
-    double a0 = wp[k] * x[k * stride], a1 = wp[k + 1] * x[(k + 1) * stride];
-    double a2 = wp[k + 2] * x[(k + 2) * stride];
-    double a3 = wp[k + 3] * x[(k + 3) * stride];
-    if (packet)
-      s = s + ((a0 + a1) + (a2 + a3));
-    else
-      s = (((s + a0) + a1) + a2) + a3;
-  }
-  for (; k < n; k++)
-    s += wp[k] * x[k * stride];
-  return s;
-}
-
 static double cfl_max(const ctx_t *c, const double *w, long c0, long c1) {
   int V = c->V, Nd = c->Nd, ndim = c->ndim;
   double MAX = 0.0;
@@ -1493,17 +1546,21 @@ static double cfl_max(const ctx_t *c, const double *w, long c0, long c1) {
   for (long cell = c0; cell < c1; cell++) {
     const double *w0 = w + cell * Nd * V;
     double q[ORA_MAXV], dq[3 * ORA_MAXV];
+    /* q = WGHT_PRODS^T wh0 (stepper.cpp:49): wh0 starts cell Nd V doubles
+     * into the reference's w buffer, with column stride V */
+    const int rot = gemv_rot(V, V, cell * Nd * V);
     for (int v = 0; v < V; v++)
-      q[v] = wavg(c->wprod, w0 + v, V, Nd, v < (V & ~1));
+      q[v] = gemv_lane(c->wprod, w0 + v, V, Nd, v < (V & ~1), rot);
     for (int d = 0; d < ndim; d++) { /* F sees dQ only in the 2nd-order form */
       if (!c->secondOrder) {
         for (int v = 0; v < V; v++)
           dq[d * V + v] = 0.0;
         continue;
       }
-      derivs(&c->T, w0, V, dw, V, d, ndim, V, c->dX[d]);
+      derivs_ref(&c->T, w0, V, dw, V, d, ndim, V, c->dX[d]);
+      /* dwh0 is a buffer of its own (stepper.cpp:38): aligned */
       for (int v = 0; v < V; v++)
-        dq[d * V + v] = wavg(c->wprod, dw + v, V, Nd, v < (V & ~1));
+        dq[d * V + v] = gemv_lane(c->wprod, dw + v, V, Nd, v < (V & ~1), 0);
     }
     double tmp = 0.0;
     for (int d = 0; d < ndim; d++) {
@@ -1608,8 +1665,8 @@ static void dg_rhs(const ctx_t *c, const double *q, const double *Ww,
         r[v] *= cc;
     }
   }
-  for (int i = 0; i < N * Nd * V; i++)
-    ret[i] = fma(ret[i], dt, Ww[i]);
+  for (int i = 0; i < N * Nd * V; i++) /* ret *= dt; ret += Ww */
+    ret[i] = ret[i] * dt + Ww[i];
 }
 
 /* Ww and the initial guess, dg.cpp:12-20, 156-171 */
@@ -2352,10 +2409,10 @@ static void bint(const ctx_t *c, double *ret, const double *qL,
     M[i] = 0.0;
   for (int i = 0; i < N; i++) {
     for (int v = 0; v < V; v++)
-      q[v] = fma(c->T.nodes[i], Dq[v], qL[v]);
+      q[v] = qL[v] + c->T.nodes[i] * Dq[v];
     c->B(b, q, d);
     for (int k = 0; k < V * V; k++)
-      M[k] = fma(c->T.wghts[i], b[k], M[k]);
+      M[k] = M[k] + c->T.wghts[i] * b[k];
   }
   for (int r = 0; r < V; r++) {
     double s = 0;
@@ -2448,9 +2505,11 @@ static void fv_range(const ctx_t *c, double *u, const double *qh,
     dqh_cell = malloc(sizeof(double) * 3 * ORA_MAXN * ORA_MAXN * ORA_MAXN *
                       ORA_MAXV * 2);
   int inds[3] = {0, 0, 0};
-  long nfc = 1;
-  for (int d = 0; d < ndim; d++)
+  long nfc = 1, nwc = 1;
+  for (int d = 0; d < ndim; d++) {
     nfc *= nX1[d];
+    nwc *= nX2[d];
+  }
   double f[ORA_MAXV], b[ORA_MAXV];
   for (long fc = 0; fc < nfc; fc++) {
     /* faces of w-cell `inds` with its +e_d neighbour; u index = inds - 1.
@@ -2487,14 +2546,22 @@ static void fv_range(const ctx_t *c, double *u, const double *qh,
           if (!valid0 && !valid1)
             continue;
           const double *qh1 = qh + qc1 * qrow + (long)t * Nd * V;
-          endpts(&c->T, qh0, V, q0, V, d, 1, ndim, V);
-          endpts(&c->T, qh1, V, q1, V, d, 0, ndim, V);
+          /* offsets of the two node blocks in the reference's qh and, for
+           * the gradients, in its dqh = ndim stacked copies of qh's shape
+           * (fv.cpp:96-122, 139-142, 159) */
+          const long off0 = qc0 * qrow + (long)t * Nd * V;
+          const long off1 = qc1 * qrow + (long)t * Nd * V;
+          endpts(&c->T, qh0, V, q0, V, d, 1, ndim, V, off0);
+          endpts(&c->T, qh1, V, q1, V, d, 0, ndim, V, off1);
           if (c->secondOrder)
             for (int d_ = 0; d_ < ndim; d_++) {
-              derivs(&c->T, qh0, V, tmpd, V, d_, ndim, V, c->dX[d_]);
-              endpts(&c->T, tmpd, V, dq0 + d_ * V, ndim * V, d, 1, ndim, V);
-              derivs(&c->T, qh1, V, tmpd, V, d_, ndim, V, c->dX[d_]);
-              endpts(&c->T, tmpd, V, dq1 + d_ * V, ndim * V, d, 0, ndim, V);
+              const long offd = d_ * nwc * qrow;
+              derivs_ref(&c->T, qh0, V, tmpd, V, d_, ndim, V, c->dX[d_]);
+              endpts(&c->T, tmpd, V, dq0 + d_ * V, ndim * V, d, 1, ndim, V,
+                     offd + off0);
+              derivs_ref(&c->T, qh1, V, tmpd, V, d_, ndim, V, c->dX[d_]);
+              endpts(&c->T, tmpd, V, dq1 + d_ * V, ndim * V, d, 0, ndim, V,
+                     offd + off1);
             }
           for (int idx = 0; idx < Nd_; idx++) {
             for (int v = 0; v < V; v++)

@@ -2,17 +2,21 @@
 // shared by the ADER-WENO kernels.
 //
 // Plain-form arithmetic is bit-faithful to the reference algorithm as
-// restated on the host: every sum below keeps the operation order of the
-// reference's Eigen expressions as the reference build evaluates them
-// (cited per function; paths relative to haranjackson/PyPDE), and the
-// translation units are compiled with --fmad=false so that no multiply-add
-// is contracted implicitly; the fused multiply-adds that are used are
-// explicit fma() calls, the same ones in the host restatement.  This
-// matters more than usual here: the Rusanov and CFL
-// eigenvalues come from a forward-difference Jacobian with step
-// h = 2^-26 max(|q|, 1) (src/eigs/NumericalDiff.h:6-44), which turns any
-// last-bit change of its input state into a ~1e-8 relative change of the
-// Jacobian.
+// restated on the host (cited per function; paths relative to
+// haranjackson/PyPDE).  The translation units are compiled with
+// --fmad=false so that no multiply-add is contracted implicitly; the fused
+// multiply-adds that are used are explicit fma() calls, the same ones in
+// the host restatement, and only inside the predictor and the eigenvalue
+// solvers, whose results the reference computes by other algorithms
+// anyway.  What becomes a callback input whose Jacobian is then taken by
+// forward differences (face states, time-step averages and gradients, B
+// path points) and the FD quotients follow the reference build's own
+// rounding: each product and sum rounded on its own, in the summation
+// order of the Eigen kernel that evaluates it.  This matters more than
+// usual here: the Rusanov and CFL eigenvalues come from a
+// forward-difference Jacobian with step h = 2^-26 max(|q|, 1)
+// (src/eigs/NumericalDiff.h:6-44), which turns any last-bit change of its
+// input state into a ~1e-8 relative change of the Jacobian.
 #pragma once
 
 #ifndef __CUDACC_RTC__
@@ -623,9 +627,8 @@ __device__ __noinline__ double max_abs_eig(double *a) {
 }
 
 // Forward-difference Jacobian of F (NumericalDiff.h:6-44 with its default
-// forwardMode=true, which both call sites use: system.cpp:15, :58).  The
-// quotient uses one reciprocal of h per column instead of V divisions; the
-// F values themselves, the part the step h amplifies, are unchanged.
+// forwardMode=true, which both call sites use: system.cpp:15, :58), each
+// entry the quotient (v2 - v1) / h as NumericalDiff.h:31 divides it.
 // wrt_dq: perturb dq[d*V+i] (second-order form) instead of q[i].
 template <class Sys>
 __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
@@ -644,9 +647,8 @@ __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
     *qi += h;
     Sys::F(v2, q, dq, d);
     *qi = qi0;
-    double ih = 1.0 / h; // one division per column
     for (int r = 0; r < V; r++)
-      jac[r * V + i] = (v2[r] - v1[r]) * ih;
+      jac[r * V + i] = (v2[r] - v1[r]) / h;
   }
 }
 
@@ -742,14 +744,14 @@ __device__ __forceinline__ bool fd_jacobian_active(double *S, double *q,
     q[i] += h;
     Sys::F(v2, q, dq, d);
     q[i] = qi0;
-    const double ih = 1.0 / h;
     int rk = 0;
 #pragma unroll
     for (int r = 0; r < V; r++) {
-      const double jr = (v2[r] - v1[r]) * ih;
+      // a passive entry (v2 - v1) / h is zero exactly when v2 - v1 is, so
+      // only the active entries are divided
       if (active >> r & 1u)
-        S[(rk++) * MA + k] = jr;
-      else if (jr != 0.0)
+        S[(rk++) * MA + k] = (v2[r] - v1[r]) / h;
+      else if (v2[r] - v1[r] != 0.0)
         ok = false;
     }
   }
@@ -813,26 +815,48 @@ __device__ __forceinline__ double max_abs_eigs_2nd(double *q, double *dq, int d,
   return 2 * (N + 1) / dXd * max_abs_eig<V>(M);
 }
 
-// Quadrature average in the summation order of the reference build's
-// Eigen column-major GEMV (stepper.cpp:49,53): blocks of four nodes summed
-// pairwise into the running total for packet lanes (v < V & ~1), left to
-// right for the odd last lane; leftover nodes left to right.
-__device__ __forceinline__ double wavg(const double *wp, const double *x,
-                                       int stride, int n, bool packet) {
+// One output lane of the column-major matrix-vector product that the
+// reference's Eigen 3.3 build evaluates for `row * matrix` and
+// `vector^T * matrix` (its GeneralMatrixVector.h:88-315, SSE2 packets of
+// two doubles, result buffer 16-byte aligned): sum_k a[k] x[k xstride]
+// over n columns.  Columns go in blocks of four from column `rot` on; a
+// packet lane adds each block as ((c0 + c1) + (c2 + c3)), the odd last
+// lane left to right; leftover columns follow left to right, and with
+// rot = 1 column 0 comes last.  Each product and sum is rounded on its
+// own, as the reference's x86-64 build (no FMA) rounds them.  Used where
+// the result is a callback input whose flux Jacobian is then taken by
+// forward differences (step ~1e-8 relative), which amplifies a last-bit
+// change of it ~1e8-fold: the quadrature averages of the time step
+// (stepper.cpp:49,53) and the face states (evaluations.cpp:49-70).
+__device__ __forceinline__ double gemv_lane(const double *a, const double *x,
+                                            int xstride, int n, bool packet,
+                                            bool rot) {
   double s = 0;
-  int k = 0;
-  for (; k + 3 < n; k += 4) {
-    double a0 = wp[k] * x[k * stride], a1 = wp[k + 1] * x[(k + 1) * stride];
-    double a2 = wp[k + 2] * x[(k + 2) * stride];
-    double a3 = wp[k + 3] * x[(k + 3) * stride];
+  const int k0 = rot ? 1 : 0;
+  const int bound = ((n - k0) / 4) * 4 + k0;
+  for (int k = k0; k < bound; k += 4) {
+    double a0 = a[k] * x[k * xstride], a1 = a[k + 1] * x[(k + 1) * xstride];
+    double a2 = a[k + 2] * x[(k + 2) * xstride];
+    double a3 = a[k + 3] * x[(k + 3) * xstride];
     if (packet)
       s = s + ((a0 + a1) + (a2 + a3));
     else
       s = (((s + a0) + a1) + a2) + a3;
   }
-  for (; k < n; k++)
-    s += wp[k] * x[k * stride];
+  for (int k = bound; k < n; k++)
+    s = s + a[k] * x[k * xstride];
+  if (rot)
+    s = s + a[0] * x[0];
   return s;
+}
+
+// Whether that product skips its first column: Eigen does so, to load the
+// later columns aligned, when there are V > 1 result lanes, the column
+// stride (in doubles) is odd and the first element lies an odd number of
+// doubles past a 16-byte boundary (the reference's buffers start on one).
+__device__ __forceinline__ bool gemv_rot(int V, long long stride,
+                                         long long offset) {
+  return V > 1 && (stride & 1) && (offset & 1);
 }
 
 // Non-negative doubles order like their bit patterns: max via integer

