@@ -19,7 +19,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_driver.so")
 REF_TIGHT_LIB = os.path.join(HERE, "_ref", "libref_driver_tight.so")
-REF_SRC = os.environ.get("PYPDE_REFERENCE", "/root/reference")
+# the reference tree: $PYPDE_REFERENCE, else a directory `reference` beside
+# this repository
+REF_SRC = os.environ.get("PYPDE_REFERENCE",
+                         os.path.abspath(os.path.join(HERE, "..", "..", "reference")))
 
 D = c_double
 dp = POINTER(c_double)

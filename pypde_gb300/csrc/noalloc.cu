@@ -32,11 +32,12 @@ static __device__ DevState g_noalloc_state = {0.0, 0.0, 0.0, 0.0, 0.0, 0, 0, 1};
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static double *g_scratch_ptr[NOALLOC_MAX_DEVICES];
 static DevState *g_state_ptr[NOALLOC_MAX_DEVICES];
+static int g_sm_count[NOALLOC_MAX_DEVICES];
 static std::mutex g_noalloc_mu;
 
-// Device addresses of the two symbols on the current device, looked up
-// once per device.
-static int noalloc_setup(double **scratch, DevState **state) {
+// Device addresses of the two symbols on the current device and its SM
+// count, looked up once per device.
+static int noalloc_setup(double **scratch, DevState **state, int *sms) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
@@ -63,11 +64,20 @@ static int noalloc_setup(double **scratch, DevState **state) {
                 cudaGetErrorString(e));
       return PYPDE_ERR_CUDA;
     }
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || n < 1) {
+      set_error(std::string("cudaDeviceGetAttribute(SM count): ") +
+                cudaGetErrorString(e));
+      return PYPDE_ERR_CUDA;
+    }
+    g_sm_count[dev] = n;
     g_scratch_ptr[dev] = (double *)p;
     g_state_ptr[dev] = (DevState *)q;
   }
   *scratch = g_scratch_ptr[dev];
   *state = g_state_ptr[dev];
+  *sms = g_sm_count[dev];
   return PYPDE_OK;
 }
 
@@ -120,7 +130,8 @@ static int weno_noalloc(double *w, const double *ub, const int *nXb, int ndim,
   }
   double *scratch;
   DevState *st;
-  int rc = noalloc_setup(&scratch, &st);
+  int sms;
+  int rc = noalloc_setup(&scratch, &st, &sms);
   if (rc)
     return rc;
   Tables T;
@@ -138,8 +149,8 @@ static int weno_noalloc(double *w, const double *ub, const int *nXb, int ndim,
     double *dst = (d == ndim - 1) ? w : scratch + off[d];
     long long total = n1 * (md - 2 * (N - 1)) * n3 * (long long)n4 * V;
     long long blocks = (total + 127) / 128;
-    if (blocks > 152 * 64)
-      blocks = 152 * 64;
+    if (blocks > (long long)sms * 64) // a grid-stride loop: 64 blocks per SM
+      blocks = (long long)sms * 64;
     if (blocks < 1)
       blocks = 1;
     void *args[] = {(void *)&src, (void *)&dst, (void *)&n1, (void *)&md,

@@ -23,6 +23,8 @@ Fixtures:
                     change of every step's dt
   stiff_*.npz       the stiff predictor of the tolerance-tightened
                     reference build (Newton-Krylov to 1e-12)
+  tightrun_*.npz    K full steps of the stiff relaxation workload through
+                    that build's pde_solver
 """
 import ctypes
 import os
@@ -189,6 +191,34 @@ def ref_run(tag, system, u0, N, bt, cfl, K, L=1.0, stiff=False, tight=False, dra
     return tag
 
 
+def ref_stiff_run(n, K, cfl=0.8, seed=0):
+    """K steps of the stiff relaxation workload (2-D Euler + relaxing heat
+    flux, 16x16 tau patches with log10 tau ~ U(-7, -2), periodic, N=2)
+    through the tolerance-tightened reference's pde_solver (Newton-Krylov
+    to 1e-12, the tolerance of the GPU forms).  The initial state is
+    workloads.relaxation(n, 2, seed); its SHA-256 is stored so that a test
+    can tell if that generator has changed."""
+    import hashlib
+    R = ora.ref(True)
+    u0 = workloads.relaxation(n, 2, seed=seed)
+    nX = np.array(u0.shape[:-1], dtype=np.int32)
+    dX = np.array([1.0 / n] * 2)
+    bta = np.array([1, 1], dtype=np.int32)
+    times = np.zeros(K)
+    R.ref_step_times(b"cattaneo", ora.ptr(u0), ora.ptr(nX), 2, ora.ptr(dX), cfl, ora.ptr(bta), 1,
+                     0, 2, 1e9, K, ora.ptr(times))
+    tf = float(times[-1])
+    u = u0.copy()
+    ret = np.zeros((1,) + u.shape)
+    R.ref_pde_solver(b"cattaneo", ora.ptr(u), tf, ora.ptr(nX), 2, ora.ptr(dX), cfl, ora.ptr(bta),
+                     1, 0, 2, 1, ora.ptr(ret), 1)
+    tag = f"tightrun_stiff{n}_N2_K{K}"
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), uK=u, tf=tf, times=times, K=K, N=2,
+                        n=n, seed=seed, cfl=cfl,
+                        u0_sha256=hashlib.sha256(u0.tobytes()).hexdigest())
+    return tag
+
+
 def ref_stiff_predictor(shape, N, seed, dt):
     R = ora.ref(tight=True)
     ndim = len(shape)
@@ -244,6 +274,8 @@ def ref_flux_points():
 def main():
     if "--runs" in sys.argv:  # only the full-run fixtures
         return main_runs()
+    if "--stiff-run" in sys.argv:  # only the stiff run (about 5 minutes)
+        return print(ref_stiff_run(128, 10))
     ref_tables()
     ref_flux_points()
     for system, shape, N, bt in [("euler", (40,), 2, [0]), ("euler", (40,), 3, [1]),
@@ -254,6 +286,7 @@ def main():
     print(ref_stages("euler", (5, 6, 7), 3, [0, 1, 1], seed=2, full=False))
     print(ref_cfl_ncp((16,), 3, 2), ref_cfl_ncp((9, 8), 2, 3))
     main_runs()
+    print(ref_stiff_run(128, 10))
     print(ref_stiff_predictor((6, 5), 2, 7, 2e-3))
     print(ref_stiff_predictor((6, 5), 1, 7, 2e-3))
     print(ref_stiff_predictor((5, 4), 3, 8, 2e-3))

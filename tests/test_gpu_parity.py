@@ -5,7 +5,8 @@ The plain FP64 form is built to be bit-identical to the restatement: same
 algorithms, same summation orders, the same explicit fma() calls and no
 implicit contraction on either side.  So every
 stage is compared for exact equality, and full runs must agree to well
-inside the 1e-10 relative L1 bar (they are expected to agree exactly).
+inside the 1e-10 relative L1 bar (they are expected to agree exactly),
+including the benchmark's own workloads at full size.
 """
 import glob
 import os
@@ -269,3 +270,43 @@ def test_roe_osher_full_run_matches_port(gpu_lib, flux):
                max_steps=8, stats=st)
     assert st["steps"] == steps == 8
     assert np.array_equal(q, u_o)
+
+
+def test_shear512_N3_full_size_matches_port():
+    """The shear-layer workload at its benchmark size (512x512 periodic,
+    N=3, CFL 0.8, Picard predictor), 10 steps: GPU and the CPU oracle
+    (all host cores) bit-identical, t included."""
+    u0 = workloads.shear(512)
+    K = 10
+    u_o, _, steps, t_o = ora.pde_solver("euler", u0, 10.0, [1.0, 1.0], [1, 1], 0.8, 3,
+                                        max_steps=K, nthreads=os.cpu_count() or 1)
+    s = systems.euler(2)
+    q = u0.copy()
+    st = {}
+    pde_solver(q, 10.0, [1.0, 1.0], F=s.F, boundaryTypes="periodic", cfl=0.8, order=3, ndt=1,
+               stiff=False, max_steps=K, stats=st)
+    assert st["steps"] == steps == K and st["t_final"] == t_o
+    assert np.array_equal(q, u_o)
+
+
+def test_stiff128_matches_port_and_tight_reference():
+    """The stiff relaxation workload at 128x128 (N=2, CFL 0.8, Newton to
+    1e-12), 10 steps to the reference's own t_10: GPU and CPU oracle
+    bit-identical, and both within 1e-8 relative L1 per variable of the
+    tolerance-tightened reference (Newton-Krylov to 1e-12; two solvers
+    stopped at one tolerance differ by its effect)."""
+    from test_oracle_golden import _stiff128_u0
+    z, u0 = _stiff128_u0()
+    tf = float(z["tf"])
+    u_o, _, steps, t_o = ora.pde_solver("cattaneo", u0, tf, [1.0, 1.0], [1, 1],
+                                        float(z["cfl"]), 2, stiff=True,
+                                        nthreads=os.cpu_count() or 1)
+    s = systems.cattaneo(2)
+    q = u0.copy()
+    st = {}
+    pde_solver(q, tf, [1.0, 1.0], F=s.F, S=s.S, boundaryTypes="periodic", cfl=float(z["cfl"]),
+               order=2, ndt=1, stiff=True, stats=st)
+    assert st["steps"] == steps == int(z["K"]) and st["t_final"] == t_o == tf
+    assert st["pred_fail"] == 0
+    assert np.array_equal(q, u_o)
+    assert np.all(l1(q, z["uK"]) <= 1e-8), l1(q, z["uK"])

@@ -203,3 +203,31 @@ def test_face_fluxes_match_reference(case, flux):
         fr, br = z[f"{key}_flux{flux}_f"][i], z[f"{key}_flux{flux}_b"][i]
         assert np.abs(f - fr).max() <= 1e-12 * np.abs(fr).max()
         assert np.abs(b - br).max() <= 1e-12 * max(np.abs(br).max(), 1e-300)
+
+
+def _stiff128_u0():
+    import hashlib
+
+    from pypde_gb300 import workloads
+    z = load("tightrun_stiff128_N2_K10.npz")
+    u0 = workloads.relaxation(int(z["n"]), 2, seed=int(z["seed"]))
+    assert hashlib.sha256(u0.tobytes()).hexdigest() == str(z["u0_sha256"]), \
+        "workloads.relaxation changed since the fixture was made"
+    return z, u0
+
+
+def test_stiff_run_matches_tight_reference():
+    """The stiff relaxation workload of the benchmark at 128x128 (16x16 tau
+    patches, log10 tau ~ U(-7, -2), N=2, CFL 0.8), 10 steps: the port's
+    locally implicit Newton to 1e-12 against the reference's Newton-Krylov
+    tightened to 1e-12 (tests/golden/make_golden.py, ref_stiff_run).  Two
+    solvers stopped at the same residual tolerance reach different points
+    within it, so the runs differ by that tolerance's effect, largest in
+    the heat flux and the momenta (which start at zero); the bound is the
+    one the stiff form is specified at, 1e-8 relative L1 per variable."""
+    z, u0 = _stiff128_u0()
+    u, _, steps, t = ora.pde_solver("cattaneo", u0, float(z["tf"]), [1.0, 1.0], [1, 1],
+                                    float(z["cfl"]), 2, stiff=True, nthreads=os.cpu_count() or 1)
+    assert steps == int(z["K"]) and t == float(z["tf"])
+    err = l1(u, z["uK"])
+    assert np.all(err <= 1e-8), err

@@ -6,7 +6,10 @@ pass-to-pass scratch in a fixed 32 MiB __device__ array.
 
 Checked through the C ABI against the existing weno_solver entry point (bit
 for bit, the tolerance of the other WENO tests), on two calls in a row so
-that the second call runs over the scratch contents the first one left.
+that the second call runs over the scratch contents the first one left;
+the device memory the driver reports free is the same before and after the
+second call, and a grid whose intermediate pass fills the scratch exactly
+is accepted while one row more is refused.
 Collected last: if it fails, a run that stops at the first failure has
 already run every other test.
 """
@@ -27,23 +30,37 @@ def _call(lib, out, u, N):
                                    u.shape[-1], None)
 
 
-@pytest.mark.parametrize("shape,N", [((20, 18), 3), ((9, 8, 7), 2), ((33,), 2)])
+# (779, 451) at N=3 with 4 variables: the one intermediate pass holds
+# 3 x 4 x 775 x 451 = 4,194,300 doubles, which rounds up to exactly the
+# 4 Mi-double scratch; one more row of cells does not fit
+AT_LIMIT = (779, 451)
+
+
+@pytest.mark.parametrize("shape,N", [((20, 18), 3), ((9, 8, 7), 2), ((33,), 2),
+                                     (AT_LIMIT, 3)])
 def test_noalloc_matches_weno_solver_twice(gpu_lib, shape, N):
     torch = pytest.importorskip("torch")
     u = workloads.random_state("euler", shape, 5)
     expect = stages.weno(u, N)  # the existing entry point, host buffers
     du = torch.from_numpy(u).cuda()
+    outs = [torch.full(expect.shape, float("nan"), dtype=torch.float64, device="cuda")
+            for _ in range(2)]
+    torch.cuda.synchronize()
     for call in range(2):
-        out = torch.full(expect.shape, float("nan"), dtype=torch.float64, device="cuda")
-        assert _call(gpu_lib, out, du, N) == _lib.PYPDE_OK
+        if call == 1:  # the first call loaded the module and its scratch
+            free0 = torch.cuda.mem_get_info()[0]
+        assert _call(gpu_lib, outs[call], du, N) == _lib.PYPDE_OK
         torch.cuda.synchronize()
-        assert np.array_equal(out.cpu().numpy(), expect), f"call {call}"
+        if call == 1:  # the entry point's contract: it allocates nothing
+            assert torch.cuda.mem_get_info()[0] == free0
+        assert np.array_equal(outs[call].cpu().numpy(), expect), f"call {call}"
 
 
-def test_noalloc_rejects_grids_beyond_its_scratch(gpu_lib):
+@pytest.mark.parametrize("shape", [(700, 700), (AT_LIMIT[0] + 1, AT_LIMIT[1])])
+def test_noalloc_rejects_grids_beyond_its_scratch(gpu_lib, shape):
     torch = pytest.importorskip("torch")
-    # a 2-D N=3 grid whose first-pass output needs more than 4 Mi doubles
-    shape, N, V = (700, 700), 3, 4
+    # 2-D N=3 grids whose first-pass output needs more than 4 Mi doubles
+    N, V = 3, 4
     du = torch.zeros(shape + (V,), dtype=torch.float64, device="cuda")
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     nX = np.array(shape, dtype=np.int32)
