@@ -13,9 +13,12 @@ synthetic data).  Forms measured on the same K steps from the same state:
   mixed          FP32 Newton sweeps, then >= 2 FP64 sweeps to the same 1e-12
   learned_mixed  both
 `value` is the learned form (the metric's "learned" form); `forms` gives
-both, each with its Newton iterations and its relative L1 error per
-variable against an oracle run at Newton tolerance 1e-15 (the GPU plain path
-is bit-identical to the CPU restatement, checked by the GPU tests).
+each with its Newton iterations and its relative L1 error per variable
+against the CPU oracle (oracle/, the C restatement of the reference's step,
+all host cores) run over the same K steps from the same initial state
+(`l1_vs_oracle`; `oracle_check.plain_bit_identical` says whether the plain
+form equals it bit for bit), and against the same steps converged to Newton
+tolerance 1e-15 (`l1_vs_converged`: the 1e-12 tolerance's own effect).
 --workload shear: 2-D Euler shear layer 512x512 N=3, plain FP64 (Picard).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference]
@@ -28,12 +31,15 @@ Our arm prints one JSON line:
                from a pinned host array: host->device copy of the state,
                K steps, device->host copy of the final state and the
                snapshot row, all inside the timed region
-  roofline     the dominant kernel (k_faces, FP64-bound): algorithmic FP64
-               flops of one launch (pypde_gb300.work_model) / its mean launch
-               time measured here with CUDA events, against the FP64 FMA
-               peak measured here (MEASURED_PEAKS.json has no FP64 figure)
-  cpu_baseline the CPU restatement of the reference (oracle/) on all host
-               cores, on a bounded sample (stated)
+  roofline     the dominant kernel (k_newton for the stiff workload, else the
+               larger of k_faces and the predictor; FP64-bound): algorithmic
+               FP64 flops of one launch (pypde_gb300.work_model) / its mean
+               launch time measured here with CUDA events, against the FP64
+               FMA peak measured here (MEASURED_PEAKS.json has no FP64
+               figure); the other kernel's entry stands beside it
+  cpu_baseline the CPU oracle's run of the K timed steps (the C restatement
+               of the reference, oracle/, on all host cores; the 3-D
+               workload on a stated 48^3 grid)
 The reference arm (--impl reference) times that CPU path alone.
 
 Multi-GPU: the reference's only parallelism is an x-slab split of one grid;
@@ -82,8 +88,6 @@ def parse():
     p.add_argument("--side", type=int, default=0, help="cells per side (0: the workload's)")
     p.add_argument("--order", type=int, default=0, help="N (0: the workload's)")
     p.add_argument("--train-iters", type=int, default=3000)
-    p.add_argument("--cpu-seconds", type=float, default=15.0,
-                   help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--batch-problems", type=int, default=256,
                    help="problems of the batched section (0: skip it)")
@@ -204,29 +208,44 @@ def cpu_run(args, u, steps, cores):
                           stiff=args.stiff, max_steps=steps, nthreads=cores)
 
 
-def cpu_baseline(args, u0, budget):
-    """The CPU restatement on all host cores: whole-grid steps until the
-    budget is used (at least one step).  Returns (cell-updates/s, cores,
-    sample description)."""
+def oracle_check(args, u0, local, warm):
+    """The CPU oracle (all host cores) for the timed region's K steps from
+    the initial state, on the workload's own grid (the 3-D workload on a
+    48^3 grid of the same kind: its full grid takes the host minutes per
+    step); each GPU form runs the same steps on the same grid.  Returns
+    the per-form relative L1 per variable ("l1"), whether the plain form
+    is bit-identical to the oracle, and the oracle's run as the CPU
+    baseline."""
+    import copy
     cores = os.cpu_count() or 1
-    if args.ndim == 3 and u0.shape[0] > 48:
-        # one whole 3-D grid step takes minutes on the host: a 48^3 sample of
-        # the same workload (same per-cell work)
+    a = args
+    if args.ndim == 3 and args.n > 48:
         from pypde_gb300 import workloads
+        a = copy.copy(args)
+        a.n = 48
         u0 = workloads.relaxation(48, 3, seed=0, log10_tau=(-6.0, -3.0), amp=0.05)
     C = int(np.prod(u0.shape[:-1]))
-    u = u0
-    steps, t0 = 0, time.perf_counter()
-    while True:
-        u, _, k, _ = cpu_run(args, u, 1, cores)
-        steps += k
-        el = time.perf_counter() - t0
-        if el >= budget or steps >= 50:
-            break
-    sample = (f"{steps} whole-grid step(s) of the same workload on a "
-              f"{'x'.join(map(str, u0.shape[:-1]))} grid, N={args.order}, from its initial "
-              f"state, {el:.1f} s")
-    return C * steps / el, cores, sample
+    t0 = time.perf_counter()
+    u_o, _, k, _ = cpu_run(a, u0, args.steps, cores)
+    el = time.perf_counter() - t0
+    R = Runner(a, local)
+    forms = [("plain", None, False)]
+    if args.stiff:
+        forms += [("learned", warm, False), ("mixed", None, True), ("learned_mixed", warm, True)]
+    l1s, bitwise = {}, None
+    for name, w, mx in forms:
+        q = u0.copy()
+        R.run(q, args.steps, warm=w, mixed=mx)
+        l1s[name] = [float(x) for x in l1(q, u_o)]
+        if name == "plain":
+            bitwise = bool(np.array_equal(q, u_o))
+    grid = "x".join(map(str, u0.shape[:-1]))
+    return {"l1": l1s, "grid": grid, "steps": k, "plain_bit_identical": bitwise,
+            "oracle": "the C restatement of the reference's step (oracle/ader_oracle.c), "
+                      "Newton tolerance 1e-12 for the stiff forms",
+            "cpu_baseline": {"value": C * k / el, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"the oracle's {k} whole-grid steps on a {grid} grid, "
+                                       f"N={args.order}, from the initial state, {el:.1f} s"}}
 
 
 class Runner:
@@ -361,9 +380,13 @@ def run_ours(args, ws, rank, local):
         forms["learned_mixed"] = measure_form(R, args, ws, u0, warm, mixed=True)[:4]
     value = ws * C * args.steps / sec
 
-    # relative L1 per variable after K steps from u0, against a tolerance
-    # 1e-15 oracle run of the same steps
-    errs = {}
+    # every form against the CPU oracle over the same K steps from u0, and
+    # against the same steps converged to Newton tolerance 1e-15 (the
+    # 1e-12 tolerance's own effect)
+    errs, conv_errs, oracle = {}, {}, None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        oracle = oracle_check(args, u0, local, warm)
+        errs = oracle.pop("l1")
     if args.stiff:
         q_o = u0.copy()
         R.run(q_o, args.steps, tol=1e-15)
@@ -371,7 +394,7 @@ def run_ours(args, ws, rank, local):
                             ("mixed", None, True), ("learned_mixed", warm, True)):
             q = u0.copy()
             R.run(q, args.steps, warm=w, mixed=mx)
-            errs[name] = [float(x) for x in l1(q, q_o)]
+            conv_errs[name] = [float(x) for x in l1(q, q_o)]
 
     def form_summary(name):
         st, sec_f, sp_f, ks = forms[name]
@@ -382,6 +405,8 @@ def run_ours(args, ws, rank, local):
         if args.stiff:
             d["newton_fallbacks"] = st["pred_fallbacks"]
             d["fp32_sweeps_per_cell"] = st["pred_iters32"] / (args.steps * Cw)
+            d["l1_vs_converged"] = conv_errs[name]
+        if name in errs:
             d["l1_vs_oracle"] = errs[name]
         return d
 
@@ -391,6 +416,32 @@ def run_ours(args, ws, rank, local):
     fpts = work_model.face_points([n] * nd, N)
     faces_launch = stage_s["faces"] / ksteps
     achieved = fpts * fpf / faces_launch / 1e12
+    # the predictor kernel: its useful work is the iterations the plain
+    # form needs from the same state (a warm start that saves iterations
+    # shows as a higher rate), over its mean launch time in the timed form
+    sp_plain = forms["plain"][2] if "plain" in forms else sp
+    ks_plain = forms["plain"][3] if "plain" in forms else ksteps
+    its_plain = sp_plain["pred_iters"] / (ks_plain * Cw)
+    per_it = (work_model.newton_flops_per_iteration if args.stiff
+              else work_model.predictor_flops_per_iteration)(args.system, nd, V, N)
+    pred_launch = stage_s["predictor"] / ksteps
+    pred_flops = Cw * its_plain * per_it
+    pred_kernel = "k_newton" if args.stiff else "k_predictor"
+    roof_pred = {"bound": "fp64", "kernel": pred_kernel,
+                 "achieved": pred_flops / pred_launch / 1e12, "peak": peak.value,
+                 "unit": "TFLOP/s", "frac": pred_flops / pred_launch / 1e12 / peak.value,
+                 "traffic": None, "traffic_source": "none: no ncu capture of this kernel "
+                                                     "at this size",
+                 "peak_source": "FP64 FMA loop measured by this run "
+                                "(MEASURED_PEAKS.json has no FP64 figure)",
+                 "flops_per_launch": pred_flops, "launch_ms": 1e3 * pred_launch,
+                 "iters_per_cell_counted": its_plain, "iters_per_cell_run": its,
+                 "note": "algorithmic flops of " + ("the Newton iteration (residual, FD "
+                         "Jacobian of S, dense LU and solve of each spatial node's (N V)^2 "
+                         "system)" if args.stiff else "the Picard iteration") +
+                         " per w-cell, times the iterations the plain form takes from the "
+                         "same state (pypde_gb300.work_model); the launch time includes "
+                         "the warm-start network's guess kernel in the learned form"}
     per_point = FACES_DRAM_BYTES_PER_POINT.get((args.system, nd, N))
     traffic = None if per_point is None else per_point * fpts
     traffic_src = ("none: no ncu capture of this workload" if per_point is None else
@@ -433,7 +484,8 @@ def run_ours(args, ws, rank, local):
                 "note": "one pde_solver call advancing the same K steps as the timed "
                         "region (from the state after the warm-up): the state goes in "
                         "once, the final state plus the snapshot row come out once"},
-        "roofline": {"bound": "fp64", "kernel": "k_faces", "achieved": achieved,
+        "roofline": None,
+        "roofline_faces": {"bound": "fp64", "kernel": "k_faces", "achieved": achieved,
                      "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
                      "traffic": traffic,
                      "traffic_source": traffic_src,
@@ -451,14 +503,20 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": st_h["kernel_launches"],
         "clocks": clk.summary(),
     }
+    # the dominant kernel's roofline is the headline one, the other beside it
+    if pred_launch >= faces_launch:
+        out["roofline"], out["roofline_predictor"] = roof_pred, None
+        del out["roofline_predictor"]
+    else:
+        out["roofline"] = out.pop("roofline_faces")
+        out["roofline_predictor"] = roof_pred
     if train:
         out["training"] = train
     if args.stiff and args.batch_problems > 0 and ws == 1:
         out["batched_workload"] = run_batched(args, local)
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        v, cores, sample = cpu_baseline(args, u0, args.cpu_seconds)
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": sample}
+    if oracle is not None:
+        out["cpu_baseline"] = oracle.pop("cpu_baseline")
+        out["oracle_check"] = oracle
     return out
 
 

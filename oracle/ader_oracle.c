@@ -1726,10 +1726,31 @@ static int dg_picard(const ctx_t *c, double *q0, const double *Ww, double dt,
   return it;
 }
 
+/* The FD step of the Newton matrix's source Jacobian: the power of two
+ * h = 2^(max(floor(log2 |x|), 0) - 26), within a factor two below the
+ * reference's sqrt(eps) max(|x|, 1), so that 1/h is exact and the
+ * difference quotients are multiplications.  Zero, subnormal, infinite
+ * and NaN x take h = 2^-26.  (The matrix only steers the simplified Newton
+ * iteration; the residual it drives to the tolerance is exact.) */
+static void fd_step_pow2(double x, double *h, double *ih) {
+  unsigned long long b;
+  memcpy(&b, &x, sizeof b);
+  int e = (int)((b >> 52) & 0x7ff);
+  int E = (e == 0 || e == 0x7ff) ? 0 : e - 1023;
+  if (E < 0)
+    E = 0;
+  const unsigned long long hb = (unsigned long long)(E - 26 + 1023) << 52;
+  const unsigned long long ib = (unsigned long long)(26 - E + 1023) << 52;
+  memcpy(h, &hb, sizeof hb);
+  memcpy(ih, &ib, sizeof ib);
+}
+
 /* LU with partial pivoting, in place (n <= 64).  A row whose multiplier is
  * zero is left alone, and zero entries are skipped in the triangular solves:
  * the Newton matrix of a source with a sparse Jacobian is mostly structural
- * zeros, so this takes the factorisation from O(n^3) to about O(n^2). */
+ * zeros, so this takes the factorisation from O(n^3) to about O(n^2).  The
+ * diagonal of U is stored as its reciprocals, which the elimination computes
+ * anyway, so that every solve multiplies instead of dividing. */
 static int lu_factor(double *a, int n, int *piv) {
   for (int k = 0; k < n; k++) {
     int p = k;
@@ -1754,6 +1775,7 @@ static int lu_factor(double *a, int n, int *piv) {
       for (int j = k + 1; j < n; j++)
         a[i * n + j] = fma(-f, a[k * n + j], a[i * n + j]);
     }
+    a[k * n + k] = rp;
   }
   return 0;
 }
@@ -1775,7 +1797,7 @@ static void lu_solve(const double *a, int n, const int *piv, double *b) {
     for (int j = i + 1; j < n; j++)
       if (a[i * n + j] != 0.0)
         s = fma(-a[i * n + j], b[j], s);
-    b[i] = s / a[i * n + i];
+    b[i] = s * a[i * n + i]; /* the pivot's reciprocal */
   }
 }
 
@@ -1857,11 +1879,11 @@ static int dg_newton(const ctx_t *c, double *q, const double *Ww, double dt,
             c->S(s0, qn);
             for (int wv = 0; wv < V; wv++) {
               double q0 = qn[wv];
-              double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
+              double h, ih;
+              fd_step_pow2(q0, &h, &ih);
               qn[wv] = q0 + h;
               c->S(s1, qn);
               qn[wv] = q0;
-              double ih = 1.0 / h;
               for (int v = 0; v < V; v++)
                 A[(t * V + v) * nl + t * V + wv] =
                     dt * c->T.wghts[t] * ((s1[v] - s0[v]) * ih);

@@ -859,6 +859,22 @@ __device__ __forceinline__ bool gemv_rot(int V, long long stride,
   return V > 1 && (stride & 1) && (offset & 1);
 }
 
+// The FD step of the stiff predictor's source Jacobian: the power of two
+// h = 2^(max(floor(log2 |x|), 0) - 26), within a factor two below
+// sqrt(eps) max(|x|, 1), so that 1/h is exact and the difference
+// quotients are multiplications.  Zero, subnormal, infinite and NaN x take
+// h = 2^-26.  The matrix only steers the simplified Newton iteration; the
+// residual that it drives to the tolerance is evaluated exactly.
+__device__ __forceinline__ void fd_step_pow2(double x, double &h, double &ih) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  int E = (e == 0 || e == 0x7ff) ? 0 : e - 1023;
+  if (E < 0)
+    E = 0;
+  h = __longlong_as_double((long long)((unsigned long long)(E - 26 + 1023) << 52));
+  ih = __longlong_as_double((long long)((unsigned long long)(26 - E + 1023) << 52));
+}
+
 // Non-negative doubles order like their bit patterns: max via integer
 // atomics.  NaN is skipped, as std::max(MAX, NaN) keeps MAX
 // (stepper.cpp:65).

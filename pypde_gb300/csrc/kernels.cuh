@@ -1021,12 +1021,11 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
         for (int wv = 0; wv < V; wv++) {
           double ih = 0.0;
           if (Sys::HAS_S) {
-            double q0 = qn[wv];
-            double h = fmax(SQRT_EPS * fabs(q0), SQRT_EPS);
+            double q0 = qn[wv], h;
+            fd_step_pow2(q0, h, ih);
             qn[wv] = q0 + h;
             Sys::S(s1, qn);
             qn[wv] = q0;
-            ih = 1.0 / h;
           }
           for (int v = 0; v < V; v++)
             for (int k = 0; k < N; k++) {
@@ -1080,14 +1079,16 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
           for (int j = k + 1; j < NL; j++)
             A[i * NL + j] = fma(-f, A[k * NL + j], A[i * NL + j]);
         }
+        A[k * NL + k] = rp; // U's diagonal kept as reciprocals for the solves
       }
       if (!ok) {
         failed = true;
       } else {
         double b[NL];
+        const double rw = 1.0 / wprod[idx];
         for (int tt = 0; tt < N; tt++)
           for (int v = 0; v < V; v++)
-            b[tt * V + v] = rr[(tt * Nd + idx) * V + v] * (1.0 / wprod[idx]);
+            b[tt * V + v] = rr[(tt * Nd + idx) * V + v] * rw;
         // rows were swapped whole (L included): permute b first
         for (int k = 0; k < NL; k++)
           if (piv[k] != k) {
@@ -1104,7 +1105,7 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
           for (int j = i + 1; j < NL; j++)
             if (mag_bits(A[i * NL + j]) != 0ULL)
               sacc = fma(-A[i * NL + j], b[j], sacc);
-          b[i] = sacc / A[i * NL + i];
+          b[i] = sacc * A[i * NL + i]; // the pivot's reciprocal
         }
         for (int tt = 0; tt < N; tt++)
           for (int v = 0; v < V; v++)
