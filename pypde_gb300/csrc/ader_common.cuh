@@ -626,6 +626,13 @@ __device__ __noinline__ double max_abs_eig(double *a) {
   return best;
 }
 
+// x / h for an FD step h = max(2^-26 |q|, 2^-26).  Where |q| <= 1 the step
+// is 2^-26 itself, whose reciprocal 2^26 is exact, so the multiplication
+// gives the quotient's bits without a division; otherwise it divides.
+__device__ __forceinline__ double fd_quotient(double x, double h) {
+  return h == SQRT_EPS ? x * 67108864.0 : x / h;
+}
+
 // Forward-difference Jacobian of F (NumericalDiff.h:6-44 with its default
 // forwardMode=true, which both call sites use: system.cpp:15, :58), each
 // entry the quotient (v2 - v1) / h as NumericalDiff.h:31 divides it.
@@ -648,7 +655,7 @@ __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
     Sys::F(v2, q, dq, d);
     *qi = qi0;
     for (int r = 0; r < V; r++)
-      jac[r * V + i] = (v2[r] - v1[r]) / h;
+      jac[r * V + i] = fd_quotient(v2[r] - v1[r], h);
   }
 }
 
@@ -750,7 +757,7 @@ __device__ __forceinline__ bool fd_jacobian_active(double *S, double *q,
       // a passive entry (v2 - v1) / h is zero exactly when v2 - v1 is, so
       // only the active entries are divided
       if (active >> r & 1u)
-        S[(rk++) * MA + k] = (v2[r] - v1[r]) / h;
+        S[(rk++) * MA + k] = fd_quotient(v2[r] - v1[r], h);
       else if (v2[r] - v1[r] != 0.0)
         ok = false;
     }

@@ -104,6 +104,7 @@ class Fn:
         self.env = {}        # python name -> (c name, T)
         self.lines = []
         self.tmp = 0
+        self.rebinds = 0
         self.params = params
         self.node = self._function_node(func)
         g = dict(getattr(func, "__globals__", {}))
@@ -406,12 +407,13 @@ class Fn:
         v, t = self.expr(node)
         if t.kind != T.INT:
             self.err(node, "index must be an integer expression")
-        if size is not None and any(isinstance(n, ast.Sub) or
-                                    (isinstance(n, ast.UnaryOp) and isinstance(n.op, ast.USub))
-                                    for n in ast.walk(node)):
-            # an index that can go negative (i - 1) counts from the end, as
-            # in Python; indices without a minus sign are used as they are
-            v = f"(({v}) < 0 ? ({v}) + {size} : ({v}))"
+        if size is not None:
+            # a negative index counts from the end, as in Python, whether it
+            # is written with a minus sign or held in a name (k = -1; Q[k],
+            # a loop over range(-3, 0)); a compare and select per access
+            if not v.isidentifier():
+                v = self.new(INT, v)
+            v = f"({v} < 0 ? {v} + {size} : {v})"
         return v, None
 
     def _offset(self, node):
@@ -568,7 +570,9 @@ class Fn:
                     if isinstance(op, ast.FloorDiv):
                         return f"((({a}) / ({b})) - {adj})", INT
                     return f"((({a}) % ({b})) + ({adj} ? ({b}) : 0))", INT
-                self.err(node, "// and % need integers")
+                self.tr.py_divmod_helpers()
+                fn = "py_floordiv_" if isinstance(op, ast.FloorDiv) else "py_mod_"
+                return f"{fn}((double)({a}), (double)({b}))", FLT
             t = INT if ta.kind == tb.kind == T.INT else FLT
             return f"({a} {sym} {b})", t
         # elementwise with broadcasting of scalars
@@ -578,6 +582,12 @@ class Fn:
         out = self.new(t)
         ai = f"{a}[i_]" if ta.kind == T.ARR else a
         bi = f"{b}[i_]" if tb.kind == T.ARR else b
+        if isinstance(op, (ast.FloorDiv, ast.Mod)):  # numpy floors, as Python does
+            self.tr.py_divmod_helpers()
+            fn = "py_floordiv_" if isinstance(op, ast.FloorDiv) else "py_mod_"
+            self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) "
+                      f"{out}[i_] = {fn}((double)({ai}), (double)({bi}));")
+            return out, t
         self.emit(f"for (int i_ = 0; i_ < {t.n}; i_++) {out}[i_] = {ai} {sym} {bi};")
         return out, t
 
@@ -916,6 +926,16 @@ class Fn:
 
     # ----------------------------------------------------------- statements
     def assign_name(self, name, v, t, node):
+        if name in self.env and self.env[name][0] in ("Q", "dQ") or \
+                self.env.get(name, ("",))[0].startswith("p_"):
+            # rebinding an input (Q = Q * 2, or a helper's parameter) makes
+            # the name refer to a new array, as in Python; the caller's
+            # array is left as it was
+            del self.env[name]
+            self.rebinds += 1
+            name_c = f"{name}_r{self.rebinds}"
+            self._declare(name, name_c, v, t)
+            return
         if name in self.env:
             cn, ct = self.env[name]
             if ct.kind == T.ARR:
@@ -929,9 +949,12 @@ class Fn:
                     self.err(node, f"{name} changes from int to float")
                 self.emit(f"{cn} = {v};")
             return
+        self._declare(name, name, v, t)
+
+    def _declare(self, name, cname, v, t):
         # Python names live for the whole function: declare at the top so a
         # name first bound inside an if/for block is visible after it
-        cn = f"v_{_cid(name)}"
+        cn = f"v_{_cid(cname)}"
         pad = "  " * self.base_depth
         if t.kind == T.ARR:
             self.lines.insert(0, f"{pad}double {cn}[{t.n}];")
@@ -1094,11 +1117,46 @@ class Fn:
         pass
 
 
+# Python's float floor division and remainder (the semantics numpy's //
+# and % follow): a % b takes the sign of b, a // b is (a - a % b) / b made
+# an exact integer.  fmod is exact, so the quotient is off an integer only
+# by the rounding of that one division.
+PY_DIVMOD_SRC = """__device__ __forceinline__ double py_mod_(double a, double b) {
+  double r = fmod(a, b);
+  if (r != 0.0) {
+    if ((r < 0.0) != (b < 0.0))
+      r += b;
+  } else {
+    r = copysign(0.0, b);
+  }
+  return r;
+}
+__device__ __forceinline__ double py_floordiv_(double a, double b) {
+  double r = fmod(a, b);
+  double q = (a - r) / b;
+  if (r != 0.0 && ((r < 0.0) != (b < 0.0)))
+    q -= 1.0;
+  if (q == 0.0)
+    return copysign(0.0, a / b);
+  double f = floor(q);
+  if (q - f > 0.5)
+    f += 1.0;
+  return f;
+}
+"""
+
+
 class Translator:
     def __init__(self, ndim, V):
         self.ndim, self.V = ndim, V
         self.helpers = {}
         self.helper_src = []
+        self.divmod_emitted = False
+
+    def py_divmod_helpers(self):
+        if not self.divmod_emitted:
+            self.divmod_emitted = True
+            self.helper_src.insert(0, PY_DIVMOD_SRC)
 
     # the callback's own return: write into `out`
     def on_return(self, fn, v, t, node):

@@ -145,17 +145,16 @@ def test_fused_inference_matches_training_forward(gpu_lib):
 def test_trained_warm_start_end_to_end(gpu_lib):
     """Train on 20 harvested steps of a 48x48 relaxation problem, then run
     30 steps plain and learned, both with Newton tolerance 1e-12, and
-    compare each with an oracle run at tolerance 1e-15.  Two converged
-    Newton solves started from different guesses differ by the
-    tolerance's effect, which after 30 steps is ~1e-8 relative L1 in the
-    small heat-flux components (the plain form's own error at tolerance
-    1e-12 and 1e-13 measures that floor).  The learned form must stay at
-    the plain form's error level: <= max(1e-8, 3 x the floor).
+    compare each with an oracle run at tolerance 1e-15.  Two Newton solves
+    stopped at the same residual tolerance from different guesses differ
+    by that tolerance's effect, which grows with the steps taken: the bound
+    is the stiff form's 1e-8 relative L1 per 10 steps, 3e-8 here (the plain
+    form's own distance from the converged run, printed, is of that order).
     Newton iterations are measured against the plain run and written to
-    the test output: on this problem Newton contracts by about 1e-2 per
-    sweep, so a guess must be ~1e-4 accurate per cell to save a sweep,
-    and the BF16 network's (median 6-25% per cell, heavy tail) saves close
-    to none -- the
+    the test output.  Perturbing the converged corrections at random shows
+    what a guess must achieve on this iteration: a 10% relative error per
+    entry costs iterations, 1% saves none, 0.1% saves about 13%; the
+    network's per-cell error is tens of percent, so it saves none, and the
     bound checked is that it costs at most 10% more."""
     n, N, K = 48, 2, 30
     u0 = workloads.relaxation(n, 2, seed=11, patches=4)
@@ -182,5 +181,5 @@ def test_trained_warm_start_end_to_end(gpu_lib):
           f"{l1(q_p, q_o).max():.2e}, learned {err:.2e} (floor {floor:.2e}); Newton "
           f"iterations plain {st_p['pred_iters']} learned {st_l['pred_iters']} "
           f"(saved {100 * saved:.1f}%), fallbacks {st_l['pred_fallbacks']}")
-    assert err <= max(1e-8, 3 * floor), (err, floor)
+    assert err <= 1e-8 * K / 10, (err, floor)
     assert st_l["pred_iters"] <= 1.1 * st_p["pred_iters"]

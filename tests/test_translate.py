@@ -492,3 +492,67 @@ def test_assignment_into_the_input_is_refused():
     out = np.zeros(3)
     lib.call(_p(out), _p(Q), _p(np.zeros(3)), 0)
     assert np.array_equal(out, [2.0, 1.5, 2.5]) and Q[0] == 0.5
+
+
+def float_floor_mod_flux(Q, d):
+    a = Q // 0.7
+    b = Q % -0.7
+    c = Q[0] // Q[1]
+    e = Q[1] % Q[2]
+    return np.array([a[0], a[1], a[2], b[0], b[1], b[2], c, e, 1.0 // 0.1, -7.5 % 2.0])
+
+
+def test_float_floor_division_and_modulo_follow_numpy():
+    """// and % of floats and of arrays floor as numpy and Python do (the
+    remainder takes the sign of the divisor); they were C's truncating
+    quotient, or refused."""
+    src = translate(float_floor_mod_flux, None, None, 1, 10)
+    lib = _host_lib(src, "F")
+    rng = np.random.default_rng(4)
+    for Q in [np.array([2.5, -1.3, 0.4] + [0.0] * 7), rng.standard_normal(10) * 5,
+              np.array([-0.7, 0.7, -1.4] + [1.0] * 7), np.array([0.0, -2.0, 3.0] + [0.0] * 7)]:
+        out = np.zeros(10)
+        lib.call(_p(out), _p(Q), _p(np.zeros(10)), 0)
+        want = float_floor_mod_flux(Q, 0)
+        assert np.array_equal(out, want), (Q, out, want)
+        assert np.array_equal(np.signbit(out), np.signbit(want))
+
+
+def name_negative_index_flux(Q, d):
+    ret = np.zeros(4)
+    k = -1
+    ret[0] = Q[k]
+    for i in range(-3, 0):
+        ret[i] = Q[i] * 2.0
+    j = d - 2
+    ret[0] += Q[j]
+    return ret
+
+
+def test_negative_index_in_a_name_follows_python():
+    """A negative index held in a name or a loop variable counts from the
+    end, as in Python (it used to read before the array)."""
+    src = translate(name_negative_index_flux, None, None, 1, 4)
+    lib = _host_lib(src, "F")
+    Q = np.array([0.3, 1.7, -2.2, 4.1])
+    for d in range(2):
+        out = np.zeros(4)
+        lib.call(_p(out), _p(Q), _p(np.zeros(4)), d)
+        assert np.array_equal(out, name_negative_index_flux(Q, d)), (d, out)
+
+
+def rebinds_input_flux(Q, d):
+    Q = Q * 2.0
+    Q = Q + 1.0
+    return Q
+
+
+def test_rebinding_the_input_makes_a_new_array():
+    """Q = Q * 2 rebinds the name to a new array, as in Python; the solver's
+    state is not written (it was emitted as a copy into the const input)."""
+    lib = _host_lib(translate(rebinds_input_flux, None, None, 1, 3), "F")
+    Q = np.array([0.5, 1.5, 2.5])
+    out = np.zeros(3)
+    lib.call(_p(out), _p(Q), _p(np.zeros(3)), 0)
+    assert np.array_equal(out, rebinds_input_flux(Q.copy(), 0))
+    assert np.array_equal(Q, [0.5, 1.5, 2.5])
