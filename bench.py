@@ -9,7 +9,10 @@ synthetic data).  Forms measured on the same K steps from the same state:
   plain          Newton from the plain guess q = w
   learned        Newton from the learned warm start (network trained here on
                  20 harvested plain steps with the library's own kernels;
-                 training time reported, not timed in `value`)
+                 training time reported, not timed in `value`), used only
+                 if it needed fewer Newton iterations than the plain guess
+                 on held-out harvested cells (else the plain guess stays)
+  learned_network  the network's guess used regardless of that check
   mixed          FP32 Newton sweeps, then >= 2 FP64 sweeps to the same 1e-12
   learned_mixed  both
 `value` is the learned form (the metric's "learned" form); `forms` gives
@@ -229,13 +232,14 @@ def oracle_check(args, u0, local, warm):
     u_o, _, k, _ = cpu_run(a, u0, args.steps, cores)
     el = time.perf_counter() - t0
     R = Runner(a, local)
-    forms = [("plain", None, False)]
+    forms = [("plain", None, False, False)]
     if args.stiff:
-        forms += [("learned", warm, False), ("mixed", None, True), ("learned_mixed", warm, True)]
+        forms += [("learned", warm, False, False), ("mixed", None, True, False),
+                  ("learned_mixed", warm, True, False), ("learned_network", warm, False, True)]
     l1s, bitwise = {}, None
-    for name, w, mx in forms:
+    for name, w, mx, force in forms:
         q = u0.copy()
-        R.run(q, args.steps, warm=w, mixed=mx)
+        R.run(q, args.steps, warm=w, mixed=mx, force=force)
         l1s[name] = [float(x) for x in l1(q, u_o)]
         if name == "plain":
             bitwise = bool(np.array_equal(q, u_o))
@@ -262,8 +266,12 @@ class Runner:
         self.dX = np.array([1.0 / args.n] * args.ndim)
         self.bt = np.array([1] * args.ndim, dtype=np.int32)
 
-    def run(self, u, steps, profile=False, warm=None, tol=0.0, mixed=False):
+    def run(self, u, steps, profile=False, warm=None, tol=0.0, mixed=False, force=False):
+        """warm: a WarmStart, used as pde_solver uses it (only if its
+        validation found a saving), or always with force."""
         _lib, a = self._lib, self.args
+        if warm is not None and not (force or warm.active):
+            warm = None
         opt = _lib.Options()
         opt.mixed_precision = int(mixed)
         opt.max_steps = steps
@@ -282,19 +290,19 @@ class Runner:
         return st.as_dict()
 
 
-def measure_form(R, args, ws, u0, warm=None, mixed=False):
+def measure_form(R, args, ws, u0, warm=None, mixed=False, force=False):
     """W warm-up steps, then exactly K timed steps (CUDA events inside the
     library), then an eagerly launched profile of min(K, 5) steps from the
     same state as the timed steps."""
     u = u0.copy()
-    R.run(u, args.warmup, warm=warm, mixed=mixed)
+    R.run(u, args.warmup, warm=warm, mixed=mixed, force=force)
     u_warm = u.copy()
     barrier(ws)
-    st = R.run(u, args.steps, warm=warm, mixed=mixed)
+    st = R.run(u, args.steps, warm=warm, mixed=mixed, force=force)
     barrier(ws)
     sec = allmax(ws, st["device_seconds"])
     ksteps = max(1, min(args.steps, 5))
-    sp = R.run(u_warm.copy(), ksteps, profile=True, warm=warm, mixed=mixed)
+    sp = R.run(u_warm.copy(), ksteps, profile=True, warm=warm, mixed=mixed, force=force)
     return st, sec, sp, ksteps, u_warm
 
 
@@ -367,7 +375,12 @@ def run_ours(args, ws, rank, local):
                                           iters=args.train_iters, seed=rank, device=local)
         train = {"seconds": time.perf_counter() - t0, "samples": warm.samples,
                  "iters": args.train_iters, "train_rms_normalised": warm.train_rms,
-                 "harvest": "20 plain steps from the initial state, 16384 cells per step"}
+                 "harvest": "20 plain steps from the initial state, 16384 cells per step; "
+                            "the last step's sample held out for validation",
+                 "validation": warm.validation, "active": bool(warm.active),
+                 "gate": "the learned form uses the network only if it needed fewer Newton "
+                         "iterations than the plain guess on the held-out cells; otherwise "
+                         "it keeps the plain guess (form learned_network forces it)"}
 
     head = "learned" if args.stiff else "plain"
     with Clocks(local) as clk:
@@ -378,6 +391,7 @@ def run_ours(args, ws, rank, local):
         forms["plain"] = measure_form(R, args, ws, u0, None)[:4]
         forms["mixed"] = measure_form(R, args, ws, u0, None, mixed=True)[:4]
         forms["learned_mixed"] = measure_form(R, args, ws, u0, warm, mixed=True)[:4]
+        forms["learned_network"] = measure_form(R, args, ws, u0, warm, force=True)[:4]
     value = ws * C * args.steps / sec
 
     # every form against the CPU oracle over the same K steps from u0, and
@@ -390,10 +404,12 @@ def run_ours(args, ws, rank, local):
     if args.stiff:
         q_o = u0.copy()
         R.run(q_o, args.steps, tol=1e-15)
-        for name, w, mx in (("plain", None, False), ("learned", warm, False),
-                            ("mixed", None, True), ("learned_mixed", warm, True)):
+        for name, w, mx, force in (("plain", None, False, False), ("learned", warm, False, False),
+                                   ("mixed", None, True, False),
+                                   ("learned_mixed", warm, True, False),
+                                   ("learned_network", warm, False, True)):
             q = u0.copy()
-            R.run(q, args.steps, warm=w, mixed=mx)
+            R.run(q, args.steps, warm=w, mixed=mx, force=force)
             conv_errs[name] = [float(x) for x in l1(q, q_o)]
 
     def form_summary(name):

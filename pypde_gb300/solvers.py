@@ -12,7 +12,8 @@ Differences from the reference, all at the callback boundary:
   * Extensions (keyword-only): ``max_steps``, ``newton_tol``, ``device``,
     ``stats`` (a dict filled with step and iteration counts), ``jit``,
     ``warm_start`` (a pypde_gb300.warmstart.WarmStart: learned initial guess
-    of the stiff predictor's Newton iteration), ``mixed_precision`` (Newton
+    of the stiff predictor's Newton iteration; one whose validation showed
+    no saving, ``active`` False, leaves the plain guess), ``mixed_precision`` (Newton
     sweeps in FP32 first, then at least two FP64 sweeps to the same
     tolerance; built-in systems).
 """
@@ -67,7 +68,8 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
     if warm_start is not None:
         if not stiff:
             raise ValueError("warm_start applies to the stiff (Newton) predictor")
-        opt.warm_start = warm_start.handle
+        if getattr(warm_start, "active", True):  # validated to save iterations
+            opt.warm_start = warm_start.handle
     opt.mixed_precision = int(bool(mixed_precision))
     st = _lib.Stats()
     lib = _lib.lib()

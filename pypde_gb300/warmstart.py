@@ -367,6 +367,7 @@ class WarmStart:
                                                       int(tau_var), ctypes.byref(h)))
         self.handle = h
         self.system, self.N, self.net, self.tau_var = system, N, net, tau_var
+        self.active = True  # train_warm_start sets it from its validation
 
     def free(self):
         if getattr(self, "handle", None) is not None and self.handle.value:
@@ -380,16 +381,43 @@ class WarmStart:
             pass
 
 
+def validate(ws, w, dt, dX, tol=1e-12):
+    """Newton iterations of the stiff predictor over held-out cells (one
+    harvested step's sample, w (cells, N^ndim, V), one dt), from the plain
+    guess and from the network: {"cells", "iters_plain", "iters_learned",
+    "fallbacks"}."""
+    V = w.shape[-1]
+    w2 = np.ascontiguousarray(np.asarray(w, dtype=np.float64).reshape(-1, V))
+    dX = np.ascontiguousarray(dX, dtype=np.float64)
+    qh = np.zeros((w2.shape[0] * ws.N, V))
+    L = _lib.lib()
+    sp, sl = _lib.Stats(), _lib.Stats()
+    _lib.check(L.pypde_predictor(ws.system.handle, _lib.c_ptr(w2), w2.shape[0], _lib.c_ptr(dX),
+                                 len(dX), ws.N, True, float(dt), tol, _lib.c_ptr(qh), sp))
+    _lib.check(L.pypde_predictor_guess(ws.system.handle, _lib.c_ptr(w2), w2.shape[0],
+                                       _lib.c_ptr(dX), len(dX), ws.N, float(dt), tol, None,
+                                       ws.handle, _lib.c_ptr(qh), sl))
+    return {"cells": int(w.shape[0]), "iters_plain": int(sp.pred_iters),
+            "iters_learned": int(sl.pred_iters), "fallbacks": int(sl.pred_fallbacks)}
+
+
 def train_warm_start(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="periodic", cfl=0.9,
                      order=2, tau_var=-1, steps=20, per_step=8192, iters=3000, batch=4096,
                      lr=2e-3, seed=0, device=0, newton_tol=None):
     """Harvest `steps` plain steps from Q0, train the network on the
-    library's kernels, upload it.  Returns a WarmStart for
-    pde_solver(..., warm_start=...)."""
+    library's kernels on all but the last step's sample, upload it, and
+    validate it on that held-out sample: the Newton iterations it needs
+    against the plain guess's (ws.validation).  A network that saves none
+    is marked inactive (ws.active False), and pde_solver then keeps the
+    plain guess (a guess that costs iterations is never used).  Returns a
+    WarmStart for pde_solver(..., warm_start=...)."""
     import torch
     ndim, V, N = Q0.ndim - 1, Q0.shape[-1], order
     w, qh, dt = harvest(Q0, tf, L, F, B, S, boundaryTypes, cfl, order, steps, per_step,
                         device, newton_tol)
+    nval = min(per_step, w.shape[0] // 2)  # the last harvested step is held out
+    w_val, dt_val = w[-nval:], dt[-1]
+    w, qh, dt = w[:-nval], qh[:-nval], dt[:-nval]
     f = features(w, dt, N, ndim, V, tau_var)
     d = targets(w, qh, N, ndim, V)
     secondOrder = F is not None and nargs(F) == 3
@@ -401,4 +429,9 @@ def train_warm_start(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="periodic"
     ws = WarmStart(system, N, net, tau_var, device)
     ws.train_rms = net.rms_error(f[:65536], d[:65536])
     ws.samples = f.shape[0]
+    nX = np.array(Q0.shape[:-1])
+    dX = np.array([L[i] / nX[i] for i in range(ndim)], dtype=np.float64)
+    with torch.cuda.device(device):
+        ws.validation = validate(ws, w_val, dt_val, dX, newton_tol or 1e-12)
+    ws.active = ws.validation["iters_learned"] < ws.validation["iters_plain"]
     return ws

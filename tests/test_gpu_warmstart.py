@@ -173,6 +173,17 @@ def test_trained_warm_start_end_to_end(gpu_lib):
     q_o, _ = run(1e-15)
     q_p, st_p = run(1e-12)
     q_p13, _ = run(1e-13)
+    # the validation gate: the network is used only if it saved iterations
+    # on the held-out harvested cells; otherwise pde_solver keeps the plain
+    # guess and gives the plain form's bits
+    v = ws.validation
+    assert ws.active == (v["iters_learned"] < v["iters_plain"]), v
+    print(f"validation on {v['cells']} held-out cells: Newton iterations plain "
+          f"{v['iters_plain']}, learned {v['iters_learned']}")
+    if not ws.active:
+        q_g, st_g = run(1e-12, ws)
+        assert np.array_equal(q_g, q_p) and st_g["pred_iters"] == st_p["pred_iters"]
+    ws.active = True  # the network's own guess from here on
     q_l, st_l = run(1e-12, ws)
     floor = max(l1(q_p, q_o).max(), l1(q_p13, q_o).max())
     err = l1(q_l, q_o).max()
