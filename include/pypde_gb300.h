@@ -211,10 +211,17 @@ typedef struct {
                             persistent queue, and keep the fastest */
   int per_pop;           /* without autotune: tiles per queue pop, 0 = one
                             block per tile */
+  int mixed_precision;   /* stiff form, built-in systems: FP32 Newton sweeps
+                            first, as in pde_solver_ex */
+  const pypde_warm_start *warm_start[4]; /* learned warm start of the
+                            stiff predictor for the problems of order N
+                            (index N = 1..3; NULL: plain guess), as in
+                            pde_solver_ex; one batched guess launch per
+                            order before its predictor */
 } pypde_batch_options;
 
-#define PYPDE_BATCH_STAGES 9 /* ghost, WENO x3, CFL, predictor, faces,
-                                centres, gather */
+#define PYPDE_BATCH_STAGES 10 /* ghost, WENO x3, CFL, predictor, faces,
+                                 centres, gather, warm-start guess */
 typedef struct {
   long long steps;              /* summed over problems */
   long long max_problem_steps;

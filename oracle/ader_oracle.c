@@ -1500,7 +1500,7 @@ static int fd_jacobian_active(const ctx_t *c, double *S, const int *act, int m,
     c->F(v2, q, dq, d);
     q[i] = qi0;
     for (int r = 0; r < V; r++) {
-      /* a passive entry (v2 - v1) / h is zero exactly when v2 - v1 is */
+      /* a passive entry is zero exactly when v2 - v1 is */
       if (pos[r] >= 0)
         S[pos[r] * m + k] = (v2[r] - v1[r]) / h;
       else if (v2[r] - v1[r] != 0.0)

@@ -54,17 +54,18 @@ class BatchProblem(Structure):
 
 class BatchOptions(Structure):
     _fields_ = [("max_steps", c_longlong), ("newton_tol", c_double), ("device", c_int),
-                ("steps_per_graph", c_int), ("autotune", c_int), ("per_pop", c_int)]
+                ("steps_per_graph", c_int), ("autotune", c_int), ("per_pop", c_int),
+                ("mixed_precision", c_int), ("warm_start", c_void_p * 4)]
 
 
 BATCH_STAGES = ("boundaries", "weno0", "weno1", "weno2", "cfl", "predictor", "faces",
-                "centers", "gather")
+                "centers", "gather", "guess")
 
 
 class BatchStats(Structure):
     _fields_ = [("steps", c_longlong), ("max_problem_steps", c_longlong),
                 ("device_seconds", c_double), ("kernel_launches", c_longlong),
-                ("pred_iters", c_ulonglong), ("nan_found", c_int), ("per_pop", c_int * 9),
+                ("pred_iters", c_ulonglong), ("nan_found", c_int), ("per_pop", c_int * 10),
                 ("tune_seconds", c_double)]
 
     def as_dict(self):

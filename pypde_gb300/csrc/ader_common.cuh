@@ -12,7 +12,7 @@
 // forward differences (face states, time-step averages and gradients, B
 // path points) and the FD quotients follow the reference build's own
 // rounding: each product and sum rounded on its own, in the summation
-// order of the Eigen kernel that evaluates it.  This matters more than
+// order of the Eigen kernel that evaluates it, quotients correctly rounded.  This matters more than
 // usual here: the Rusanov and CFL eigenvalues come from a
 // forward-difference Jacobian with step h = 2^-26 max(|q|, 1)
 // (src/eigs/NumericalDiff.h:6-44), which turns any last-bit change of its
@@ -626,16 +626,44 @@ __device__ __noinline__ double max_abs_eig(double *a) {
   return best;
 }
 
-// x / h for an FD step h = max(2^-26 |q|, 2^-26).  Where |q| <= 1 the step
-// is 2^-26 itself, whose reciprocal 2^26 is exact, so the multiplication
-// gives the quotient's bits without a division; otherwise it divides.
-__device__ __forceinline__ double fd_quotient(double x, double h) {
-  return h == SQRT_EPS ? x * 67108864.0 : x / h;
+// The reciprocal of an FD step h split in two, y_hi + y_lo = 1/h to about
+// 2^-106 relative: y_hi = RN(1/h) (one division per column), and y_lo from
+// the residual 1 - h y_hi, which an FMA gives exactly.
+struct FdStep {
+  double h, hi, lo;
+};
+__device__ __forceinline__ FdStep fd_step(double h) {
+  FdStep s;
+  s.h = h;
+  s.hi = 1.0 / h;
+  s.lo = fma(-h, s.hi, 1.0) * s.hi;
+  return s;
+}
+
+// x / h correctly rounded, as NumericalDiff.h:31 divides each entry,
+// without a division per entry: q0 = x y_hi + x y_lo is within half an ulp
+// and a hair of x / h, so it is a faithful quotient and its remainder
+// x - h q0 is exact (one FMA); one correction q0 + (x - h q0) y_hi then
+// rounds to the correctly rounded quotient, by Markstein's theorem (P.
+// Markstein, IBM J. Res. Dev. 34 (1990) 111-119; Cornea, Golliver and
+// Markstein, ARITH 14 (1999), Theorem 1: y_hi within half an ulp of 1/h,
+// q0 within one ulp of x / h).  Zeros (for their sign), and quotients or
+// steps far enough towards the ends of the exponent range that a
+// remainder or y_lo could be subnormal, take the division itself.
+__device__ __forceinline__ double fd_div(double x, const FdStep &s) {
+  const double q0 = fma(x, s.hi, x * s.lo);
+  const double a = fabs(q0);
+  if (!(a >= 0x1p-900 && a <= 0x1p+900 && s.h <= 0x1p+900))
+    return x / s.h;
+  return fma(fma(-q0, s.h, x), s.hi, q0);
 }
 
 // Forward-difference Jacobian of F (NumericalDiff.h:6-44 with its default
 // forwardMode=true, which both call sites use: system.cpp:15, :58), each
-// entry the quotient (v2 - v1) / h as NumericalDiff.h:31 divides it.
+// entry (v2 - v1) / h correctly rounded as NumericalDiff.h:31 divides it:
+// the Jacobian equals the reference's bit for bit on the same state (the
+// one-ulp differences of a reciprocal multiply, small as they are, move
+// every step's dt and add up over a long run).
 // wrt_dq: perturb dq[d*V+i] (second-order form) instead of q[i].
 template <class Sys>
 __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
@@ -654,8 +682,9 @@ __device__ __forceinline__ void fd_jacobian(double *jac, double *q, double *dq,
     *qi += h;
     Sys::F(v2, q, dq, d);
     *qi = qi0;
+    const FdStep fs = fd_step(h);
     for (int r = 0; r < V; r++)
-      jac[r * V + i] = fd_quotient(v2[r] - v1[r], h);
+      jac[r * V + i] = fd_div(v2[r] - v1[r], fs);
   }
 }
 
@@ -751,13 +780,14 @@ __device__ __forceinline__ bool fd_jacobian_active(double *S, double *q,
     q[i] += h;
     Sys::F(v2, q, dq, d);
     q[i] = qi0;
+    const FdStep fs = fd_step(h);
     int rk = 0;
 #pragma unroll
     for (int r = 0; r < V; r++) {
-      // a passive entry (v2 - v1) / h is zero exactly when v2 - v1 is, so
-      // only the active entries are divided
+      // a passive entry is zero exactly when v2 - v1 is: only the active
+      // entries are divided
       if (active >> r & 1u)
-        S[(rk++) * MA + k] = fd_quotient(v2[r] - v1[r], h);
+        S[(rk++) * MA + k] = fd_div(v2[r] - v1[r], fs);
       else if (v2[r] - v1[r] != 0.0)
         ok = false;
     }

@@ -296,6 +296,32 @@ int pde_solver_batch(const pypde_system *sys, bool STIFF, int FLUX, int nprob,
     a.steps_per_graph = opt->steps_per_graph;
     a.autotune = opt->autotune != 0;
     a.per_pop = opt->per_pop >= 0 ? opt->per_pop : 1;
+    a.mixed = opt->mixed_precision != 0;
+    for (int n = 1; n <= 3 && n <= MAXN; n++) {
+      const pypde_warm_start *w = opt->warm_start[n];
+      if (!w)
+        continue;
+      if (w->N != n || w->V != sys->desc->V || w->ndim != sys->desc->ndim) {
+        set_error("batch warm_start[" + std::to_string(n) +
+                  "] was built for another system, order or ndim");
+        return PYPDE_ERR_ARG;
+      }
+      a.warm[n] = w->ws;
+    }
+    if (opt->warm_start[0]) {
+      set_error("batch warm_start is indexed by order: entry 0 must be NULL");
+      return PYPDE_ERR_ARG;
+    }
+  }
+  if (a.mixed) {
+    if (!STIFF) {
+      set_error("mixed_precision applies to the stiff (Newton) predictor");
+      return PYPDE_ERR_ARG;
+    }
+    if (sys->desc->module) {
+      set_error("mixed_precision needs FP32 callbacks: built-in systems only");
+      return PYPDE_ERR_UNSUPPORTED;
+    }
   }
   BatchStats st;
   st.steps_per_problem = steps_out;

@@ -110,12 +110,16 @@ __global__ void kb_predictor(const BatchProblem *P, TileQueue q, int per_pop,
   });
 }
 
+// flags: bit 0, start from the guess already in qh (the learned warm
+// start of this order group); bit 1, FP32 sweeps first (mixed precision)
 template <class Sys, int N>
 __global__ void kb_newton(const BatchProblem *P, TileQueue q, int per_pop,
-                          const __grid_constant__ Tables T, double tol) {
+                          const __grid_constant__ Tables T, double tol,
+                          int flags) {
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
-    k_newton_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st, tol, 0, 0);
+    k_newton_body<Sys, N>(vb, b.w, b.qh, b.g, T, b.wprod, b.st, tol, flags & 1,
+                          (flags >> 1) & 1);
   });
 }
 

@@ -148,7 +148,7 @@ const char *KERNELS[] = {"k_cfl",       "k_predictor", "k_newton",
                          "k_centers",   "k_gather",    "k_mlp_guess",
                          "kb_cfl",      "kb_predictor", "kb_newton",
                          "kb_faces0",   "kb_faces1",   "kb_faces2",
-                         "kb_centers",  "kb_gather"};
+                         "kb_centers",  "kb_gather",   "kb_mlp_guess"};
 
 } // namespace
 
@@ -204,7 +204,8 @@ int jit_ensure(SystemDesc &d, int N) {
       "&pypde::kb_faces<UserSystem, " + ns + ", 1>",
       "&pypde::kb_faces<UserSystem, " + ns + ", 2>",
       "&pypde::kb_centers<UserSystem, " + ns + ">",
-      "&pypde::kb_gather<UserSystem, " + ns + ">"};
+      "&pypde::kb_gather<UserSystem, " + ns + ">",
+      "&pypde::kb_mlp_guess<UserSystem, " + ns + ">"};
   const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17",
                         "--fmad=false", "-lineinfo", "-DPYPDE_JIT=1"};
   const int nopts = 5;
@@ -302,7 +303,7 @@ int jit_ensure(SystemDesc &d, int N) {
                     &d.sets[N].kb_predictor,  &d.sets[N].kb_newton,
                     &d.sets[N].kb_faces[0],   &d.sets[N].kb_faces[1],
                     &d.sets[N].kb_faces[2],   &d.sets[N].kb_centers,
-                    &d.sets[N].kb_gather};
+                    &d.sets[N].kb_gather,     &d.sets[N].kb_guess};
   for (size_t i = 0; i < exprs.size(); i++) {
     void *f = nullptr;
     if (lowered[i].empty() || getfn(&f, mod, lowered[i].c_str()) != 0) {
@@ -336,6 +337,7 @@ int jit_ensure(SystemDesc &d, int N) {
     d.sets[N].guess_feat = cfg[10];
   } else {
     d.sets[N].guess = KFunc();
+    d.sets[N].kb_guess = KFunc();
   }
   d.have[N] = true;
   return PYPDE_OK;

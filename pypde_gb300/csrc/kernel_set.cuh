@@ -33,6 +33,7 @@ template <class Sys, int N> KernelSet make_kernel_set() {
   k.newton_smem = NewtonCfg<Sys, N>::SMEM_BYTES;
   if constexpr (MlpShape<Sys, N>::OK && Sys::HAS_S) {
     k.guess.aot = (const void *)&k_mlp_guess<Sys, N>;
+    k.kb_guess.aot = (const void *)&kb_mlp_guess<Sys, N>;
     k.guess_smem = MlpShape<Sys, N>::SMEM;
     k.guess_k1 = MlpShape<Sys, N>::K1;
     k.guess_no = MlpShape<Sys, N>::NO;

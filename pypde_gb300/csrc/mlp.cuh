@@ -27,6 +27,7 @@
 // variation, and so does the network's error.
 #pragma once
 
+#include "batch.cuh"
 #include "kernels.cuh"
 
 namespace pypde {
@@ -122,6 +123,157 @@ __device__ __forceinline__ void mlp_hidden(const unsigned int (&a)[KT][4],
   }
 }
 
+// Shared-memory layout of the guess: the network (staged once per block)
+// and each warp's 16 cells of features and scales.
+struct MlpSmem {
+  unsigned short *W1, *W2, *W3;
+  float *b1, *b2, *b3, *xm, *xs, *ym, *ys, *F, *R;
+};
+
+// Stage the network in shared memory (all threads; ends with a barrier).
+template <class Sys, int N>
+__device__ __forceinline__ MlpSmem mlp_stage(const MlpModel &m) {
+  using S = MlpShape<Sys, N>;
+  constexpr int K1 = S::K1, NO = S::NO;
+  extern __shared__ float4 mlp_smem4[];
+  MlpSmem sm;
+  sm.W1 = (unsigned short *)mlp_smem4;
+  sm.W2 = sm.W1 + MLP_H * S::S1;
+  sm.W3 = sm.W2 + MLP_H * S::S2;
+  float *sp = (float *)mlp_smem4 + (S::W_ELEMS + 1) / 2;
+  sm.b1 = sp;
+  sm.b2 = sm.b1 + MLP_H;
+  sm.b3 = sm.b2 + MLP_H;
+  sm.xm = sm.b3 + NO;
+  sm.xs = sm.xm + K1;
+  sm.ym = sm.xs + K1;
+  sm.ys = sm.ym + NO;
+  sm.F = sm.ys + NO;              // [CELLS][K1]
+  sm.R = sm.F + S::CELLS * K1;    // [CELLS] per-cell scale r
+  for (int i = threadIdx.x; i < MLP_H * K1; i += blockDim.x)
+    sm.W1[(i / K1) * S::S1 + i % K1] = m.W1[i];
+  for (int i = threadIdx.x; i < MLP_H * MLP_H; i += blockDim.x)
+    sm.W2[(i / MLP_H) * S::S2 + i % MLP_H] = m.W2[i];
+  for (int i = threadIdx.x; i < NO * MLP_H; i += blockDim.x)
+    sm.W3[(i / MLP_H) * S::S2 + i % MLP_H] = m.W3[i];
+  for (int i = threadIdx.x; i < MLP_H; i += blockDim.x) {
+    sm.b1[i] = m.b1[i];
+    sm.b2[i] = m.b2[i];
+  }
+  for (int i = threadIdx.x; i < NO; i += blockDim.x) {
+    sm.b3[i] = m.b3[i];
+    sm.ym[i] = m.y_mean[i];
+    sm.ys[i] = m.y_scale[i];
+  }
+  for (int i = threadIdx.x; i < K1; i += blockDim.x) {
+    sm.xm[i] = m.x_mean[i];
+    sm.xs[i] = m.x_scale[i];
+  }
+  __syncthreads();
+  return sm;
+}
+
+// One tile of CELLS reconstruction cells (cells tile*CELLS ...) of one
+// grid, each warp 16 of them: qh = w + the network's correction at every
+// space-time node.  lg_dt = log10 of the step's dt.
+template <class Sys, int N>
+__device__ __forceinline__ void mlp_guess_tile(const MlpSmem &sm,
+                                               const double *__restrict__ w,
+                                               double *__restrict__ qh,
+                                               long long Cw, int tau_var,
+                                               double lg_dt, long long tile) {
+  using S = MlpShape<Sys, N>;
+  constexpr int V = S::V, Nd = S::Nd, NT = S::NT, K1 = S::K1, NO = S::NO;
+  constexpr int KT1 = K1 / 16;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gr = lane >> 2, c = lane & 3;
+  float *F = sm.F + warp * 16 * K1;
+  float *R = sm.R + warp * 16;
+  const long long cell0 = tile * S::CELLS + warp * 16;
+  if (lane < 16) {
+    const long long cell = cell0 + lane;
+    float *f = F + lane * K1;
+    if (cell < Cw) {
+      const double *wc = w + cell * Nd * V;
+      double tau_mean = 0.0;
+      for (int v = 0; v < V; v++) {
+        double s = wc[v];
+        for (int idx = 1; idx < Nd; idx++)
+          s += wc[idx * V + v];
+        const double mean = s * (1.0 / Nd);
+        f[v] = (float)mean;
+        for (int idx = 0; idx < Nd; idx++)
+          f[V + idx * V + v] = (float)(wc[idx * V + v] - mean);
+        if (v == tau_var)
+          tau_mean = mean;
+      }
+      f[V + Nd * V] = (float)(tau_var >= 0 ? lg_dt - tau_mean : lg_dt);
+      for (int k = 0; k < S::FEAT - 1; k++)
+        f[k] = (f[k] - sm.xm[k]) * sm.xs[k];
+      float ss = 0.0f;
+      for (int k = V; k < V + Nd * V; k++)
+        ss += f[k] * f[k];
+      const float r = fmaxf(sqrtf(ss * (1.0f / (float)(Nd * V))), 1e-30f);
+      const float rr = 1.0f / r;
+      for (int k = V; k < V + Nd * V; k++)
+        f[k] = f[k] * rr;
+      f[S::FEAT - 1] = (log10f(r) - sm.xm[S::FEAT - 1]) * sm.xs[S::FEAT - 1];
+      for (int k = S::FEAT; k < K1; k++)
+        f[k] = 0.0f;
+      R[lane] = r;
+    } else {
+      for (int k = 0; k < K1; k++)
+        f[k] = 0.0f;
+      R[lane] = 0.0f;
+    }
+  }
+  __syncwarp();
+  unsigned int a1[KT1][4];
+#pragma unroll
+  for (int kt = 0; kt < KT1; kt++) {
+    const float *r0 = F + gr * K1 + kt * 16 + 2 * c;
+    const float *r1 = r0 + 8 * K1;
+    a1[kt][0] = pack_bf16(r0[0], r0[1]);
+    a1[kt][1] = pack_bf16(r1[0], r1[1]);
+    a1[kt][2] = pack_bf16(r0[8], r0[9]);
+    a1[kt][3] = pack_bf16(r1[8], r1[9]);
+  }
+  __syncwarp();
+  unsigned int a2[8][4], a3[8][4];
+  mlp_hidden<KT1>(a1, sm.W1, S::S1, sm.b1, lane, a2);
+  mlp_hidden<8>(a2, sm.W2, S::S2, sm.b2, lane, a3);
+  // output layer, one n-tile of 8 outputs at a time
+#pragma unroll 1
+  for (int nt = 0; nt < NO / 8; nt++) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const unsigned short *wr = sm.W3 + (nt * 8 + gr) * S::S2 + 2 * c;
+#pragma unroll
+    for (int kt = 0; kt < 8; kt++) {
+      unsigned int b0 = *(const unsigned int *)(wr + kt * 16);
+      unsigned int b1 = *(const unsigned int *)(wr + kt * 16 + 8);
+      mma_bf16_16816(acc, a3[kt], b0, b1);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const long long cell = cell0 + gr + 8 * h;
+      if (cell >= Cw)
+        continue;
+      const float r = R[gr + 8 * h];
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const int o = nt * 8 + 2 * c + e;
+        if (o >= NT * V)
+          continue;
+        const float y = acc[2 * h + e] + sm.b3[o];
+        const float corr = (y * sm.ys[o] + sm.ym[o]) * r;
+        const int idx = (o / V) % Nd, v = o % V;
+        qh[cell * NT * V + o] = w[(cell * Nd + idx) * V + v] + (double)corr;
+      }
+    }
+  }
+  __syncwarp(); // R and F are rewritten by the next tile
+}
+
 // The guess kernel: a persistent grid over tiles of 128 reconstruction
 // cells, one warp per 16 cells; the weights are staged in shared memory
 // once per block.  Writes qh = w + correction for every space-time node.
@@ -130,130 +282,28 @@ __global__ void __launch_bounds__(256)
     k_mlp_guess(const double *__restrict__ w, double *__restrict__ qh, Geom g,
                 MlpModel m, const DevState *st) {
   using S = MlpShape<Sys, N>;
-  constexpr int V = S::V, Nd = S::Nd, NT = S::NT, K1 = S::K1, NO = S::NO;
-  constexpr int KT1 = K1 / 16;
   if (!step_active(st))
     return;
-  extern __shared__ float4 mlp_smem4[];
-  unsigned short *sW1 = (unsigned short *)mlp_smem4;
-  unsigned short *sW2 = sW1 + MLP_H * S::S1;
-  unsigned short *sW3 = sW2 + MLP_H * S::S2;
-  float *sp = (float *)mlp_smem4 + (S::W_ELEMS + 1) / 2;
-  float *sb1 = sp, *sb2 = sb1 + MLP_H, *sb3 = sb2 + MLP_H;
-  float *sxm = sb3 + NO, *sxs = sxm + K1, *sym = sxs + K1, *sys = sym + NO;
-  float *sF = sys + NO;          // [CELLS][K1]
-  float *sR = sF + S::CELLS * K1; // [CELLS] per-cell scale r
-  for (int i = threadIdx.x; i < MLP_H * K1; i += blockDim.x)
-    sW1[(i / K1) * S::S1 + i % K1] = m.W1[i];
-  for (int i = threadIdx.x; i < MLP_H * MLP_H; i += blockDim.x)
-    sW2[(i / MLP_H) * S::S2 + i % MLP_H] = m.W2[i];
-  for (int i = threadIdx.x; i < NO * MLP_H; i += blockDim.x)
-    sW3[(i / MLP_H) * S::S2 + i % MLP_H] = m.W3[i];
-  for (int i = threadIdx.x; i < MLP_H; i += blockDim.x) {
-    sb1[i] = m.b1[i];
-    sb2[i] = m.b2[i];
-  }
-  for (int i = threadIdx.x; i < NO; i += blockDim.x) {
-    sb3[i] = m.b3[i];
-    sym[i] = m.y_mean[i];
-    sys[i] = m.y_scale[i];
-  }
-  for (int i = threadIdx.x; i < K1; i += blockDim.x) {
-    sxm[i] = m.x_mean[i];
-    sxs[i] = m.x_scale[i];
-  }
-  __syncthreads();
-
+  const MlpSmem sm = mlp_stage<Sys, N>(m);
   const double lg_dt = log10(st->dt);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gr = lane >> 2, c = lane & 3;
-  float *F = sF + warp * 16 * K1;
-  float *R = sR + warp * 16;
-  for (long long tile = blockIdx.x; tile * S::CELLS < g.Cw; tile += gridDim.x) {
-    const long long cell0 = tile * S::CELLS + warp * 16;
-    if (lane < 16) {
-      const long long cell = cell0 + lane;
-      float *f = F + lane * K1;
-      if (cell < g.Cw) {
-        const double *wc = w + cell * Nd * V;
-        double tau_mean = 0.0;
-        for (int v = 0; v < V; v++) {
-          double s = wc[v];
-          for (int idx = 1; idx < Nd; idx++)
-            s += wc[idx * V + v];
-          const double mean = s * (1.0 / Nd);
-          f[v] = (float)mean;
-          for (int idx = 0; idx < Nd; idx++)
-            f[V + idx * V + v] = (float)(wc[idx * V + v] - mean);
-          if (v == m.tau_var)
-            tau_mean = mean;
-        }
-        f[V + Nd * V] = (float)(m.tau_var >= 0 ? lg_dt - tau_mean : lg_dt);
-        for (int k = 0; k < S::FEAT - 1; k++)
-          f[k] = (f[k] - sxm[k]) * sxs[k];
-        float ss = 0.0f;
-        for (int k = V; k < V + Nd * V; k++)
-          ss += f[k] * f[k];
-        const float r = fmaxf(sqrtf(ss * (1.0f / (float)(Nd * V))), 1e-30f);
-        const float rr = 1.0f / r;
-        for (int k = V; k < V + Nd * V; k++)
-          f[k] = f[k] * rr;
-        f[S::FEAT - 1] = (log10f(r) - sxm[S::FEAT - 1]) * sxs[S::FEAT - 1];
-        for (int k = S::FEAT; k < K1; k++)
-          f[k] = 0.0f;
-        R[lane] = r;
-      } else {
-        for (int k = 0; k < K1; k++)
-          f[k] = 0.0f;
-        R[lane] = 0.0f;
-      }
-    }
-    __syncwarp();
-    unsigned int a1[KT1][4];
-#pragma unroll
-    for (int kt = 0; kt < KT1; kt++) {
-      const float *r0 = F + gr * K1 + kt * 16 + 2 * c;
-      const float *r1 = r0 + 8 * K1;
-      a1[kt][0] = pack_bf16(r0[0], r0[1]);
-      a1[kt][1] = pack_bf16(r1[0], r1[1]);
-      a1[kt][2] = pack_bf16(r0[8], r0[9]);
-      a1[kt][3] = pack_bf16(r1[8], r1[9]);
-    }
-    __syncwarp();
-    unsigned int a2[8][4], a3[8][4];
-    mlp_hidden<KT1>(a1, sW1, S::S1, sb1, lane, a2);
-    mlp_hidden<8>(a2, sW2, S::S2, sb2, lane, a3);
-    // output layer, one n-tile of 8 outputs at a time
-#pragma unroll 1
-    for (int nt = 0; nt < NO / 8; nt++) {
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      const unsigned short *wr = sW3 + (nt * 8 + gr) * S::S2 + 2 * c;
-#pragma unroll
-      for (int kt = 0; kt < 8; kt++) {
-        unsigned int b0 = *(const unsigned int *)(wr + kt * 16);
-        unsigned int b1 = *(const unsigned int *)(wr + kt * 16 + 8);
-        mma_bf16_16816(acc, a3[kt], b0, b1);
-      }
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const long long cell = cell0 + gr + 8 * h;
-        if (cell >= g.Cw)
-          continue;
-        const float r = R[gr + 8 * h];
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-          const int o = nt * 8 + 2 * c + e;
-          if (o >= NT * V)
-            continue;
-          const float y = acc[2 * h + e] + sb3[o];
-          const float corr = (y * sys[o] + sym[o]) * r;
-          const int idx = (o / V) % Nd, v = o % V;
-          qh[cell * NT * V + o] = w[(cell * Nd + idx) * V + v] + (double)corr;
-        }
-      }
-    }
-    __syncwarp(); // R and F are rewritten by the next tile
-  }
+  for (long long tile = blockIdx.x; tile * S::CELLS < g.Cw; tile += gridDim.x)
+    mlp_guess_tile<Sys, N>(sm, w, qh, g.Cw, m.tau_var, lg_dt, tile);
+}
+
+// The learned warm start of an order group: the network is staged in
+// shared memory once per CTA, then every tile (128 reconstruction cells of
+// one problem) writes qh = w + the network's correction, as k_mlp_guess
+// does for that problem alone.
+template <class Sys, int N>
+__global__ void __launch_bounds__(256)
+    kb_mlp_guess(const BatchProblem *P, TileQueue q, int per_pop, MlpModel m) {
+  const MlpSmem sm = mlp_stage<Sys, N>(m);
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    if (step_active(b.st))
+      mlp_guess_tile<Sys, N>(sm, b.w, b.qh, b.g.Cw, m.tau_var, log10(b.st->dt),
+                             vb.b);
+  });
 }
 
 } // namespace pypde

@@ -913,6 +913,8 @@ struct BatchGroup {
   int threads[BS_COUNT] = {};
   size_t smem[BS_COUNT] = {};
   int resident[BS_COUNT] = {};
+  bool guess = false; // a learned warm start for this order
+  MlpModel model;
 };
 
 struct BatchCtx {
@@ -921,7 +923,7 @@ struct BatchCtx {
   int np = 0, ndim = 1, nsm = 152;
   unsigned long long *heads = nullptr;
   bool stiff = false, faces = true, centers = true;
-  int flux = 0;
+  int flux = 0, mixed = 0;
   double tol = 1e-12;
 };
 } // namespace
@@ -978,8 +980,13 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
   for (size_t gi = 0; gi < c.G.size(); gi++) {
     BatchGroup &g = c.G[gi];
     double tol = c.tol;
+    int flags = (g.guess ? 1 : 0) | (c.mixed ? 2 : 0);
+    if (g.guess &&
+        (e = stage(gi, BS_GUESS, (void *)&g.model, nullptr, nullptr)))
+      return e;
     if ((e = stage(gi, BS_PREDICTOR, (void *)&g.T,
-                   c.stiff ? (void *)&tol : nullptr, nullptr)))
+                   c.stiff ? (void *)&tol : nullptr,
+                   c.stiff ? (void *)&flags : nullptr)))
       return e;
     if (c.faces && (e = stage(gi, BS_FACES, (void *)&g.T, nullptr, nullptr)))
       return e;
@@ -1043,6 +1050,7 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
   c.stiff = a.stiff;
   c.flux = a.flux;
   c.tol = a.newton_tol;
+  c.mixed = a.mixed ? 1 : 0;
   c.faces = sys.has_F || sys.has_B;
   c.centers = sys.has_B || sys.has_S;
 
@@ -1071,6 +1079,16 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
       return PYPDE_ERR_UNSUPPORTED;
     }
     make_tables(N, &g.T);
+    if (a.warm[N]) {
+      if ((rc = check_warm(sys, N, a.stiff, a.device, a.warm[N])))
+        return rc;
+      if (!g.ks->kb_guess.valid()) {
+        set_error("no batched warm-start kernel for system " + sys.name);
+        return PYPDE_ERR_UNSUPPORTED;
+      }
+      g.guess = true;
+      g.model = a.warm[N]->model;
+    }
     std::stable_sort(g.idx.begin(), g.idx.end(),
                      [&](int x, int y) { return geo[x].C > geo[y].C; });
     c.G.push_back(g);
@@ -1181,6 +1199,7 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
       tl[BS_FACES] = c.faces ? tiles(fis[p].off[ndim], 128) : 0;
       tl[BS_CENTERS] = c.centers ? tiles(ge.C * NT, 128) : 0;
       tl[BS_GATHER] = tiles(ge.C * V, 256);
+      tl[BS_GUESS] = g.guess ? tiles(ge.Cw, 128) : 0; // MlpShape::CELLS
       for (int st = 0; st < BS_COUNT; st++)
         off[st].push_back(off[st].back() + tl[st]);
       order.push_back(b);
@@ -1223,6 +1242,11 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
     g.threads[BS_CENTERS] = 128;
     g.fn[BS_GATHER] = k.kb_gather;
     g.threads[BS_GATHER] = 256;
+    if (g.guess) {
+      g.fn[BS_GUESS] = k.kb_guess;
+      g.threads[BS_GUESS] = 256;
+      g.smem[BS_GUESS] = k.guess_smem;
+    }
     for (int st = 0; st < BS_COUNT; st++) {
       if (g.tiles[st] == 0)
         continue;

@@ -31,8 +31,9 @@ struct KernelSet {
   size_t newton_smem = 0;
   // batched launches over many problems of this order (batch.cuh)
   KFunc kb_cfl, kb_predictor, kb_newton, kb_faces[3], kb_centers, kb_gather;
-  // learned warm start (k_mlp_guess); guess_k1 == 0: not available
-  KFunc guess;
+  // learned warm start (k_mlp_guess, batched kb_mlp_guess); guess_k1 == 0:
+  // not available
+  KFunc guess, kb_guess;
   size_t guess_smem = 0;
   int guess_k1 = 0, guess_no = 0, guess_feat = 0;
 };
@@ -148,6 +149,7 @@ enum BatchStage {
   BS_FACES,
   BS_CENTERS,
   BS_GATHER,
+  BS_GUESS, // the learned warm start, before the predictor
   BS_COUNT
 };
 
@@ -162,6 +164,8 @@ struct BatchArgs {
   long long max_steps = -1; // per problem
   bool autotune = true;
   int per_pop = 1; // tiles per queue pop when not autotuning
+  bool mixed = false;                     // FP32 Newton sweeps first
+  const WarmStart *warm[MAXN + 1] = {};   // learned warm start per order
 };
 
 struct BatchStats {

@@ -91,7 +91,7 @@ ader_solver = pde_solver
 
 def pde_solver_batch(problems, F=None, B=None, S=None, stiff=True, flux="rusanov", *,
                      max_steps=None, newton_tol=None, device=0, autotune=True, per_pop=1,
-                     stats=None, jit=False):
+                     stats=None, jit=False, warm_start=None, mixed_precision=False):
     """Step many independent problems of one system together (one persistent
     launch per stage and order, see include/pypde_gb300.h).
 
@@ -100,7 +100,13 @@ def pde_solver_batch(problems, F=None, B=None, S=None, stiff=True, flux="rusanov
     order (2), boundaryTypes ('transitive'), cfl (0.9).  All problems share
     F, B, S; sizes, orders, boundary types and end times may differ.
     Returns the list of final states (the Q0 arrays).  stats (a dict) gets
-    the batch statistics plus per-problem 'steps' and 't_final' lists."""
+    the batch statistics plus per-problem 'steps' and 't_final' lists.
+    warm_start: a WarmStart, or a dict {order: WarmStart}, the learned warm
+    start of the stiff predictor for the problems of that order (one whose
+    validation found no saving, ``active`` False, is not used);
+    mixed_precision: FP32 Newton sweeps first (built-in systems).  Each
+    problem gives the bits pde_solver gives it alone with the same
+    options."""
     if not problems:
         raise ValueError("no problems")
     Q0s = [p["Q0"] for p in problems]
@@ -133,6 +139,16 @@ def pde_solver_batch(problems, F=None, B=None, S=None, stiff=True, flux="rusanov
     opt.device = int(device)
     opt.autotune = int(bool(autotune))
     opt.per_pop = int(per_pop)
+    opt.mixed_precision = int(bool(mixed_precision))
+    if warm_start is not None:
+        if not stiff:
+            raise ValueError("warm_start applies to the stiff (Newton) predictor")
+        ws = warm_start if isinstance(warm_start, dict) else {warm_start.N: warm_start}
+        for n, w in ws.items():
+            if w.N != n or not 1 <= n <= 3:
+                raise ValueError(f"warm start for order {w.N} given for order {n}")
+            if getattr(w, "active", True):
+                opt.warm_start[n] = w.handle.value
     st = _lib.BatchStats()
     steps = (ctypes.c_longlong * len(problems))()
     tout = np.zeros(len(problems))

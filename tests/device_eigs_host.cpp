@@ -71,3 +71,11 @@ extern "C" double host_max_abs_eigs(const char *name, int ndim, double *q,
   }
   return std::nan("");
 }
+
+// The device FD quotient (fd_step + fd_div) over n pairs: out[i] = x[i] /
+// h[i] as the kernels form it.
+extern "C" void host_fd_div(const double *x, const double *h, double *out,
+                            long n) {
+  for (long i = 0; i < n; i++)
+    out[i] = pypde::fd_div(x[i], pypde::fd_step(h[i]));
+}

@@ -728,7 +728,7 @@ void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
       dt_dev(P[p].st);
     if (stiff)
       stage(B_PRED, NewtonCfg<Sys, N>::THREADS, NewtonCfg<Sys, N>::SMEM_BYTES,
-            [&](TileQueue q, int pp) { kb_newton<Sys, N>(dP, q, pp, T, tol); });
+            [&](TileQueue q, int pp) { kb_newton<Sys, N>(dP, q, pp, T, tol, 0); });
     else
       stage(B_PRED, PredCfg<Sys, N>::THREADS,
             (size_t)PredCfg<Sys, N>::SMEM_DOUBLES * 8,

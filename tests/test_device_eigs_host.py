@@ -116,3 +116,33 @@ def test_device_face_fluxes_equal_port(flux_lib, case):
                 assert np.array_equal(f1, f0), (N, flux, i, f1 - f0)
                 assert np.array_equal(b1, b0), (N, flux, i, b1 - b0)
 
+
+
+def test_fd_quotient_is_correctly_rounded(host_lib):
+    """The kernels form each FD Jacobian entry (v2 - v1) / h from one
+    reciprocal of h per column (fd_step, fd_div: a faithful quotient and one
+    Markstein correction); it must equal IEEE division bit for bit.  Steps
+    h = 2^-26 max(|q|, 1) over the magnitudes states take, and beyond;
+    differences v2 - v1 over the range of a flux's finite differences,
+    including zeros of both signs, tiny, huge, infinite and NaN values, and
+    random mantissas; 4 million pairs plus quotients that lie exactly half
+    way between two doubles' neighbours of x / h."""
+    host_lib.host_fd_div.argtypes = [ora.dp, ora.dp, ora.dp, ctypes.c_long]
+    rng = np.random.default_rng(17)
+    n = 1 << 22
+    q = rng.uniform(0.5, 2.0, n) * 10.0 ** rng.integers(-12, 13, n)
+    q[: n // 8] = 10.0 ** rng.uniform(-300, 300, n // 8)
+    h = np.maximum(2.0 ** -26 * np.abs(q), 2.0 ** -26)
+    x = rng.standard_normal(n) * 10.0 ** rng.uniform(-30, 10, n)
+    x[: n // 16] = (rng.uniform(-1, 1, n // 16) * 10.0 ** rng.uniform(-320, 300, n // 16))
+    x[n // 16: n // 16 + 6] = [0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324]
+    # near-ties: x = h (m + 1/2 + tiny) for integers m with few bits
+    k = n // 4
+    m = rng.integers(1, 1 << 20, k).astype(np.float64)
+    x[-k:] = h[-k:] * (m + 0.5) * (1.0 + rng.choice([-1, 1], k) * 2.0 ** -52)
+    out = np.empty(n)
+    host_lib.host_fd_div(ora.ptr(x), ora.ptr(h), ora.ptr(out), n)
+    want = x / h
+    same = (out == want) | (np.isnan(out) & np.isnan(want))
+    assert same.all(), (x[~same][:5], h[~same][:5], out[~same][:5], want[~same][:5])
+    assert np.array_equal(np.signbit(out[~np.isnan(out)]), np.signbit(want[~np.isnan(want)]))

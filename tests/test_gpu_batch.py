@@ -72,3 +72,41 @@ def test_batch_max_steps_and_jit(gpu_lib):
     assert stats["steps_per_problem"] == [3] * 4
     for p, q in zip(batch, singles):
         assert np.array_equal(p["Q0"], q)
+
+
+def test_batch_learned_and_mixed_forms_match_single_problems(gpu_lib):
+    """The learned warm start (one network per order, its guess computed by
+    one batched launch per order) and the FP32 Newton sweeps through the
+    batch: every problem gives the bits pde_solver gives it alone with the
+    same warm start and precision, for each of the three forms."""
+    from pypde_gb300 import warmstart
+    s = systems.cattaneo(2)
+    probs = _problems("cattaneo", 5, True)
+    nets = {}
+    for N in (1, 2, 3):
+        u0 = workloads.relaxation(16, 2, seed=20 + N, patches=4)
+        ws = warmstart.train_warm_start(u0, 10.0, [1.0, 1.0], F=s.F, S=s.S, cfl=0.8,
+                                        order=N, tau_var=6, steps=4, per_step=128, iters=100,
+                                        seed=N)
+        ws.active = True  # use the network whatever its validation found
+        nets[N] = ws
+    for opts in ({"warm_start": nets}, {"mixed_precision": True},
+                 {"warm_start": nets, "mixed_precision": True}):
+        singles = []
+        for p in probs:
+            q = p["Q0"].copy()
+            st = {}
+            pde_solver(q, p["tf"], p["L"], F=s.F, S=s.S, boundaryTypes=p["boundaryTypes"],
+                       cfl=p["cfl"], order=p["order"], ndt=1, stiff=True, stats=st,
+                       warm_start=nets[p["order"]] if "warm_start" in opts else None,
+                       mixed_precision=opts.get("mixed_precision", False))
+            singles.append((q, st))
+        batch = [dict(p, Q0=p["Q0"].copy()) for p in probs]
+        stats = {}
+        pde_solver_batch(batch, F=s.F, S=s.S, stiff=True, stats=stats, **opts)
+        for p, (q, st), k in zip(batch, singles, stats["steps_per_problem"]):
+            assert k == st["steps"]
+            assert np.array_equal(p["Q0"], q), opts.keys()
+        assert stats["pred_iters"] == sum(st["pred_iters"] for _, st in singles)
+        if "warm_start" in opts:
+            assert stats["per_pop"]["guess"] in (0, 1, 2, 4, 8)

@@ -146,7 +146,7 @@ def _nvrtc_compile(src, kernels):
         except OSError:
             pytest.skip("NVRTC not available")
     here = os.path.join(os.path.dirname(__file__), "..", "pypde_gb300", "csrc")
-    names = ["kernels.cuh", "ader_common.cuh", "eig_full.cuh", "mlp.cuh"]
+    names = ["kernels.cuh", "ader_common.cuh", "eig_full.cuh", "mlp.cuh", "batch.cuh"]
     hdrs = [open(os.path.join(here, n)).read().encode() for n in names]
     src = ('#include "mlp.cuh"\n' + src).encode()
     prog = ctypes.c_void_p()
@@ -167,7 +167,8 @@ def _nvrtc_compile(src, kernels):
 def test_nvrtc_compiles_the_kernels_for_a_translated_system():
     _nvrtc_compile(translate(user_euler2, user_ncp, user_src, 2, 4),
                    ["k_faces<UserSystem, 2, 0>", "k_newton<UserSystem, 2>",
-                    "k_mlp_guess<UserSystem, 2>"])
+                    "k_mlp_guess<UserSystem, 2>", "kb_mlp_guess<UserSystem, 2>",
+                    "kb_newton<UserSystem, 2>"])
 
 
 def test_lambda_callback_translates():
