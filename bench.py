@@ -362,6 +362,8 @@ def run_ours(args, ws, rank, local):
     R = Runner(args, local)
     peak = _lib.ctypes.c_double()
     _lib.check(L.pypde_measure_fp64_peak(local, peak))
+    dmma = _lib.ctypes.c_double()
+    _lib.check(L.pypde_measure_dmma_peak(local, dmma))
     s = systems.cattaneo(nd) if args.system == "cattaneo" else systems.euler(nd)
 
     forms = {}
@@ -515,6 +517,10 @@ def run_ours(args, ws, rank, local):
                              "than that"},
         "stage_ms_per_step": {k: 1e3 * v / ksteps for k, v in stage_s.items()},
         "step_fp64_tflops": sum(flops.values()) / (sec / args.steps) / 1e12,
+        "fp64_pipes": {"fma_tflops": peak.value, "dmma_tflops": dmma.value,
+                       "note": "FP64 FMA loop and FP64 tensor-core mma.sync m8n8k4 loop, both "
+                               "measured by this run: the predictor's contractions could "
+                               "gain from DMMA only if the second were above the first"},
         "predictor_iters_per_cell": its,
         "gpu_launches": st_h["kernel_launches"],
         "clocks": clk.summary(),

@@ -184,6 +184,12 @@ int pypde_tables(int N, double *out);
  * Bench support; no reference counterpart. */
 int pypde_measure_fp64_peak(int device, double *tflops);
 
+/* FP64 tensor-core (mma.sync m8n8k4 f64) throughput in TFLOP/s, measured by
+ * independent chains of DMMA per warp: whether the predictor's small
+ * contractions could gain from the tensor pipe.  Bench support; no
+ * reference counterpart. */
+int pypde_measure_dmma_peak(int device, double *tflops);
+
 /* ---------------- batched problems (no reference counterpart) -----------
  * Many independent problems of one system (sizes, orders, boundary types
  * and end times may all differ) stepped together: every stage of a step is

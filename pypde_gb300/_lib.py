@@ -96,6 +96,7 @@ SIGNATURES = {
     "pypde_fv": (c_int, [c_void_p, dp, dp, ip, dp, c_int, c_int, c_int, c_double]),
     "pypde_tables": (c_int, [c_int, dp]),
     "pypde_measure_fp64_peak": (c_int, [c_int, dp]),
+    "pypde_measure_dmma_peak": (c_int, [c_int, dp]),
     "pde_solver_batch": (c_int, [c_void_p, c_bool, c_int, c_int, POINTER(BatchProblem),
                                  POINTER(BatchOptions), POINTER(BatchStats),
                                  POINTER(c_longlong), dp]),

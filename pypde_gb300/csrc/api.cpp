@@ -578,6 +578,14 @@ int pypde_measure_fp64_peak(int device, double *tflops) {
   return measure_fp64(device, tflops);
 }
 
+int pypde_measure_dmma_peak(int device, double *tflops) {
+  if (!tflops) {
+    set_error("null argument");
+    return PYPDE_ERR_ARG;
+  }
+  return measure_dmma(device, tflops);
+}
+
 const char *pypde_last_error(void) { return last_error(); }
 
 } // extern "C"

@@ -1726,4 +1726,58 @@ int measure_fp64(int device, double *tflops) {
   return PYPDE_OK;
 }
 
+// FP64 tensor-core throughput: every warp runs 4 independent chains of
+// mma.sync m8n8k4 (D = A B + C, FP64), 8 x 8 x 4 FMAs each.  The study of
+// moving the predictor's contractions to DMMA asks whether this rate is
+// above the FMA pipe's at all.
+__global__ void k_dmma_peak(double *out, double a0, int iters) {
+  double a = a0 + (threadIdx.x & 7) * 1e-6, b = 1.0 - (threadIdx.x & 3) * 1e-7;
+  double c[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 "
+                   "{%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                   : "+d"(c[k][0]), "+d"(c[k][1])
+                   : "d"(a), "d"(b));
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] =
+      c[0][0] + c[0][1] + c[1][0] + c[1][1] + c[2][0] + c[2][1] + c[3][0] +
+      c[3][1];
+}
+
+int measure_dmma(int device, double *tflops) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  Arena *ar;
+  int rc = arena_for(device, &ar);
+  if (rc)
+    return rc;
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int blocks = sms * 8, threads = 256, iters = 1024;
+  Buf out;
+  CK(ensure(out, (size_t)blocks * threads * 8));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; rep++) {
+    CK(cudaEventRecord(e0, ar->stream));
+    k_dmma_peak<<<blocks, threads, 0, ar->stream>>>((double *)out.p, 1e-3,
+                                                     iters);
+    CK(cudaEventRecord(e1, ar->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best)
+      best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out.p);
+  const double warps = (double)blocks * threads / 32;
+  *tflops = 2.0 * 8 * 8 * 4 * 4 * iters * warps / (best * 1e-3) / 1e12;
+  return PYPDE_OK;
+}
+
 } // namespace pypde

@@ -198,6 +198,7 @@ int stage_fv(const SystemDesc &sys, double *u, const double *qh,
              double dt);
 
 int measure_fp64(int device, double *tflops);
+int measure_dmma(int device, double *tflops);
 
 // Instantiation helper used by the per-system units.
 template <class Sys, int N> KernelSet make_kernel_set();
