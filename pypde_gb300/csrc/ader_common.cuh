@@ -628,16 +628,24 @@ __device__ __noinline__ double max_abs_eig(double *a) {
 
 // The reciprocal of an FD step h split in two, y_hi + y_lo = 1/h to about
 // 2^-106 relative: y_hi = RN(1/h) (one division per column), and y_lo from
-// the residual 1 - h y_hi, which an FMA gives exactly.
+// the residual 1 - h y_hi, which an FMA gives exactly.  ok: h is far
+// enough from the top of the exponent range that y_lo is not subnormal.
 struct FdStep {
   double h, hi, lo;
+  bool ok;
 };
 __device__ __forceinline__ FdStep fd_step(double h) {
   FdStep s;
   s.h = h;
   s.hi = 1.0 / h;
   s.lo = fma(-h, s.hi, 1.0) * s.hi;
+  s.ok = h <= 0x1p+900;
   return s;
+}
+
+// The rare quotients fd_div does not form itself, out of line.
+__device__ __noinline__ double fd_div_slow(double x, double h) {
+  return x / h;
 }
 
 // x / h correctly rounded, as NumericalDiff.h:31 divides each entry,
@@ -647,14 +655,19 @@ __device__ __forceinline__ FdStep fd_step(double h) {
 // rounds to the correctly rounded quotient, by Markstein's theorem (P.
 // Markstein, IBM J. Res. Dev. 34 (1990) 111-119; Cornea, Golliver and
 // Markstein, ARITH 14 (1999), Theorem 1: y_hi within half an ulp of 1/h,
-// q0 within one ulp of x / h).  Zeros (for their sign), and quotients or
-// steps far enough towards the ends of the exponent range that a
-// remainder or y_lo could be subnormal, take the division itself.
+// q0 within one ulp of x / h).  A zero x gives the signed zero x y_hi (the
+// quotient's bits); a quotient beyond 2^+-900, where a remainder could be
+// subnormal, and non-finite values take the division itself.  The tests
+// are on the integer pipe.
 __device__ __forceinline__ double fd_div(double x, const FdStep &s) {
+  const unsigned long long xb = (unsigned long long)__double_as_longlong(x);
+  if ((xb << 1) == 0ULL)
+    return x * s.hi;
   const double q0 = fma(x, s.hi, x * s.lo);
-  const double a = fabs(q0);
-  if (!(a >= 0x1p-900 && a <= 0x1p+900 && s.h <= 0x1p+900))
-    return x / s.h;
+  const unsigned e =
+      (unsigned)(((unsigned long long)__double_as_longlong(q0) >> 52) & 0x7ffu);
+  if (e - 123u > 1800u || !s.ok)
+    return fd_div_slow(x, s.h);
   return fma(fma(-q0, s.h, x), s.hi, q0);
 }
 

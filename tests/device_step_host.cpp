@@ -13,9 +13,10 @@
 //   once every thread that has not returned waits there, with the AND/OR
 //   of the predicate; a thread that returned takes no part, as an exited
 //   thread on the GPU;
-// - __syncwarp releases a warp once its remaining lanes wait there, and
-//   __shfl_down_sync exchanges values through a per-warp buffer between two
-//   such warp barriers;
+// - __syncwarp(mask) releases the lanes of `mask` once every one of them
+//   that has not returned waits at a warp barrier with that mask (the full
+//   mask: the whole warp), and __shfl_down_sync exchanges values through a
+//   per-warp buffer between two full-warp barriers;
 // - a block whose threads wait at barriers that can never all be released
 //   (some lanes of a warp at a warp barrier, others at the block barrier)
 //   is reported as a deadlock;
@@ -70,7 +71,8 @@ struct Fiber {
   char *stack = nullptr;
   State state = DONE;
   int pred = 0;
-  unsigned long long slot = 0; // shuffle buffer
+  unsigned wmask = 0xffffffffu; // lanes of the warp barrier it waits at
+  unsigned long long slot = 0;   // shuffle buffer
 };
 
 constexpr size_t STACK_BYTES = 512 * 1024;
@@ -129,16 +131,23 @@ static void run_block(unsigned n) {
     bool released = false;
     for (unsigned w0 = 0; w0 < n; w0 += 32) {
       const unsigned w1 = w0 + 32 < n ? w0 + 32 : n;
-      int live = 0, at = 0;
-      for (unsigned i = w0; i < w1; i++)
-        if (g_f[i].state != DONE) {
-          live++;
-          at += g_f[i].state == AT_WARP;
+      for (unsigned i = w0; i < w1; i++) {
+        if (g_f[i].state != AT_WARP)
+          continue;
+        // every lane of i's mask that has not returned waits with it
+        const unsigned m = g_f[i].wmask;
+        bool all = true;
+        for (unsigned j = w0; j < w1; j++) {
+          if (!(m >> (j - w0) & 1u) || g_f[j].state == DONE)
+            continue;
+          if (g_f[j].state != AT_WARP || g_f[j].wmask != m)
+            all = false;
         }
-      if (live > 0 && at == live) {
-        for (unsigned i = w0; i < w1; i++)
-          if (g_f[i].state == AT_WARP)
-            g_f[i].state = RUNNABLE;
+        if (!all)
+          continue;
+        for (unsigned j = w0; j < w1; j++)
+          if ((m >> (j - w0) & 1u) && g_f[j].state == AT_WARP)
+            g_f[j].state = RUNNABLE;
         released = true;
       }
     }
@@ -189,13 +198,15 @@ static double *host_dynamic_smem() { return emu::g_smem.data(); }
 static inline void __syncthreads() { emu::block_sync(1, 0); }
 static inline int __syncthreads_and(int p) { return emu::block_sync(p, 1); }
 static inline int __syncthreads_or(int p) { return emu::block_sync(p, 2); }
-static inline void __syncwarp(unsigned = 0xffffffffu) {
+static inline void __syncwarp(unsigned mask = 0xffffffffu) {
+  emu::g_f[threadIdx.x].wmask = mask;
   emu::wait_in(emu::AT_WARP);
 }
 template <class T> static inline T __shfl_down_sync(unsigned, T v, int off) {
   static_assert(sizeof(T) <= 8, "shuffle of a wider type");
   const unsigned lane = threadIdx.x % 32, base = threadIdx.x - lane;
   std::memcpy(&emu::g_f[threadIdx.x].slot, &v, sizeof(T));
+  emu::g_f[threadIdx.x].wmask = 0xffffffffu;
   emu::wait_in(emu::AT_WARP);
   T r = v;
   const unsigned src = base + lane + off;
