@@ -644,7 +644,7 @@ __device__ __forceinline__ FdStep fd_step(double h) {
 }
 
 // The rare quotients fd_div does not form itself, out of line.
-__device__ __noinline__ double fd_div_slow(double x, double h) {
+static __device__ __noinline__ double fd_div_slow(double x, double h) {
   return x / h;
 }
 

@@ -919,8 +919,13 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   const int lc = threadIdx.x / NT;
   const int node = threadIdx.x % NT;
   const int t = node / Nd, idx = node % Nd;
-  const long long cell = (long long)vb_.b * CPB + lc;
-  const bool valid = (lc < CPB) && (cell < g.Cw);
+  // slot lc runs cell vb_.b CPB + lc and then, without FP32 sweeps, every
+  // cstride-th cell after it: a slot whose cell has converged takes its
+  // next cell instead of idling until the block's slowest cell is done (a
+  // launch of fewer blocks than tiles gives each slot many cells)
+  const long long cstride = mixed ? 0 : (long long)vb_.n * CPB;
+  long long cell = (long long)vb_.b * CPB + lc;
+  bool valid = (lc < CPB) && (cell < g.Cw);
   int digs[D > 0 ? D : 1];
   {
     int rem = idx;
@@ -933,29 +938,33 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   double *rr = s_r + (lc * NT) * V;
   double *ff = s_f + (lc * NT) * D * V;
   double Ww[V];
-  if (threadIdx.x < CPB) {
-    cell_done[threadIdx.x] = 0;
-    on_guess[threadIdx.x] = guess != 0;
-    prev_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL); // +inf
-    last_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL);
-    have_lu[threadIdx.x] = 0;
-  }
-  __syncthreads();
-  const double *wc = w + (cell * Nd + idx) * V;
-  if (valid) {
-    double cc = T.endvals[t];
-    for (int d = 0; d < D; d++)
-      cc *= wg[digs[d]];
-    const double *gq = qh + (cell * NT + node) * V;
-#pragma unroll
-    for (int v = 0; v < V; v++) {
-      double x = wc[v];
-      Ww[v] = cc * x;
-      q[node * V + v] = guess ? gq[v] : x;
+  const double *wc = w;
+  // a slot's start on a cell: its state flags (node 0), and each node's
+  // Ww and initial q
+  auto load_cell = [&]() {
+    wc = w + (cell * Nd + idx) * V;
+    if (node == 0 && lc < CPB) {
+      cell_done[lc] = valid ? 0 : 1;
+      on_guess[lc] = guess != 0;
+      prev_res[lc] = __longlong_as_double(0x7ff0000000000000LL); // +inf
+      last_res[lc] = __longlong_as_double(0x7ff0000000000000LL);
+      have_lu[lc] = 0;
     }
-  } else if (lc < CPB && node == 0) {
-    cell_done[lc] = 1;
-  }
+    if (valid) {
+      double cc = T.endvals[t];
+      for (int d = 0; d < D; d++)
+        cc *= wg[digs[d]];
+      const double *gq = qh + (cell * NT + node) * V;
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        double x = wc[v];
+        Ww[v] = cc * x;
+        q[node * V + v] = guess ? gq[v] : x;
+      }
+    }
+  };
+  __syncthreads(); // the tables in shared memory
+  load_cell();
   if constexpr (Sys::HAS_FP32) {
     if (mixed) {
       __syncthreads();
@@ -970,7 +979,8 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   const int min_updates = mixed ? 2 : 0;
   int iters = 0;
   bool failed = false;
-  for (int it = 0; it < NEWTON_MAXIT; it++) {
+  int it = 0; // the slot's iterations on its current cell
+  for (;;) {
     if (lc < CPB && node == 0) {
       res_bits[lc] = 0ULL;
       scale_bits[lc] = 0ULL;
@@ -1216,23 +1226,35 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
     }
     if (active && conv && node == 0)
       iters = it;
-    bool all_done = true;
-    if (node == 0 && lc < CPB)
-      all_done = cell_done[lc] != 0;
-    if (__syncthreads_and(all_done))
-      break;
-  }
-  if (valid) {
-    double *o = qh + (cell * NT + node) * V;
+    // NEWTON_MAXIT iterations without convergence end the cell (a failure)
+    if (active && !conv && node == 0 && it + 1 >= NEWTON_MAXIT)
+      cell_done[lc] |= 4;
+    __syncthreads();
+    const int fin = valid ? cell_done[lc] : 0;
+    __syncthreads(); // every thread has read its slot's flag
+    if (fin) {
+      // the cell is done: write it out, then the slot takes its next cell
+      double *o = qh + (cell * NT + node) * V;
 #pragma unroll
-    for (int v = 0; v < V; v++)
-      o[v] = q[node * V + v];
-    if (node == 0) {
-      atomicAdd(&st->pred_iters, (unsigned long long)iters);
-      atomicMax(&st->pred_max_iters, iters);
-      if (cell_done[lc] != 1)
-        atomicAdd(&st->pred_fail, 1);
+      for (int v = 0; v < V; v++)
+        o[v] = q[node * V + v];
+      if (node == 0) {
+        atomicAdd(&st->pred_iters, (unsigned long long)iters);
+        atomicMax(&st->pred_max_iters, iters);
+        if (fin != 1)
+          atomicAdd(&st->pred_fail, 1);
+      }
+      cell += cstride;
+      valid = cstride > 0 && cell < g.Cw;
+      iters = 0;
+      failed = false;
+      it = 0;
+      load_cell();
+    } else {
+      it++;
     }
+    if (__syncthreads_and(!valid))
+      break;
   }
 }
 
