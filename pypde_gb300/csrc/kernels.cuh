@@ -484,99 +484,6 @@ __global__ void k_predictor(const double *__restrict__ w,
 // ---------------------------------------------------------------------
 constexpr int NEWTON_MAXIT = 200;
 
-// LU with partial pivoting of the n x n matrix A (row-major, shared
-// memory), by one thread: the pivot is the first row of largest magnitude
-// at or below the diagonal; rows whose multiplier is zero are left alone
-// (structural zeros); U's diagonal is kept as the pivots' reciprocals.
-// piv[k] = the row swapped with row k.  False at a zero pivot.
-template <int NL>
-__device__ __forceinline__ bool lu_factor_one(double *A, int *piv) {
-  for (int k = 0; k < NL; k++) {
-    int p = k;
-    unsigned long long pm = mag_bits(A[k * NL + k]);
-    for (int i = k + 1; i < NL; i++) {
-      const unsigned long long m = mag_bits(A[i * NL + k]);
-      if (m > pm) {
-        p = i;
-        pm = m;
-      }
-    }
-    piv[k] = p;
-    if (pm == 0ULL)
-      return false;
-    if (p != k)
-      for (int j = 0; j < NL; j++) {
-        double tmp = A[k * NL + j];
-        A[k * NL + j] = A[p * NL + j];
-        A[p * NL + j] = tmp;
-      }
-    const double rp = 1.0 / A[k * NL + k];
-    for (int i = k + 1; i < NL; i++) {
-      double f = A[i * NL + k] * rp;
-      A[i * NL + k] = f;
-      if (mag_bits(f) == 0ULL) // structural zero: the row is unchanged
-        continue;
-      for (int j = k + 1; j < NL; j++)
-        A[i * NL + j] = fma(-f, A[k * NL + j], A[i * NL + j]);
-    }
-    A[k * NL + k] = rp; // U's diagonal kept as reciprocals for the solves
-  }
-  return true;
-}
-
-// The same factorisation by the NT threads t = 0 .. NT-1 of one warp
-// (lanes `mask`): every thread makes the pivot decision itself (the same
-// integer comparisons on the same values), thread t swaps and updates the
-// columns j with j % NT == t, and column k (its multipliers and the
-// pivot's reciprocal) is written by its owner once every thread has read
-// it.  Each element sees the operations of lu_factor_one, in its order.
-template <int NL, int NT>
-__device__ __forceinline__ bool lu_factor_shared(double *A, int *piv, int t,
-                                                 unsigned mask) {
-  double f[NL];
-  for (int k = 0; k < NL; k++) {
-    int p = k;
-    unsigned long long pm = mag_bits(A[k * NL + k]);
-    for (int i = k + 1; i < NL; i++) {
-      const unsigned long long m = mag_bits(A[i * NL + k]);
-      if (m > pm) {
-        p = i;
-        pm = m;
-      }
-    }
-    if (t == 0)
-      piv[k] = p;
-    if (pm == 0ULL)
-      return false; // every thread returns here: the same decision
-    __syncwarp(mask); // every thread has searched column k before the swap
-    if (p != k)
-      for (int j = t; j < NL; j += NT) {
-        double tmp = A[k * NL + j];
-        A[k * NL + j] = A[p * NL + j];
-        A[p * NL + j] = tmp;
-      }
-    __syncwarp(mask);
-    const double rp = 1.0 / A[k * NL + k];
-    for (int i = k + 1; i < NL; i++)
-      f[i] = A[i * NL + k] * rp;
-    __syncwarp(mask);
-    if (k % NT == t) {
-      for (int i = k + 1; i < NL; i++)
-        A[i * NL + k] = f[i];
-      A[k * NL + k] = rp;
-    }
-    const int j0 = k + 1 + ((t - (k + 1)) % NT + NT) % NT;
-    for (int i = k + 1; i < NL; i++) {
-      if (mag_bits(f[i]) == 0ULL) // structural zero: the row is unchanged
-        continue;
-      for (int j = j0; j < NL; j += NT)
-        A[i * NL + j] = fma(-f[i], A[k * NL + j], A[i * NL + j]);
-    }
-    __syncwarp(mask);
-  }
-  return true;
-}
-
 template <class Sys, int N> struct NewtonCfg {
   static constexpr int V = Sys::V, D = Sys::NDIM;
   static constexpr int Nd = IPow<N, D>::value;
@@ -919,13 +826,8 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   const int lc = threadIdx.x / NT;
   const int node = threadIdx.x % NT;
   const int t = node / Nd, idx = node % Nd;
-  // slot lc runs cell vb_.b CPB + lc and then, without FP32 sweeps, every
-  // cstride-th cell after it: a slot whose cell has converged takes its
-  // next cell instead of idling until the block's slowest cell is done (a
-  // launch of fewer blocks than tiles gives each slot many cells)
-  const long long cstride = mixed ? 0 : (long long)vb_.n * CPB;
-  long long cell = (long long)vb_.b * CPB + lc;
-  bool valid = (lc < CPB) && (cell < g.Cw);
+  const long long cell = (long long)vb_.b * CPB + lc;
+  const bool valid = (lc < CPB) && (cell < g.Cw);
   int digs[D > 0 ? D : 1];
   {
     int rem = idx;
@@ -938,33 +840,29 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   double *rr = s_r + (lc * NT) * V;
   double *ff = s_f + (lc * NT) * D * V;
   double Ww[V];
-  const double *wc = w;
-  // a slot's start on a cell: its state flags (node 0), and each node's
-  // Ww and initial q
-  auto load_cell = [&]() {
-    wc = w + (cell * Nd + idx) * V;
-    if (node == 0 && lc < CPB) {
-      cell_done[lc] = valid ? 0 : 1;
-      on_guess[lc] = guess != 0;
-      prev_res[lc] = __longlong_as_double(0x7ff0000000000000LL); // +inf
-      last_res[lc] = __longlong_as_double(0x7ff0000000000000LL);
-      have_lu[lc] = 0;
-    }
-    if (valid) {
-      double cc = T.endvals[t];
-      for (int d = 0; d < D; d++)
-        cc *= wg[digs[d]];
-      const double *gq = qh + (cell * NT + node) * V;
+  if (threadIdx.x < CPB) {
+    cell_done[threadIdx.x] = 0;
+    on_guess[threadIdx.x] = guess != 0;
+    prev_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL); // +inf
+    last_res[threadIdx.x] = __longlong_as_double(0x7ff0000000000000LL);
+    have_lu[threadIdx.x] = 0;
+  }
+  __syncthreads();
+  const double *wc = w + (cell * Nd + idx) * V;
+  if (valid) {
+    double cc = T.endvals[t];
+    for (int d = 0; d < D; d++)
+      cc *= wg[digs[d]];
+    const double *gq = qh + (cell * NT + node) * V;
 #pragma unroll
-      for (int v = 0; v < V; v++) {
-        double x = wc[v];
-        Ww[v] = cc * x;
-        q[node * V + v] = guess ? gq[v] : x;
-      }
+    for (int v = 0; v < V; v++) {
+      double x = wc[v];
+      Ww[v] = cc * x;
+      q[node * V + v] = guess ? gq[v] : x;
     }
-  };
-  __syncthreads(); // the tables in shared memory
-  load_cell();
+  } else if (lc < CPB && node == 0) {
+    cell_done[lc] = 1;
+  }
   if constexpr (Sys::HAS_FP32) {
     if (mixed) {
       __syncthreads();
@@ -979,8 +877,7 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
   const int min_updates = mixed ? 2 : 0;
   int iters = 0;
   bool failed = false;
-  int it = 0; // the slot's iterations on its current cell
-  for (;;) {
+  for (int it = 0; it < NEWTON_MAXIT; it++) {
     if (lc < CPB && node == 0) {
       res_bits[lc] = 0ULL;
       scale_bits[lc] = 0ULL;
@@ -1144,13 +1041,7 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
       }
     }
     __syncthreads();
-    // The N time-node threads of a spatial node share its LU when they sit
-    // in one warp (a cell's N N^d threads do when that number divides 32):
-    // each elimination step's updates are split by columns between them,
-    // so its FP64 work runs on every lane instead of one lane in N.  Every
-    // element gets the same operations in the same order either way.
-    constexpr bool SPLIT_LU = N >= 2 && 32 % NT == 0;
-    if (active && !conv && !reset && (SPLIT_LU || t == 0)) {
+    if (active && !conv && !reset && t == 0) {
       // LU with partial pivoting of A (when refreshed), then solve for the
       // update of node idx at every time node (lu_factor / lu_solve of the
       // restatement).  Magnitude comparisons and zero tests are done on
@@ -1158,47 +1049,67 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
       double *A = s_A + ((lc * Nd) + idx) * NL * NL;
       int *piv = s_piv + ((lc * Nd) + idx) * NL;
       bool ok = true;
-      if (refresh) {
-        if constexpr (SPLIT_LU) {
-          unsigned mask = 0;
-          for (int tt = 0; tt < N; tt++)
-            mask |= 1u << ((lc * NT + tt * Nd + idx) & 31);
-          ok = lu_factor_shared<NL, N>(A, piv, t, mask);
-        } else {
-          ok = lu_factor_one<NL>(A, piv);
-        }
-      }
-      if (t == 0) {
-        if (!ok) {
-          failed = true;
-        } else {
-          double b[NL];
-          const double rw = 1.0 / wprod[idx];
-          for (int tt = 0; tt < N; tt++)
-            for (int v = 0; v < V; v++)
-              b[tt * V + v] = rr[(tt * Nd + idx) * V + v] * rw;
-          // rows were swapped whole (L included): permute b first
-          for (int k = 0; k < NL; k++)
-            if (piv[k] != k) {
-              double tmp = b[k];
-              b[k] = b[piv[k]];
-              b[piv[k]] = tmp;
-            }
-          for (int k = 0; k < NL; k++)
-            for (int i = k + 1; i < NL; i++)
-              if (mag_bits(A[i * NL + k]) != 0ULL)
-                b[i] = fma(-A[i * NL + k], b[k], b[i]);
-          for (int i = NL - 1; i >= 0; i--) {
-            double sacc = b[i];
-            for (int j = i + 1; j < NL; j++)
-              if (mag_bits(A[i * NL + j]) != 0ULL)
-                sacc = fma(-A[i * NL + j], b[j], sacc);
-            b[i] = sacc * A[i * NL + i]; // the pivot's reciprocal
+      for (int k = 0; k < NL && ok && refresh; k++) {
+        int p = k;
+        unsigned long long pm = mag_bits(A[k * NL + k]);
+        for (int i = k + 1; i < NL; i++) {
+          const unsigned long long m = mag_bits(A[i * NL + k]);
+          if (m > pm) {
+            p = i;
+            pm = m;
           }
-          for (int tt = 0; tt < N; tt++)
-            for (int v = 0; v < V; v++)
-              q[(tt * Nd + idx) * V + v] -= b[tt * V + v];
         }
+        piv[k] = p;
+        if (pm == 0ULL) {
+          ok = false;
+          break;
+        }
+        if (p != k)
+          for (int j = 0; j < NL; j++) {
+            double tmp = A[k * NL + j];
+            A[k * NL + j] = A[p * NL + j];
+            A[p * NL + j] = tmp;
+          }
+        const double rp = 1.0 / A[k * NL + k];
+        for (int i = k + 1; i < NL; i++) {
+          double f = A[i * NL + k] * rp;
+          A[i * NL + k] = f;
+          if (mag_bits(f) == 0ULL) // structural zero: the row is unchanged
+            continue;
+          for (int j = k + 1; j < NL; j++)
+            A[i * NL + j] = fma(-f, A[k * NL + j], A[i * NL + j]);
+        }
+        A[k * NL + k] = rp; // U's diagonal kept as reciprocals for the solves
+      }
+      if (!ok) {
+        failed = true;
+      } else {
+        double b[NL];
+        const double rw = 1.0 / wprod[idx];
+        for (int tt = 0; tt < N; tt++)
+          for (int v = 0; v < V; v++)
+            b[tt * V + v] = rr[(tt * Nd + idx) * V + v] * rw;
+        // rows were swapped whole (L included): permute b first
+        for (int k = 0; k < NL; k++)
+          if (piv[k] != k) {
+            double tmp = b[k];
+            b[k] = b[piv[k]];
+            b[piv[k]] = tmp;
+          }
+        for (int k = 0; k < NL; k++)
+          for (int i = k + 1; i < NL; i++)
+            if (mag_bits(A[i * NL + k]) != 0ULL)
+              b[i] = fma(-A[i * NL + k], b[k], b[i]);
+        for (int i = NL - 1; i >= 0; i--) {
+          double sacc = b[i];
+          for (int j = i + 1; j < NL; j++)
+            if (mag_bits(A[i * NL + j]) != 0ULL)
+              sacc = fma(-A[i * NL + j], b[j], sacc);
+          b[i] = sacc * A[i * NL + i]; // the pivot's reciprocal
+        }
+        for (int tt = 0; tt < N; tt++)
+          for (int v = 0; v < V; v++)
+            q[(tt * Nd + idx) * V + v] -= b[tt * V + v];
       }
     }
     if (failed)
@@ -1226,35 +1137,23 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
     }
     if (active && conv && node == 0)
       iters = it;
-    // NEWTON_MAXIT iterations without convergence end the cell (a failure)
-    if (active && !conv && node == 0 && it + 1 >= NEWTON_MAXIT)
-      cell_done[lc] |= 4;
-    __syncthreads();
-    const int fin = valid ? cell_done[lc] : 0;
-    __syncthreads(); // every thread has read its slot's flag
-    if (fin) {
-      // the cell is done: write it out, then the slot takes its next cell
-      double *o = qh + (cell * NT + node) * V;
-#pragma unroll
-      for (int v = 0; v < V; v++)
-        o[v] = q[node * V + v];
-      if (node == 0) {
-        atomicAdd(&st->pred_iters, (unsigned long long)iters);
-        atomicMax(&st->pred_max_iters, iters);
-        if (fin != 1)
-          atomicAdd(&st->pred_fail, 1);
-      }
-      cell += cstride;
-      valid = cstride > 0 && cell < g.Cw;
-      iters = 0;
-      failed = false;
-      it = 0;
-      load_cell();
-    } else {
-      it++;
-    }
-    if (__syncthreads_and(!valid))
+    bool all_done = true;
+    if (node == 0 && lc < CPB)
+      all_done = cell_done[lc] != 0;
+    if (__syncthreads_and(all_done))
       break;
+  }
+  if (valid) {
+    double *o = qh + (cell * NT + node) * V;
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      o[v] = q[node * V + v];
+    if (node == 0) {
+      atomicAdd(&st->pred_iters, (unsigned long long)iters);
+      atomicMax(&st->pred_max_iters, iters);
+      if (cell_done[lc] != 1)
+        atomicAdd(&st->pred_fail, 1);
+    }
   }
 }
 

@@ -341,8 +341,6 @@ struct StepCtx {
   int hsteps;
 };
 
-static int resident_blocks(const KFunc &f, int threads, size_t smem);
-
 static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
   const KernelSet &k = *c.ks;
   Geom g = c.g;
@@ -370,23 +368,7 @@ static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
     void *na[] = {(void *)&c.w,     (void *)&c.qh, (void *)&g,
                   (void *)&T,       (void *)&c.wprod, (void *)&c.st,
                   (void *)&tol,     (void *)&guess, (void *)&mixed};
-    // one block per CPB cells with FP32 sweeps; otherwise one wave of
-    // resident blocks whose cell slots each take a new cell when theirs
-    // converges (k_newton_body)
     long long blocks = (g.Cw + k.newton_cpb - 1) / k.newton_cpb;
-    if (!mixed) {
-      int dev = 0, nsm = 0;
-      if (cudaGetDevice(&dev) == cudaSuccess &&
-          cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) ==
-              cudaSuccess &&
-          nsm > 0) {
-        const long long wave =
-            (long long)resident_blocks(k.newton, k.newton_threads,
-                                       k.newton_smem) * nsm;
-        if (wave > 0 && wave < blocks)
-          blocks = wave;
-      }
-    }
     return launch(k.newton, dim3((unsigned)blocks), dim3(k.newton_threads),
                   k.newton_smem, s, na);
   }

@@ -379,12 +379,7 @@ void predictor_stage(bool stiff, const double *w, double *qh, const Geom &g,
                      double tol, int mixed, int guess = 0) {
   if (stiff) {
     using NC = NewtonCfg<Sys, N>;
-    // the runtime launches one wave of resident blocks without FP32 sweeps
-    // (each cell slot then takes many cells); here a "wave" of 3 blocks
-    // gives the slots several cells each on the test grids
-    unsigned blocks = (unsigned)((g.Cw + NC::CPB - 1) / NC::CPB);
-    if (!mixed && blocks > 3)
-      blocks = 3;
+    const unsigned blocks = (unsigned)((g.Cw + NC::CPB - 1) / NC::CPB);
     emu::launch(blocks, NC::THREADS, NC::SMEM_BYTES, [&] {
       k_newton<Sys, N>(w, qh, g, T, wprod, st, tol, guess, mixed);
     });
