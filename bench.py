@@ -34,8 +34,8 @@ Our arm prints one JSON line:
                from a pinned host array: host->device copy of the state,
                K steps, device->host copy of the final state and the
                snapshot row, all inside the timed region
-  roofline     the dominant kernel (k_newton for the stiff workload, else the
-               larger of k_faces and the predictor; FP64-bound): algorithmic
+  roofline     the dominant kernel (the larger of k_faces and the predictor,
+               k_newton or k_predictor; FP64-bound): algorithmic
                FP64 flops of one launch (pypde_gb300.work_model) / its mean
                launch time measured here with CUDA events, against the FP64
                FMA peak measured here (MEASURED_PEAKS.json has no FP64

@@ -410,10 +410,11 @@ class Fn:
         if size is not None:
             # a negative index counts from the end, as in Python, whether it
             # is written with a minus sign or held in a name (k = -1; Q[k],
-            # a loop over range(-3, 0)); a compare and select per access
-            if not v.isidentifier():
-                v = self.new(INT, v)
-            v = f"({v} < 0 ? {v} + {size} : {v})"
+            # a loop over range(-3, 0)); a compare and select per access.
+            # The expression stays where it is written (not hoisted into a
+            # temporary), so that one under a conditional expression is not
+            # evaluated when its branch is not taken
+            v = f"(({v}) < 0 ? ({v}) + {size} : ({v}))"
         return v, None
 
     def _offset(self, node):
