@@ -74,11 +74,11 @@ WORKLOADS = {
 
 # DRAM bytes (read + write) of one k_faces launch per face point, from ncu
 # captures of smaller grids of the same workload (a full-size launch is
-# scaled by its face points): the relaxation system at 512^2, N=2 (238 MB
-# read + 393 MB written over 2,101,248 face points); the Euler shear layer
+# scaled by its face points): the relaxation system at 512^2, N=2 (237.7 MB
+# read + 366.3 MB written over 2,101,248 face points); the Euler shear layer
 # at 256^2, N=3 (108 + 67 MB over 1,184,256).  The command lines are in
 # the k_faces summaries under profiles/.
-FACES_DRAM_BYTES_PER_POINT = {("cattaneo", 2, 2): 300.0, ("euler", 2, 3): 147.8}
+FACES_DRAM_BYTES_PER_POINT = {("cattaneo", 2, 2): 287.5, ("euler", 2, 3): 147.8}
 
 
 def parse():
