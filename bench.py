@@ -95,6 +95,11 @@ def parse():
     p.add_argument("--batch-problems", type=int, default=256,
                    help="problems of the batched section (0: skip it)")
     p.add_argument("--batch-steps", type=int, default=6)
+    p.add_argument("--batch-full", action="store_true",
+                   help="batched section: every problem to its own tf (plain form only)")
+    p.add_argument("--forms", default="all",
+                   help="stiff workloads: comma list of forms to time besides the head "
+                        "(plain,mixed,learned_mixed,learned_network) or 'all'")
     a = p.parse_args()
     system, ndim, n, N, cfl, stiff = WORKLOADS[a.workload]
     a.system, a.ndim, a.cfl, a.stiff = system, ndim, cfl, stiff
@@ -211,7 +216,7 @@ def cpu_run(args, u, steps, cores):
                           stiff=args.stiff, max_steps=steps, nthreads=cores)
 
 
-def oracle_check(args, u0, local, warm):
+def oracle_check(args, u0, local, warm, forms):
     """The CPU oracle (all host cores) for the timed region's K steps from
     the initial state, on the workload's own grid (the 3-D workload on a
     48^3 grid of the same kind: its full grid takes the host minutes per
@@ -232,10 +237,6 @@ def oracle_check(args, u0, local, warm):
     u_o, _, k, _ = cpu_run(a, u0, args.steps, cores)
     el = time.perf_counter() - t0
     R = Runner(a, local)
-    forms = [("plain", None, False, False)]
-    if args.stiff:
-        forms += [("learned", warm, False, False), ("mixed", None, True, False),
-                  ("learned_mixed", warm, True, False), ("learned_network", warm, False, True)]
     l1s, bitwise = {}, None
     for name, w, mx, force in forms:
         q = u0.copy()
@@ -266,9 +267,11 @@ class Runner:
         self.dX = np.array([1.0 / args.n] * args.ndim)
         self.bt = np.array([1] * args.ndim, dtype=np.int32)
 
-    def run(self, u, steps, profile=False, warm=None, tol=0.0, mixed=False, force=False):
+    def run(self, u, steps, profile=False, warm=None, tol=0.0, mixed=False, force=False,
+            tf=10.0):
         """warm: a WarmStart, used as pde_solver uses it (only if its
-        validation found a saving), or always with force."""
+        validation found a saving), or always with force.  steps < 0: run
+        to tf."""
         _lib, a = self._lib, self.args
         if warm is not None and not (force or warm.active):
             warm = None
@@ -283,7 +286,7 @@ class Runner:
         st = _lib.Stats()
         s = self.sys
         _lib.check(self.L.pde_solver_ex(s.handle, s.has_F, s.has_B, s.has_S, _lib.c_ptr(u),
-                                        10.0, _lib.c_ptr(self.nX), a.ndim,
+                                        float(tf), _lib.c_ptr(self.nX), a.ndim,
                                         _lib.c_ptr(self.dX),
                                         a.cfl, _lib.c_ptr(self.bt), a.stiff, 0, a.order, 1,
                                         None, opt, st))
@@ -323,9 +326,19 @@ def run_batched(args, local):
                    stiff=True, max_steps=2, device=local)
     b = [dict(p, Q0=p["Q0"].copy()) for p in probs]
     st = {}
-    pde_solver_batch(b, F=s.F, S=s.S, stiff=True, max_steps=K, stats=st, device=local)
+    pde_solver_batch(b, F=s.F, S=s.S, stiff=True, max_steps=None if args.batch_full else K,
+                     stats=st, device=local)
     upd = sum(p["Q0"].shape[0] * p["Q0"].shape[1] * k
               for p, k in zip(probs, st["steps_per_problem"]))
+    if args.batch_full:  # every problem to its own tf, the batched launch alone
+        return {"problems": len(probs), "to_tf": float(probs[0]["tf"]),
+                "cells": int(sum(p["Q0"].shape[0] * p["Q0"].shape[1] for p in probs)),
+                "steps_per_problem_min_max": [int(min(st["steps_per_problem"])),
+                                              int(max(st["steps_per_problem"]))],
+                "cell_updates": int(upd),
+                "batched": {"value": upd / st["device_seconds"], "unit": UNIT,
+                            "seconds": st["device_seconds"], "tune_seconds": st["tune_seconds"],
+                            "newton_iters": st["pred_iters"], "nan_found": st["nan_found"]}}
     seq = 0.0
     same = True
     for p, pb in zip(probs, b):
@@ -335,6 +348,37 @@ def run_batched(args, local):
                    order=p["order"], stiff=True, max_steps=K, stats=s1, device=local)
         seq += s1["device_seconds"]
         same &= bool(np.array_equal(q, pb["Q0"]))
+    # the learned form through the batch: one network per order, trained on
+    # a 64^2 problem of that order and validated like the one-problem form
+    # (gated); its own guess forced on; and the FP32-sweep form.  Each
+    # against the plain batched result (relative L1, largest over problems)
+    from pypde_gb300 import warmstart
+    nets, gates = {}, {}
+    for N in (1, 2, 3):
+        u0 = workloads.relaxation(64, 2, seed=40 + N, patches=4)
+        ws = warmstart.train_warm_start(u0, 10.0, [1.0, 1.0], F=s.F, S=s.S, cfl=0.8, order=N,
+                                        tau_var=6, steps=8, per_step=1024, iters=300, seed=N,
+                                        device=local)
+        nets[N], gates[N] = ws, {"active": bool(ws.active), **ws.validation}
+
+    def batched_form(**opts):
+        bb = [dict(p, Q0=p["Q0"].copy()) for p in probs]
+        st2 = {}
+        pde_solver_batch(bb, F=s.F, S=s.S, stiff=True, max_steps=K, stats=st2, device=local,
+                         **opts)
+        err = max(float(l1(q2["Q0"], q1["Q0"]).max()) for q2, q1 in zip(bb, b))
+        return {"value": upd / st2["device_seconds"], "unit": UNIT,
+                "seconds": st2["device_seconds"],
+                "over_sequential_plain": seq / st2["device_seconds"],
+                "newton_iters": st2["pred_iters"], "l1_vs_plain_batched": err}
+
+    forms = {"learned": batched_form(warm_start=nets)}
+    for ws in nets.values():
+        ws.active = True
+    forms["learned_network"] = batched_form(warm_start=nets)
+    forms["mixed"] = batched_form(mixed_precision=True)
+    forms["plain_newton_iters"] = st["pred_iters"]
+    forms["warm_start_gates"] = gates
     orders = np.bincount([p["order"] for p in probs], minlength=4)[1:].tolist()
     return {"problems": len(probs), "orders_1_2_3": orders,
             "cells": int(sum(p["Q0"].shape[0] * p["Q0"].shape[1] for p in probs)),
@@ -345,7 +389,8 @@ def run_batched(args, local):
                         "tiles_per_pop": st["per_pop"]},
             "sequential": {"value": upd / seq, "unit": UNIT, "seconds": seq},
             "batched_over_sequential": seq / st["device_seconds"],
-            "bit_identical_to_sequential": same}
+            "bit_identical_to_sequential": same,
+            "forms": forms}
 
 
 def run_ours(args, ws, rank, local):
@@ -369,7 +414,12 @@ def run_ours(args, ws, rank, local):
     forms = {}
     warm = None
     train = None
-    if args.stiff:
+    # the stiff workloads' forms: all five, or (--forms) plain and the ones
+    # listed, without the network when no learned form is listed
+    allf = ["plain", "mixed", "learned_mixed", "learned_network"]
+    sel = allf if args.forms == "all" else [f for f in args.forms.split(",") if f in allf]
+    learned = args.stiff and (args.forms == "all" or any("learned" in f for f in sel))
+    if learned:
         from pypde_gb300 import warmstart
         t0 = time.perf_counter()
         warm = warmstart.train_warm_start(u0, 10.0, Ls, F=s.F, S=s.S, cfl=args.cfl,
@@ -384,16 +434,19 @@ def run_ours(args, ws, rank, local):
                          "iterations than the plain guess on the held-out cells; otherwise "
                          "it keeps the plain guess (form learned_network forces it)"}
 
-    head = "learned" if args.stiff else "plain"
+    head = "learned" if learned else "plain"
     with Clocks(local) as clk:
-        st_h, sec, sp, ksteps, u_warm = measure_form(R, args, ws, u0,
-                                                      warm if args.stiff else None)
+        st_h, sec, sp, ksteps, u_warm = measure_form(R, args, ws, u0, warm)
     forms[head] = (st_h, sec, sp, ksteps)
+    # (name, warm start, FP32 sweeps, network forced)
+    spec = {"plain": (None, False, False), "learned": (warm, False, False),
+            "mixed": (None, True, False), "learned_mixed": (warm, True, False),
+            "learned_network": (warm, False, True)}
     if args.stiff:
-        forms["plain"] = measure_form(R, args, ws, u0, None)[:4]
-        forms["mixed"] = measure_form(R, args, ws, u0, None, mixed=True)[:4]
-        forms["learned_mixed"] = measure_form(R, args, ws, u0, warm, mixed=True)[:4]
-        forms["learned_network"] = measure_form(R, args, ws, u0, warm, force=True)[:4]
+        for f in sel:
+            if f not in forms:
+                w, mx, fc = spec[f]
+                forms[f] = measure_form(R, args, ws, u0, w, mixed=mx, force=fc)[:4]
     value = ws * C * args.steps / sec
 
     # every form against the CPU oracle over the same K steps from u0, and
@@ -401,15 +454,13 @@ def run_ours(args, ws, rank, local):
     # 1e-12 tolerance's own effect)
     errs, conv_errs, oracle = {}, {}, None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        oracle = oracle_check(args, u0, local, warm)
+        oracle = oracle_check(args, u0, local, warm, [(f,) + spec[f] for f in forms])
         errs = oracle.pop("l1")
     if args.stiff:
         q_o = u0.copy()
         R.run(q_o, args.steps, tol=1e-15)
-        for name, w, mx, force in (("plain", None, False, False), ("learned", warm, False, False),
-                                   ("mixed", None, True, False),
-                                   ("learned_mixed", warm, True, False),
-                                   ("learned_network", warm, False, True)):
+        for name in forms:
+            w, mx, force = spec[name]
             q = u0.copy()
             R.run(q, args.steps, warm=w, mixed=mx, force=force)
             conv_errs[name] = [float(x) for x in l1(q, q_o)]
@@ -428,6 +479,14 @@ def run_ours(args, ws, rank, local):
             d["l1_vs_oracle"] = errs[name]
         return d
 
+    full = None
+    if args.workload == "shear":
+        # the shear layer's whole run to its end time tf = 0.5 (CFL 0.8)
+        q = u0.copy()
+        stf = R.run(q, -1, tf=0.5)
+        full = {"tf": 0.5, "steps": stf["steps"], "seconds": stf["device_seconds"],
+                "value": ws * C * stf["steps"] / stf["device_seconds"], "unit": UNIT,
+                "t_final": stf["t_final"], "nan_found": bool(stf["nan_found"])}
     stage_s = sp["stage_seconds"]
     its = sp["pred_iters"] / (ksteps * Cw)
     fpf = work_model.face_point_flops(args.system, nd, V, N)
@@ -534,6 +593,8 @@ def run_ours(args, ws, rank, local):
         out["roofline_predictor"] = roof_pred
     if train:
         out["training"] = train
+    if full:
+        out["full_run"] = full
     if args.stiff and args.batch_problems > 0 and ws == 1:
         out["batched_workload"] = run_batched(args, local)
     if oracle is not None:
