@@ -837,6 +837,15 @@ __device__ __forceinline__ double max_abs_eigs(double *q, double *dq, int d,
   return max_abs_eig_sys<Sys>(M, d);
 }
 
+// max_abs_eigs as a call rather than inlined: the face kernel evaluates it
+// twice per face point (both states), and one out-of-line copy lets the two
+// evaluations share their registers and stack instead of spilling.
+template <class Sys>
+__device__ __noinline__ double max_abs_eigs_call(double *q, double *dq, int d,
+                                                 double *f0) {
+  return max_abs_eigs<Sys>(q, dq, d, f0);
+}
+
 // The FD Jacobian + B itself (src/eigs/system.cpp:6-26).
 template <class Sys>
 __device__ __forceinline__ void system_matrix(double *M, double *q, double *dq,

@@ -1199,8 +1199,14 @@ __device__ __forceinline__ void rusanov_flux(double *f, double *qL,
                                              double *dqR, int d, double dXd) {
   constexpr int V = Sys::V;
   double fL[V], fR[V]; // F(qL), F(qR) come out of the FD Jacobians
-  double m1 = max_abs_eigs<Sys>(qL, dqL, d, fL);
-  double m2 = max_abs_eigs<Sys>(qR, dqR, d, fR);
+  double m1, m2;
+  if constexpr (V >= 6) { // a large system's eigen work spills when inlined twice
+    m1 = max_abs_eigs_call<Sys>(qL, dqL, d, fL);
+    m2 = max_abs_eigs_call<Sys>(qR, dqR, d, fR);
+  } else {
+    m1 = max_abs_eigs<Sys>(qL, dqL, d, fL);
+    m2 = max_abs_eigs<Sys>(qR, dqR, d, fR);
+  }
   double m = fmax(m1, m2);
 #pragma unroll
   for (int v = 0; v < V; v++)
