@@ -97,6 +97,9 @@ def parse():
     p.add_argument("--batch-steps", type=int, default=6)
     p.add_argument("--batch-full", action="store_true",
                    help="batched section: every problem to its own tf (plain form only)")
+    p.add_argument("--strips", type=int, default=0,
+                   help="predictor strips overlapped with the faces (0: the library's choice, "
+                        "1: none)")
     p.add_argument("--forms", default="all",
                    help="stiff workloads: comma list of forms to time besides the head "
                         "(plain,mixed,learned_mixed,learned_network) or 'all'")
@@ -281,6 +284,7 @@ class Runner:
         opt.device = self.local
         opt.profile_stages = int(profile)
         opt.newton_tol = tol
+        opt.strips = a.strips
         if warm is not None:
             opt.warm_start = warm.handle
         st = _lib.Stats()
@@ -541,7 +545,8 @@ def run_ours(args, ws, rank, local):
     t0 = time.perf_counter()
     pde_solver(pinned, 10.0, Ls, F=s.F, S=s.S if args.stiff else None,
                boundaryTypes="periodic", cfl=args.cfl, order=N, ndt=1, stiff=args.stiff,
-               max_steps=args.steps, device=local, warm_start=warm if args.stiff else None)
+               max_steps=args.steps, device=local, warm_start=warm if args.stiff else None,
+               strips=args.strips)
     e2e_s = allmax(ws, time.perf_counter() - t0)
     barrier(ws)
 
@@ -550,7 +555,7 @@ def run_ours(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_name(args), "form": head, "cells": C, "order": N,
-                   "vars": V,
+                   "vars": V, "strips": args.strips or "library's choice",
                    "l2": "working set > L2 (qh alone is "
                          f"{Cw * N ** (nd + 1) * V * 8 / 1e6:.0f} MB); no flush",
                    "parallelism": f"replicas x{ws}"},

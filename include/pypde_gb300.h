@@ -54,6 +54,11 @@ typedef struct {
   int mixed_precision;   /* stiff form: Newton sweeps in FP32 first, then at
                             least two FP64 sweeps to the same tolerance
                             (systems with FP32 callbacks only) */
+  int strips;            /* the predictor runs in this many strips of cells,
+                            the faces of finished strips on a second stream
+                            meanwhile (results are identical for every
+                            value); 0 -> automatic, 1 -> one launch each,
+                            at most 32 */
 } pypde_options;
 
 /* Stages timed by pypde_options.profile_stages, in this order. */

@@ -23,7 +23,7 @@ PYPDE_ERR_COMPILE = 5
 class Options(Structure):
     _fields_ = [("max_steps", c_longlong), ("newton_tol", c_double),
                 ("device", c_int), ("steps_per_graph", c_int), ("profile_stages", c_int),
-                ("warm_start", c_void_p), ("mixed_precision", c_int)]
+                ("warm_start", c_void_p), ("mixed_precision", c_int), ("strips", c_int)]
 
 STAGES = ("boundaries", "weno", "cfl", "predictor", "faces", "centers", "gather", "other")
 

@@ -149,6 +149,11 @@ int pde_solver_ex(const pypde_system *sys, bool useF, bool useB, bool useS,
     a.device = opt->device;
     a.steps_per_graph = opt->steps_per_graph;
     a.profile = opt->profile_stages != 0;
+    if (opt->strips < 0 || opt->strips > 32) {
+      set_error("strips must be 0 (automatic) to 32");
+      return PYPDE_ERR_ARG;
+    }
+    a.strips = opt->strips;
     if (opt->warm_start) {
       const pypde_warm_start *w = opt->warm_start;
       if (w->N != N || w->V != sys->desc->V || w->ndim != ndim) {

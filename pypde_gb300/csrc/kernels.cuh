@@ -459,8 +459,9 @@ template <class Sys, int N>
 __global__ void k_predictor(const double *__restrict__ w,
                             double *__restrict__ qh, const __grid_constant__ Geom g, const __grid_constant__ Tables T,
                             const double *__restrict__ wprod_g,
-                            DevState *st) {
-  k_predictor_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st);
+                            DevState *st, long long b0) {
+  // b0: first block of a strip of cells (0 for the whole grid)
+  k_predictor_body<Sys, N>(VBlock{b0 + blockIdx.x, b0 + gridDim.x}, w, qh, g, T, wprod_g, st);
 }
 
 // ---------------------------------------------------------------------
@@ -1160,8 +1161,9 @@ __device__ __forceinline__ void k_newton_body(VBlock vb_, const double *__restri
 template <class Sys, int N>
 __global__ void k_newton(const double *__restrict__ w, double *__restrict__ qh,
                          const __grid_constant__ Geom g, const __grid_constant__ Tables T, const double *__restrict__ wprod_g,
-                         DevState *st, double tol, int guess, int mixed) {
-  k_newton_body<Sys, N>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, w, qh, g, T, wprod_g, st, tol, guess, mixed);
+                         DevState *st, double tol, int guess, int mixed, long long b0) {
+  // b0: first block of a strip of cells (0 for the whole grid)
+  k_newton_body<Sys, N>(VBlock{b0 + blockIdx.x, b0 + gridDim.x}, w, qh, g, T, wprod_g, st, tol, guess, mixed);
 }
 
 // ---------------------------------------------------------------------
@@ -1366,16 +1368,22 @@ struct FaceIndex {
   long long nface[3]; // faces per direction
 };
 
+// The face points one launch of k_faces covers: n[d] points of direction d
+// from point lo[d] on.  A whole-grid launch has lo[d] = off[d] and
+// n[d] = off[d+1] - off[d]; a strip launch has the points of the faces
+// whose cells a set of predictor strips has finished.
+struct FaceSpan {
+  long long lo[3], n[3];
+};
+
+// Face point p: its two face states, flux and path integral, and the
+// amounts written to contrib[p].
 template <class Sys, int N, int FLUX>
-__device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restrict__ qh, double *__restrict__ contrib,
-            const Geom &g, const Tables &T, const FaceIndex &fi, DevState *st) {
+__device__ __forceinline__ void face_point(long long p, const double *__restrict__ qh, double *__restrict__ contrib,
+            const Geom &g, const Tables &T, const FaceIndex &fi, double dt) {
   constexpr int V = Sys::V, D = Sys::NDIM;
   constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
-  if (!step_active(st))
-    return;
-  const double dt = st->dt;
-  for (long long p = vb_.b * (long long)blockDim.x + threadIdx.x;
-       p < fi.off[D]; p += (long long)vb_.n * blockDim.x) {
+  {
     int d = 0;
     while (d + 1 < D && p >= fi.off[d + 1])
       d++;
@@ -1470,11 +1478,38 @@ __device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restric
   }
 }
 
+// Every face point of the grid (one tile of a batched launch).
+template <class Sys, int N, int FLUX>
+__device__ __forceinline__ void k_faces_body(VBlock vb_, const double *__restrict__ qh, double *__restrict__ contrib,
+            const Geom &g, const Tables &T, const FaceIndex &fi, DevState *st) {
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  for (long long p = vb_.b * (long long)blockDim.x + threadIdx.x;
+       p < fi.off[Sys::NDIM]; p += (long long)vb_.n * blockDim.x)
+    face_point<Sys, N, FLUX>(p, qh, contrib, g, T, fi, dt);
+}
+
+// The face points of span sp, direction by direction.
 template <class Sys, int N, int FLUX = 0>
 __global__ void __launch_bounds__(128)
     k_faces(const double *__restrict__ qh, double *__restrict__ contrib,
-            const __grid_constant__ Geom g, const __grid_constant__ Tables T, const __grid_constant__ FaceIndex fi, DevState *st) {
-  k_faces_body<Sys, N, FLUX>(VBlock{(long long)blockIdx.x, (long long)gridDim.x}, qh, contrib, g, T, fi, st);
+            const __grid_constant__ Geom g, const __grid_constant__ Tables T, const __grid_constant__ FaceIndex fi, DevState *st,
+            const __grid_constant__ FaceSpan sp) {
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  long long total = 0;
+  for (int d = 0; d < Sys::NDIM; d++)
+    total += sp.n[d];
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    long long r = q;
+    int d = 0;
+    while (d + 1 < Sys::NDIM && r >= sp.n[d])
+      r -= sp.n[d++];
+    face_point<Sys, N, FLUX>(sp.lo[d] + r, qh, contrib, g, T, fi, dt);
+  }
 }
 
 // ---------------------------------------------------------------------

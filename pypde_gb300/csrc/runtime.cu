@@ -7,6 +7,7 @@
 // only synchronises between graph launches (to drain snapshots and to see
 // whether t reached tf; kernels of steps past the end return at once).
 #include "runtime.h"
+#include "strips.h"
 #include "step_kernels.cuh"
 #include "../../include/pypde_gb300.h"
 
@@ -173,6 +174,8 @@ struct Arena {
   Buf u, uprev, ub, tmpA, tmpB, w, qh, contrib, cen, ring, state, wprod;
   DevState *host_state = nullptr; // pinned
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;    // faces of finished predictor strips
+  cudaEvent_t strip_ev[MAX_STRIPS + 1] = {};
 };
 static std::mutex g_mu;
 static std::map<int, Arena> g_arena;
@@ -188,6 +191,11 @@ static int arena_for(int device, Arena **out) {
   Arena &a = g_arena[device];
   if (!a.stream)
     CK(cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking));
+  if (!a.side) {
+    CK(cudaStreamCreateWithFlags(&a.side, cudaStreamNonBlocking));
+    for (int i = 0; i <= MAX_STRIPS; i++)
+      CK(cudaEventCreateWithFlags(&a.strip_ev[i], cudaEventDisableTiming));
+  }
   if (!a.host_state)
     CK(cudaMallocHost(&a.host_state, sizeof(DevState)));
   *out = &a;
@@ -339,42 +347,108 @@ struct StepCtx {
   double *hw, *hq, *hdt;
   long long hstride, hper;
   int hsteps;
+  // predictor strips overlapped with the faces (null: one launch each)
+  const StripPlan *plan;
+  cudaStream_t side;
+  cudaEvent_t *strip_ev;
 };
 
-static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
+// Whether a step runs its predictor in strips with the faces of finished
+// strips on the side stream (not in the stage-timing mode, whose events
+// bracket one stage at a time).
+static bool overlapped(const StepCtx &c, bool profile) {
+  return !profile && c.plan && c.plan->S > 1 && c.faces;
+}
+
+static FaceSpan whole_span(const StepCtx &c) {
+  FaceSpan sp;
+  for (int d = 0; d < 3; d++) {
+    sp.lo[d] = d < c.g.ndim ? c.fi.off[d] : 0;
+    sp.n[d] = d < c.g.ndim ? c.fi.off[d + 1] - c.fi.off[d] : 0;
+  }
+  return sp;
+}
+
+static FaceSpan strip_span(const StripPlan &p, int i) {
+  FaceSpan sp;
+  for (int d = 0; d < 3; d++) {
+    sp.lo[d] = p.lo[i][d];
+    sp.n[d] = p.n[i][d];
+  }
+  return sp;
+}
+
+static long long span_points(const FaceSpan &sp) {
+  return sp.n[0] + sp.n[1] + sp.n[2];
+}
+
+static cudaError_t enqueue_faces(const StepCtx &c, cudaStream_t s,
+                                 const FaceSpan &span) {
+  const long long n = span_points(span);
+  if (n == 0)
+    return cudaSuccess;
+  Geom g = c.g;
+  Tables T = c.T;
+  FaceIndex fi = c.fi;
+  FaceSpan sp = span;
+  void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
+               (void *)&fi,   (void *)&c.st,      (void *)&sp};
+  return launch(c.ks->faces_flux[c.flux], dim3(grid_for(n, 128, 152 * 256)),
+                dim3(128), 0, s, a);
+}
+
+// The warm-start network's guess of qh (learned form): qh = w + its
+// correction, from which the Newton iteration starts.
+static cudaError_t enqueue_guess(const StepCtx &c, cudaStream_t s) {
+  if (!c.stiff || !c.warm)
+    return cudaSuccess;
+  const KernelSet &k = *c.ks;
+  Geom g = c.g;
+  MlpModel m = c.warm->model;
+  void *ga[] = {(void *)&c.w, (void *)&c.qh, (void *)&g, (void *)&m,
+                (void *)&c.st};
+  long long tiles = (g.Cw + 127) / 128;
+  unsigned gb = (unsigned)(tiles < 152 * 2 ? tiles : 152 * 2);
+  return launch(k.guess, dim3(gb), dim3(256), k.guess_smem, s, ga);
+}
+
+static int predictor_cpb(const StepCtx &c) {
+  return c.stiff ? c.ks->newton_cpb : c.ks->pred_cpb;
+}
+
+// Predictor blocks [b_lo, b_hi): cells [b_lo cpb, b_hi cpb) of the w-grid.
+static cudaError_t enqueue_predictor_blocks(const StepCtx &c, cudaStream_t s,
+                                            long long b_lo, long long b_hi) {
+  if (b_hi <= b_lo)
+    return cudaSuccess;
   const KernelSet &k = *c.ks;
   Geom g = c.g;
   Tables T = c.T;
   double tol = c.tol;
-  void *args[] = {(void *)&c.w, (void *)&c.qh, (void *)&g,   (void *)&T,
-                  (void *)&c.wprod, (void *)&c.st, (void *)&tol};
+  long long b0 = b_lo;
+  const dim3 grid((unsigned)(b_hi - b_lo));
   if (c.stiff) {
-    int guess = 0;
-    if (c.warm) {
-      // qh = w + the network's correction, then Newton from there
-      MlpModel m = c.warm->model;
-      void *ga[] = {(void *)&c.w, (void *)&c.qh, (void *)&g, (void *)&m,
-                    (void *)&c.st};
-      long long tiles = (g.Cw + 127) / 128;
-      unsigned gb = (unsigned)(tiles < 152 * 2 ? tiles : 152 * 2);
-      cudaError_t e = launch(k.guess, dim3(gb), dim3(256), k.guess_smem, s, ga);
-      if (e != cudaSuccess)
-        return e;
-      guess = 1;
-    } else if (c.guess) {
-      guess = 1;
-    }
+    int guess = (c.warm || c.guess) ? 1 : 0;
     int mixed = c.mixed;
-    void *na[] = {(void *)&c.w,     (void *)&c.qh, (void *)&g,
+    void *na[] = {(void *)&c.w,     (void *)&c.qh,    (void *)&g,
                   (void *)&T,       (void *)&c.wprod, (void *)&c.st,
-                  (void *)&tol,     (void *)&guess, (void *)&mixed};
-    long long blocks = (g.Cw + k.newton_cpb - 1) / k.newton_cpb;
-    return launch(k.newton, dim3((unsigned)blocks), dim3(k.newton_threads),
-                  k.newton_smem, s, na);
+                  (void *)&tol,     (void *)&guess,   (void *)&mixed,
+                  (void *)&b0};
+    return launch(k.newton, grid, dim3(k.newton_threads), k.newton_smem, s,
+                  na);
   }
-  unsigned blocks = (unsigned)((g.Cw + k.pred_cpb - 1) / k.pred_cpb);
-  return launch(k.predictor, dim3(blocks), dim3(k.pred_threads), k.pred_smem,
-                s, args);
+  void *args[] = {(void *)&c.w,     (void *)&c.qh, (void *)&g, (void *)&T,
+                  (void *)&c.wprod, (void *)&c.st, (void *)&b0};
+  return launch(k.predictor, grid, dim3(k.pred_threads), k.pred_smem, s,
+                args);
+}
+
+static cudaError_t enqueue_predictor(const StepCtx &c, cudaStream_t s) {
+  cudaError_t e = enqueue_guess(c, s);
+  if (e != cudaSuccess)
+    return e;
+  const int cpb = predictor_cpb(c);
+  return enqueue_predictor_blocks(c, s, 0, (c.g.Cw + cpb - 1) / cpb);
 }
 
 static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
@@ -384,11 +458,7 @@ static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
   FaceIndex fi = c.fi;
   cudaError_t e;
   if (c.faces) {
-    void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
-                 (void *)&fi,   (void *)&c.st};
-    e = launch(k.faces_flux[c.flux],
-               dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)), dim3(128), 0,
-               s, a);
+    e = enqueue_faces(c, s, whole_span(c));
     if (e != cudaSuccess)
       return e;
   }
@@ -409,8 +479,17 @@ static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
 }
 
 // Kernels one step launches (the count reported as kernel_launches).
-static int kernels_per_step(const StepCtx &c) {
-  return 10 + c.g.ndim + (c.faces ? 1 : 0) + (c.centers ? 1 : 0) +
+static int kernels_per_step(const StepCtx &c, bool profile) {
+  int pred = 1, faces = c.faces ? 1 : 0;
+  if (overlapped(c, profile)) {
+    pred = faces = 0;
+    for (int i = 0; i < c.plan->S; i++) {
+      pred += c.plan->blk[i + 1] > c.plan->blk[i];
+      faces += span_points(strip_span(*c.plan, i)) > 0;
+    }
+  }
+  // step begin, copy of u, ghost fill, CFL, dt, gather, step end, snapshot
+  return 8 + c.g.ndim + pred + faces + (c.centers ? 1 : 0) +
          (c.stiff && c.warm ? 1 : 0) + (c.hw ? 1 : 0);
 }
 
@@ -455,7 +534,28 @@ static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
   }
   k_dt<<<1, 1, 0, s>>>(c.st);
   mark(3);
-  e = enqueue_predictor(c, s);
+  const bool strips = overlapped(c, ev != nullptr);
+  bool side_used = false;
+  if (strips) {
+    // strip i of the predictor on s, then the faces it releases on the side
+    // stream while strip i+1 is predicted; the two streams write disjoint
+    // parts of qh and contrib
+    const StripPlan &p = *c.plan;
+    e = enqueue_guess(c, s);
+    for (int i = 0; i < p.S && e == cudaSuccess; i++) {
+      e = enqueue_predictor_blocks(c, s, p.blk[i], p.blk[i + 1]);
+      const FaceSpan sp = strip_span(p, i);
+      if (e != cudaSuccess || span_points(sp) == 0)
+        continue;
+      if ((e = cudaEventRecord(c.strip_ev[i], s)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(c.side, c.strip_ev[i], 0)) != cudaSuccess)
+        break;
+      side_used = true;
+      e = enqueue_faces(c, c.side, sp);
+    }
+  } else {
+    e = enqueue_predictor(c, s);
+  }
   if (e != cudaSuccess)
     return e;
   if (c.hw) {
@@ -466,36 +566,31 @@ static cudaError_t enqueue_step(const StepCtx &c, cudaStream_t s,
         c.hsteps, c.hper);
   }
   mark(4);
+  if (c.faces && !strips) {
+    e = enqueue_faces(c, s, whole_span(c));
+    if (e != cudaSuccess)
+      return e;
+  }
+  mark(5);
+  if (c.centers) {
+    // with strips, beside the last faces
+    long long nn = (long long)c.N * ipow(c.N, c.g.ndim);
+    Geom g = c.g;
+    Tables T = c.T;
+    void *a[] = {(void *)&c.qh, (void *)&c.cen, (void *)&g, (void *)&T,
+                 (void *)&c.st};
+    e = launch(c.ks->centers, dim3(grid_for(g.C * nn, 128, 152 * 256)),
+               dim3(128), 0, s, a);
+    if (e != cudaSuccess)
+      return e;
+  }
+  mark(6);
+  if (side_used) { // the gather reads every face's contribution
+    if ((e = cudaEventRecord(c.strip_ev[MAX_STRIPS], c.side)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(s, c.strip_ev[MAX_STRIPS], 0)) != cudaSuccess)
+      return e;
+  }
   {
-    StepCtx f = c;
-    f.centers = false;
-    if (c.faces) {
-      // faces only (the gather is launched below)
-      const KernelSet &k = *c.ks;
-      Geom g = c.g;
-      Tables T = c.T;
-      FaceIndex fi = c.fi;
-      void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
-                   (void *)&fi,   (void *)&c.st};
-      e = launch(k.faces_flux[c.flux],
-                 dim3(grid_for(fi.off[c.g.ndim], 128, 152 * 256)), dim3(128),
-                 0, s, a);
-      if (e != cudaSuccess)
-        return e;
-    }
-    mark(5);
-    if (c.centers) {
-      long long nn = (long long)c.N * ipow(c.N, c.g.ndim);
-      Geom g = c.g;
-      Tables T = c.T;
-      void *a[] = {(void *)&c.qh, (void *)&c.cen, (void *)&g, (void *)&T,
-                   (void *)&c.st};
-      e = launch(c.ks->centers, dim3(grid_for(g.C * nn, 128, 152 * 256)),
-                 dim3(128), 0, s, a);
-      if (e != cudaSuccess)
-        return e;
-    }
-    mark(6);
     Geom g = c.g;
     FaceIndex fi = c.fi;
     int uc = c.centers ? 1 : 0, uf = c.faces ? 1 : 0;
@@ -675,6 +770,24 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   c.hsteps = 0;
   c.faces = sys.has_F || sys.has_B;
   c.centers = sys.has_B || sys.has_S;
+  StripPlan plan;
+  {
+    const int cpb = predictor_cpb(c);
+    const long long blocks = (c.g.Cw + cpb - 1) / cpb;
+    // Automatic: 4 strips for the Newton predictor when each holds at least
+    // 4 blocks per SM (1024^2 relaxation: 85.0 ms a step against 90.0 in
+    // one launch each; 8 strips 85.2, 16 strips 85.5).  The Picard
+    // predictor is a small part of its step and gains nothing (512^2 shear
+    // layer, N=3: 13.9 ms with 8 strips against 13.65).
+    int S = a.strips;
+    if (S == 0)
+      S = (c.stiff && blocks >= 4LL * 152 * 4) ? 4 : 1;
+    plan_strips(S, a.ndim, c.g.nX, c.g.nXw, c.g.Cw, cpb, c.N, c.fi.off,
+                &plan);
+  }
+  c.plan = &plan;
+  c.side = ar->side;
+  c.strip_ev = ar->strip_ev;
   const int V = c.V, N = c.N, Nd = ipow(N, a.ndim);
   long long usz = c.g.C * V;
   int K = a.steps_per_graph;
@@ -778,10 +891,10 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   for (;;) {
     if (a.profile) {
       CK(enqueue_step(c, s, pev));
-      launches += kernels_per_step(c);
+      launches += kernels_per_step(c, true);
     } else {
       CK(cudaGraphLaunch(exec, s));
-      launches += (long long)K * kernels_per_step(c);
+      launches += (long long)K * kernels_per_step(c, false);
     }
     CK(cudaMemcpyAsync(ar->host_state, c.st, sizeof(DevState),
                        cudaMemcpyDeviceToHost, s));

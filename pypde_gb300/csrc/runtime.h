@@ -103,6 +103,7 @@ struct RunArgs {
   double newton_tol = 1e-12;
   int device = 0;
   int steps_per_graph = 0;
+  int strips = 0; // predictor strips overlapped with faces; 0 -> automatic
   bool profile = false;
   bool useF = true, useB = true, useS = true;
   const WarmStart *warm = nullptr;    // learned warm start of the Newton predictor

@@ -31,7 +31,7 @@ FLUXES = {"rusanov": 0, "roe": 1, "osher": 2}
 def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cfl=0.9,
                order=2, ndt=100, flux="rusanov", stiff=True, nThreads=-1, *, M=None,
                max_steps=None, newton_tol=None, device=0, stats=None, jit=False,
-               warm_start=None, mixed_precision=False):
+               warm_start=None, mixed_precision=False, strips=0):
     """Solve dQ/dt + div F(Q, grad Q) + B(Q) . grad Q = S(Q) on [0, L] (see
     pypde/solvers.py:28-175 for the full description of the arguments).
 
@@ -39,6 +39,10 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
     first reaches (k+1) tf / ndt, row ndt-1 the state at tf.  Like the
     reference, the final state is also written into Q0 when Q0 is a
     contiguous float64 array.
+
+    strips: the predictor runs in this many strips of cells while the faces
+    of finished strips run on a second CUDA stream (0: the library's choice,
+    1: no overlap); the results do not depend on it.
     """
     if M is not None:
         # the reference's pde_solver (pypde/solvers.py:13-25) has no M
@@ -71,6 +75,7 @@ def pde_solver(Q0, tf, L, F=None, B=None, S=None, boundaryTypes="transitive", cf
         if getattr(warm_start, "active", True):  # validated to save iterations
             opt.warm_start = warm_start.handle
     opt.mixed_precision = int(bool(mixed_precision))
+    opt.strips = int(strips)
     st = _lib.Stats()
     lib = _lib.lib()
     code = lib.pde_solver_ex(system.handle, useF, useB, useS, _lib.c_ptr(ur), float(tf),

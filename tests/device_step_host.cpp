@@ -266,6 +266,7 @@ using std::pow;
 using std::sqrt;
 
 #include "step_kernels.cuh"
+#include "strips.h"
 #include "systems.cuh"
 
 namespace {
@@ -373,23 +374,38 @@ std::vector<double> make_wprod(const Tables &T, int ndim) {
 // The predictor stage of one step: Picard (k_predictor) or Newton
 // (k_newton), launched as enqueue_predictor does.
 // With guess = 1 the Newton iteration starts from the qh already given.
+// Blocks [b_lo, b_hi) only (a strip of cells) when b_hi >= 0.
 template <class Sys, int N>
 void predictor_stage(bool stiff, const double *w, double *qh, const Geom &g,
                      const Tables &T, const double *wprod, DevState *st,
-                     double tol, int mixed, int guess = 0) {
+                     double tol, int mixed, int guess = 0, long long b_lo = 0,
+                     long long b_hi = -1) {
   if (stiff) {
     using NC = NewtonCfg<Sys, N>;
-    const unsigned blocks = (unsigned)((g.Cw + NC::CPB - 1) / NC::CPB);
-    emu::launch(blocks, NC::THREADS, NC::SMEM_BYTES, [&] {
-      k_newton<Sys, N>(w, qh, g, T, wprod, st, tol, guess, mixed);
+    if (b_hi < 0)
+      b_hi = (g.Cw + NC::CPB - 1) / NC::CPB;
+    if (b_hi <= b_lo)
+      return;
+    emu::launch((unsigned)(b_hi - b_lo), NC::THREADS, NC::SMEM_BYTES, [&] {
+      k_newton<Sys, N>(w, qh, g, T, wprod, st, tol, guess, mixed, b_lo);
     });
   } else {
     using PC = PredCfg<Sys, N>;
-    const unsigned blocks = (unsigned)((g.Cw + PC::CPB - 1) / PC::CPB);
-    emu::launch(blocks, PC::THREADS, (size_t)PC::SMEM_DOUBLES * 8,
-                [&] { k_predictor<Sys, N>(w, qh, g, T, wprod, st); });
+    if (b_hi < 0)
+      b_hi = (g.Cw + PC::CPB - 1) / PC::CPB;
+    if (b_hi <= b_lo)
+      return;
+    emu::launch((unsigned)(b_hi - b_lo), PC::THREADS,
+                (size_t)PC::SMEM_DOUBLES * 8,
+                [&] { k_predictor<Sys, N>(w, qh, g, T, wprod, st, b_lo); });
   }
 }
+
+// Strips of the step (as run_solver plans them; 1: one launch each).  The
+// emulation runs strip i's faces right after strip i's predictor, before
+// strip i+1 is predicted, so a face that read a cell of a later strip
+// would read last step's qh (or zeros) and miss the restatement.
+int g_strips = 1;
 
 // Steps of the one-problem run, in the order of enqueue_step, until the
 // step is inactive (t >= tf, the step cap, or a NaN).  Returns the steps
@@ -472,12 +488,29 @@ long long run_steps(double *u, int ndim, const int *nX, const int *bt,
       k_cfl<Sys, N>(w.data(), g, T, wprod.data(), &st);
     });
     dt_dev(&st);
-    predictor_stage<Sys, N>(stiff != 0, w.data(), qh.data(), g, T, wprod.data(),
-                            &st, tol, mixed);
-    if (faces)
-      emu::launch(grid_for(fi.off[ndim], 128, 152 * 256), 128, 0, [&] {
-        k_faces<Sys, N, FLUX>(qh.data(), contrib.data(), g, T, fi, &st);
-      });
+    {
+      StripPlan plan;
+      const int cpb = stiff ? NewtonCfg<Sys, N>::CPB : PredCfg<Sys, N>::CPB;
+      plan_strips(faces ? g_strips : 1, ndim, g.nX, g.nXw, g.Cw, cpb, N,
+                  fi.off, &plan);
+      for (int i = 0; i < plan.S; i++) {
+        predictor_stage<Sys, N>(stiff != 0, w.data(), qh.data(), g, T,
+                                wprod.data(), &st, tol, mixed, 0, plan.blk[i],
+                                plan.blk[i + 1]);
+        FaceSpan sp;
+        long long np = 0;
+        for (int d = 0; d < 3; d++) {
+          sp.lo[d] = plan.lo[i][d];
+          sp.n[d] = plan.n[i][d];
+          np += sp.n[d];
+        }
+        if (faces && np > 0)
+          emu::launch(grid_for(np, 128, 152 * 256), 128, 0, [&] {
+            k_faces<Sys, N, FLUX>(qh.data(), contrib.data(), g, T, fi, &st,
+                                  sp);
+          });
+      }
+    }
     if (centers)
       emu::launch(grid_for(g.C * N * Nd, 128, 152 * 256), 128, 0, [&] {
         k_centers<Sys, N>(qh.data(), cen.data(), g, T, &st);
@@ -567,6 +600,29 @@ void predictor_only(int ndim, int stiff, const double *w, long long nrows,
 
 // Fibers run in reverse thread order when reverse is non-zero.
 HOST_API void host_set_order(int reverse) { emu::g_reverse = reverse != 0; }
+
+// Predictor strips of the following host_run calls (1 to 32).
+HOST_API void host_set_strips(int strips) { g_strips = strips; }
+
+// The strip plan of a grid: returns the strips S and fills blk[0..S] and
+// lo/n[s*3 + d] (the arrays hold MAX_STRIPS + 1 and 3 MAX_STRIPS entries).
+HOST_API int host_plan_strips(int S, int ndim, const int *nX, int N, int cpb,
+                              long long *blk, long long *lo, long long *n) {
+  const int ones[3] = {1, 1, 1};
+  const double dX[3] = {1, 1, 1};
+  const Geom g = make_geom(ndim, nX, ones, dX, N);
+  const FaceIndex fi = make_face_index(g, N);
+  StripPlan p;
+  plan_strips(S, ndim, g.nX, g.nXw, g.Cw, cpb, N, fi.off, &p);
+  for (int s = 0; s <= p.S; s++)
+    blk[s] = p.blk[s];
+  for (int s = 0; s < p.S; s++)
+    for (int d = 0; d < 3; d++) {
+      lo[s * 3 + d] = p.lo[s][d];
+      n[s * 3 + d] = p.n[s][d];
+    }
+  return p.S;
+}
 
 // K steps of a built-in system through the device kernels; returns the
 // steps taken, -1 for a combination this unit does not instantiate, or -2

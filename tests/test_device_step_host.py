@@ -38,12 +38,14 @@ def step_lib(tmp_path_factory):
     return load_device_host(build_device_host(tmp_path_factory.mktemp("devstep")))
 
 
-def _run(L, name, u0, N, bt, cfl, K, stiff=False, flux=0, tol=1e-12, mixed=0, reverse=False):
+def _run(L, name, u0, N, bt, cfl, K, stiff=False, flux=0, tol=1e-12, mixed=0, reverse=False,
+         strips=1):
     nX = np.array(u0.shape[:-1], dtype=np.int32)
     dX = np.array([1.0 / n for n in nX])
     u = np.ascontiguousarray(u0, dtype=np.float64).copy()
     t, its = ctypes.c_double(), ctypes.c_ulonglong()
     L.host_set_order(int(reverse))
+    L.host_set_strips(int(strips))
     steps = L.host_run(name.encode(), len(nX), N, flux, ora.ptr(u), ora.ptr(nX),
                        ora.ptr(np.array(bt, dtype=np.int32)), ora.ptr(dX),
                        ora.ptr(stages.tables(N)), 10.0, cfl, int(stiff), tol, mixed, K,
@@ -102,6 +104,81 @@ def test_device_step_equals_port(step_lib, run):
     assert np.array_equal(u_f, u_o), np.abs(u_f - u_o).max()
     assert (steps_r, t_r, its_r) == (steps_f, t_f, its_f)
     assert np.array_equal(u_r, u_f)
+
+
+STRIP_RUNS = [r for r in RUNS if r[-1] in (
+    "sod40-N2", "euler24-N3", "shear16-N2", "euler12x10-N3", "euler3d-N2", "euler2d-osher",
+    "ncp12x10-N2", "relax24-stiff-N2", "relax12-stiff-N3", "cattaneo3d-stiff-N2",
+    "cattaneo10x8-picard")]
+
+
+@pytest.mark.parametrize("strips", [2, 5, 32])
+@pytest.mark.parametrize("run", STRIP_RUNS, ids=[r[-1] for r in STRIP_RUNS])
+def test_device_step_in_strips_equals_port(step_lib, run, strips):
+    """The predictor in strips with each strip's faces run before the next
+    strip is predicted (the order the second stream may take on the GPU):
+    a face that read a cell of a later strip would read the last step's qh
+    and miss the restatement."""
+    name, u0, N, bt, cfl, K, stiff, flux, _ = run
+    u_o, _, steps_o, t_o = ora.pde_solver(name, u0, 10.0, [1.0] * (u0.ndim - 1), bt, cfl, N,
+                                          stiff=stiff, flux=flux, max_steps=K)
+    u, steps, t, _ = _run(step_lib, name, u0, N, bt, cfl, K, stiff, flux, strips=strips)
+    assert steps == steps_o == K and t == t_o
+    assert np.array_equal(u, u_o), np.abs(u - u_o).max()
+
+
+def _face_cells(nX, N, d, p_local):
+    """Low- and high-side w-cells of face point p_local of direction d (the
+    numbering of k_faces: face, time node, transverse node)."""
+    ndim = len(nX)
+    face = p_local // (N * N ** (ndim - 1))
+    ext = [n + 1 if e == d else n for e, n in enumerate(nX)]
+    O = list(np.unravel_index(face, ext))
+    O = [o if e == d else o + 1 for e, o in enumerate(O)]
+    nXw = [n + 2 for n in nX]
+    lo = np.ravel_multi_index(O, nXw)
+    O[d] += 1
+    return lo, np.ravel_multi_index(O, nXw)
+
+
+@pytest.mark.parametrize("shape,N,cpb,S", [((40,), 2, 12, 4), ((13, 9), 2, 12, 8),
+                                           ((9, 13), 3, 5, 32), ((5, 6, 7), 2, 12, 6),
+                                           ((64, 3), 1, 7, 32), ((2, 50), 2, 12, 8),
+                                           ((4, 4, 4), 3, 1, 32), ((1, 1), 2, 12, 3)])
+def test_strip_plan_partitions_faces_after_their_cells(step_lib, shape, N, cpb, S):
+    """Every face point is released by exactly one strip, in its own
+    direction's range, and only once the strips so far have predicted both
+    of its cells."""
+    L = step_lib
+    nX = np.array(shape, dtype=np.int32)
+    blk = np.zeros(33, dtype=np.int64)
+    lo = np.zeros(96, dtype=np.int64)
+    n = np.zeros(96, dtype=np.int64)
+    i64 = ctypes.POINTER(ctypes.c_longlong)
+    S_ = L.host_plan_strips(S, len(shape), ora.ptr(nX), N, cpb, blk.ctypes.data_as(i64),
+                            lo.ctypes.data_as(i64), n.ctypes.data_as(i64))
+    Cw = int(np.prod(nX + 2))
+    nblocks = -(-Cw // cpb)
+    assert 1 <= S_ <= min(S, nblocks)
+    assert blk[0] == 0 and blk[S_] == nblocks and np.all(np.diff(blk[:S_ + 1]) >= 0)
+    nodes = N * N ** (len(shape) - 1)
+    nface = [np.prod([m + 1 if e == d else m for e, m in enumerate(shape)]) * nodes
+             for d in range(len(shape))]
+    off = np.concatenate([[0], np.cumsum(nface)])
+    seen = np.zeros(off[-1], dtype=np.int32)
+    for s in range(S_):
+        done = Cw if s == S_ - 1 else min(blk[s + 1] * cpb, Cw)
+        for d in range(3):
+            lo_, n_ = lo[s * 3 + d], n[s * 3 + d]
+            if d >= len(shape):
+                assert n_ == 0
+                continue
+            assert n_ >= 0 and off[d] <= lo_ and lo_ + n_ <= off[d + 1]
+            seen[lo_:lo_ + n_] += 1
+            for p in range(lo_, lo_ + n_, max(1, n_ // 50)):
+                c0, c1 = _face_cells(shape, N, d, p - off[d])
+                assert c0 < done and c1 < done, (s, d, p)
+    assert np.all(seen == 1)
 
 
 PRED_CASES = [("cattaneo", (10, 8), 2, True), ("cattaneo", (6, 5, 4), 2, True),
@@ -303,17 +380,18 @@ def test_device_step_fuzzed_small_grids(step_lib):
         # a periodic axis needs at least N cells (the reference's wrap rule)
         bt = [draw(st.integers(0, 1)) if n >= N else 0 for n in shape]
         return name, shape, N, flux, stiff, bt, draw(st.integers(0, 2 ** 16)), \
-            draw(st.integers(1, 3)), draw(st.sampled_from([0.5, 0.8, 0.9]))
+            draw(st.integers(1, 3)), draw(st.sampled_from([0.5, 0.8, 0.9])), \
+            draw(st.sampled_from([1, 2, 3, 8]))
 
     @hyp.settings(max_examples=40, deadline=None, derandomize=True,
                   suppress_health_check=list(hyp.HealthCheck))
     @hyp.given(problems())
     def check(prob):
-        name, shape, N, flux, stiff, bt, seed, K, cfl = prob
+        name, shape, N, flux, stiff, bt, seed, K, cfl, strips = prob
         u0 = _state(name, shape, seed)
         u_o, _, steps_o, t_o = ora.pde_solver(name, u0, 10.0, [1.0] * len(shape), bt, cfl, N,
                                               stiff=stiff, flux=flux, max_steps=K)
-        u, steps, t, _ = _run(step_lib, name, u0, N, bt, cfl, K, stiff, flux)
+        u, steps, t, _ = _run(step_lib, name, u0, N, bt, cfl, K, stiff, flux, strips=strips)
         assert steps == steps_o == K and t == t_o
         assert np.array_equal(u, u_o, equal_nan=True), (prob, np.abs(u - u_o).max())
 

@@ -310,3 +310,29 @@ def test_stiff128_matches_port_and_tight_reference():
     assert st["pred_fail"] == 0
     assert np.array_equal(q, u_o)
     assert np.all(l1(q, z["uK"]) <= 1e-8), l1(q, z["uK"])
+
+
+@pytest.mark.parametrize("case", [("cattaneo", (192, 160), 2, True, [0, 0]),
+                                  ("euler", (24, 20, 16), 2, False, [1, 0, 1]),
+                                  ("euler", (3000,), 3, False, [0])],
+                         ids=["stiff-192x160-N2", "euler-3d-N2", "euler-1d-N3"])
+def test_predictor_strips_equal_port(case):
+    """The predictor in strips with the faces of finished strips on a second
+    stream (the overlapped step the large workloads take by default): every
+    strip count gives the restatement's state bit for bit."""
+    name, shape, N, stiff, bt = case
+    u0 = _state(name, shape, 3)
+    if name == "cattaneo":
+        u0 = workloads.relaxation(shape[0], 2, seed=3)[:, :shape[1]].copy()
+    K = 4
+    u_o, _, steps, t_o = ora.pde_solver(name, u0, 10.0, [1.0] * len(shape), bt, 0.8, N,
+                                        stiff=stiff, max_steps=K, nthreads=os.cpu_count() or 1)
+    s = getattr(systems, name)(len(shape))
+    for strips in (1, 2, 8, 32, 0):
+        q = u0.copy()
+        st = {}
+        pde_solver(q, 10.0, [1.0] * len(shape), F=s.F, S=s.S if stiff else None,
+                   boundaryTypes=[["transitive", "periodic"][b] for b in bt],
+                   cfl=0.8, order=N, ndt=1, stiff=stiff, max_steps=K, stats=st, strips=strips)
+        assert st["steps"] == steps == K and st["t_final"] == t_o, strips
+        assert np.array_equal(q, u_o), (strips, np.abs(q - u_o).max())
