@@ -39,6 +39,11 @@ template <class Sys, int N> KernelSet make_kernel_set() {
     k.guess_no = MlpShape<Sys, N>::NO;
     k.guess_feat = MlpShape<Sys, N>::FEAT;
   }
+  if constexpr (FaceSplit<Sys>::OK) {
+    k.faces_pre.aot = (const void *)&k_faces_pre<Sys, N>;
+    k.faces_eig.aot = (const void *)&k_faces_eig<Sys, N>;
+    k.face_rec = FaceSplit<Sys>::REC;
+  }
   k.pred_threads = Cfg::THREADS;
   k.pred_cpb = Cfg::CPB;
   k.pred_smem = (size_t)Cfg::SMEM_DOUBLES * sizeof(double);

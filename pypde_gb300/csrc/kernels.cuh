@@ -1376,99 +1376,298 @@ struct FaceSpan {
   long long lo[3], n[3];
 };
 
+// Where face point p sits: its direction d, time node t, transverse node
+// idx, and the qh offsets of its low- and high-side cells at time node t.
+struct FaceAt {
+  int d, t, idx;
+  long long off0, off1;
+};
+
+template <class Sys, int N>
+__device__ __forceinline__ FaceAt face_at(long long p, const Geom &g,
+                                          const FaceIndex &fi) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
+  FaceAt f;
+  int d = 0;
+  while (d + 1 < D && p >= fi.off[d + 1])
+    d++;
+  long long r = p - fi.off[d];
+  f.d = d;
+  f.idx = (int)(r % Nd_);
+  r /= Nd_;
+  f.t = (int)(r % N);
+  long long face = r / N;
+  // low-side w-cell O from the face index (row-major over the face box)
+  int O[3];
+  long long rem = face;
+  for (int e = D - 1; e >= 0; e--) {
+    int ext = (e == d) ? g.nX[e] + 1 : g.nX[e];
+    int i = (int)(rem % ext);
+    rem /= ext;
+    O[e] = (e == d) ? i : i + 1;
+  }
+  long long qc0 = 0, qc1 = 0;
+  for (int e = 0; e < D; e++) {
+    qc0 = qc0 * g.nXw[e] + O[e];
+    qc1 = qc1 * g.nXw[e] + O[e] + (e == d);
+  }
+  f.off0 = (qc0 * N + f.t) * (long long)Nd * V;
+  f.off1 = (qc1 * N + f.t) * (long long)Nd * V;
+  return f;
+}
+
+// The quadrature weight of a face point times dt / (2 dX_d) (fv.cpp:
+// 176-193).
+template <class Sys, int N>
+__device__ __forceinline__ double face_weight(const FaceAt &f, double dt,
+                                              const Geom &g, const Tables &T) {
+  constexpr int D = Sys::NDIM;
+  double tmp = dt * T.wghts[f.t] / (2. * g.dX[f.d]);
+  int rm = f.idx;
+  int dg[3] = {0, 0, 0};
+  for (int e = D - 2; e >= 0; e--) {
+    dg[e] = rm % N;
+    rm /= N;
+  }
+  for (int e = 0; e < D - 1; e++)
+    tmp *= T.wghts[dg[e]];
+  return tmp;
+}
+
 // Face point p: its two face states, flux and path integral, and the
 // amounts written to contrib[p].
 template <class Sys, int N, int FLUX>
 __device__ __forceinline__ void face_point(long long p, const double *__restrict__ qh, double *__restrict__ contrib,
             const Geom &g, const Tables &T, const FaceIndex &fi, double dt) {
   constexpr int V = Sys::V, D = Sys::NDIM;
-  constexpr int Nd = IPow<N, D>::value, Nd_ = IPow<N, D - 1>::value;
-  {
+  constexpr int Nd = IPow<N, D>::value;
+  const FaceAt fa = face_at<Sys, N>(p, g, fi);
+  const int d = fa.d, idx = fa.idx;
+  const long long off0 = fa.off0, off1 = fa.off1;
+  const double *qh0 = qh + off0;
+  const double *qh1 = qh + off1;
+  double q0[V], q1[V], dq0[D * V], dq1[D * V];
+  endpoints<Sys, N>(qh0, T, d, 1, idx, q0, off0);
+  endpoints<Sys, N>(qh1, T, d, 0, idx, q1, off1);
+#pragma unroll
+  for (int k = 0; k < D * V; k++)
+    dq0[k] = dq1[k] = 0.0;
+  if (Sys::SECOND_ORDER) {
+    // gradients at the face point: endpoints of derivs of qh
+    // (fv.cpp:87-122), both rounded as the reference rounds them; its
+    // dqh stacks one qh-shaped block per direction d_
+    double tmpd[Nd * V];
+    for (int d_ = 0; d_ < D; d_++) {
+      for (int side = 0; side < 2; side++) {
+        const double *src = side ? qh1 : qh0;
+        int sd = 1;
+        for (int e = d_ + 1; e < D; e++)
+          sd *= N;
+        for (int n = 0; n < Nd; n++) {
+          int id = (n / sd) % N;
+          int base = n - id * sd;
+          for (int v = 0; v < V; v++) {
+            double s = 0;
+            for (int j = 0; j < N; j++)
+              s = s + T.dervals[id * N + j] * src[(base + j * sd) * V + v];
+            tmpd[n * V + v] = s / g.dX[d_];
+          }
+        }
+        double e_out[V];
+        const long long offd = d_ * g.Cw * (long long)(N * Nd * V);
+        endpoints<Sys, N>(tmpd, T, d, side ? 0 : 1, idx, e_out,
+                          offd + (side ? off1 : off0));
+        for (int v = 0; v < V; v++)
+          (side ? dq1 : dq0)[d_ * V + v] = e_out[v];
+      }
+    }
+  }
+  double f[V], b[V];
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    f[v] = b[v] = 0.0;
+  if (Sys::HAS_F) {
+    if (FLUX == 0)
+      rusanov_flux<Sys, N>(f, q0, q1, dq0, dq1, d, g.dX[d]);
+    else
+      eig_flux<Sys, N, FLUX>(f, q0, q1, dq0, dq1, d, g.dX[d], T);
+  }
+  if (Sys::HAS_B)
+    bint<Sys, N>(b, q0, q1, d, T);
+  const double tmp = face_weight<Sys, N>(fa, dt, g, T);
+  double *o = contrib + p * 2 * V;
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    o[v] = tmp * (b[v] + f[v]);
+    o[V + v] = tmp * (b[v] - f[v]);
+  }
+}
+
+// Face point q of a launch's span (direction by direction).
+__device__ __forceinline__ long long span_point(const FaceSpan &sp, int D,
+                                                long long q) {
+  int d = 0;
+  while (d + 1 < D && q >= sp.n[d])
+    q -= sp.n[d++];
+  return sp.lo[d] + q;
+}
+
+// ---------------------------------------------------------------------
+// The Rusanov faces of a first-order flux system without B in two
+// launches.  Alone, the face kernel needs 255 registers a thread: the face
+// states and fluxes stay live across the eigenvalue solves, which need
+// about 127 of their own.  Split, k_faces_pre (states, F, the FD
+// Jacobians) and k_faces_eig (max|eig|, the Rusanov flux, contrib) each
+// need far fewer, and an SM holds twice the warps.  k_faces_pre writes, per
+// face point j of a chunk, a record of REC doubles, component-major with
+// stride ch (coalesced):
+//   [0, MS^2)        the matrix max_abs_eig takes at the low-side state
+//   [MS^2, 2 MS^2)   the same at the high-side state
+//   qL (V), qR (V), fL + fR (V), the face weight, ok (1 + 2: the low /
+//   high side's matrix is the active block of max_abs_eigs, else
+//   k_faces_eig runs max_abs_eigs on the state itself)
+// Every value is computed by the same operations as in face_point, so the
+// results are the same bits.
+// ---------------------------------------------------------------------
+template <class S, class = void> struct EigBlock {
+  static constexpr int value = S::V;
+};
+template <class S>
+struct EigBlock<S, void_t_<decltype(S::EIG_ACTIVE)>> {
+  static constexpr int value = S::EIG_ACTIVE;
+};
+
+template <class Sys> struct FaceSplit {
+  static constexpr bool OK = Sys::HAS_F && !Sys::HAS_B && !Sys::SECOND_ORDER;
+  static constexpr int MS = EigBlock<Sys>::value;
+  static constexpr int REC = 2 * MS * MS + 3 * Sys::V + 2;
+};
+
+// The first half of max_abs_eigs: the matrix max_abs_eig takes and F(q)
+// in f0.  False when a system's active block does not apply (its passive
+// rows are not zero); max_abs_eigs must then run on q itself.
+template <class Sys>
+__device__ __forceinline__ bool eig_matrix(double *S, double *q, double *dq,
+                                           int d, double *f0) {
+  if constexpr (HasEigActive<Sys>::value) {
+    return fd_jacobian_active<Sys>(S, q, dq, d, f0);
+  } else {
+    fd_jacobian<Sys>(S, q, dq, d, false, f0);
+    return true;
+  }
+}
+
+// Points [q0, q0 + min(ch, total - q0)) of span sp.
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    k_faces_pre(const double *__restrict__ qh, double *__restrict__ rec, long long ch,
+                const __grid_constant__ Geom g, const __grid_constant__ Tables T,
+                const __grid_constant__ FaceIndex fi, DevState *st,
+                const __grid_constant__ FaceSpan sp, long long q0) {
+  constexpr int V = Sys::V, D = Sys::NDIM, MS = FaceSplit<Sys>::MS;
+  if (!step_active(st))
+    return;
+  const double dt = st->dt;
+  const long long total = sp.n[0] + sp.n[1] + sp.n[2];
+  const long long n = (total - q0 < ch) ? total - q0 : ch;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long p = span_point(sp, D, q0 + j);
+    const FaceAt fa = face_at<Sys, N>(p, g, fi);
+    double *r = rec + j;
+    double q[V], dq[D * V], S[MS * MS], fL[V], fR[V];
+#pragma unroll
+    for (int k = 0; k < D * V; k++)
+      dq[k] = 0.0;
+    // one side at a time, each written out before the next is formed
+    endpoints<Sys, N>(qh + fa.off0, T, fa.d, 1, fa.idx, q, fa.off0);
+    const bool okL = eig_matrix<Sys>(S, q, dq, fa.d, fL);
+#pragma unroll
+    for (int k = 0; k < MS * MS; k++)
+      r[k * ch] = S[k];
+    double *rs = r + 2 * MS * MS * ch;
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      rs[v * ch] = q[v];
+    endpoints<Sys, N>(qh + fa.off1, T, fa.d, 0, fa.idx, q, fa.off1);
+    const bool okR = eig_matrix<Sys>(S, q, dq, fa.d, fR);
+#pragma unroll
+    for (int k = 0; k < MS * MS; k++)
+      r[(MS * MS + k) * ch] = S[k];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      rs[(V + v) * ch] = q[v];
+      rs[(2 * V + v) * ch] = fL[v] + fR[v];
+    }
+    rs[3 * V * ch] = face_weight<Sys, N>(fa, dt, g, T);
+    rs[(3 * V + 1) * ch] = (double)((okL ? 1 : 0) + (okR ? 2 : 0));
+  }
+}
+
+// max_abs_eigs on a face state read from a record (the rare side whose
+// active block did not apply), out of line so that the eigenvalue kernel
+// keeps no state for it.
+template <class Sys>
+__device__ __noinline__ double max_abs_eigs_rec(const double *rq, long long ch,
+                                                int d) {
+  constexpr int V = Sys::V, D = Sys::NDIM;
+  double q[V], dq[D * V];
+  for (int v = 0; v < V; v++)
+    q[v] = rq[v * ch];
+  for (int k = 0; k < D * V; k++)
+    dq[k] = 0.0;
+  return max_abs_eigs<Sys>(q, dq, d);
+}
+
+// The records of k_faces_pre for the same points: max|eig| on both sides,
+// the Rusanov flux (fluxes.cpp:86-101, as rusanov_flux) and contrib.
+template <class Sys, int N>
+__global__ void __launch_bounds__(128, 4)
+    k_faces_eig(const double *__restrict__ rec, long long ch, double *__restrict__ contrib,
+                const __grid_constant__ FaceIndex fi, DevState *st,
+                const __grid_constant__ FaceSpan sp, long long q0) {
+  constexpr int V = Sys::V, D = Sys::NDIM, MS = FaceSplit<Sys>::MS;
+  if (!step_active(st))
+    return;
+  const long long total = sp.n[0] + sp.n[1] + sp.n[2];
+  const long long n = (total - q0 < ch) ? total - q0 : ch;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long p = span_point(sp, D, q0 + j);
     int d = 0;
     while (d + 1 < D && p >= fi.off[d + 1])
       d++;
-    long long r = p - fi.off[d];
-    int idx = (int)(r % Nd_);
-    r /= Nd_;
-    int t = (int)(r % N);
-    long long face = r / N;
-    // low-side w-cell O from the face index (row-major over the face box)
-    int O[3];
-    long long rem = face;
-    for (int e = D - 1; e >= 0; e--) {
-      int ext = (e == d) ? g.nX[e] + 1 : g.nX[e];
-      int i = (int)(rem % ext);
-      rem /= ext;
-      O[e] = (e == d) ? i : i + 1;
-    }
-    long long qc0 = 0, qc1 = 0;
-    for (int e = 0; e < D; e++) {
-      qc0 = qc0 * g.nXw[e] + O[e];
-      qc1 = qc1 * g.nXw[e] + O[e] + (e == d);
-    }
-    const long long off0 = (qc0 * N + t) * (long long)Nd * V;
-    const long long off1 = (qc1 * N + t) * (long long)Nd * V;
-    const double *qh0 = qh + off0;
-    const double *qh1 = qh + off1;
-    double q0[V], q1[V], dq0[D * V], dq1[D * V];
-    endpoints<Sys, N>(qh0, T, d, 1, idx, q0, off0);
-    endpoints<Sys, N>(qh1, T, d, 0, idx, q1, off1);
+    const double *r = rec + j;
+    const double *rs = r + 2 * MS * MS * ch;
+    const int ok = (int)rs[(3 * V + 1) * ch];
+    double m1, m2;
+    {
+      double S[MS * MS];
 #pragma unroll
-    for (int k = 0; k < D * V; k++)
-      dq0[k] = dq1[k] = 0.0;
-    if (Sys::SECOND_ORDER) {
-      // gradients at the face point: endpoints of derivs of qh
-      // (fv.cpp:87-122), both rounded as the reference rounds them; its
-      // dqh stacks one qh-shaped block per direction d_
-      double tmpd[Nd * V];
-      for (int d_ = 0; d_ < D; d_++) {
-        for (int side = 0; side < 2; side++) {
-          const double *src = side ? qh1 : qh0;
-          int sd = 1;
-          for (int e = d_ + 1; e < D; e++)
-            sd *= N;
-          for (int n = 0; n < Nd; n++) {
-            int id = (n / sd) % N;
-            int base = n - id * sd;
-            for (int v = 0; v < V; v++) {
-              double s = 0;
-              for (int j = 0; j < N; j++)
-                s = s + T.dervals[id * N + j] * src[(base + j * sd) * V + v];
-              tmpd[n * V + v] = s / g.dX[d_];
-            }
-          }
-          double e_out[V];
-          const long long offd = d_ * g.Cw * (long long)(N * Nd * V);
-          endpoints<Sys, N>(tmpd, T, d, side ? 0 : 1, idx, e_out,
-                            offd + (side ? off1 : off0));
-          for (int v = 0; v < V; v++)
-            (side ? dq1 : dq0)[d_ * V + v] = e_out[v];
-        }
-      }
+      for (int k = 0; k < MS * MS; k++)
+        S[k] = r[k * ch];
+      m1 = (ok & 1) ? max_abs_eig<MS>(S) : max_abs_eigs_rec<Sys>(rs, ch, d);
     }
+    {
+      double S[MS * MS];
+#pragma unroll
+      for (int k = 0; k < MS * MS; k++)
+        S[k] = r[(MS * MS + k) * ch];
+      m2 = (ok & 2) ? max_abs_eig<MS>(S)
+                    : max_abs_eigs_rec<Sys>(rs + V * ch, ch, d);
+    }
+    const double m = fmax(m1, m2);
+    const double tmp = rs[3 * V * ch];
     double f[V], b[V];
 #pragma unroll
+    for (int v = 0; v < V; v++) {
+      b[v] = 0.0;
+      f[v] = m * (rs[v * ch] - rs[(V + v) * ch]);
+    }
+#pragma unroll
     for (int v = 0; v < V; v++)
-      f[v] = b[v] = 0.0;
-    if (Sys::HAS_F) {
-      if (FLUX == 0)
-        rusanov_flux<Sys, N>(f, q0, q1, dq0, dq1, d, g.dX[d]);
-      else
-        eig_flux<Sys, N, FLUX>(f, q0, q1, dq0, dq1, d, g.dX[d], T);
-    }
-    if (Sys::HAS_B)
-      bint<Sys, N>(b, q0, q1, d, T);
-    double tmp = dt * T.wghts[t] / (2. * g.dX[d]);
-    {
-      int rm = idx;
-      int dg[3] = {0, 0, 0};
-      for (int e = D - 2; e >= 0; e--) {
-        dg[e] = rm % N;
-        rm /= N;
-      }
-      for (int e = 0; e < D - 1; e++)
-        tmp *= T.wghts[dg[e]];
-    }
+      f[v] += rs[(2 * V + v) * ch];
     double *o = contrib + p * 2 * V;
 #pragma unroll
     for (int v = 0; v < V; v++) {
@@ -1503,13 +1702,8 @@ __global__ void __launch_bounds__(128)
   for (int d = 0; d < Sys::NDIM; d++)
     total += sp.n[d];
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-       q += (long long)gridDim.x * blockDim.x) {
-    long long r = q;
-    int d = 0;
-    while (d + 1 < Sys::NDIM && r >= sp.n[d])
-      r -= sp.n[d++];
-    face_point<Sys, N, FLUX>(sp.lo[d] + r, qh, contrib, g, T, fi, dt);
-  }
+       q += (long long)gridDim.x * blockDim.x)
+    face_point<Sys, N, FLUX>(span_point(sp, Sys::NDIM, q), qh, contrib, g, T, fi, dt);
 }
 
 // ---------------------------------------------------------------------

@@ -172,6 +172,7 @@ static cudaError_t ensure(Buf &b, size_t bytes) {
 }
 struct Arena {
   Buf u, uprev, ub, tmpA, tmpB, w, qh, contrib, cen, ring, state, wprod;
+  Buf facerec; // records between k_faces_pre and k_faces_eig
   DevState *host_state = nullptr; // pinned
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;    // faces of finished predictor strips
@@ -351,7 +352,14 @@ struct StepCtx {
   const StripPlan *plan;
   cudaStream_t side;
   cudaEvent_t *strip_ev;
+  // Rusanov faces in two launches, face_ch points at a time (null: one)
+  double *facerec;
+  long long face_ch;
 };
+
+// Face points per k_faces_pre / k_faces_eig pair: the record buffer holds
+// this many (73 doubles each for the 2-D relaxation system: 2.4 GB).
+constexpr long long FACE_CHUNK = 1LL << 22;
 
 // Whether a step runs its predictor in strips with the faces of finished
 // strips on the side stream (not in the stage-timing mode, whose events
@@ -382,6 +390,10 @@ static long long span_points(const FaceSpan &sp) {
   return sp.n[0] + sp.n[1] + sp.n[2];
 }
 
+static bool split_faces(const StepCtx &c) {
+  return c.flux == 0 && c.facerec && c.ks->face_rec > 0;
+}
+
 static cudaError_t enqueue_faces(const StepCtx &c, cudaStream_t s,
                                  const FaceSpan &span) {
   const long long n = span_points(span);
@@ -391,10 +403,38 @@ static cudaError_t enqueue_faces(const StepCtx &c, cudaStream_t s,
   Tables T = c.T;
   FaceIndex fi = c.fi;
   FaceSpan sp = span;
+  if (split_faces(c)) { // chunks of face_ch points through the records
+    long long ch = c.face_ch;
+    for (long long q0 = 0; q0 < n; q0 += ch) {
+      const long long m = (n - q0 < ch) ? n - q0 : ch;
+      const dim3 grid(grid_for(m, 128, 152 * 256));
+      void *pa[] = {(void *)&c.qh, (void *)&c.facerec, (void *)&ch,
+                    (void *)&g,    (void *)&T,         (void *)&fi,
+                    (void *)&c.st, (void *)&sp,        (void *)&q0};
+      cudaError_t e = launch(c.ks->faces_pre, grid, dim3(128), 0, s, pa);
+      if (e != cudaSuccess)
+        return e;
+      void *ea[] = {(void *)&c.facerec, (void *)&ch, (void *)&c.contrib,
+                    (void *)&fi,        (void *)&c.st, (void *)&sp,
+                    (void *)&q0};
+      e = launch(c.ks->faces_eig, grid, dim3(128), 0, s, ea);
+      if (e != cudaSuccess)
+        return e;
+    }
+    return cudaSuccess;
+  }
   void *a[] = {(void *)&c.qh, (void *)&c.contrib, (void *)&g, (void *)&T,
                (void *)&fi,   (void *)&c.st,      (void *)&sp};
   return launch(c.ks->faces_flux[c.flux], dim3(grid_for(n, 128, 152 * 256)),
                 dim3(128), 0, s, a);
+}
+
+// Launches enqueue_faces makes for a span.
+static int face_launches(const StepCtx &c, const FaceSpan &sp) {
+  const long long n = span_points(sp);
+  if (n == 0)
+    return 0;
+  return split_faces(c) ? (int)(2 * ((n + c.face_ch - 1) / c.face_ch)) : 1;
 }
 
 // The warm-start network's guess of qh (learned form): qh = w + its
@@ -480,12 +520,12 @@ static cudaError_t enqueue_fv(const StepCtx &c, cudaStream_t s) {
 
 // Kernels one step launches (the count reported as kernel_launches).
 static int kernels_per_step(const StepCtx &c, bool profile) {
-  int pred = 1, faces = c.faces ? 1 : 0;
+  int pred = 1, faces = c.faces ? face_launches(c, whole_span(c)) : 0;
   if (overlapped(c, profile)) {
     pred = faces = 0;
     for (int i = 0; i < c.plan->S; i++) {
       pred += c.plan->blk[i + 1] > c.plan->blk[i];
-      faces += span_points(strip_span(*c.plan, i)) > 0;
+      faces += face_launches(c, strip_span(*c.plan, i));
     }
   }
   // step begin, copy of u, ghost fill, CFL, dt, gather, step end, snapshot
@@ -775,19 +815,26 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
     const int cpb = predictor_cpb(c);
     const long long blocks = (c.g.Cw + cpb - 1) / cpb;
     // Automatic: 4 strips for the Newton predictor when each holds at least
-    // 4 blocks per SM (1024^2 relaxation: 85.0 ms a step against 90.0 in
-    // one launch each; 8 strips 85.2, 16 strips 85.5).  The Picard
-    // predictor is a small part of its step and gains nothing (512^2 shear
-    // layer, N=3: 13.9 ms with 8 strips against 13.65).
+    // 4 blocks per SM and the faces run as the one-launch k_faces (255
+    // registers, 2 blocks an SM: 1024^2 relaxation with that kernel, 85.0
+    // ms a step against 90.0 without strips; 8 strips 85.2, 16 strips
+    // 85.5).  The two-launch Rusanov faces fill the SMs themselves (128
+    // registers, 4 blocks an SM) and lose with strips (79.3 ms a step
+    // without, 83.6 with 4, 83.8 with 2).  The Picard predictor is a small
+    // part of its step and gains nothing (512^2 shear layer, N=3: 13.9 ms
+    // with 8 strips against 13.65).
+    const bool two_launch_faces = c.faces && c.flux == 0 && c.ks->face_rec > 0;
     int S = a.strips;
     if (S == 0)
-      S = (c.stiff && blocks >= 4LL * 152 * 4) ? 4 : 1;
+      S = (c.stiff && !two_launch_faces && blocks >= 4LL * 152 * 4) ? 4 : 1;
     plan_strips(S, a.ndim, c.g.nX, c.g.nXw, c.g.Cw, cpb, c.N, c.fi.off,
                 &plan);
   }
   c.plan = &plan;
   c.side = ar->side;
   c.strip_ev = ar->strip_ev;
+  c.facerec = nullptr;
+  c.face_ch = 0;
   const int V = c.V, N = c.N, Nd = ipow(N, a.ndim);
   long long usz = c.g.C * V;
   int K = a.steps_per_graph;
@@ -807,6 +854,12 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   CK(ensure(ar->contrib, (c.faces ? c.fi.off[a.ndim] : 1) * 2 * V * 8));
   CK(ensure(ar->cen, (c.centers ? c.g.C * N * Nd : 1) * V * 8));
   CK(ensure(ar->ring, c.ring * usz * 8));
+  if (c.faces && c.flux == 0 && c.ks->face_rec > 0) {
+    const long long pts = c.fi.off[a.ndim];
+    c.face_ch = pts < FACE_CHUNK ? pts : FACE_CHUNK;
+    CK(ensure(ar->facerec, (long long)c.ks->face_rec * c.face_ch * 8));
+    c.facerec = (double *)ar->facerec.p;
+  }
   CK(ensure(ar->state, sizeof(DevState)));
   CK(ensure(ar->wprod, Nd * 8));
   c.u = (double *)ar->u.p;

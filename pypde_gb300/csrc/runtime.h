@@ -36,6 +36,11 @@ struct KernelSet {
   KFunc guess, kb_guess;
   size_t guess_smem = 0;
   int guess_k1 = 0, guess_no = 0, guess_feat = 0;
+  // Rusanov faces in two launches (k_faces_pre, k_faces_eig) through a
+  // record buffer of face_rec doubles per face point; face_rec == 0: the
+  // one-launch k_faces only
+  KFunc faces_pre, faces_eig;
+  int face_rec = 0;
 };
 
 struct SystemDesc {

@@ -504,11 +504,28 @@ long long run_steps(double *u, int ndim, const int *nX, const int *bt,
           sp.n[d] = plan.n[i][d];
           np += sp.n[d];
         }
-        if (faces && np > 0)
+        if (faces && np > 0 && FLUX == 0 && FaceSplit<Sys>::OK) {
+          // two launches per chunk through the records, as enqueue_faces;
+          // a small odd chunk makes chunks straddle the directions
+          const long long ch = 61;
+          std::vector<double> rec((size_t)FaceSplit<Sys>::REC * ch);
+          for (long long q0 = 0; q0 < np; q0 += ch) {
+            const long long m = np - q0 < ch ? np - q0 : ch;
+            emu::launch(grid_for(m, 128, 152 * 256), 128, 0, [&] {
+              k_faces_pre<Sys, N>(qh.data(), rec.data(), ch, g, T, fi, &st,
+                                  sp, q0);
+            });
+            emu::launch(grid_for(m, 128, 152 * 256), 128, 0, [&] {
+              k_faces_eig<Sys, N>(rec.data(), ch, contrib.data(), fi, &st,
+                                  sp, q0);
+            });
+          }
+        } else if (faces && np > 0) {
           emu::launch(grid_for(np, 128, 152 * 256), 128, 0, [&] {
             k_faces<Sys, N, FLUX>(qh.data(), contrib.data(), g, T, fi, &st,
                                   sp);
           });
+        }
       }
     }
     if (centers)
