@@ -34,7 +34,8 @@ Our arm prints one JSON line:
                from a pinned host array: host->device copy of the state,
                K steps, device->host copy of the final state and the
                snapshot row, all inside the timed region
-  roofline     the dominant kernel (the larger of k_faces and the predictor,
+  roofline     the dominant kernel (the larger of the faces stage, k_faces or
+               the Rusanov pair k_faces_pre + k_faces_eig, and the predictor,
                k_newton or k_predictor; FP64-bound): algorithmic
                FP64 flops of one launch (pypde_gb300.work_model) / its mean
                launch time measured here with CUDA events, against the FP64
@@ -72,13 +73,15 @@ WORKLOADS = {
     "shear": ("euler", 2, 512, 3, 0.8, False),
 }
 
-# DRAM bytes (read + write) of one k_faces launch per face point, from ncu
-# captures of smaller grids of the same workload (a full-size launch is
-# scaled by its face points): the relaxation system at 512^2, N=2 (237.7 MB
-# read + 366.3 MB written over 2,101,248 face points); the Euler shear layer
-# at 256^2, N=3 (108 + 67 MB over 1,184,256).  The command lines are in
-# the k_faces summaries under profiles/.
-FACES_DRAM_BYTES_PER_POINT = {("cattaneo", 2, 2): 287.5, ("euler", 2, 3): 147.8}
+# DRAM bytes (read + write) of the faces stage per face point (the Rusanov
+# pair k_faces_pre + k_faces_eig), from ncu captures of smaller grids of
+# the same workload (a full-size stage is scaled by its face points): the
+# relaxation system at 512^2, N=2 (k_faces_pre 0.241 GB read + 1.633 GB
+# written, k_faces_eig 1.306 + 1.412 GB, over 2,101,248 face points).  Most
+# of it is the records between the two kernels (73 doubles written and read
+# per face point) and the eigen solver's stack lines evicted to DRAM.  The
+# command lines are in the k_faces summaries under profiles/.
+FACES_DRAM_BYTES_PER_POINT = {("cattaneo", 2, 2): 2185.4}
 
 
 def parse():
@@ -526,9 +529,9 @@ def run_ours(args, ws, rank, local):
     per_point = FACES_DRAM_BYTES_PER_POINT.get((args.system, nd, N))
     traffic = None if per_point is None else per_point * fpts
     traffic_src = ("none: no ncu capture of this workload" if per_point is None else
-                   f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_faces launch "
-                   f"of this workload captured on another grid size, {per_point:.0f} B per "
-                   f"face point, "
+                   f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_faces_pre + "
+                   f"k_faces_eig pair of this workload captured on another grid size, "
+                   f"{per_point:.0f} B per face point, "
                    f"times {fpts} face points; the algorithmic bytes are "
                    f"{work_model.faces_bytes_per_launch([n] * nd, V, N):.3e}")
     flops = work_model.step_flops(args.system, [n] * nd, V, N, its, stiff=args.stiff)
@@ -567,7 +570,8 @@ def run_ours(args, ws, rank, local):
                         "region (from the state after the warm-up): the state goes in "
                         "once, the final state plus the snapshot row come out once"},
         "roofline": None,
-        "roofline_faces": {"bound": "fp64", "kernel": "k_faces", "achieved": achieved,
+        "roofline_faces": {"bound": "fp64", "kernel": "k_faces_pre + k_faces_eig (Rusanov "
+                           "faces in two launches)", "achieved": achieved,
                      "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
                      "traffic": traffic,
                      "traffic_source": traffic_src,
@@ -578,7 +582,10 @@ def run_ours(args, ws, rank, local):
                              "Hessenberg + Francis QR of the m x m active block of the flux "
                              "Jacobian (m = V, or V minus the system's passive variables); "
                              "the kernel's mixed-precision eigensolver does less FP64 work "
-                             "than that"},
+                             "than that; launch_ms is the faces stage timed alone (both "
+                             "kernels); the records between the two kernels add 1168 B of "
+                             "DRAM traffic per face point to a stage that is FP64-bound "
+                             "(DRAM under 10% of its peak)"},
         "stage_ms_per_step": {k: 1e3 * v / ksteps for k, v in stage_s.items()},
         "step_fp64_tflops": sum(flops.values()) / (sec / args.steps) / 1e12,
         "fp64_pipes": {"fma_tflops": peak.value, "dmma_tflops": dmma.value,
