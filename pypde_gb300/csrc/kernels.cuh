@@ -1558,6 +1558,42 @@ __device__ __forceinline__ bool eig_matrix(double *S, double *q, double *dq,
   }
 }
 
+// The record of face point p at r, components ch apart.
+template <class Sys, int N>
+__device__ __forceinline__ void face_pre_point(long long p, const double *__restrict__ qh,
+                                               double *r, long long ch, const Geom &g,
+                                               const Tables &T, const FaceIndex &fi,
+                                               double dt) {
+  constexpr int V = Sys::V, D = Sys::NDIM, MS = FaceSplit<Sys>::MS;
+  const FaceAt fa = face_at<Sys, N>(p, g, fi);
+  double q[V], dq[D * V], S[MS * MS], fL[V], fR[V];
+#pragma unroll
+  for (int k = 0; k < D * V; k++)
+    dq[k] = 0.0;
+  // one side at a time, each written out before the next is formed
+  endpoints<Sys, N>(qh + fa.off0, T, fa.d, 1, fa.idx, q, fa.off0);
+  const bool okL = eig_matrix<Sys>(S, q, dq, fa.d, fL);
+#pragma unroll
+  for (int k = 0; k < MS * MS; k++)
+    r[k * ch] = S[k];
+  double *rs = r + 2 * MS * MS * ch;
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    rs[v * ch] = q[v];
+  endpoints<Sys, N>(qh + fa.off1, T, fa.d, 0, fa.idx, q, fa.off1);
+  const bool okR = eig_matrix<Sys>(S, q, dq, fa.d, fR);
+#pragma unroll
+  for (int k = 0; k < MS * MS; k++)
+    r[(MS * MS + k) * ch] = S[k];
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    rs[(V + v) * ch] = q[v];
+    rs[(2 * V + v) * ch] = fL[v] + fR[v];
+  }
+  rs[3 * V * ch] = face_weight<Sys, N>(fa, dt, g, T);
+  rs[(3 * V + 1) * ch] = (double)((okL ? 1 : 0) + (okR ? 2 : 0));
+}
+
 // Points [q0, q0 + min(ch, total - q0)) of span sp.
 template <class Sys, int N>
 __global__ void __launch_bounds__(128)
@@ -1565,44 +1601,15 @@ __global__ void __launch_bounds__(128)
                 const __grid_constant__ Geom g, const __grid_constant__ Tables T,
                 const __grid_constant__ FaceIndex fi, DevState *st,
                 const __grid_constant__ FaceSpan sp, long long q0) {
-  constexpr int V = Sys::V, D = Sys::NDIM, MS = FaceSplit<Sys>::MS;
   if (!step_active(st))
     return;
   const double dt = st->dt;
   const long long total = sp.n[0] + sp.n[1] + sp.n[2];
   const long long n = (total - q0 < ch) ? total - q0 : ch;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n;
-       j += (long long)gridDim.x * blockDim.x) {
-    const long long p = span_point(sp, D, q0 + j);
-    const FaceAt fa = face_at<Sys, N>(p, g, fi);
-    double *r = rec + j;
-    double q[V], dq[D * V], S[MS * MS], fL[V], fR[V];
-#pragma unroll
-    for (int k = 0; k < D * V; k++)
-      dq[k] = 0.0;
-    // one side at a time, each written out before the next is formed
-    endpoints<Sys, N>(qh + fa.off0, T, fa.d, 1, fa.idx, q, fa.off0);
-    const bool okL = eig_matrix<Sys>(S, q, dq, fa.d, fL);
-#pragma unroll
-    for (int k = 0; k < MS * MS; k++)
-      r[k * ch] = S[k];
-    double *rs = r + 2 * MS * MS * ch;
-#pragma unroll
-    for (int v = 0; v < V; v++)
-      rs[v * ch] = q[v];
-    endpoints<Sys, N>(qh + fa.off1, T, fa.d, 0, fa.idx, q, fa.off1);
-    const bool okR = eig_matrix<Sys>(S, q, dq, fa.d, fR);
-#pragma unroll
-    for (int k = 0; k < MS * MS; k++)
-      r[(MS * MS + k) * ch] = S[k];
-#pragma unroll
-    for (int v = 0; v < V; v++) {
-      rs[(V + v) * ch] = q[v];
-      rs[(2 * V + v) * ch] = fL[v] + fR[v];
-    }
-    rs[3 * V * ch] = face_weight<Sys, N>(fa, dt, g, T);
-    rs[(3 * V + 1) * ch] = (double)((okL ? 1 : 0) + (okR ? 2 : 0));
-  }
+       j += (long long)gridDim.x * blockDim.x)
+    face_pre_point<Sys, N>(span_point(sp, Sys::NDIM, q0 + j), qh, rec + j, ch, g,
+                           T, fi, dt);
 }
 
 // max_abs_eigs on a face state read from a record (the rare side whose
@@ -1620,61 +1627,68 @@ __device__ __noinline__ double max_abs_eigs_rec(const double *rq, long long ch,
   return max_abs_eigs<Sys>(q, dq, d);
 }
 
-// The records of k_faces_pre for the same points: max|eig| on both sides,
-// the Rusanov flux (fluxes.cpp:86-101, as rusanov_flux) and contrib.
+// Face point p from its record at r (components ch apart): max|eig| on
+// both sides, the Rusanov flux (fluxes.cpp:86-101, as rusanov_flux) and
+// contrib[p].
+template <class Sys, int N>
+__device__ __forceinline__ void face_eig_point(long long p, const double *r, long long ch,
+                                               double *__restrict__ contrib,
+                                               const FaceIndex &fi) {
+  constexpr int V = Sys::V, D = Sys::NDIM, MS = FaceSplit<Sys>::MS;
+  int d = 0;
+  while (d + 1 < D && p >= fi.off[d + 1])
+    d++;
+  const double *rs = r + 2 * MS * MS * ch;
+  const int ok = (int)rs[(3 * V + 1) * ch];
+  double m1, m2;
+  {
+    double S[MS * MS];
+#pragma unroll
+    for (int k = 0; k < MS * MS; k++)
+      S[k] = r[k * ch];
+    m1 = (ok & 1) ? max_abs_eig<MS>(S) : max_abs_eigs_rec<Sys>(rs, ch, d);
+  }
+  {
+    double S[MS * MS];
+#pragma unroll
+    for (int k = 0; k < MS * MS; k++)
+      S[k] = r[(MS * MS + k) * ch];
+    m2 = (ok & 2) ? max_abs_eig<MS>(S)
+                  : max_abs_eigs_rec<Sys>(rs + V * ch, ch, d);
+  }
+  const double m = fmax(m1, m2);
+  const double tmp = rs[3 * V * ch];
+  double f[V], b[V];
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    b[v] = 0.0;
+    f[v] = m * (rs[v * ch] - rs[(V + v) * ch]);
+  }
+#pragma unroll
+  for (int v = 0; v < V; v++)
+    f[v] += rs[(2 * V + v) * ch];
+  double *o = contrib + p * 2 * V;
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    o[v] = tmp * (b[v] + f[v]);
+    o[V + v] = tmp * (b[v] - f[v]);
+  }
+}
+
+// The records of k_faces_pre for the same points.
 template <class Sys, int N>
 __global__ void __launch_bounds__(128, 4)
     k_faces_eig(const double *__restrict__ rec, long long ch, double *__restrict__ contrib,
                 const __grid_constant__ FaceIndex fi, DevState *st,
                 const __grid_constant__ FaceSpan sp, long long q0) {
-  constexpr int V = Sys::V, D = Sys::NDIM, MS = FaceSplit<Sys>::MS;
   if (!step_active(st))
     return;
   const long long total = sp.n[0] + sp.n[1] + sp.n[2];
   const long long n = (total - q0 < ch) ? total - q0 : ch;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n;
-       j += (long long)gridDim.x * blockDim.x) {
-    const long long p = span_point(sp, D, q0 + j);
-    int d = 0;
-    while (d + 1 < D && p >= fi.off[d + 1])
-      d++;
-    const double *r = rec + j;
-    const double *rs = r + 2 * MS * MS * ch;
-    const int ok = (int)rs[(3 * V + 1) * ch];
-    double m1, m2;
-    {
-      double S[MS * MS];
-#pragma unroll
-      for (int k = 0; k < MS * MS; k++)
-        S[k] = r[k * ch];
-      m1 = (ok & 1) ? max_abs_eig<MS>(S) : max_abs_eigs_rec<Sys>(rs, ch, d);
-    }
-    {
-      double S[MS * MS];
-#pragma unroll
-      for (int k = 0; k < MS * MS; k++)
-        S[k] = r[(MS * MS + k) * ch];
-      m2 = (ok & 2) ? max_abs_eig<MS>(S)
-                    : max_abs_eigs_rec<Sys>(rs + V * ch, ch, d);
-    }
-    const double m = fmax(m1, m2);
-    const double tmp = rs[3 * V * ch];
-    double f[V], b[V];
-#pragma unroll
-    for (int v = 0; v < V; v++) {
-      b[v] = 0.0;
-      f[v] = m * (rs[v * ch] - rs[(V + v) * ch]);
-    }
-#pragma unroll
-    for (int v = 0; v < V; v++)
-      f[v] += rs[(2 * V + v) * ch];
-    double *o = contrib + p * 2 * V;
-#pragma unroll
-    for (int v = 0; v < V; v++) {
-      o[v] = tmp * (b[v] + f[v]);
-      o[V + v] = tmp * (b[v] - f[v]);
-    }
-  }
+       j += (long long)gridDim.x * blockDim.x)
+    face_eig_point<Sys, N>(span_point(sp, Sys::NDIM, q0 + j), rec + j, ch, contrib,
+                           fi);
 }
 
 // Every face point of the grid (one tile of a batched launch).
