@@ -21,6 +21,10 @@ struct BatchProblem {
   FaceIndex fi;
   int N, V;
   double *u, *ub, *w, *qh, *contrib, *cen, *wprod;
+  // records of the two-launch Rusanov faces (kb_faces_pre, kb_faces_eig):
+  // REC doubles per face point, component-major with the problem's face
+  // points as stride; null where the faces run as one launch
+  double *rec;
   // WENO pass d reads win[d] and writes wout[d] (the last writes w)
   const double *win[3];
   double *wout[3];
@@ -129,6 +133,38 @@ __global__ void __launch_bounds__(128)
   drain(q, per_pop, [&](int p, VBlock vb) {
     const BatchProblem &b = P[p];
     k_faces_body<Sys, N, FLUX>(vb, b.qh, b.contrib, b.g, T, b.fi, b.st);
+  });
+}
+
+// The Rusanov faces of a first-order flux system without B in two batched
+// launches, as the one-problem step runs them (k_faces_pre, k_faces_eig):
+// tile = 128 face points of one problem.
+template <class Sys, int N>
+__global__ void __launch_bounds__(128)
+    kb_faces_pre(const BatchProblem *P, TileQueue q, int per_pop,
+                 const __grid_constant__ Tables T) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    if (!step_active(b.st))
+      return;
+    const long long n = b.fi.off[Sys::NDIM];
+    const long long pt = vb.b * 128 + threadIdx.x;
+    if (pt < n)
+      face_pre_point<Sys, N>(pt, b.qh, b.rec + pt, n, b.g, T, b.fi, b.st->dt);
+  });
+}
+
+template <class Sys, int N>
+__global__ void __launch_bounds__(128, 4)
+    kb_faces_eig(const BatchProblem *P, TileQueue q, int per_pop) {
+  drain(q, per_pop, [&](int p, VBlock vb) {
+    const BatchProblem &b = P[p];
+    if (!step_active(b.st))
+      return;
+    const long long n = b.fi.off[Sys::NDIM];
+    const long long pt = vb.b * 128 + threadIdx.x;
+    if (pt < n)
+      face_eig_point<Sys, N>(pt, b.rec + pt, n, b.contrib, b.fi);
   });
 }
 

@@ -43,6 +43,8 @@ template <class Sys, int N> KernelSet make_kernel_set() {
     k.faces_pre.aot = (const void *)&k_faces_pre<Sys, N>;
     k.faces_eig.aot = (const void *)&k_faces_eig<Sys, N>;
     k.face_rec = FaceSplit<Sys>::REC;
+    k.kb_faces_pre.aot = (const void *)&kb_faces_pre<Sys, N>;
+    k.kb_faces_eig.aot = (const void *)&kb_faces_eig<Sys, N>;
   }
   k.pred_threads = Cfg::THREADS;
   k.pred_cpb = Cfg::CPB;

@@ -1079,9 +1079,17 @@ struct BatchGroup {
   int threads[BS_COUNT] = {};
   size_t smem[BS_COUNT] = {};
   int resident[BS_COUNT] = {};
+  // the faces stage in two launches (kb_faces_pre as fn[BS_FACES], then
+  // this one over the same tiles, with its own queue)
+  KFunc faces_eig;
+  int faces_eig_resident = 0;
   bool guess = false; // a learned warm start for this order
   MlpModel model;
 };
+
+// Queue heads per group: one per stage, and one for the second launch of
+// the two-launch faces.
+constexpr int HEADS = BS_COUNT + 1;
 
 struct BatchCtx {
   std::vector<BatchGroup> G;
@@ -1099,7 +1107,7 @@ struct BatchCtx {
 static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
                                       cudaEvent_t *ev = nullptr) {
   cudaError_t e = cudaMemsetAsync(
-      c.heads, 0, sizeof(unsigned long long) * c.G.size() * BS_COUNT, s);
+      c.heads, 0, sizeof(unsigned long long) * c.G.size() * HEADS, s);
   if (e != cudaSuccess)
     return e;
   const unsigned pb = (unsigned)((c.np + 127) / 128);
@@ -1109,7 +1117,7 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
     BatchGroup &g = c.G[gi];
     if (g.tiles[st] == 0)
       return cudaSuccess;
-    TileQueue q{g.dOff[st], (int)g.idx.size(), c.heads + gi * BS_COUNT + st};
+    TileQueue q{g.dOff[st], (int)g.idx.size(), c.heads + gi * HEADS + st};
     int pp = g.per_pop[st] >= 0 ? g.per_pop[st] : 1;
     unsigned grid;
     if (pp == 0) { // one block per tile, no queue
@@ -1125,6 +1133,19 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
       cudaEventRecord(ev[(gi * BS_COUNT + st) * 2], s);
     cudaError_t r = launch(g.fn[st], dim3(grid), dim3(g.threads[st]),
                            g.smem[st], s, args);
+    if (r == cudaSuccess && st == BS_FACES && g.faces_eig.valid()) {
+      // the second launch of the faces: the same tiles, its own queue
+      TileQueue q2{g.dOff[st], (int)g.idx.size(),
+                   c.heads + gi * HEADS + BS_COUNT};
+      unsigned grid2 = grid;
+      if (pp != 0) {
+        long long want = (g.tiles[st] + pp - 1) / pp;
+        long long cap = (long long)g.faces_eig_resident * c.nsm;
+        grid2 = (unsigned)(want < cap ? want : cap);
+      }
+      void *args2[3] = {(void *)&g.dP, (void *)&q2, (void *)&pp};
+      r = launch(g.faces_eig, dim3(grid2), dim3(128), 0, s, args2);
+    }
     if (ev)
       cudaEventRecord(ev[(gi * BS_COUNT + st) * 2 + 1], s);
     return r;
@@ -1169,10 +1190,13 @@ static cudaError_t enqueue_batch_step(BatchCtx &c, cudaStream_t s,
 
 static int batch_launches_per_step(const BatchCtx &c) {
   int n = 3;
-  for (auto &g : c.G)
+  for (auto &g : c.G) {
     for (int st = 0; st < BS_COUNT; st++)
       if (g.tiles[st] > 0)
         n++;
+    if (g.tiles[BS_FACES] > 0 && g.faces_eig.valid())
+      n++; // the faces' second launch
+  }
   return n;
 }
 
@@ -1272,6 +1296,16 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
     tot += (doubles + 31) / 32 * 32; // 256-byte aligned
     return at;
   };
+  // The Rusanov faces of a first-order flux system without B run in two
+  // launches, through records of every face point of the batch (73 doubles
+  // a point for the 2-D relaxation system: 76 GB for 256 problems of 64^2
+  // to 512^2 cells and orders 1-3, within the GPU's memory).
+  std::vector<size_t> o_rec(a.np);
+  size_t t_rec = 0;
+  auto two_launch_faces = [&](int N) {
+    const KernelSet &k = sys.sets[N];
+    return c.faces && a.flux == 0 && k.kb_faces_pre.valid() && k.face_rec > 0;
+  };
   for (int p = 0; p < a.np; p++) {
     const int N = a.probs[p].N, Nd = ipow(N, ndim);
     const Geom &g = geo[p];
@@ -1285,8 +1319,11 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
     o_ct[p] = carve(t_ct, c.faces ? fis[p].off[ndim] * 2 * V : 1);
     o_cen[p] = carve(t_cen, c.centers ? g.C * N * Nd * V : 1);
     o_wp[p] = carve(t_wp, Nd);
+    o_rec[p] = carve(t_rec, two_launch_faces(N)
+                                ? fis[p].off[ndim] * sys.sets[N].face_rec
+                                : 0);
   }
-  double *b_u, *b_ub, *b_ta, *b_tb, *b_w, *b_qh, *b_ct, *b_cen, *b_wp;
+  double *b_u, *b_ub, *b_ta, *b_tb, *b_w, *b_qh, *b_ct, *b_cen, *b_wp, *b_rec;
   DevState *b_st;
   CK(mem.alloc((void **)&b_u, t_u * 8));
   CK(mem.alloc((void **)&b_ub, t_ub * 8));
@@ -1297,9 +1334,10 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
   CK(mem.alloc((void **)&b_ct, t_ct * 8));
   CK(mem.alloc((void **)&b_cen, t_cen * 8));
   CK(mem.alloc((void **)&b_wp, t_wp * 8));
+  CK(mem.alloc((void **)&b_rec, (t_rec ? t_rec : 1) * 8));
   CK(mem.alloc((void **)&b_st, sizeof(DevState) * a.np));
   CK(mem.alloc((void **)&c.heads,
-               sizeof(unsigned long long) * c.G.size() * BS_COUNT));
+               sizeof(unsigned long long) * c.G.size() * HEADS));
 
   // problem descriptors and tile tables, in group order
   std::vector<BatchProblem> order;
@@ -1324,6 +1362,7 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
       b.contrib = b_ct + o_ct[p];
       b.cen = b_cen + o_cen[p];
       b.wprod = b_wp + o_wp[p];
+      b.rec = two_launch_faces(N) ? b_rec + o_rec[p] : nullptr;
       b.st = b_st + p;
       long long tw[3] = {0, 0, 0};
       int m[3] = {ge.nXb[0], ge.nXb[1], ge.nXb[2]};
@@ -1402,7 +1441,12 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
       g.threads[BS_PREDICTOR] = k.pred_threads;
       g.smem[BS_PREDICTOR] = k.pred_smem;
     }
-    g.fn[BS_FACES] = k.kb_faces[a.flux];
+    if (two_launch_faces(N)) {
+      g.fn[BS_FACES] = k.kb_faces_pre;
+      g.faces_eig = k.kb_faces_eig;
+    } else {
+      g.fn[BS_FACES] = k.kb_faces[a.flux];
+    }
     g.threads[BS_FACES] = 128;
     g.fn[BS_CENTERS] = k.kb_centers;
     g.threads[BS_CENTERS] = 128;
@@ -1419,6 +1463,8 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
       CK(set_smem(g.fn[st], g.smem[st]));
       g.resident[st] = resident_blocks(g.fn[st], g.threads[st], g.smem[st]);
     }
+    if (g.faces_eig.valid())
+      g.faces_eig_resident = resident_blocks(g.faces_eig, 128, 0);
   }
   CK(mem.alloc((void **)&c.dPall, sizeof(BatchProblem) * order.size()));
   CK(cudaMemcpyAsync(c.dPall, order.data(), sizeof(BatchProblem) * order.size(),

@@ -41,6 +41,7 @@ struct KernelSet {
   // one-launch k_faces only
   KFunc faces_pre, faces_eig;
   int face_rec = 0;
+  KFunc kb_faces_pre, kb_faces_eig; // their batched forms
 };
 
 struct SystemDesc {

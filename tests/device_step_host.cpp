@@ -731,6 +731,9 @@ void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
     b.contrib = buf((faces ? b.fi.off[ndim] : 1) * 2 * V);
     b.cen = buf((centers ? b.g.C * NT : 1) * V);
     b.wprod = const_cast<double *>(wprod.data());
+    // records of the two-launch faces, as run_batch carves them
+    if constexpr (FLUX == 0 && FaceSplit<Sys>::OK)
+      b.rec = buf(b.fi.off[ndim] * FaceSplit<Sys>::REC);
     long long tw[3] = {0, 0, 0};
     int m[3] = {b.g.nXb[0], b.g.nXb[1], b.g.nXb[2]};
     const double *src = b.ub;
@@ -817,9 +820,15 @@ void run_batch_steps(int np, double *u_all, int ndim, const int *nX_all,
       stage(B_PRED, PredCfg<Sys, N>::THREADS,
             (size_t)PredCfg<Sys, N>::SMEM_DOUBLES * 8,
             [&](TileQueue q, int pp) { kb_predictor<Sys, N>(dP, q, pp, T); });
-    if (faces)
+    if (faces && FLUX == 0 && FaceSplit<Sys>::OK) { // two launches, own queues
+      stage(B_FACES, 128, 0,
+            [&](TileQueue q, int pp) { kb_faces_pre<Sys, N>(dP, q, pp, T); });
+      stage(B_FACES, 128, 0,
+            [&](TileQueue q, int pp) { kb_faces_eig<Sys, N>(dP, q, pp); });
+    } else if (faces) {
       stage(B_FACES, 128, 0,
             [&](TileQueue q, int pp) { kb_faces<Sys, N, FLUX>(dP, q, pp, T); });
+    }
     if (centers)
       stage(B_CEN, 128, 0,
             [&](TileQueue q, int pp) { kb_centers<Sys, N>(dP, q, pp, T); });
