@@ -1542,6 +1542,12 @@ template <class Sys> struct FaceSplit {
   static constexpr bool OK = Sys::HAS_F && !Sys::HAS_B && !Sys::SECOND_ORDER;
   static constexpr int MS = EigBlock<Sys>::value;
   static constexpr int REC = 2 * MS * MS + 3 * Sys::V + 2;
+  // CTAs an SM that k_faces_eig is compiled for: 6 (80 registers) for a
+  // 5x5 block, where max_abs_eig<5> then spills and the stage is still
+  // faster (2-D relaxation system at 1024^2: 31.7 ms a step against 32.1
+  // with 4 CTAs and 32.2 with 5); 4 (128 registers, no spills in the
+  // solver) otherwise
+  static constexpr int EIG_CTAS = MS == 5 ? 6 : 4;
 };
 
 // The first half of max_abs_eigs: the matrix max_abs_eig takes and F(q)
@@ -1675,9 +1681,10 @@ __device__ __forceinline__ void face_eig_point(long long p, const double *r, lon
   }
 }
 
-// The records of k_faces_pre for the same points.
+// The records of k_faces_pre for the same points, FaceSplit<Sys>::EIG_CTAS
+// CTAs an SM.
 template <class Sys, int N>
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(128, FaceSplit<Sys>::EIG_CTAS)
     k_faces_eig(const double *__restrict__ rec, long long ch, double *__restrict__ contrib,
                 const __grid_constant__ FaceIndex fi, DevState *st,
                 const __grid_constant__ FaceSpan sp, long long q0) {
