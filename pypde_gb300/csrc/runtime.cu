@@ -856,9 +856,14 @@ int run_solver(const SystemDesc &sys, const RunArgs &a, Stats *out) {
   CK(ensure(ar->ring, c.ring * usz * 8));
   if (c.faces && c.flux == 0 && c.ks->face_rec > 0) {
     const long long pts = c.fi.off[a.ndim];
-    c.face_ch = pts < FACE_CHUNK ? pts : FACE_CHUNK;
-    CK(ensure(ar->facerec, (long long)c.ks->face_rec * c.face_ch * 8));
-    c.facerec = (double *)ar->facerec.p;
+    const long long ch = pts < FACE_CHUNK ? pts : FACE_CHUNK;
+    if (ensure(ar->facerec, (long long)c.ks->face_rec * ch * 8) ==
+        cudaSuccess) {
+      c.face_ch = ch;
+      c.facerec = (double *)ar->facerec.p;
+    } else { // no room for the records: the faces run as one launch
+      cudaGetLastError();
+    }
   }
   CK(ensure(ar->state, sizeof(DevState)));
   CK(ensure(ar->wprod, Nd * 8));
@@ -1300,11 +1305,14 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
   // launches, through records of every face point of the batch (73 doubles
   // a point for the 2-D relaxation system: 76 GB for 256 problems of 64^2
   // to 512^2 cells and orders 1-3, within the GPU's memory).
+  // Without room for them the faces run as one launch (recs_ok false).
   std::vector<size_t> o_rec(a.np);
   size_t t_rec = 0;
+  bool recs_ok = true;
   auto two_launch_faces = [&](int N) {
     const KernelSet &k = sys.sets[N];
-    return c.faces && a.flux == 0 && k.kb_faces_pre.valid() && k.face_rec > 0;
+    return recs_ok && c.faces && a.flux == 0 && k.kb_faces_pre.valid() &&
+           k.face_rec > 0;
   };
   for (int p = 0; p < a.np; p++) {
     const int N = a.probs[p].N, Nd = ipow(N, ndim);
@@ -1323,7 +1331,8 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
                                 ? fis[p].off[ndim] * sys.sets[N].face_rec
                                 : 0);
   }
-  double *b_u, *b_ub, *b_ta, *b_tb, *b_w, *b_qh, *b_ct, *b_cen, *b_wp, *b_rec;
+  double *b_u, *b_ub, *b_ta, *b_tb, *b_w, *b_qh, *b_ct, *b_cen, *b_wp;
+  double *b_rec = nullptr;
   DevState *b_st;
   CK(mem.alloc((void **)&b_u, t_u * 8));
   CK(mem.alloc((void **)&b_ub, t_ub * 8));
@@ -1334,7 +1343,12 @@ int run_batch(const SystemDesc &sys, const BatchArgs &a, BatchStats *out) {
   CK(mem.alloc((void **)&b_ct, t_ct * 8));
   CK(mem.alloc((void **)&b_cen, t_cen * 8));
   CK(mem.alloc((void **)&b_wp, t_wp * 8));
-  CK(mem.alloc((void **)&b_rec, (t_rec ? t_rec : 1) * 8));
+  if (t_rec == 0) {
+    recs_ok = false;
+  } else if (mem.alloc((void **)&b_rec, t_rec * 8) != cudaSuccess) {
+    cudaGetLastError(); // the failed allocation
+    recs_ok = false;
+  }
   CK(mem.alloc((void **)&b_st, sizeof(DevState) * a.np));
   CK(mem.alloc((void **)&c.heads,
                sizeof(unsigned long long) * c.G.size() * HEADS));
