@@ -196,3 +196,30 @@ def test_boundary_codes_checked_before_device_work(gpu_lib):
                                       _lib.c_ptr(ub))
         assert rc == _lib.PYPDE_ERR_ARG
         assert b"boundaryTypes" in gpu_lib.pypde_last_error()
+
+
+def test_strip_count_checked_before_device_work(gpu_lib):
+    """pypde_options.strips outside 0-32 is refused with PYPDE_ERR_ARG on
+    the host, before any device work."""
+    import ctypes
+
+    from pypde_gb300 import _lib
+    u = np.ones((8, 3))
+    nX = np.array([8], dtype=np.int32)
+    dX = np.array([1.0 / 8])
+    bt = np.array([0], dtype=np.int32)
+    ret = np.zeros((1, 8, 3))
+    h = ctypes.c_void_p()
+    _lib.check(gpu_lib.pypde_system_builtin(b"euler", 1, ctypes.byref(h)))
+    try:
+        for strips in (-1, 33):
+            opt = _lib.Options()
+            opt.strips = strips
+            rc = gpu_lib.pde_solver_ex(h, True, False, False, _lib.c_ptr(u), 0.1,
+                                       _lib.c_ptr(nX), 1, _lib.c_ptr(dX), 0.9,
+                                       _lib.c_ptr(bt), False, 0, 2, 1, _lib.c_ptr(ret),
+                                       ctypes.byref(opt), None)
+            assert rc == _lib.PYPDE_ERR_ARG
+            assert b"strips" in gpu_lib.pypde_last_error()
+    finally:
+        gpu_lib.pypde_system_free(h)
